@@ -1,0 +1,367 @@
+"""Generate the golden fixtures in this folder by running the reference.
+
+Run from the repository root in a container that has the reference source
+(``RADIOBEAR_REF``, default ``/root/reference``):
+
+    python tests/golden/make_golden.py            # all fixtures
+    python tests/golden/make_golden.py bench c0   # a subset
+
+Fixtures (all float64, ``numpy.savez_compressed``):
+
+``catalogs_real.npz``
+    The real catalogues as the reference's loaders prepare them (default
+    Jupiter truncation): ``ammonia.npz``, ``nh3.npz``, ``h2s.npz`` (121
+    lines), ``ph3jh.npz`` + ``PH3WGT.npz`` (33 lines) and the 15 built-in
+    ``h2o_bk`` lines.  Keys are ``<catalogue>__<column>``.
+``benchmark.npz``
+    ``scripts/benchmark.py``: Jupiter, ``Jupiter/config_benchmark.par``,
+    6 freqs x 4 equatorial rays.  Holds the regridded atmosphere the
+    reference built (gas + R, N), its alpha layers and per-gas alpha, the
+    float64 Tb it computed, the float32 expected table ``T_rb`` quoted in
+    ``scripts/benchmark.py:20-24`` and the ray paths.
+``c0.npz``
+    Configuration 0 (synthetic, 200 layers, 21 freqs, 200 NH3 lines): inputs,
+    per-gas alpha for every layer, Tb for b=[0,0] and for 'disc', ray paths
+    for nadir, off-nadir, oblique and limb rays (tangent/egress restored by
+    the sqrt patch), with orientation (0,0) and (10,25) deg.
+``c1_alpha.npz``
+    Configuration 1 line lists (2000 NH3, 500 H2O, 200 H2S, 33 PH3) and
+    256 freqs: per-gas alpha for 40 layers including the 400-500 bar
+    nh3_hs/nh3_sjs blend layers.
+``c1_tb.npz``
+    Configuration 1: Tb of 6 Gauss-Legendre rays (incl. the two outermost)
+    from the reference's full 1000-layer alpha.
+``scale_cases.npz``
+    ``Alpha.get_layers`` with number, list and dict scales on the C0
+    atmosphere, plus the ``save_alpha='memory'`` cube.
+"""
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+import refharness as rh  # noqa: E402
+from radiobear_gb300 import synth  # noqa: E402
+
+GAS_KEEP = ['Z', 'T', 'P', 'H2', 'HE', 'CH4', 'NH3', 'H2O', 'H2S', 'PH3']
+
+
+def _flatten(prefix, d):
+    return {'{}__{}'.format(prefix, k): np.asarray(v, dtype=np.float64) for k, v in d.items()}
+
+
+def real_catalogues():
+    path = os.path.join(HERE, 'catalogs_real.npz')
+    if os.path.exists(path):
+        z = np.load(path)
+        out = {}
+        for k in z.files:
+            cat, col = k.split('__', 1)
+            out.setdefault(cat, {})[col] = z[k]
+        return out
+    cats = rh.load_real_catalogues()
+    flat = {}
+    for cat, d in cats.items():
+        flat.update(_flatten(cat, d))
+    np.savez_compressed(path, **flat)
+    print('wrote', path, {c: len(next(iter(d.values()))) for c, d in cats.items()})
+    return cats
+
+
+def _ray_record(ray):
+    if ray.ds is None:
+        return np.zeros(0), np.zeros(0, dtype=np.int64), np.zeros(0)
+    return (np.asarray(ray.ds, dtype=np.float64), np.asarray(ray.layer4ds, dtype=np.int64),
+            np.asarray(ray.r4ds, dtype=np.float64))
+
+
+def _gas_arrays(atm):
+    C = atm.config.C
+    return {('gas_' + k): np.asarray(atm.gas[C[k]], dtype=np.float64) for k in GAS_KEEP}
+
+
+def _prop_arrays(atm):
+    LP = atm.config.LP
+    return {'prop_R': np.asarray(atm.property[LP['R']]), 'prop_N': np.asarray(atm.property[LP['N']])}
+
+
+def golden_benchmark():
+    rh.import_reference()
+    rh.reset_lines()
+    rh.patch_limb_sqrt(False)
+    import radiobear.raypath as rp
+    work = tempfile.mkdtemp(prefix='rbgold_bench_')
+    rh.benchmark_planet_dir(work)
+    cwd = os.getcwd()
+    os.chdir(work)
+    try:
+        j = rh.make_planet('config_benchmark.par')
+        freqs = [0.6, 1.25, 2.6, 5.2, 10, 21.9]
+        b = [[0.0, 0.0], [np.sin(np.radians(15)), 0.0], [np.sin(np.radians(30)), 0.0],
+             [np.sin(np.radians(45)), 0.0]]
+        rv = j.run(freqs, b=b, reuse_override='False', save_alpha='memory')
+        atm = j.atmos[0]
+        out = dict(freqs=np.array(freqs, dtype=np.float64), b=np.array(b),
+                   Tb=np.array(j.Tb, dtype=np.float64), Tb_f32=np.asarray(rv.Tb),
+                   alpha_layers=np.asarray(j.alpha[0].layers),
+                   alpha_gas=np.asarray(j.alpha[0].memory.alpha_data),
+                   Req=j.config.Req, Rpol=j.config.Rpol)
+        out.update(_gas_arrays(atm))
+        out.update(_prop_arrays(atm))
+        out['T_rb'] = np.array(
+            [[805.38385, 424.58337, 298.74915, 227.0338, 179.9148, 147.3627],
+             [790.66736, 420.24728, 296.62033, 225.69223, 179.22531, 147.24104],
+             [745.55975, 407.28714, 290.07492, 221.56863, 177.13437, 146.8625],
+             [668.4528, 385.59015, 278.51672, 214.30847, 173.56506, 146.17966]], dtype=np.float32)
+        for i, bv in enumerate(b):
+            ds, lay, r4 = _ray_record(rp.compute_ds(atm, bv))
+            out['ray{}_ds'.format(i)] = ds
+            out['ray{}_layer'.format(i)] = lay
+        out['ordered_constituents'] = np.array(j.alpha[0].ordered_constituents)
+    finally:
+        os.chdir(cwd)
+    dev = np.max(np.abs(out['Tb'].astype(np.float32) - out['T_rb']))
+    print('benchmark: max |Tb(f32) - T_rb| =', dev)
+    assert dev <= 1e-3, dev
+    path = os.path.join(HERE, 'benchmark.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
+def _synth_planet(work, wl, orientation=(0.0, 0.0), name='config_synth.par'):
+    rh.scratch_planet_dir(work, wl.gas, synth.GAS_COLUMNS, config_name=name,
+                          orientation=orientation)
+    return rh.make_planet(name)
+
+
+C0_RAYS = [[0.0, 0.0], [0.3, 0.0], [0.7, 0.0], [0.95, 0.0], [0.0, 0.5], [0.4, 0.4],
+           [0.997, 0.0], [0.9985, 0.0], [0.99, 0.05], [0.0, 0.92], [0.5, -0.6], [1.2, 0.0]]
+
+
+def golden_c0():
+    cats = real_catalogues()
+    rh.import_reference()
+    import radiobear.raypath as rp
+    wl = synth.make_workload(0, real=cats)
+    rh.reset_lines()
+    lines = dict(wl.lines)
+    lines['ph3wgt'] = cats['ph3wgt']
+    work = tempfile.mkdtemp(prefix='rbgold_c0_')
+    cwd = os.getcwd()
+    os.chdir(work)
+    out = {}
+    try:
+        j = _synth_planet(work, wl)
+        rh.inject_lines(lines)
+        rh.patch_limb_sqrt(False)
+        freqs = '1:100:5'
+        j.run(freqs, b=[0.0, 0.0], reuse_override='False', save_alpha='memory')
+        out['Tb_nadir'] = np.array(j.Tb[0], dtype=np.float64)
+        out['alpha_layers'] = np.asarray(j.alpha[0].layers)
+        out['alpha_gas'] = np.asarray(j.alpha[0].memory.alpha_data)
+        out['freqs'] = np.asarray(j.freqs, dtype=np.float64)
+        j.run(freqs, b='disc', reuse_override='False')
+        out['Tb_disc'] = np.array(j.Tb[0], dtype=np.float64)
+        bri = j.bright
+        out['disc_tau'] = np.asarray(bri.tau)
+        out['disc_W'] = np.asarray(bri.W)
+        out['disc_intW'] = np.asarray(bri.integrated_W)
+        atm = j.atmos[0]
+        out.update(_gas_arrays(atm))
+        out.update(_prop_arrays(atm))
+        # rays: unpatched for on-disc, patched (tangent branch restored) for all
+        rh.patch_limb_sqrt(True)
+        tbs = []
+        for i, bv in enumerate(C0_RAYS):
+            ds, lay, r4 = _ray_record(rp.compute_ds(atm, bv))
+            out['ray{}_ds'.format(i)] = ds
+            out['ray{}_layer'.format(i)] = lay
+            out['ray{}_r4ds'.format(i)] = r4
+            tb = j.bright.single(bv, out['freqs'].tolist(), atm, j.alpha[0], j.config.orientation)
+            tbs.append(np.array(tb, dtype=np.float64))
+        out['Tb_rays'] = np.array(tbs)
+        out['rays_b'] = np.array(C0_RAYS)
+        rh.patch_limb_sqrt(False)
+    finally:
+        os.chdir(cwd)
+    # tilted planet: orientation (10, 25) deg
+    work2 = tempfile.mkdtemp(prefix='rbgold_c0o_')
+    os.chdir(work2)
+    try:
+        j2 = _synth_planet(work2, wl, orientation=(10.0, 25.0), name='config_tilt.par')
+        rh.inject_lines(lines)
+        rh.patch_limb_sqrt(True)
+        atm2 = j2.atmos[0]
+        j2.alpha[0].get_layers(out['freqs'].tolist(), atm2)
+        tilt_rays = [[0.0, 0.0], [0.3, 0.2], [-0.5, 0.6], [0.9, -0.3], [0.999, 0.0]]
+        tbs = []
+        for i, bv in enumerate(tilt_rays):
+            ds, lay, r4 = _ray_record(rp.compute_ds(atm2, bv))
+            out['tilt{}_ds'.format(i)] = ds
+            out['tilt{}_layer'.format(i)] = lay
+            tb = j2.bright.single(bv, out['freqs'].tolist(), atm2, j2.alpha[0], j2.config.orientation)
+            tbs.append(np.array(tb, dtype=np.float64))
+        out['tilt_Tb'] = np.array(tbs)
+        out['tilt_b'] = np.array(tilt_rays)
+        out['tilt_orientation'] = np.array([10.0, 25.0])
+        rh.patch_limb_sqrt(False)
+    finally:
+        os.chdir(cwd)
+    # synthetic inputs, so the fixture is self-contained
+    for k, v in wl.lines['ammonia'].items():
+        out['ammonia__' + k] = v
+    for k, v in wl.lines['nh3'].items():
+        out['nh3__' + k] = v
+    out['ordered_constituents'] = np.array(j.alpha[0].ordered_constituents)
+    path = os.path.join(HERE, 'c0.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
+C1_LAYERS = None
+
+
+def c1_layer_subset(P):
+    idx = set(np.linspace(0, len(P) - 1, 24).astype(int).tolist())
+    idx.update(np.nonzero(P >= 380.0)[0].tolist())
+    return np.array(sorted(idx))
+
+
+def golden_c1_alpha():
+    cats = real_catalogues()
+    rh.import_reference()
+    wl = synth.make_workload(1, real=cats)
+    rh.reset_lines()
+    lines = dict(wl.lines)
+    lines['ph3wgt'] = cats['ph3wgt']
+    work = tempfile.mkdtemp(prefix='rbgold_c1_')
+    cwd = os.getcwd()
+    os.chdir(work)
+    try:
+        j = _synth_planet(work, wl)
+        rh.inject_lines(lines)
+        atm = j.atmos[0]
+        C = atm.config.C
+        P = atm.gas[C['P']]
+        sel = c1_layer_subset(P)
+        freqs = wl.freqs.tolist()
+        t0 = time.time()
+        per = []
+        for layer in sel:
+            a = j.alpha[0].get_alpha_from_calc(freqs, atm.gas[C['T']][layer], P[layer],
+                                               atm.gas[:, layer], C, atm.cloud[:, layer],
+                                               atm.config.Cl, units='invcm')
+            per.append(np.asarray(a, dtype=np.float64))
+        print('c1 alpha subset: {} layers in {:.1f} s'.format(len(sel), time.time() - t0))
+        out = dict(layers=sel, alpha_gas=np.array(per), freqs=wl.freqs,
+                   ordered_constituents=np.array(j.alpha[0].ordered_constituents))
+        out.update(_gas_arrays(atm))
+    finally:
+        os.chdir(cwd)
+    path = os.path.join(HERE, 'c1_alpha.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
+def golden_c1_tb():
+    cats = real_catalogues()
+    rh.import_reference()
+    wl = synth.make_workload(1, real=cats)
+    rh.reset_lines()
+    lines = dict(wl.lines)
+    lines['ph3wgt'] = cats['ph3wgt']
+    work = tempfile.mkdtemp(prefix='rbgold_c1tb_')
+    cwd = os.getcwd()
+    os.chdir(work)
+    try:
+        j = _synth_planet(work, wl)
+        rh.inject_lines(lines)
+        rh.patch_limb_sqrt(True)
+        atm = j.atmos[0]
+        t0 = time.time()
+        j.alpha[0].get_layers(wl.freqs.tolist(), atm)
+        print('c1 full alpha: {:.1f} s'.format(time.time() - t0))
+        ray_idx = np.array([0, 1, 2, 20, 40, 63])
+        tbs = []
+        for k in ray_idx:
+            tb = j.bright.single(wl.b[k].tolist(), wl.freqs.tolist(), atm, j.alpha[0],
+                                 j.config.orientation)
+            tbs.append(np.array(tb, dtype=np.float64))
+        rh.patch_limb_sqrt(False)
+        out = dict(ray_idx=ray_idx, b=wl.b[ray_idx], Tb=np.array(tbs), freqs=wl.freqs)
+        out.update(_gas_arrays(atm))
+        out.update(_prop_arrays(atm))
+    finally:
+        os.chdir(cwd)
+    path = os.path.join(HERE, 'c1_tb.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
+def golden_scale_cases():
+    cats = real_catalogues()
+    rh.import_reference()
+    wl = synth.make_workload(0, real=cats)
+    rh.reset_lines()
+    lines = dict(wl.lines)
+    lines['ph3wgt'] = cats['ph3wgt']
+    work = tempfile.mkdtemp(prefix='rbgold_scale_')
+    cwd = os.getcwd()
+    os.chdir(work)
+    try:
+        j = _synth_planet(work, wl)
+        rh.inject_lines(lines)
+        atm = j.atmos[0]
+        nL = atm.gas.shape[1]
+        P = atm.gas[atm.config.C['P']]
+        freqs = [1.0, 5.0, 22.0, 31.0, 60.0]
+        al = j.alpha[0]
+        out = dict(freqs=np.array(freqs))
+        al.get_layers(freqs, atm, scale=False, save_alpha='memory')
+        out['plain'] = np.asarray(al.layers)
+        out['saved'] = np.asarray(al.memory.alpha_data)
+        al.get_layers(freqs, atm, scale=0.5)
+        out['number'] = np.asarray(al.layers)
+        ramp = (2.0 * (P[-1] - P / 1.5) / P[-1])
+        al.get_layers(freqs, atm, scale=ramp.tolist())
+        out['list'] = np.asarray(al.layers)
+        out['list_scale'] = ramp
+        dscale = {'nh3': np.where(P > 1.0, 0.25, 2.0).tolist(),
+                  'h2o': np.where(P > 10.0, 0.5, 1.0e-4).tolist()}
+        al.get_layers(freqs, atm, scale=dscale)
+        out['dict'] = np.asarray(al.layers)
+        out['dict_nh3'] = np.array(dscale['nh3'])
+        out['dict_h2o'] = np.array(dscale['h2o'])
+        # reuse of the saved cube with a dict scale (scripts/demo_batch.py path)
+        al.get_layers(freqs, atm, scale=False, save_alpha='memory')
+        al.get_layers(freqs, atm, scale=dscale, get_alpha='memory')
+        out['dict_from_memory'] = np.asarray(al.layers)
+        # unsorted frequencies straddling 30 GHz (nh3_hs output ordering)
+        fun = [40.0, 10.0, 22.2, 35.0, 2.0]
+        al.get_layers(fun, atm)
+        out['unsorted_freqs'] = np.array(fun)
+        out['unsorted'] = np.asarray(al.layers)
+        assert out['plain'].shape == (len(freqs), nL)
+    finally:
+        os.chdir(cwd)
+    path = os.path.join(HERE, 'scale_cases.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
+JOBS = dict(cats=real_catalogues, bench=golden_benchmark, c0=golden_c0,
+            c1a=golden_c1_alpha, c1tb=golden_c1_tb, scale=golden_scale_cases)
+
+if __name__ == '__main__':
+    which = sys.argv[1:] or list(JOBS)
+    for name in which:
+        t0 = time.time()
+        JOBS[name]()
+        print('[{}] {:.1f} s'.format(name, time.time() - t0))
