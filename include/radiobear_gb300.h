@@ -1,0 +1,173 @@
+/*
+ * radiobear_gb300 — C ABI of the GB300 (sm_103a) radioBEAR forward model.
+ *
+ * Plain C: opaque handle, plain pointers and sizes, int status codes, no
+ * exceptions across the boundary.  The caller owns every buffer it passes;
+ * the library owns the device memory behind a handle.  One handle per host
+ * thread; calls on a handle are synchronous unless the name ends in
+ * _device (those enqueue on the given CUDA stream and return).
+ *
+ * Units follow the reference: frequencies GHz, pressure bar, temperature K,
+ * radii and path lengths km, absorption cm^-1 (dB/km when units_db = 1).
+ *
+ * Reference interfaces each entry point replaces (paths relative to the
+ * david-deboer/radiobear project root):
+ *   rb_set_lines      the catalogue loaders readInputFiles of
+ *                     radiobear/constituents/nh3/nh3_hs.py:62-67,
+ *                     nh3/nh3_sjs.py:17-23, h2o/h2o_bk.py:17-62,
+ *                     h2s/h2s_ddb.py:14-39, ph3/ph3_jh.py:18-61
+ *   rb_set_formalisms Alpha.setup_formalisms, radiobear/alpha.py:49-102
+ *   rb_alpha          Alpha.get_layers / get_alpha_from_calc /
+ *                     total_layer_alpha, radiobear/alpha.py:151-305, and the
+ *                     per-gas plugins alpha(freq, T, P, X, P_dict, other_dict)
+ *   rb_raypath        raypath.compute_ds, radiobear/raypath.py:108-273
+ *   rb_brightness     Brightness.single, radiobear/brightness.py:30-126
+ *   rb_forward        Planet.run's alpha_layers + b loop + bright_run,
+ *                     radiobear/planet.py:59-160 (one call per spectrum set)
+ */
+#ifndef RADIOBEAR_GB300_H
+#define RADIOBEAR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RB_ABI_VERSION 1
+
+typedef struct rb_handle rb_handle;
+
+/* status codes */
+#define RB_OK 0
+#define RB_EINVAL 1  /* bad argument (message in rb_last_error) */
+#define RB_ECUDA 2   /* CUDA runtime error */
+#define RB_ENOMEM 3  /* device allocation failed */
+#define RB_ESTATE 4  /* call out of order (e.g. no lines uploaded) */
+
+/* line families (rb_set_lines) and their column order */
+#define RB_FAM_NH3_INV 0 /* fo, Io, Eo, gammaNH3o                (ammonia.npz) */
+#define RB_FAM_NH3_ROT 1 /* fo_rot, Io_rot, Eo_rot, gNH3_rot, gH2_rot, gHe_rot */
+#define RB_FAM_NH3_V2 2  /* fo_v2, Io_v2, Eo_v2 */
+#define RB_FAM_NH3_SJS 3 /* f0, I0, E, G0                         (nh3.npz) */
+#define RB_FAM_H2O 4     /* f_o, I_o, E_o, w_s, x_s, w_h2, w_he, x_h2, x_he, SR */
+#define RB_FAM_H2S 5     /* f0, I0, E, GH2S                       (h2s.npz) */
+#define RB_FAM_PH3 6     /* f0, I0, E, WgtI0, WgtFGB, WgtSB       (ph3jh + PH3WGT) */
+
+/* NH3 formalism (rb_set_formalisms) */
+#define RB_NH3_OFF 0
+#define RB_NH3_HS 1     /* nh3_hs */
+#define RB_NH3_SJS 2    /* nh3_sjs */
+#define RB_NH3_HS_SJS 3 /* nh3_hs_sjs pressure blend */
+
+/* gas slots of per-gas outputs: the reference's sorted constituent order */
+#define RB_GAS_H2 0
+#define RB_GAS_H2O 1
+#define RB_GAS_H2S 2
+#define RB_GAS_NH3 3
+#define RB_GAS_PH3 4
+#define RB_NGAS 5
+
+/* rows of the abundance array X[RB_NX][nL] (mole fractions) */
+#define RB_X_H2 0
+#define RB_X_HE 1
+#define RB_X_CH4 2
+#define RB_X_NH3 3
+#define RB_X_H2O 4
+#define RB_X_H2S 5
+#define RB_X_PH3 6
+#define RB_NX 7
+
+/* geometry switches */
+#define RB_GTYPE_ELLIPSE 0
+#define RB_GTYPE_SPHERE 1
+#define RB_LIMB_SHAPE 0
+#define RB_LIMB_SEC 1
+
+int rb_abi_version(void);
+/* Last error message of the calling thread ("" if none). */
+const char* rb_last_error(void);
+
+/* Create a handle on CUDA device `device`. */
+int rb_create(rb_handle** out, int device);
+int rb_destroy(rb_handle* h);
+
+/* Upload one line family.  cols is column-major: cols[c*n + i] is column c
+ * of line i, columns in the order listed above.  Truncation by strength or
+ * frequency is the caller's (the reference applies it in its loaders).
+ * Lines are sorted by centre internally.  n = 0 clears the family. */
+int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols);
+
+/* Select formalisms: nh3 one of RB_NH3_*, the others 0/1;
+ * h2state 'e' (equilibrium) or 'n' (normal) H2 for the CIA prefactor. */
+int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2s, int use_ph3,
+                      int h2state);
+
+/* Absorption of nL layers at nf frequencies.
+ *   P[nL] bar, T[nL] K, X[RB_NX][nL] mole fractions, freqs[nf] GHz.
+ *   scale:      nullable, [nL][RB_NGAS] multipliers (number, per-layer list
+ *               and per-constituent dict scales of Alpha.get_layers all map
+ *               onto this form).
+ *   layers_out: nullable, [nf][nL]  total (Alpha.layers)
+ *   gas_out:    nullable, [nL][nf][RB_NGAS] scaled per gas (Alpha.tosave)
+ * units_db = 1 returns dB/km (the nh3_hs clamp then acts in dB/km). */
+int rb_alpha(rb_handle* h, int nL, const double* P, const double* T, const double* X, int nf,
+             const double* freqs, const double* scale, int units_db, double* layers_out,
+             double* gas_out);
+
+/* Ray paths of nb impact parameters b[nb][2] (fraction of R[0]).
+ *   R[nL] equatorial layer radii (km, top first), N[nL] refractive index,
+ *   Req/Rpol (km) set the shell ellipse and the aspect flattening,
+ *   orient0/orient1 the orientation (deg), gtype/limb the switches above.
+ * Outputs per ray: nseg[nb]; ds[nb][max_seg] km; layer[nb][max_seg];
+ * nullable r4ds[nb][max_seg]; nullable latlng[nb][max_seg+1][2] (deg) of
+ * each path point; nullable end_code[nb] (0 no path, 1 ran to the last
+ * layer, 2 left the atmosphere, 3 max_seg too small).
+ * max_seg >= 2*nL + 4 always suffices. */
+int rb_raypath(rb_handle* h, int nL, const double* R, const double* N, double Req, double Rpol,
+               double orient0, double orient1, int gtype, int limb, int nb, const double* b,
+               int max_seg, int32_t* nseg, double* ds, int32_t* layer, double* r4ds,
+               double* latlng, int32_t* end_code);
+
+/* Brightness temperature of nb paths given absorption layers[nf][nL]
+ * (cm^-1) and T[nL].  disc = 1 uses the 2 E2(tau) weighting of b = 'disc'.
+ * Tb_out[nb][nf]; nullable intW_out[nb][nf]; nullable profiles
+ * tau/W/TbL [nb][nf][max_seg] (entry 0 is the zero start value). */
+int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* layers, int nb,
+                  const int32_t* nseg, const double* ds, const int32_t* layer, int max_seg,
+                  int disc, double* Tb_out, double* intW_out, double* tau_out, double* W_out,
+                  double* TbL_out);
+
+/* Fused forward model from host buffers: absorption, ray paths and Tb for
+ * nb rays with device-resident intermediates.  Optional weights[nb] give
+ * Tb_avg[nf] = sum_k weights[k] Tb[k][:].  disc = 1 evaluates every ray as
+ * the reference's b = 'disc' (nadir, E2 weighting).
+ * Outputs (all nullable): Tb_out[nb][nf], Tb_avg[nf], layers_out[nf][nL]. */
+int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const double* X,
+               const double* R, const double* N, int nf, const double* freqs, const double* scale,
+               double Req, double Rpol, double orient0, double orient1, int gtype, int limb,
+               int nb, const double* b, const double* weights, int disc, double* Tb_out,
+               double* Tb_avg, double* layers_out);
+
+/* Same as rb_forward but every array argument is a device pointer, the
+ * work is enqueued on `stream` (a cudaStream_t, 0 = legacy default) and the
+ * call returns without synchronising.  Frequencies are planned from the
+ * HOST array freqs_host (nf values) and cached on the handle. */
+int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
+                      const double* X, const double* R, const double* N, int nf,
+                      const double* freqs_host, const double* scale, double Req, double Rpol,
+                      double orient0, double orient1, int gtype, int limb, int nb,
+                      const double* b, const double* weights, int disc, double* Tb_out,
+                      double* Tb_avg);
+
+/* Number of this library's kernel launches made by the last rb_forward /
+ * rb_forward_device call (for launch accounting). */
+int rb_last_launch_count(rb_handle* h);
+
+/* E2(x) evaluated by the device routine used for b = 'disc' (test hook). */
+int rb_debug_e2(rb_handle* h, int n, const double* x, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RADIOBEAR_GB300_H */

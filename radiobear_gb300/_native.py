@@ -1,0 +1,260 @@
+"""ctypes binding of the C ABI in ``include/radiobear_gb300.h``.
+
+The shared library is built in-tree by :mod:`radiobear_gb300.build`.  There
+is no CPU fallback: if the library cannot be loaded, or no CUDA device is
+present, every compute call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+RB_OK = 0
+FAM = dict(NH3_INV=0, NH3_ROT=1, NH3_V2=2, NH3_SJS=3, H2O=4, H2S=5, PH3=6)
+NH3_MODE = dict(off=0, nh3_hs=1, nh3_sjs=2, nh3_hs_sjs=3)
+GASES = ('h2', 'h2o', 'h2s', 'nh3', 'ph3')        # RB_GAS_* order
+X_ROWS = ('H2', 'HE', 'CH4', 'NH3', 'H2O', 'H2S', 'PH3')   # RB_X_* order
+GTYPE = dict(ellipse=0, sphere=1, circle=1)
+LIMB = dict(shape=0, sec=1)
+
+# column order per family (the reference catalogue keys)
+FAMILY_COLUMNS = {
+    'NH3_INV': ('fo', 'Io', 'Eo', 'gammaNH3o'),
+    'NH3_ROT': ('fo_rot', 'Io_rot', 'Eo_rot', 'gNH3_rot', 'gH2_rot', 'gHe_rot'),
+    'NH3_V2': ('fo_v2', 'Io_v2', 'Eo_v2'),
+    'NH3_SJS': ('f0', 'I0', 'E', 'G0'),
+    'H2O': ('f_o', 'I_o', 'E_o', 'w_s', 'x_s', 'w_h2', 'w_he', 'x_h2', 'x_he', 'SR'),
+    'H2S': ('f0', 'I0', 'E', 'GH2S'),
+    'PH3': ('f0', 'I0', 'E', 'WgtI0', 'WgtFGB', 'WgtSB'),
+}
+
+EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set_lines',
+           'rb_set_formalisms', 'rb_alpha', 'rb_raypath', 'rb_brightness', 'rb_forward',
+           'rb_forward_device', 'rb_last_launch_count', 'rb_debug_e2')
+
+_lib = None
+_lock = threading.Lock()
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+
+class RBError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+
+def load_library(path=None):
+    """Load (once) and return the ctypes library with typed prototypes."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RBError('radiobear_gb300 CUDA library not built ({}); run '
+                          '`python -m radiobear_gb300.build`'.format(p))
+        lib = ctypes.CDLL(p)
+        c_int, c_double = ctypes.c_int, ctypes.c_double
+        lib.rb_abi_version.restype = c_int
+        lib.rb_last_error.restype = ctypes.c_char_p
+        lib.rb_create.argtypes = [ctypes.POINTER(_vp), c_int]
+        lib.rb_destroy.argtypes = [_vp]
+        lib.rb_set_lines.argtypes = [_vp, c_int, c_int, c_int, _d]
+        lib.rb_set_formalisms.argtypes = [_vp, c_int, c_int, c_int, c_int, c_int, c_int]
+        lib.rb_alpha.argtypes = [_vp, c_int, _d, _d, _d, c_int, _d, _d, c_int, _d, _d]
+        lib.rb_raypath.argtypes = [_vp, c_int, _d, _d, c_double, c_double, c_double, c_double,
+                                   c_int, c_int, c_int, _d, c_int, _i, _d, _i, _d, _d, _i]
+        lib.rb_brightness.argtypes = [_vp, c_int, _d, c_int, _d, c_int, _i, _d, _i, c_int, c_int,
+                                      _d, _d, _d, _d, _d]
+        lib.rb_forward.argtypes = [_vp, c_int, _d, _d, _d, _d, _d, c_int, _d, _d, c_double,
+                                   c_double, c_double, c_double, c_int, c_int, c_int, _d, _d,
+                                   c_int, _d, _d, _d]
+        lib.rb_forward_device.argtypes = [_vp, _vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _d, _vp,
+                                          c_double, c_double, c_double, c_double, c_int, c_int,
+                                          c_int, _vp, _vp, c_int, _vp, _vp]
+        lib.rb_last_launch_count.argtypes = [_vp]
+        lib.rb_debug_e2.argtypes = [_vp, c_int, _d, _d]
+        for name in EXPORTS:
+            getattr(lib, name).restype = getattr(lib, name).restype or c_int
+        lib.rb_last_error.restype = ctypes.c_char_p
+        _lib = lib
+        return lib
+
+
+def _ptr(a, ctype=ctypes.c_double):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _check(lib, rc, what):
+    if rc != RB_OK:
+        msg = lib.rb_last_error().decode(errors='replace')
+        if rc == 1:
+            raise ValueError('{}: {}'.format(what, msg))
+        raise RBError('{} failed (status {}): {}'.format(what, rc, msg))
+
+
+class Engine:
+    """One device handle: catalogues, formalism switches and workspaces."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = _vp()
+        _check(self.lib, self.lib.rb_create(ctypes.byref(h), int(device)), 'rb_create')
+        self._h = h
+        self.device = device
+        self.families = {}
+
+    def close(self):
+        if getattr(self, '_h', None):
+            self.lib.rb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ catalogues
+    def set_lines(self, family, table):
+        """Upload a family from a dict with the reference's catalogue keys."""
+        cols = FAMILY_COLUMNS[family]
+        if table is None:
+            n = 0
+            arr = np.zeros(len(cols))
+        else:
+            n = len(np.asarray(table[cols[0]]))
+            arr = np.concatenate([_f64(table[c]).reshape(-1) for c in cols]) if n else np.zeros(len(cols))
+        _check(self.lib, self.lib.rb_set_lines(self._h, FAM[family], n, len(cols), _ptr(arr)),
+               'rb_set_lines')
+        self.families[family] = n
+
+    def set_formalisms(self, nh3='nh3_hs_sjs', h2=True, h2o=True, h2s=True, ph3=True, h2state='e'):
+        _check(self.lib, self.lib.rb_set_formalisms(self._h, NH3_MODE[nh3 or 'off'], int(h2), int(h2o),
+                                                    int(h2s), int(ph3), ord(h2state)),
+               'rb_set_formalisms')
+
+    # ------------------------------------------------------------ compute
+    def alpha(self, P, T, X, freqs, scale=None, units_db=False, per_gas=False, layers=True):
+        """Absorption: returns (layers [nf, nL] or None, gas [nL, nf, 5] or None)."""
+        P, T, X, f = _f64(P), _f64(T), _f64(X), _f64(freqs)
+        nL, nf = P.size, f.size
+        sc = None if scale is None else _f64(scale)
+        lay = np.empty((nf, nL)) if layers else None
+        gas = np.empty((nL, nf, len(GASES))) if per_gas else None
+        rc = self.lib.rb_alpha(self._h, nL, _ptr(P), _ptr(T), _ptr(X), nf, _ptr(f), _ptr(sc),
+                               int(units_db), _ptr(lay), _ptr(gas))
+        _check(self.lib, rc, 'rb_alpha')
+        return lay, gas
+
+    def raypath(self, R, N, b, Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse', limb='shape',
+                max_seg=None, extras=False):
+        R, N = _f64(R), _f64(N)
+        b = _f64(np.atleast_2d(b))
+        nL, nb = R.size, b.shape[0]
+        ms = max_seg or 2 * nL + 4
+        nseg = np.zeros(nb, dtype=np.int32)
+        ds = np.zeros((nb, ms))
+        lay = np.zeros((nb, ms), dtype=np.int32)
+        r4 = np.zeros((nb, ms)) if extras else None
+        ll = np.zeros((nb, ms + 1, 2)) if extras else None
+        end = np.zeros(nb, dtype=np.int32)
+        rc = self.lib.rb_raypath(self._h, nL, _ptr(R), _ptr(N), float(Req), float(Rpol),
+                                 float(orientation[0]), float(orientation[1]), GTYPE[gtype],
+                                 LIMB[limb], nb, _ptr(b), ms, _ptr(nseg, ctypes.c_int32), _ptr(ds),
+                                 _ptr(lay, ctypes.c_int32), _ptr(r4), _ptr(ll),
+                                 _ptr(end, ctypes.c_int32))
+        _check(self.lib, rc, 'rb_raypath')
+        out = dict(nseg=nseg, ds=ds, layer=lay, end=end, max_seg=ms)
+        if extras:
+            out.update(r4ds=r4, latlng=ll)
+        return out
+
+    def brightness(self, T, layers, nseg, ds, layer, disc=False, profiles=False):
+        T, layers = _f64(T), _f64(layers)
+        nf, nL = layers.shape
+        nseg = np.ascontiguousarray(nseg, dtype=np.int32)
+        ds = _f64(ds)
+        layer = np.ascontiguousarray(layer, dtype=np.int32)
+        nb, ms = ds.shape
+        Tb = np.empty((nb, nf))
+        iw = np.empty((nb, nf))
+        tau = W = tbl = None
+        if profiles:
+            tau, W, tbl = (np.empty((nb, nf, ms)) for _ in range(3))
+        rc = self.lib.rb_brightness(self._h, nL, _ptr(T), nf, _ptr(layers), nb,
+                                    _ptr(nseg, ctypes.c_int32), _ptr(ds),
+                                    _ptr(layer, ctypes.c_int32), ms, int(disc), _ptr(Tb), _ptr(iw),
+                                    _ptr(tau), _ptr(W), _ptr(tbl))
+        _check(self.lib, rc, 'rb_brightness')
+        return dict(Tb=Tb, intW=iw, tau=tau, W=W, TbL=tbl)
+
+    def forward(self, P, T, X, R, N, freqs, b, Req, Rpol, orientation=(0.0, 0.0),
+                gtype='ellipse', limb='shape', weights=None, disc=False, scale=None,
+                want_layers=False, want_rays=True):
+        P, T, X, R, N, f = (_f64(v) for v in (P, T, X, R, N, freqs))
+        b = _f64(np.atleast_2d(b))
+        nL, nf, nb = P.size, f.size, b.shape[0]
+        w = None if weights is None else _f64(weights)
+        sc = None if scale is None else _f64(scale)
+        Tb = np.empty((nb, nf)) if want_rays else None
+        avg = np.empty(nf) if w is not None else None
+        lay = np.empty((nf, nL)) if want_layers else None
+        rc = self.lib.rb_forward(self._h, nL, _ptr(P), _ptr(T), _ptr(X), _ptr(R), _ptr(N), nf,
+                                 _ptr(f), _ptr(sc), float(Req), float(Rpol), float(orientation[0]),
+                                 float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _ptr(b),
+                                 _ptr(w), int(disc), _ptr(Tb), _ptr(avg), _ptr(lay))
+        _check(self.lib, rc, 'rb_forward')
+        return dict(Tb=Tb, Tb_avg=avg, layers=lay)
+
+    def forward_device(self, stream, nL, nb, P, T, X, R, N, freqs_host, b, Req, Rpol, Tb_out,
+                       weights=None, Tb_avg=None, orientation=(0.0, 0.0), gtype='ellipse',
+                       limb='shape', scale=None):
+        """Device-pointer variant of :meth:`forward`: P, T, X, R, N, b,
+        weights, scale, Tb_out and Tb_avg are integer device addresses (for
+        example ``tensor.data_ptr()``), ``stream`` an integer cudaStream_t.
+        The work is enqueued on ``stream`` and the call returns at once."""
+        f = _f64(freqs_host)
+
+        def vp(x):
+            return None if x is None else _vp(int(x))
+
+        rc = self.lib.rb_forward_device(
+            self._h, _vp(int(stream)), int(nL), vp(P), vp(T), vp(X), vp(R), vp(N), f.size, _ptr(f),
+            vp(scale), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]),
+            GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), 0, vp(Tb_out), vp(Tb_avg))
+        _check(self.lib, rc, 'rb_forward_device')
+
+    def last_launch_count(self):
+        return int(self.lib.rb_last_launch_count(self._h))
+
+    def debug_e2(self, x):
+        x = _f64(x)
+        out = np.empty_like(x)
+        _check(self.lib, self.lib.rb_debug_e2(self._h, x.size, _ptr(x), _ptr(out)), 'rb_debug_e2')
+        return out
+
+
+def x_matrix(gas, C):
+    """[RB_NX, nL] abundance rows from a reference gas table and index dict
+    (missing constituents are zero)."""
+    nL = gas.shape[1]
+    X = np.zeros((len(X_ROWS), nL))
+    for i, k in enumerate(X_ROWS):
+        if k in C:
+            X[i] = gas[C[k]]
+    return X

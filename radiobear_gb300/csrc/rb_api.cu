@@ -1,0 +1,763 @@
+// C ABI of the GB300 radioBEAR forward model (include/radiobear_gb300.h):
+// handle, device-memory management, catalogue preprocessing, frequency
+// plans and the launch sequences.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/radiobear_gb300.h"
+#include "rb_args.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define RB_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(e_ == cudaErrorMemoryAllocation ? RB_ENOMEM : RB_ECUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                  \
+  } while (0)
+
+struct DBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, (size_t)256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+int family_ncols(int fam) {
+  switch (fam) {
+    case rb::FAM_NH3_INV: return 4;
+    case rb::FAM_NH3_ROT: return 6;
+    case rb::FAM_NH3_V2: return 3;
+    case rb::FAM_NH3_SJS: return 4;
+    case rb::FAM_H2O: return 10;
+    case rb::FAM_H2S: return 4;
+    case rb::FAM_PH3: return 6;
+  }
+  return -1;
+}
+
+struct FamilyStore {
+  int n = 0;
+  std::vector<double> centre;   // sorted, host copy (near-range search)
+  DBuf c2h, c2l, ch, cl, lnI, E, w1, w2, w3, x1, x2, x3, lnI32, E32;
+  rb::LineTable table() const {
+    rb::LineTable t{};
+    t.n = n;
+    t.c2h = c2h.as<float>();
+    t.c2l = c2l.as<float>();
+    t.ch = ch.as<float>();
+    t.cl = cl.as<float>();
+    t.lnI = lnI.as<double>();
+    t.E = E.as<double>();
+    t.w1 = w1.as<float>();
+    t.w2 = w2.as<float>();
+    t.w3 = w3.as<float>();
+    t.x1 = x1.as<float>();
+    t.x2 = x2.as<float>();
+    t.x3 = x3.as<float>();
+    t.lnI32 = lnI32.as<float>();
+    t.E32 = E32.as<float>();
+    return t;
+  }
+  void release() {
+    for (DBuf* b : {&c2h, &c2l, &ch, &cl, &lnI, &E, &w1, &w2, &w3, &x1, &x2, &x3, &lnI32, &E32})
+      b->release();
+  }
+};
+
+}  // namespace
+
+struct rb_handle {
+  int device = 0;
+  cudaStream_t st = nullptr, side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  FamilyStore fam[rb::NFAM];
+  rb::AlphaConfig cfg{rb::NH3_HS_SJS, 1, 1, 1, 1, 'e', 0};
+  // frequency plan
+  std::vector<double> plan_f;
+  int plan_block = 0, plan_ntile = 0;
+  DBuf d_f, d_fhs, d_near;
+  // workspaces
+  DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
+      d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x;
+  int launches = 0;
+};
+
+// launchers implemented in the kernel translation units
+namespace rb {
+cudaError_t launch_alpha(const PrepArgs& pa, const AlphaArgs& aa, int block, int ntile,
+                         cudaStream_t st);
+cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
+cudaError_t launch_tb(const TbArgs& a, cudaStream_t st);
+cudaError_t launch_disc_avg(int nb, int nf, const double* Tb, const double* w, double* out,
+                            cudaStream_t st);
+cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st);
+}  // namespace rb
+
+namespace {
+
+bool finite_all(const double* v, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+template <class T>
+cudaError_t upload(DBuf& b, const T* src, size_t count, cudaStream_t st) {
+  cudaError_t e = b.ensure(count * sizeof(T));
+  if (e != cudaSuccess || count == 0) return e;
+  return cudaMemcpyAsync(b.p, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+// Frequency plan: the nh3_hs output order (nh3_hs.py:70-88: <=30 GHz block
+// then >30 GHz block), tile shape and, per warp and family, the index range
+// of lines whose centre is within [0.75 fmin, 1.3 fmax] of the warp's
+// frequencies (those take the double-float F - K path).
+int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st) {
+  if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
+  for (int i = 0; i < nf; ++i)
+    if (!std::isfinite(freqs[i]) || freqs[i] < 0.0)
+      return fail(RB_EINVAL, "frequency %d is not a finite non-negative number", i);
+  if ((int)h->plan_f.size() == nf && std::equal(freqs, freqs + nf, h->plan_f.begin()))
+    return RB_OK;
+  std::vector<double> fhs;
+  fhs.reserve(nf);
+  for (int i = 0; i < nf; ++i)
+    if (freqs[i] <= 30.0) fhs.push_back(freqs[i]);
+  for (int i = 0; i < nf; ++i)
+    if (freqs[i] > 30.0) fhs.push_back(freqs[i]);
+  int block = std::min(256, ((nf + 31) / 32) * 32);
+  int ntile = (nf + block - 1) / block;
+  int nw = block / 32;
+  std::vector<int2> nearv((size_t)ntile * nw * rb::NFAM, make_int2(0, 0));
+  for (int t = 0; t < ntile; ++t)
+    for (int w = 0; w < nw; ++w) {
+      int j0 = t * block + w * 32, j1 = std::min(nf, j0 + 32);
+      if (j0 >= nf) continue;
+      for (int fam = 0; fam < rb::NFAM; ++fam) {
+        const bool hs = fam == rb::FAM_NH3_INV || fam == rb::FAM_NH3_ROT || fam == rb::FAM_NH3_V2;
+        const double* fv = hs ? fhs.data() : freqs;
+        double lo = fv[j0], hi = fv[j0];
+        for (int j = j0; j < j1; ++j) {
+          lo = std::min(lo, fv[j]);
+          hi = std::max(hi, fv[j]);
+        }
+        const std::vector<double>& c = h->fam[fam].centre;
+        int a = (int)(std::lower_bound(c.begin(), c.end(), 0.75 * lo) - c.begin());
+        int b = (int)(std::upper_bound(c.begin(), c.end(), 1.3 * hi) - c.begin());
+        nearv[((size_t)t * nw + w) * rb::NFAM + fam] = make_int2(a, std::max(a, b));
+      }
+    }
+  RB_CUDA(upload(h->d_f, freqs, nf, st));
+  RB_CUDA(upload(h->d_fhs, fhs.data(), nf, st));
+  RB_CUDA(upload(h->d_near, nearv.data(), nearv.size(), st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  h->plan_f.assign(freqs, freqs + nf);
+  h->plan_block = block;
+  h->plan_ntile = ntile;
+  return RB_OK;
+}
+
+int validate_atm(int nL, const double* P, const double* T, const double* X) {
+  if (nL < 1) return fail(RB_EINVAL, "nL must be >= 1");
+  for (int i = 0; i < nL; ++i) {
+    if (!(P[i] > 0.0) || !std::isfinite(P[i])) return fail(RB_EINVAL, "P[%d] must be > 0", i);
+    if (!(T[i] > 0.0) || !std::isfinite(T[i])) return fail(RB_EINVAL, "T[%d] must be > 0", i);
+  }
+  if (!finite_all(X, (size_t)rb::NX * nL)) return fail(RB_EINVAL, "X has non-finite entries");
+  return RB_OK;
+}
+
+void fill_prep(rb_handle* h, rb::PrepArgs& pa, int nL, const double* dP, const double* dT,
+               const double* dX) {
+  pa.nL = nL;
+  pa.P = dP;
+  pa.T = dT;
+  pa.X = dX;
+  pa.cfg = h->cfg;
+  for (int f = 0; f < rb::NFAM; ++f) pa.tab[f] = h->fam[f].table();
+  pa.out = h->d_lp.as<rb::LayerParams>();
+}
+
+int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
+                  const double* dX, const double* dscale, int units_db, double* d_layers64,
+                  double* d_gas64) {
+  RB_CUDA(h->d_lp.ensure(sizeof(rb::LayerParams) * (size_t)nL));
+  const int nf = (int)h->plan_f.size();
+  RB_CUDA(h->d_a32.ensure(sizeof(float) * (size_t)nL * nf));
+  rb::PrepArgs pa{};
+  fill_prep(h, pa, nL, dP, dT, dX);
+  pa.cfg.units_db = units_db;
+  rb::AlphaArgs aa{};
+  aa.nL = nL;
+  aa.nf = nf;
+  aa.nwarps_tile = h->plan_block / 32;
+  aa.freqs = h->d_f.as<double>();
+  aa.freqs_hs = h->d_fhs.as<double>();
+  aa.lp = h->d_lp.as<rb::LayerParams>();
+  for (int f = 0; f < rb::NFAM; ++f) aa.tab[f] = h->fam[f].table();
+  aa.near = h->d_near.as<int2>();
+  aa.cfg = pa.cfg;
+  aa.scale = dscale;
+  aa.alpha32 = h->d_a32.as<float>();
+  aa.layers64 = d_layers64;
+  aa.gas64 = d_gas64;
+  RB_CUDA(rb::launch_alpha(pa, aa, h->plan_block, h->plan_ntile, st));
+  h->launches += 2;
+  return RB_OK;
+}
+
+void aspect_matrix(double Req, double Rpol, double o0, double o1, double* M) {
+  // computeAspect (raypath.py:39-44) and rotate2planet = rotX(rotate) rotZ(tip)
+  const double f = 1.0 - Rpol / Req;
+  const double tip = -o0 * M_PI / 180.0;
+  const double rotate = -std::atan(std::tan(o1 * M_PI / 180.0) * (1.0 - f) * (1.0 - f));
+  const double cz = std::cos(tip), sz = std::sin(tip), cx = std::cos(rotate), sx = std::sin(rotate);
+  M[0] = cz;
+  M[1] = -sz;
+  M[2] = 0.0;
+  M[3] = cx * sz;
+  M[4] = cx * cz;
+  M[5] = -sx;
+  M[6] = sx * sz;
+  M[7] = sx * cz;
+  M[8] = cx;
+}
+
+int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, const double* dN,
+                    double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
+                    const double* db, int max_seg, int* dnseg, double* dds, int* dlayer,
+                    double* dr4, double* dll, int* dend) {
+  rb::RayArgs ra{};
+  ra.nL = nL;
+  ra.R = dR;
+  ra.N = dN;
+  ra.k = gtype == RB_GTYPE_ELLIPSE ? Rpol / Req : 1.0;
+  aspect_matrix(Req, Rpol, o0, o1, ra.rot);
+  ra.limb_sec = limb == RB_LIMB_SEC;
+  ra.nb = nb;
+  ra.b = db;
+  ra.max_seg = max_seg;
+  ra.nseg = dnseg;
+  ra.ds = dds;
+  ra.layer = dlayer;
+  ra.r4ds = dr4;
+  ra.latlng = dll;
+  ra.end_code = dend;
+  RB_CUDA(rb::launch_raypath(ra, st));
+  h->launches += 1;
+  return RB_OK;
+}
+
+int validate_geom(int nL, const double* R, const double* N, double Req, double Rpol, int gtype,
+                  int limb, int nb, const double* b) {
+  if (nL < 2) return fail(RB_EINVAL, "ray paths need nL >= 2");
+  if (!(Req > 0.0) || !(Rpol > 0.0)) return fail(RB_EINVAL, "Req and Rpol must be > 0");
+  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE)
+    return fail(RB_EINVAL, "gtype must be RB_GTYPE_ELLIPSE or RB_GTYPE_SPHERE");
+  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC)
+    return fail(RB_EINVAL, "limb must be RB_LIMB_SHAPE or RB_LIMB_SEC");
+  if (nb < 0) return fail(RB_EINVAL, "nb must be >= 0");
+  if (!finite_all(R, nL) || !finite_all(N, nL)) return fail(RB_EINVAL, "R/N not finite");
+  if (!(R[0] > 0.0)) return fail(RB_EINVAL, "R[0] must be > 0");
+  if (nb && !finite_all(b, 2 * (size_t)nb)) return fail(RB_EINVAL, "b not finite");
+  return RB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rb_abi_version(void) { return RB_ABI_VERSION; }
+
+const char* rb_last_error(void) { return g_err.c_str(); }
+
+int rb_create(rb_handle** out, int device) {
+  if (!out) return fail(RB_EINVAL, "out is null");
+  *out = nullptr;
+  int ndev = 0;
+  RB_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(RB_EINVAL, "device %d not present (%d)", device, ndev);
+  RB_CUDA(cudaSetDevice(device));
+  rb_handle* h = new rb_handle();
+  h->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    rb_destroy(h);
+    return fail(RB_ECUDA, "stream/event creation: %s", cudaGetErrorString(e));
+  }
+  *out = h;
+  return RB_OK;
+}
+
+int rb_destroy(rb_handle* h) {
+  if (!h) return RB_OK;
+  cudaSetDevice(h->device);
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->side) cudaStreamSynchronize(h->side);
+  for (auto& f : h->fam) f.release();
+  for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_near, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
+                  &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
+                  &h->d_ds, &h->d_layer, &h->d_r4, &h->d_ll, &h->d_end, &h->d_Tb, &h->d_avg,
+                  &h->d_iw, &h->d_tau, &h->d_W, &h->d_tbl, &h->d_x})
+    b->release();
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->st) cudaStreamDestroy(h->st);
+  if (h->side) cudaStreamDestroy(h->side);
+  delete h;
+  return RB_OK;
+}
+
+int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (family < 0 || family >= rb::NFAM) return fail(RB_EINVAL, "unknown family %d", family);
+  if (ncols != family_ncols(family))
+    return fail(RB_EINVAL, "family %d takes %d columns, got %d", family, family_ncols(family), ncols);
+  if (n < 0 || (n > 0 && !cols)) return fail(RB_EINVAL, "bad line count / pointer");
+  RB_CUDA(cudaSetDevice(h->device));
+  FamilyStore& F = h->fam[family];
+  h->plan_f.clear();
+  if (!finite_all(cols, (size_t)n * ncols)) return fail(RB_EINVAL, "line columns not finite");
+  auto col = [&](int c, int i) { return cols[(size_t)c * n + i]; };
+  std::vector<double> centre(n);
+  for (int i = 0; i < n; ++i) {
+    const double fo = col(0, i);
+    if (!(fo > 0.0) || fo > 2.0e4)
+      return fail(RB_EINVAL, "line %d: centre %g GHz outside (0, 2e4]", i, fo);
+    const double I = col(1, i);
+    if (I < 0.0) return fail(RB_EINVAL, "line %d: negative intensity", i);
+    centre[i] = family == rb::FAM_H2O ? fo + col(9, i) : fo;
+    if (family == rb::FAM_H2O && !(centre[i] > 0.0))
+      return fail(RB_EINVAL, "line %d: f_o + SR must be > 0", i);
+  }
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return centre[a] < centre[b]; });
+  std::vector<float> c2h(n), c2l(n), ch(n), cl(n), w1(n), w2(n), w3(n), x1(n), x2(n), x3(n),
+      lnI32(n), E32(n);
+  std::vector<double> lnI(n), E(n), cs(n);
+  for (int k = 0; k < n; ++k) {
+    const int i = order[k];
+    const double fo = col(0, i);
+    const double I = col(1, i);
+    cs[k] = centre[i];
+    rb::split_double(fo * fo, c2h[k], c2l[k]);
+    rb::split_double(centre[i], ch[k], cl[k]);
+    E[k] = col(2, i);
+    double lI = I > 0.0 ? std::log(I) : -INFINITY;
+    w1[k] = w2[k] = w3[k] = 0.f;
+    x1[k] = x2[k] = x3[k] = 0.f;
+    switch (family) {
+      case rb::FAM_NH3_INV:  // fo Io Eo gammaNH3o
+        lI -= 2.0 * std::log(fo);
+        w1[k] = (float)col(3, i);
+        break;
+      case rb::FAM_NH3_ROT:  // fo Io Eo gNH3 gH2 gHe
+        w1[k] = (float)col(4, i);
+        w2[k] = (float)col(5, i);
+        w3[k] = (float)col(3, i);
+        break;
+      case rb::FAM_NH3_V2:   // fixed widths (nh3_hs.py:272-274)
+        w1[k] = 1.4f;
+        w2[k] = 0.68f;
+        w3[k] = 9.5f;
+        break;
+      case rb::FAM_NH3_SJS:  // f0 I0 E G0
+      case rb::FAM_H2S:      // f0 I0 E GH2S
+        lI -= 2.0 * std::log(fo);
+        w1[k] = (float)col(3, i);
+        break;
+      case rb::FAM_PH3: {    // f0 I0 E WgtI0 WgtFGB WgtSB
+        const double wI = col(3, i);
+        if (wI < 0.0) return fail(RB_EINVAL, "line %d: negative WgtI0", i);
+        lI = (I > 0.0 && wI > 0.0) ? std::log(I * wI) - 2.0 * std::log(fo) : -INFINITY;
+        w1[k] = (float)col(4, i);
+        w2[k] = (float)col(5, i);
+        break;
+      }
+      case rb::FAM_H2O:      // f_o I_o E_o w_s x_s w_h2 w_he x_h2 x_he SR
+        lI -= 2.0 * std::log(fo) + std::log(M_PI);
+        w1[k] = (float)col(3, i);
+        x1[k] = (float)col(4, i);
+        w2[k] = (float)col(5, i);
+        x2[k] = (float)col(7, i);
+        w3[k] = (float)col(6, i);
+        x3[k] = (float)col(8, i);
+        break;
+    }
+    lnI[k] = lI;
+    lnI32[k] = (float)lI;
+    E32[k] = (float)E[k];
+  }
+  F.n = 0;
+  F.centre = cs;
+  cudaStream_t st = h->st;
+  RB_CUDA(upload(F.c2h, c2h.data(), n, st));
+  RB_CUDA(upload(F.c2l, c2l.data(), n, st));
+  RB_CUDA(upload(F.ch, ch.data(), n, st));
+  RB_CUDA(upload(F.cl, cl.data(), n, st));
+  RB_CUDA(upload(F.lnI, lnI.data(), n, st));
+  RB_CUDA(upload(F.E, E.data(), n, st));
+  RB_CUDA(upload(F.w1, w1.data(), n, st));
+  RB_CUDA(upload(F.w2, w2.data(), n, st));
+  RB_CUDA(upload(F.w3, w3.data(), n, st));
+  RB_CUDA(upload(F.x1, x1.data(), n, st));
+  RB_CUDA(upload(F.x2, x2.data(), n, st));
+  RB_CUDA(upload(F.x3, x3.data(), n, st));
+  RB_CUDA(upload(F.lnI32, lnI32.data(), n, st));
+  RB_CUDA(upload(F.E32, E32.data(), n, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  F.n = n;
+  return RB_OK;
+}
+
+int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2s, int use_ph3,
+                      int h2state) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (nh3 < RB_NH3_OFF || nh3 > RB_NH3_HS_SJS) return fail(RB_EINVAL, "bad nh3 formalism %d", nh3);
+  if (h2state != 'e' && h2state != 'n') return fail(RB_EINVAL, "h2state must be 'e' or 'n'");
+  h->cfg.nh3_mode = nh3;
+  h->cfg.use_h2 = use_h2 != 0;
+  h->cfg.use_h2o = use_h2o != 0;
+  h->cfg.use_h2s = use_h2s != 0;
+  h->cfg.use_ph3 = use_ph3 != 0;
+  h->cfg.h2state = h2state;
+  return RB_OK;
+}
+
+int rb_alpha(rb_handle* h, int nL, const double* P, const double* T, const double* X, int nf,
+             const double* freqs, const double* scale, int units_db, double* layers_out,
+             double* gas_out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !freqs) return fail(RB_EINVAL, "null input array");
+  int rc = validate_atm(nL, P, T, X);
+  if (rc) return rc;
+  if (scale && !finite_all(scale, (size_t)nL * rb::NGAS)) return fail(RB_EINVAL, "scale not finite");
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  RB_CUDA(upload(h->d_P, P, nL, st));
+  RB_CUDA(upload(h->d_T, T, nL, st));
+  RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
+  const double* dscale = nullptr;
+  if (scale) {
+    RB_CUDA(upload(h->d_scale, scale, (size_t)nL * rb::NGAS, st));
+    dscale = h->d_scale.as<double>();
+  }
+  double* dl = nullptr;
+  double* dg = nullptr;
+  if (layers_out) {
+    RB_CUDA(h->d_l64.ensure(sizeof(double) * (size_t)nf * nL));
+    dl = h->d_l64.as<double>();
+  }
+  if (gas_out) {
+    RB_CUDA(h->d_g64.ensure(sizeof(double) * (size_t)nf * nL * rb::NGAS));
+    dg = h->d_g64.as<double>();
+  }
+  h->launches = 0;
+  if ((rc = enqueue_alpha(h, st, nL, h->d_P.as<double>(), h->d_T.as<double>(), h->d_X.as<double>(),
+                          dscale, units_db, dl, dg)))
+    return rc;
+  if (dl) RB_CUDA(cudaMemcpyAsync(layers_out, dl, sizeof(double) * (size_t)nf * nL, cudaMemcpyDeviceToHost, st));
+  if (dg)
+    RB_CUDA(cudaMemcpyAsync(gas_out, dg, sizeof(double) * (size_t)nf * nL * rb::NGAS,
+                            cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
+
+int rb_raypath(rb_handle* h, int nL, const double* R, const double* N, double Req, double Rpol,
+               double orient0, double orient1, int gtype, int limb, int nb, const double* b,
+               int max_seg, int32_t* nseg, double* ds, int32_t* layer, double* r4ds,
+               double* latlng, int32_t* end_code) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!R || !N || (nb > 0 && (!b || !nseg || !ds || !layer))) return fail(RB_EINVAL, "null array");
+  int rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
+  if (rc) return rc;
+  if (max_seg < 1) return fail(RB_EINVAL, "max_seg must be >= 1");
+  if (nb == 0) return RB_OK;
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  RB_CUDA(upload(h->d_R, R, nL, st));
+  RB_CUDA(upload(h->d_N, N, nL, st));
+  RB_CUDA(upload(h->d_b, b, 2 * (size_t)nb, st));
+  const size_t ns = (size_t)nb * max_seg;
+  RB_CUDA(h->d_nseg.ensure(sizeof(int) * nb));
+  RB_CUDA(h->d_end.ensure(sizeof(int) * nb));
+  RB_CUDA(h->d_ds.ensure(sizeof(double) * ns));
+  RB_CUDA(h->d_layer.ensure(sizeof(int) * ns));
+  if (r4ds) RB_CUDA(h->d_r4.ensure(sizeof(double) * ns));
+  if (latlng) RB_CUDA(h->d_ll.ensure(sizeof(double) * (size_t)nb * (max_seg + 1) * 2));
+  h->launches = 0;
+  if ((rc = enqueue_raypath(h, st, nL, h->d_R.as<double>(), h->d_N.as<double>(), Req, Rpol,
+                            orient0, orient1, gtype, limb, nb, h->d_b.as<double>(), max_seg,
+                            h->d_nseg.as<int>(), h->d_ds.as<double>(), h->d_layer.as<int>(),
+                            r4ds ? h->d_r4.as<double>() : nullptr,
+                            latlng ? h->d_ll.as<double>() : nullptr, h->d_end.as<int>())))
+    return rc;
+  RB_CUDA(cudaMemcpyAsync(nseg, h->d_nseg.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaMemcpyAsync(ds, h->d_ds.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaMemcpyAsync(layer, h->d_layer.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+  if (r4ds) RB_CUDA(cudaMemcpyAsync(r4ds, h->d_r4.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+  if (latlng)
+    RB_CUDA(cudaMemcpyAsync(latlng, h->d_ll.p, sizeof(double) * (size_t)nb * (max_seg + 1) * 2,
+                            cudaMemcpyDeviceToHost, st));
+  if (end_code) RB_CUDA(cudaMemcpyAsync(end_code, h->d_end.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
+
+int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* layers, int nb,
+                  const int32_t* nseg, const double* ds, const int32_t* layer, int max_seg,
+                  int disc, double* Tb_out, double* intW_out, double* tau_out, double* W_out,
+                  double* TbL_out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (nL < 1 || nf < 1 || nb < 0 || max_seg < 1) return fail(RB_EINVAL, "bad sizes");
+  if (!T || !layers || (nb > 0 && (!nseg || !ds || !layer || !Tb_out))) return fail(RB_EINVAL, "null array");
+  const bool prof = tau_out || W_out || TbL_out;
+  if (prof && !(tau_out && W_out && TbL_out)) return fail(RB_EINVAL, "profiles need tau, W and TbL");
+  if (nb == 0) return RB_OK;
+  for (int r = 0; r < nb; ++r) {
+    if (nseg[r] < 0 || nseg[r] > max_seg) return fail(RB_EINVAL, "nseg[%d] out of range", r);
+    for (int i = 0; i < nseg[r]; ++i) {
+      const int l = layer[(size_t)r * max_seg + i];
+      if (l < -nL || l >= nL) return fail(RB_EINVAL, "layer index %d out of range", l);
+    }
+  }
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  // absorption as float32 [nL][nf]; layer indices wrapped like Python's
+  std::vector<float> a32((size_t)nL * nf);
+  for (int f = 0; f < nf; ++f)
+    for (int l = 0; l < nL; ++l) a32[(size_t)l * nf + f] = (float)layers[(size_t)f * nL + l];
+  std::vector<int> lay((size_t)nb * max_seg, 0);
+  for (int r = 0; r < nb; ++r)
+    for (int i = 0; i < nseg[r]; ++i) {
+      int l = layer[(size_t)r * max_seg + i];
+      lay[(size_t)r * max_seg + i] = l < 0 ? l + nL : l;
+    }
+  RB_CUDA(upload(h->d_a32, a32.data(), a32.size(), st));
+  RB_CUDA(upload(h->d_T, T, nL, st));
+  RB_CUDA(upload(h->d_nseg, nseg, nb, st));
+  RB_CUDA(upload(h->d_ds, ds, (size_t)nb * max_seg, st));
+  RB_CUDA(upload(h->d_layer, lay.data(), lay.size(), st));
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
+  RB_CUDA(h->d_iw.ensure(sizeof(double) * (size_t)nb * nf));
+  const size_t np = (size_t)nb * nf * max_seg;
+  if (prof) {
+    RB_CUDA(h->d_tau.ensure(sizeof(double) * np));
+    RB_CUDA(h->d_W.ensure(sizeof(double) * np));
+    RB_CUDA(h->d_tbl.ensure(sizeof(double) * np));
+  }
+  rb::TbArgs ta{};
+  ta.nL = nL;
+  ta.nf = nf;
+  ta.nb = nb;
+  ta.max_seg = max_seg;
+  ta.alpha32 = h->d_a32.as<float>();
+  ta.T = h->d_T.as<double>();
+  ta.nseg = h->d_nseg.as<int>();
+  ta.ds = h->d_ds.as<double>();
+  ta.layer = h->d_layer.as<int>();
+  ta.disc = disc != 0;
+  ta.Tb = h->d_Tb.as<double>();
+  ta.intW = h->d_iw.as<double>();
+  ta.tau = prof ? h->d_tau.as<double>() : nullptr;
+  ta.W = prof ? h->d_W.as<double>() : nullptr;
+  ta.TbL = prof ? h->d_tbl.as<double>() : nullptr;
+  h->launches = 1;
+  RB_CUDA(rb::launch_tb(ta, st));
+  RB_CUDA(cudaMemcpyAsync(Tb_out, ta.Tb, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
+  if (intW_out)
+    RB_CUDA(cudaMemcpyAsync(intW_out, ta.intW, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
+  if (prof) {
+    RB_CUDA(cudaMemcpyAsync(tau_out, ta.tau, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+    RB_CUDA(cudaMemcpyAsync(W_out, ta.W, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+    RB_CUDA(cudaMemcpyAsync(TbL_out, ta.TbL, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+  }
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
+
+static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
+                        const double* dX, const double* dR, const double* dN, const double* dscale,
+                        double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
+                        const double* db, const double* dw, int disc, double* dTb, double* davg,
+                        double* dl64) {
+  const int nf = (int)h->plan_f.size();
+  const int max_seg = 2 * nL + 4;
+  const size_t ns = (size_t)nb * max_seg;
+  RB_CUDA(h->d_nseg.ensure(sizeof(int) * std::max(nb, 1)));
+  RB_CUDA(h->d_ds.ensure(sizeof(double) * std::max(ns, (size_t)1)));
+  RB_CUDA(h->d_layer.ensure(sizeof(int) * std::max(ns, (size_t)1)));
+  h->launches = 0;
+  // ray paths on the side stream, concurrent with the absorption kernels
+  RB_CUDA(cudaEventRecord(h->ev_fork, st));
+  RB_CUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+  int rc;
+  if (nb > 0) {
+    if ((rc = enqueue_raypath(h, h->side, nL, dR, dN, Req, Rpol, o0, o1, gtype, limb, nb, db,
+                              max_seg, h->d_nseg.as<int>(), h->d_ds.as<double>(),
+                              h->d_layer.as<int>(), nullptr, nullptr, nullptr)))
+      return rc;
+  }
+  RB_CUDA(cudaEventRecord(h->ev_join, h->side));
+  if ((rc = enqueue_alpha(h, st, nL, dP, dT, dX, dscale, 0, dl64, nullptr))) return rc;
+  RB_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
+  if (nb > 0) {
+    rb::TbArgs ta{};
+    ta.nL = nL;
+    ta.nf = nf;
+    ta.nb = nb;
+    ta.max_seg = max_seg;
+    ta.alpha32 = h->d_a32.as<float>();
+    ta.T = dT;
+    ta.nseg = h->d_nseg.as<int>();
+    ta.ds = h->d_ds.as<double>();
+    ta.layer = h->d_layer.as<int>();
+    ta.disc = disc != 0;
+    ta.Tb = dTb;
+    RB_CUDA(rb::launch_tb(ta, st));
+    h->launches += 1;
+    if (davg && dw) {
+      RB_CUDA(rb::launch_disc_avg(nb, nf, dTb, dw, davg, st));
+      h->launches += 1;
+    }
+  }
+  return RB_OK;
+}
+
+int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const double* X,
+               const double* R, const double* N, int nf, const double* freqs, const double* scale,
+               double Req, double Rpol, double orient0, double orient1, int gtype, int limb,
+               int nb, const double* b, const double* weights, int disc, double* Tb_out,
+               double* Tb_avg, double* layers_out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs || (nb > 0 && !b)) return fail(RB_EINVAL, "null input array");
+  int rc = validate_atm(nL, P, T, X);
+  if (rc) return rc;
+  std::vector<double> bb;
+  if (disc) {  // 'disc' evaluates the nadir ray (brightness.py:32-34)
+    bb.assign(2 * (size_t)nb, 0.0);
+    b = bb.data();
+  }
+  if ((rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b))) return rc;
+  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
+  if (weights && !finite_all(weights, nb)) return fail(RB_EINVAL, "weights not finite");
+  if (scale && !finite_all(scale, (size_t)nL * rb::NGAS)) return fail(RB_EINVAL, "scale not finite");
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  RB_CUDA(upload(h->d_P, P, nL, st));
+  RB_CUDA(upload(h->d_T, T, nL, st));
+  RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
+  RB_CUDA(upload(h->d_R, R, nL, st));
+  RB_CUDA(upload(h->d_N, N, nL, st));
+  if (nb > 0) RB_CUDA(upload(h->d_b, b, 2 * (size_t)nb, st));
+  const double* dscale = nullptr;
+  if (scale) {
+    RB_CUDA(upload(h->d_scale, scale, (size_t)nL * rb::NGAS, st));
+    dscale = h->d_scale.as<double>();
+  }
+  const double* dw = nullptr;
+  if (weights && nb > 0) {
+    RB_CUDA(upload(h->d_w, weights, nb, st));
+    dw = h->d_w.as<double>();
+  }
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * std::max((size_t)nb * nf, (size_t)1)));
+  RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
+  double* dl = nullptr;
+  if (layers_out) {
+    RB_CUDA(h->d_l64.ensure(sizeof(double) * (size_t)nf * nL));
+    dl = h->d_l64.as<double>();
+  }
+  if ((rc = forward_core(h, st, nL, h->d_P.as<double>(), h->d_T.as<double>(), h->d_X.as<double>(),
+                         h->d_R.as<double>(), h->d_N.as<double>(), dscale, Req, Rpol, orient0,
+                         orient1, gtype, limb, nb, h->d_b.as<double>(), dw, disc,
+                         h->d_Tb.as<double>(), Tb_avg ? h->d_avg.as<double>() : nullptr, dl)))
+    return rc;
+  if (Tb_out && nb > 0)
+    RB_CUDA(cudaMemcpyAsync(Tb_out, h->d_Tb.p, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
+  if (Tb_avg && nb > 0)
+    RB_CUDA(cudaMemcpyAsync(Tb_avg, h->d_avg.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
+  if (dl) RB_CUDA(cudaMemcpyAsync(layers_out, dl, sizeof(double) * (size_t)nf * nL, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
+
+int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
+                      const double* X, const double* R, const double* N, int nf,
+                      const double* freqs_host, const double* scale, double Req, double Rpol,
+                      double orient0, double orient1, int gtype, int limb, int nb,
+                      const double* b, const double* weights, int disc, double* Tb_out,
+                      double* Tb_avg) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs_host || (nb > 0 && (!b || !Tb_out)))
+    return fail(RB_EINVAL, "null array");
+  if (nL < 2 || nb < 0) return fail(RB_EINVAL, "bad sizes");
+  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
+  if (disc) return fail(RB_EINVAL, "rb_forward_device: pass nadir rays explicitly for disc");
+  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
+  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
+  return forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
+                      nb, b, weights, disc, Tb_out, Tb_avg, nullptr);
+}
+
+int rb_last_launch_count(rb_handle* h) { return h ? h->launches : 0; }
+
+int rb_debug_e2(rb_handle* h, int n, const double* x, double* out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (n < 0 || (n > 0 && (!x || !out))) return fail(RB_EINVAL, "bad arguments");
+  if (n == 0) return RB_OK;
+  RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(upload(h->d_x, x, n, h->st));
+  RB_CUDA(h->d_iw.ensure(sizeof(double) * n));
+  RB_CUDA(rb::launch_e2(n, h->d_x.as<double>(), h->d_iw.as<double>(), h->st));
+  RB_CUDA(cudaMemcpyAsync(out, h->d_iw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  RB_CUDA(cudaStreamSynchronize(h->st));
+  return RB_OK;
+}
+
+}  // extern "C"
