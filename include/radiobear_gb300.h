@@ -164,6 +164,17 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
  * rb_forward_device call (for launch accounting). */
 int rb_last_launch_count(rb_handle* h);
 
+/* Phase timing.  With profiling on, rb_forward / rb_forward_device record
+ * CUDA events around each kernel on the stream it is launched on;
+ * rb_phase_times then fills ms[0..4] = layer prep, absorption, ray paths,
+ * brightness, disc average of the last call (synchronises the handle). */
+int rb_set_profiling(rb_handle* h, int on);
+int rb_phase_times(rb_handle* h, double* ms, int n);
+
+/* Float32 FMA throughput of the device (TFLOP/s), measured with a probe
+ * kernel at the current clocks: the roofline denominator of the line sums. */
+int rb_probe_fp32_peak(rb_handle* h, double* tflops);
+
 /* E2(x) evaluated by the device routine used for b = 'disc' (test hook). */
 int rb_debug_e2(rb_handle* h, int n, const double* x, double* out);
 

@@ -37,7 +37,8 @@ FAMILY_COLUMNS = {
 
 EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set_lines',
            'rb_set_formalisms', 'rb_alpha', 'rb_raypath', 'rb_brightness', 'rb_forward',
-           'rb_forward_device', 'rb_last_launch_count', 'rb_debug_e2')
+           'rb_forward_device', 'rb_last_launch_count', 'rb_set_profiling', 'rb_phase_times',
+           'rb_probe_fp32_peak', 'rb_debug_e2')
 
 _lib = None
 _lock = threading.Lock()
@@ -82,6 +83,9 @@ def load_library(path=None):
                                           c_int, _vp, _vp, c_int, _vp, _vp]
         lib.rb_last_launch_count.argtypes = [_vp]
         lib.rb_debug_e2.argtypes = [_vp, c_int, _d, _d]
+        lib.rb_set_profiling.argtypes = [_vp, c_int]
+        lib.rb_phase_times.argtypes = [_vp, _d, c_int]
+        lib.rb_probe_fp32_peak.argtypes = [_vp, _d]
         for name in EXPORTS:
             getattr(lib, name).restype = getattr(lib, name).restype or c_int
         lib.rb_last_error.restype = ctypes.c_char_p
@@ -241,6 +245,22 @@ class Engine:
 
     def last_launch_count(self):
         return int(self.lib.rb_last_launch_count(self._h))
+
+    def set_profiling(self, on=True):
+        _check(self.lib, self.lib.rb_set_profiling(self._h, int(on)), 'rb_set_profiling')
+
+    PHASES = ('prep', 'alpha', 'raypath', 'brightness', 'disc_avg')
+
+    def phase_times(self):
+        """Milliseconds of each phase of the last forward call."""
+        ms = np.zeros(5)
+        _check(self.lib, self.lib.rb_phase_times(self._h, _ptr(ms), 5), 'rb_phase_times')
+        return dict(zip(self.PHASES, ms.tolist()))
+
+    def probe_fp32_peak(self):
+        out = np.zeros(1)
+        _check(self.lib, self.lib.rb_probe_fp32_peak(self._h, _ptr(out)), 'rb_probe_fp32_peak')
+        return float(out[0])
 
     def debug_e2(self, x):
         x = _f64(x)

@@ -588,11 +588,12 @@ __global__ void __launch_bounds__(256) rb_alpha_kernel(AlphaArgs a) {
 }
 
 // ------------------------------------------------------------------ launch
-cudaError_t launch_alpha(const PrepArgs& pa, const AlphaArgs& aa, int block, int ntile,
-                         cudaStream_t st) {
+cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st) {
   rb_layer_prep_kernel<<<pa.nL, 32, 0, st>>>(pa);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_alpha_lines(const AlphaArgs& aa, int block, int ntile, cudaStream_t st) {
   dim3 grid(aa.nL, ntile);
   rb_alpha_kernel<<<grid, block, 0, st>>>(aa);
   return cudaGetLastError();

@@ -115,17 +115,23 @@ struct rb_handle {
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x;
   int launches = 0;
+  // phase timing (rb_set_profiling)
+  int profiling = 0;
+  cudaEvent_t pev[10] = {};
+  float phase_ms[5] = {0, 0, 0, 0, 0};
+  DBuf d_probe;
 };
 
 // launchers implemented in the kernel translation units
 namespace rb {
-cudaError_t launch_alpha(const PrepArgs& pa, const AlphaArgs& aa, int block, int ntile,
-                         cudaStream_t st);
+cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
+cudaError_t launch_alpha_lines(const AlphaArgs& aa, int block, int ntile, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
 cudaError_t launch_tb(const TbArgs& a, cudaStream_t st);
 cudaError_t launch_disc_avg(int nb, int nf, const double* Tb, const double* w, double* out,
                             cudaStream_t st);
 cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st);
+cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, cudaStream_t st);
 }  // namespace rb
 
 namespace {
@@ -236,7 +242,11 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   aa.alpha32 = h->d_a32.as<float>();
   aa.layers64 = d_layers64;
   aa.gas64 = d_gas64;
-  RB_CUDA(rb::launch_alpha(pa, aa, h->plan_block, h->plan_ntile, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[0], st));
+  RB_CUDA(rb::launch_prep(pa, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[1], st));
+  RB_CUDA(rb::launch_alpha_lines(aa, h->plan_block, h->plan_ntile, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[2], st));
   h->launches += 2;
   return RB_OK;
 }
@@ -278,7 +288,9 @@ int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, con
   ra.r4ds = dr4;
   ra.latlng = dll;
   ra.end_code = dend;
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[3], st));
   RB_CUDA(rb::launch_raypath(ra, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[4], st));
   h->launches += 1;
   return RB_OK;
 }
@@ -338,6 +350,9 @@ int rb_destroy(rb_handle* h) {
                   &h->d_ds, &h->d_layer, &h->d_r4, &h->d_ll, &h->d_end, &h->d_Tb, &h->d_avg,
                   &h->d_iw, &h->d_tau, &h->d_W, &h->d_tbl, &h->d_x})
     b->release();
+  for (auto& e : h->pev)
+    if (e) cudaEventDestroy(e);
+  h->d_probe.release();
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->st) cudaStreamDestroy(h->st);
@@ -655,12 +670,15 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
     ta.layer = h->d_layer.as<int>();
     ta.disc = disc != 0;
     ta.Tb = dTb;
+    if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[5], st));
     RB_CUDA(rb::launch_tb(ta, st));
+    if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[6], st));
     h->launches += 1;
     if (davg && dw) {
       RB_CUDA(rb::launch_disc_avg(nb, nf, dTb, dw, davg, st));
       h->launches += 1;
     }
+    if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[7], st));
   }
   return RB_OK;
 }
@@ -746,6 +764,57 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
 }
 
 int rb_last_launch_count(rb_handle* h) { return h ? h->launches : 0; }
+
+int rb_set_profiling(rb_handle* h, int on) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  RB_CUDA(cudaSetDevice(h->device));
+  if (on && !h->pev[0])
+    for (auto& e : h->pev) RB_CUDA(cudaEventCreate(&e));
+  h->profiling = on != 0;
+  return RB_OK;
+}
+
+int rb_phase_times(rb_handle* h, double* ms, int n) {
+  if (!h || !ms) return fail(RB_EINVAL, "null argument");
+  if (!h->profiling) return fail(RB_ESTATE, "profiling is off (rb_set_profiling)");
+  RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(cudaEventSynchronize(h->pev[7]));
+  float t[5] = {0, 0, 0, 0, 0};
+  RB_CUDA(cudaEventElapsedTime(&t[0], h->pev[0], h->pev[1]));
+  RB_CUDA(cudaEventElapsedTime(&t[1], h->pev[1], h->pev[2]));
+  RB_CUDA(cudaEventElapsedTime(&t[2], h->pev[3], h->pev[4]));
+  RB_CUDA(cudaEventElapsedTime(&t[3], h->pev[5], h->pev[6]));
+  RB_CUDA(cudaEventElapsedTime(&t[4], h->pev[6], h->pev[7]));
+  for (int i = 0; i < n && i < 5; ++i) ms[i] = t[i];
+  return RB_OK;
+}
+
+int rb_probe_fp32_peak(rb_handle* h, double* tflops) {
+  if (!h || !tflops) return fail(RB_EINVAL, "null argument");
+  RB_CUDA(cudaSetDevice(h->device));
+  int sms = 0;
+  RB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  RB_CUDA(h->d_probe.ensure(256 * sizeof(float)));
+  cudaEvent_t e0, e1;
+  RB_CUDA(cudaEventCreate(&e0));
+  RB_CUDA(cudaEventCreate(&e1));
+  const int blocks = sms * 8, iters = 1 << 14;
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    RB_CUDA(cudaEventRecord(e0, h->st));
+    RB_CUDA(rb::launch_fp32_probe(blocks, iters, h->d_probe.as<float>(), h->st));
+    RB_CUDA(cudaEventRecord(e1, h->st));
+    RB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    RB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return RB_OK;
+}
 
 int rb_debug_e2(rb_handle* h, int n, const double* x, double* out) {
   if (!h) return fail(RB_EINVAL, "null handle");
