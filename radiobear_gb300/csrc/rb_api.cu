@@ -73,7 +73,8 @@ int family_ncols(int fam) {
 struct FamilyStore {
   int n = 0;
   std::vector<double> centre;   // sorted, host copy (near-range search)
-  DBuf c2h, c2l, ch, cl, lnI, E, w1, w2, w3, x1, x2, x3, lnI32, E32;
+  float l2Imax = 0.f, Emin = 0.f, Emax = 0.f;
+  DBuf c2h, c2l, ch, cl, l2Ih, l2Il, Eh, El, w1, w2, w3, x1, x2, x3;
   rb::LineTable table() const {
     rb::LineTable t{};
     t.n = n;
@@ -81,20 +82,23 @@ struct FamilyStore {
     t.c2l = c2l.as<float>();
     t.ch = ch.as<float>();
     t.cl = cl.as<float>();
-    t.lnI = lnI.as<double>();
-    t.E = E.as<double>();
+    t.l2Ih = l2Ih.as<float>();
+    t.l2Il = l2Il.as<float>();
+    t.Eh = Eh.as<float>();
+    t.El = El.as<float>();
     t.w1 = w1.as<float>();
     t.w2 = w2.as<float>();
     t.w3 = w3.as<float>();
     t.x1 = x1.as<float>();
     t.x2 = x2.as<float>();
     t.x3 = x3.as<float>();
-    t.lnI32 = lnI32.as<float>();
-    t.E32 = E32.as<float>();
+    t.l2Imax = l2Imax;
+    t.Emin = Emin;
+    t.Emax = Emax;
     return t;
   }
   void release() {
-    for (DBuf* b : {&c2h, &c2l, &ch, &cl, &lnI, &E, &w1, &w2, &w3, &x1, &x2, &x3, &lnI32, &E32})
+    for (DBuf* b : {&c2h, &c2l, &ch, &cl, &l2Ih, &l2Il, &Eh, &El, &w1, &w2, &w3, &x1, &x2, &x3})
       b->release();
   }
 };
@@ -109,11 +113,12 @@ struct rb_handle {
   rb::AlphaConfig cfg{rb::NH3_HS_SJS, 1, 1, 1, 1, 'e', 0};
   // frequency plan
   std::vector<double> plan_f;
-  int plan_block = 0, plan_ntile = 0;
-  DBuf d_f, d_fhs, d_near;
+  int plan_block = 0, plan_ntile = 0, plan_nslot = 0;
+  DBuf d_f, d_fhs, d_near, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset;
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
-      d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x;
+      d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
+      d_T32, d_hds, d_Tb32, d_part;
   int launches = 0;
   // phase timing (rb_set_profiling)
   int profiling = 0;
@@ -126,9 +131,13 @@ struct rb_handle {
 namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
 cudaError_t launch_alpha_lines(const AlphaArgs& aa, int block, int ntile, cudaStream_t st);
+cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
+                             float* R32, float* T32, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
-cudaError_t launch_tb(const TbArgs& a, cudaStream_t st);
-cudaError_t launch_disc_avg(int nb, int nf, const double* Tb, const double* w, double* out,
+cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st);
+cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st);
+int tb_nchunk(int max_seg);
+cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
                             cudaStream_t st);
 cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st);
 cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, cudaStream_t st);
@@ -149,10 +158,14 @@ cudaError_t upload(DBuf& b, const T* src, size_t count, cudaStream_t st) {
   return cudaMemcpyAsync(b.p, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
 }
 
-// Frequency plan: the nh3_hs output order (nh3_hs.py:70-88: <=30 GHz block
-// then >30 GHz block), tile shape and, per warp and family, the index range
-// of lines whose centre is within [0.75 fmin, 1.3 fmax] of the warp's
-// frequencies (those take the double-float F - K path).
+// Frequency plan.
+//  * nh3_hs output order (nh3_hs.py:70-88): slot j evaluates nh3_hs at the
+//    j-th element of [freqs <= 30 GHz in order, freqs > 30 GHz in order];
+//  * slots: two per thread, the <=30 GHz block padded to an even length so
+//    no thread pair straddles the coefficient switch;
+//  * per warp (64 slots) and family, the index range of lines whose centre
+//    is within [0.75 fmin, 1.3 fmax] of the warp's frequencies (those take
+//    the double-float F - K path).
 int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st) {
   if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
   for (int i = 0; i < nf; ++i)
@@ -164,24 +177,54 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
   fhs.reserve(nf);
   for (int i = 0; i < nf; ++i)
     if (freqs[i] <= 30.0) fhs.push_back(freqs[i]);
+  const int n_lo = (int)fhs.size();
   for (int i = 0; i < nf; ++i)
     if (freqs[i] > 30.0) fhs.push_back(freqs[i]);
-  int block = std::min(256, ((nf + 31) / 32) * 32);
-  int ntile = (nf + block - 1) / block;
-  int nw = block / 32;
+  std::vector<int> slot_j;
+  for (int j = 0; j < n_lo; ++j) slot_j.push_back(j);
+  if (n_lo % 2) slot_j.push_back(-1);
+  for (int j = n_lo; j < nf; ++j) slot_j.push_back(j);
+  if (slot_j.size() % 2) slot_j.push_back(-1);
+  const int npair = (int)slot_j.size() / 2;
+  const int block = std::min(128, ((npair + 31) / 32) * 32);
+  const int ntile = (npair + block - 1) / block;
+  const int nslot = ntile * block * 2;
+  slot_j.resize(nslot, -1);
+  std::vector<float2> sF(nslot), sFhs(nslot), sf(nslot);
+  std::vector<float> swJ(nslot, 0.f);
+  std::vector<int> sset(nslot, 0);
+  for (int s = 0; s < nslot; ++s) {
+    const int j = slot_j[s];
+    const int jj = j >= 0 ? j : (s % 2 ? slot_j[s - 1] : -1);   // padding mirrors its partner
+    const double f = jj >= 0 ? freqs[jj] : 1.0, fh = jj >= 0 ? fhs[jj] : 1.0;
+    float a, b;
+    rb::split_double(f * f, a, b);
+    sF[s] = make_float2(a, b);
+    rb::split_double(fh * fh, a, b);
+    sFhs[s] = make_float2(a, b);
+    rb::split_double(f, a, b);
+    sf[s] = make_float2(a, b);
+    swJ[s] = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)((f - 26.0) / 8.0));
+    sset[s] = (jj >= n_lo) ? 1 : 0;
+  }
+  for (int s = 0; s + 1 < nslot; s += 2) sset[s + 1] = sset[s] = std::max(sset[s], sset[s + 1]) *
+                                                                 (slot_j[s] >= 0 || slot_j[s + 1] >= 0);
+  const int nw = block / 32;
   std::vector<int2> nearv((size_t)ntile * nw * rb::NFAM, make_int2(0, 0));
   for (int t = 0; t < ntile; ++t)
     for (int w = 0; w < nw; ++w) {
-      int j0 = t * block + w * 32, j1 = std::min(nf, j0 + 32);
-      if (j0 >= nf) continue;
+      const int s0 = (t * block + w * 32) * 2, s1 = s0 + 64;
       for (int fam = 0; fam < rb::NFAM; ++fam) {
         const bool hs = fam == rb::FAM_NH3_INV || fam == rb::FAM_NH3_ROT || fam == rb::FAM_NH3_V2;
-        const double* fv = hs ? fhs.data() : freqs;
-        double lo = fv[j0], hi = fv[j0];
-        for (int j = j0; j < j1; ++j) {
-          lo = std::min(lo, fv[j]);
-          hi = std::max(hi, fv[j]);
+        double lo = INFINITY, hi = -INFINITY;
+        for (int s = s0; s < s1; ++s) {
+          const int j = slot_j[s];
+          if (j < 0) continue;
+          const double v = hs ? fhs[j] : freqs[j];
+          lo = std::min(lo, v);
+          hi = std::max(hi, v);
         }
+        if (!(lo <= hi)) continue;
         const std::vector<double>& c = h->fam[fam].centre;
         int a = (int)(std::lower_bound(c.begin(), c.end(), 0.75 * lo) - c.begin());
         int b = (int)(std::upper_bound(c.begin(), c.end(), 1.3 * hi) - c.begin());
@@ -191,10 +234,17 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
   RB_CUDA(upload(h->d_f, freqs, nf, st));
   RB_CUDA(upload(h->d_fhs, fhs.data(), nf, st));
   RB_CUDA(upload(h->d_near, nearv.data(), nearv.size(), st));
+  RB_CUDA(upload(h->d_sj, slot_j.data(), slot_j.size(), st));
+  RB_CUDA(upload(h->d_sF, sF.data(), sF.size(), st));
+  RB_CUDA(upload(h->d_sFhs, sFhs.data(), sFhs.size(), st));
+  RB_CUDA(upload(h->d_sf, sf.data(), sf.size(), st));
+  RB_CUDA(upload(h->d_swJ, swJ.data(), swJ.size(), st));
+  RB_CUDA(upload(h->d_sset, sset.data(), sset.size(), st));
   RB_CUDA(cudaStreamSynchronize(st));
   h->plan_f.assign(freqs, freqs + nf);
   h->plan_block = block;
   h->plan_ntile = ntile;
+  h->plan_nslot = nslot;
   return RB_OK;
 }
 
@@ -208,17 +258,6 @@ int validate_atm(int nL, const double* P, const double* T, const double* X) {
   return RB_OK;
 }
 
-void fill_prep(rb_handle* h, rb::PrepArgs& pa, int nL, const double* dP, const double* dT,
-               const double* dX) {
-  pa.nL = nL;
-  pa.P = dP;
-  pa.T = dT;
-  pa.X = dX;
-  pa.cfg = h->cfg;
-  for (int f = 0; f < rb::NFAM; ++f) pa.tab[f] = h->fam[f].table();
-  pa.out = h->d_lp.as<rb::LayerParams>();
-}
-
 int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
                   const double* dX, const double* dscale, int units_db, double* d_layers64,
                   double* d_gas64) {
@@ -226,19 +265,36 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   const int nf = (int)h->plan_f.size();
   RB_CUDA(h->d_a32.ensure(sizeof(float) * (size_t)nL * nf));
   rb::PrepArgs pa{};
-  fill_prep(h, pa, nL, dP, dT, dX);
+  pa.nL = nL;
+  pa.P = dP;
+  pa.T = dT;
+  pa.X = dX;
+  pa.scale = dscale;
+  pa.cfg = h->cfg;
   pa.cfg.units_db = units_db;
+  for (int f = 0; f < rb::NFAM; ++f) {
+    pa.l2Imax[f] = h->fam[f].l2Imax;
+    pa.Emin[f] = h->fam[f].Emin;
+    pa.Emax[f] = h->fam[f].Emax;
+    pa.nlines[f] = h->fam[f].n;
+  }
+  pa.out = h->d_lp.as<rb::LayerParams>();
   rb::AlphaArgs aa{};
   aa.nL = nL;
   aa.nf = nf;
-  aa.nwarps_tile = h->plan_block / 32;
+  aa.nslot = h->plan_nslot;
+  aa.sp.j = h->d_sj.as<int>();
+  aa.sp.F = h->d_sF.as<float2>();
+  aa.sp.Fhs = h->d_sFhs.as<float2>();
+  aa.sp.f = h->d_sf.as<float2>();
+  aa.sp.wJ = h->d_swJ.as<float>();
+  aa.sp.set = h->d_sset.as<int>();
   aa.freqs = h->d_f.as<double>();
   aa.freqs_hs = h->d_fhs.as<double>();
   aa.lp = h->d_lp.as<rb::LayerParams>();
   for (int f = 0; f < rb::NFAM; ++f) aa.tab[f] = h->fam[f].table();
   aa.near = h->d_near.as<int2>();
   aa.cfg = pa.cfg;
-  aa.scale = dscale;
   aa.alpha32 = h->d_a32.as<float>();
   aa.layers64 = d_layers64;
   aa.gas64 = d_gas64;
@@ -268,14 +324,25 @@ void aspect_matrix(double Req, double Rpol, double o0, double o1, double* M) {
   M[8] = cx;
 }
 
+// Geometry tables (float radii differences, float T) then the ray walk.
+// T may be null (no float temperature table needed).
 int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, const double* dN,
-                    double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
-                    const double* db, int max_seg, int* dnseg, double* dds, int* dlayer,
-                    double* dr4, double* dll, int* dend) {
+                    const double* dT, double Req, double Rpol, double o0, double o1, int gtype,
+                    int limb, int nb, const double* db, int max_seg, int* dnseg, double* dds,
+                    float* dhds, int* dlayer, double* dr4, double* dll, int* dend) {
+  RB_CUDA(h->d_dR.ensure(sizeof(float) * nL));
+  RB_CUDA(h->d_sR.ensure(sizeof(float2) * nL));
+  RB_CUDA(h->d_R32.ensure(sizeof(float) * nL));
+  RB_CUDA(h->d_T32.ensure(sizeof(float) * nL));
+  RB_CUDA(rb::launch_geom_prep(nL, dR, dT, h->d_sR.as<float2>(), h->d_dR.as<float>(),
+                               h->d_R32.as<float>(), h->d_T32.as<float>(), st));
   rb::RayArgs ra{};
   ra.nL = nL;
   ra.R = dR;
   ra.N = dN;
+  ra.dR2 = h->d_sR.as<float2>();
+  ra.dR = h->d_dR.as<float>();
+  ra.R32 = h->d_R32.as<float>();
   ra.k = gtype == RB_GTYPE_ELLIPSE ? Rpol / Req : 1.0;
   aspect_matrix(Req, Rpol, o0, o1, ra.rot);
   ra.limb_sec = limb == RB_LIMB_SEC;
@@ -284,6 +351,7 @@ int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, con
   ra.max_seg = max_seg;
   ra.nseg = dnseg;
   ra.ds = dds;
+  ra.hds = dhds;
   ra.layer = dlayer;
   ra.r4ds = dr4;
   ra.latlng = dll;
@@ -291,7 +359,7 @@ int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, con
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[3], st));
   RB_CUDA(rb::launch_raypath(ra, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[4], st));
-  h->launches += 1;
+  h->launches += 2;
   return RB_OK;
 }
 
@@ -345,6 +413,9 @@ int rb_destroy(rb_handle* h) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->side) cudaStreamSynchronize(h->side);
   for (auto& f : h->fam) f.release();
+  for (DBuf* b : {&h->d_sj, &h->d_sF, &h->d_sFhs, &h->d_sf, &h->d_swJ, &h->d_sset, &h->d_dR,
+                  &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part})
+    b->release();
   for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_near, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
                   &h->d_ds, &h->d_layer, &h->d_r4, &h->d_ll, &h->d_end, &h->d_Tb, &h->d_avg,
@@ -387,8 +458,9 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return centre[a] < centre[b]; });
   std::vector<float> c2h(n), c2l(n), ch(n), cl(n), w1(n), w2(n), w3(n), x1(n), x2(n), x3(n),
-      lnI32(n), E32(n);
-  std::vector<double> lnI(n), E(n), cs(n);
+      l2Ih(n), l2Il(n), Eh(n), El(n);
+  std::vector<double> cs(n);
+  double l2max = -INFINITY, emin = INFINITY, emax = -INFINITY;
   for (int k = 0; k < n; ++k) {
     const int i = order[k];
     const double fo = col(0, i);
@@ -396,7 +468,8 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
     cs[k] = centre[i];
     rb::split_double(fo * fo, c2h[k], c2l[k]);
     rb::split_double(centre[i], ch[k], cl[k]);
-    E[k] = col(2, i);
+    const double E = col(2, i);
+    rb::split_double(E, Eh[k], El[k]);
     double lI = I > 0.0 ? std::log(I) : -INFINITY;
     w1[k] = w2[k] = w3[k] = 0.f;
     x1[k] = x2[k] = x3[k] = 0.f;
@@ -438,27 +511,37 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
         x3[k] = (float)col(8, i);
         break;
     }
-    lnI[k] = lI;
-    lnI32[k] = (float)lI;
-    E32[k] = (float)E[k];
+    const double l2 = lI * 1.4426950408889634;     // log2
+    if (std::isfinite(l2)) {
+      rb::split_double(l2, l2Ih[k], l2Il[k]);
+      l2max = std::max(l2max, l2);
+    } else {
+      l2Ih[k] = -1.0e30f;                           // zero strength
+      l2Il[k] = 0.f;
+    }
+    emin = std::min(emin, E);
+    emax = std::max(emax, E);
   }
   F.n = 0;
   F.centre = cs;
+  F.l2Imax = n > 0 && std::isfinite(l2max) ? (float)l2max + 1e-3f : 0.f;
+  F.Emin = n > 0 ? (float)emin : 0.f;
+  F.Emax = n > 0 ? (float)emax : 0.f;
   cudaStream_t st = h->st;
   RB_CUDA(upload(F.c2h, c2h.data(), n, st));
   RB_CUDA(upload(F.c2l, c2l.data(), n, st));
   RB_CUDA(upload(F.ch, ch.data(), n, st));
   RB_CUDA(upload(F.cl, cl.data(), n, st));
-  RB_CUDA(upload(F.lnI, lnI.data(), n, st));
-  RB_CUDA(upload(F.E, E.data(), n, st));
+  RB_CUDA(upload(F.l2Ih, l2Ih.data(), n, st));
+  RB_CUDA(upload(F.l2Il, l2Il.data(), n, st));
+  RB_CUDA(upload(F.Eh, Eh.data(), n, st));
+  RB_CUDA(upload(F.El, El.data(), n, st));
   RB_CUDA(upload(F.w1, w1.data(), n, st));
   RB_CUDA(upload(F.w2, w2.data(), n, st));
   RB_CUDA(upload(F.w3, w3.data(), n, st));
   RB_CUDA(upload(F.x1, x1.data(), n, st));
   RB_CUDA(upload(F.x2, x2.data(), n, st));
   RB_CUDA(upload(F.x3, x3.data(), n, st));
-  RB_CUDA(upload(F.lnI32, lnI32.data(), n, st));
-  RB_CUDA(upload(F.E32, E32.data(), n, st));
   RB_CUDA(cudaStreamSynchronize(st));
   F.n = n;
   return RB_OK;
@@ -542,10 +625,10 @@ int rb_raypath(rb_handle* h, int nL, const double* R, const double* N, double Re
   if (r4ds) RB_CUDA(h->d_r4.ensure(sizeof(double) * ns));
   if (latlng) RB_CUDA(h->d_ll.ensure(sizeof(double) * (size_t)nb * (max_seg + 1) * 2));
   h->launches = 0;
-  if ((rc = enqueue_raypath(h, st, nL, h->d_R.as<double>(), h->d_N.as<double>(), Req, Rpol,
-                            orient0, orient1, gtype, limb, nb, h->d_b.as<double>(), max_seg,
-                            h->d_nseg.as<int>(), h->d_ds.as<double>(), h->d_layer.as<int>(),
-                            r4ds ? h->d_r4.as<double>() : nullptr,
+  if ((rc = enqueue_raypath(h, st, nL, h->d_R.as<double>(), h->d_N.as<double>(), nullptr, Req,
+                            Rpol, orient0, orient1, gtype, limb, nb, h->d_b.as<double>(), max_seg,
+                            h->d_nseg.as<int>(), h->d_ds.as<double>(), nullptr,
+                            h->d_layer.as<int>(), r4ds ? h->d_r4.as<double>() : nullptr,
                             latlng ? h->d_ll.as<double>() : nullptr, h->d_end.as<int>())))
     return rc;
   RB_CUDA(cudaMemcpyAsync(nseg, h->d_nseg.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
@@ -579,21 +662,19 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
   }
   RB_CUDA(cudaSetDevice(h->device));
   cudaStream_t st = h->st;
-  // absorption as float32 [nL][nf]; layer indices wrapped like Python's
-  std::vector<float> a32((size_t)nL * nf);
+  // absorption as float32 [nL][nf], T as float, ds/2 in cm as float
+  std::vector<float> a32((size_t)nL * nf), t32(nL), hd((size_t)nb * max_seg, 0.f);
   for (int f = 0; f < nf; ++f)
     for (int l = 0; l < nL; ++l) a32[(size_t)l * nf + f] = (float)layers[(size_t)f * nL + l];
-  std::vector<int> lay((size_t)nb * max_seg, 0);
+  for (int l = 0; l < nL; ++l) t32[l] = (float)T[l];
   for (int r = 0; r < nb; ++r)
-    for (int i = 0; i < nseg[r]; ++i) {
-      int l = layer[(size_t)r * max_seg + i];
-      lay[(size_t)r * max_seg + i] = l < 0 ? l + nL : l;
-    }
+    for (int i = 0; i < nseg[r]; ++i)
+      hd[(size_t)r * max_seg + i] = (float)(ds[(size_t)r * max_seg + i] * 1.0e3 / 1.0e-2 / 2.0);
   RB_CUDA(upload(h->d_a32, a32.data(), a32.size(), st));
-  RB_CUDA(upload(h->d_T, T, nL, st));
+  RB_CUDA(upload(h->d_T32, t32.data(), t32.size(), st));
   RB_CUDA(upload(h->d_nseg, nseg, nb, st));
-  RB_CUDA(upload(h->d_ds, ds, (size_t)nb * max_seg, st));
-  RB_CUDA(upload(h->d_layer, lay.data(), lay.size(), st));
+  RB_CUDA(upload(h->d_hds, hd.data(), hd.size(), st));
+  RB_CUDA(upload(h->d_layer, layer, (size_t)nb * max_seg, st));
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
   RB_CUDA(h->d_iw.ensure(sizeof(double) * (size_t)nb * nf));
   const size_t np = (size_t)nb * nf * max_seg;
@@ -608,9 +689,9 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
   ta.nb = nb;
   ta.max_seg = max_seg;
   ta.alpha32 = h->d_a32.as<float>();
-  ta.T = h->d_T.as<double>();
+  ta.T32 = h->d_T32.as<float>();
   ta.nseg = h->d_nseg.as<int>();
-  ta.ds = h->d_ds.as<double>();
+  ta.hds = h->d_hds.as<float>();
   ta.layer = h->d_layer.as<int>();
   ta.disc = disc != 0;
   ta.Tb = h->d_Tb.as<double>();
@@ -618,8 +699,16 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
   ta.tau = prof ? h->d_tau.as<double>() : nullptr;
   ta.W = prof ? h->d_W.as<double>() : nullptr;
   ta.TbL = prof ? h->d_tbl.as<double>() : nullptr;
-  h->launches = 1;
-  RB_CUDA(rb::launch_tb(ta, st));
+  if (prof || disc) {
+    h->launches = 1;
+    RB_CUDA(rb::launch_tb_seq(ta, st));
+  } else {
+    ta.nchunk = rb::tb_nchunk(max_seg);
+    RB_CUDA(h->d_part.ensure(sizeof(float4) * (size_t)nb * ta.nchunk * nf));
+    ta.part = h->d_part.as<float4>();
+    h->launches = 2;
+    RB_CUDA(rb::launch_tb_chunked(ta, st));
+  }
   RB_CUDA(cudaMemcpyAsync(Tb_out, ta.Tb, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
   if (intW_out)
     RB_CUDA(cudaMemcpyAsync(intW_out, ta.intW, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
@@ -639,21 +728,22 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
                         double* dl64) {
   const int nf = (int)h->plan_f.size();
   const int max_seg = 2 * nL + 4;
-  const size_t ns = (size_t)nb * max_seg;
+  const size_t ns = (size_t)std::max(nb, 1) * max_seg;
   RB_CUDA(h->d_nseg.ensure(sizeof(int) * std::max(nb, 1)));
-  RB_CUDA(h->d_ds.ensure(sizeof(double) * std::max(ns, (size_t)1)));
-  RB_CUDA(h->d_layer.ensure(sizeof(int) * std::max(ns, (size_t)1)));
+  RB_CUDA(h->d_hds.ensure(sizeof(float) * ns));
+  RB_CUDA(h->d_layer.ensure(sizeof(int) * ns));
+  RB_CUDA(h->d_Tb32.ensure(sizeof(float) * (size_t)std::max(nb, 1) * nf));
+  const int nchunk = rb::tb_nchunk(max_seg);
+  if (!disc) RB_CUDA(h->d_part.ensure(sizeof(float4) * (size_t)std::max(nb, 1) * nchunk * nf));
   h->launches = 0;
-  // ray paths on the side stream, concurrent with the absorption kernels
+  // geometry + ray paths on the side stream, concurrent with the absorption
   RB_CUDA(cudaEventRecord(h->ev_fork, st));
   RB_CUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
   int rc;
-  if (nb > 0) {
-    if ((rc = enqueue_raypath(h, h->side, nL, dR, dN, Req, Rpol, o0, o1, gtype, limb, nb, db,
-                              max_seg, h->d_nseg.as<int>(), h->d_ds.as<double>(),
-                              h->d_layer.as<int>(), nullptr, nullptr, nullptr)))
-      return rc;
-  }
+  if ((rc = enqueue_raypath(h, h->side, nL, dR, dN, dT, Req, Rpol, o0, o1, gtype, limb,
+                            std::max(nb, 0), db, max_seg, h->d_nseg.as<int>(), nullptr,
+                            h->d_hds.as<float>(), h->d_layer.as<int>(), nullptr, nullptr, nullptr)))
+    return rc;
   RB_CUDA(cudaEventRecord(h->ev_join, h->side));
   if ((rc = enqueue_alpha(h, st, nL, dP, dT, dX, dscale, 0, dl64, nullptr))) return rc;
   RB_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
@@ -664,18 +754,26 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
     ta.nb = nb;
     ta.max_seg = max_seg;
     ta.alpha32 = h->d_a32.as<float>();
-    ta.T = dT;
+    ta.T32 = h->d_T32.as<float>();
     ta.nseg = h->d_nseg.as<int>();
-    ta.ds = h->d_ds.as<double>();
+    ta.hds = h->d_hds.as<float>();
     ta.layer = h->d_layer.as<int>();
     ta.disc = disc != 0;
     ta.Tb = dTb;
+    ta.Tb32 = h->d_Tb32.as<float>();
+    ta.nchunk = nchunk;
+    ta.part = h->d_part.as<float4>();
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[5], st));
-    RB_CUDA(rb::launch_tb(ta, st));
+    if (disc) {
+      RB_CUDA(rb::launch_tb_seq(ta, st));
+      h->launches += 1;
+    } else {
+      RB_CUDA(rb::launch_tb_chunked(ta, st));
+      h->launches += 2;
+    }
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[6], st));
-    h->launches += 1;
     if (davg && dw) {
-      RB_CUDA(rb::launch_disc_avg(nb, nf, dTb, dw, davg, st));
+      RB_CUDA(rb::launch_disc_avg(nb, nf, h->d_Tb32.as<float>(), dw, davg, st));
       h->launches += 1;
     }
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[7], st));

@@ -2,10 +2,13 @@
 //
 // Layout conventions (all device buffers owned by an rb_handle):
 //   * line catalogues: structure-of-arrays per family, lines sorted by
-//     centre frequency, derived columns precomputed on the host in float64;
-//   * per-layer scalars (partial pressures, width coefficients, strength
-//     prefactors) live in an array of LayerParams, one per layer, computed
-//     by rb_layer_prep_kernel in float64;
+//     centre frequency, derived columns precomputed on the host in float64
+//     and stored as float pairs (double-float) where float32 would lose
+//     digits;
+//   * per-layer scalars (width coefficients, strength prefactors as
+//     mantissa x 2^exponent) live in an array of LayerParams, one per layer;
+//   * frequencies are planned into "slots": two slots per thread, padded so
+//     a thread's pair never straddles the nh3_hs 30 GHz coefficient switch;
 //   * absorption for the brightness scan is float32 [nL][nf] (frequency
 //     contiguous, so a warp reading 32 frequencies of one layer is one
 //     128-byte transaction).
@@ -40,49 +43,53 @@ enum Nh3Mode : int { NH3_OFF = 0, NH3_HS = 1, NH3_SJS = 2, NH3_HS_SJS = 3 };
 // One line family on the device (SoA, sorted by centre).
 struct LineTable {
   int n;
-  // centre terms (float pairs = exact-ish double-float of a float64 value)
-  const float* c2h;    // centre^2 high part   (BR/Gross: fo^2; VVW: unused)
-  const float* c2l;    // centre^2 low part
-  const float* ch;     // centre high part     (VVW: fo + SR; BR: fo)
-  const float* cl;     // centre low part
-  const double* lnI;   // log strength incl. line weights and the 1/fo^2 of (f/fo)^2
-  const double* E;     // lower-state energy term multiplying LayerFam::cE
+  const float* c2h;    // centre^2 high part   (Ben-Reuven / Gross / sjs: fo^2)
+  const float* c2l;    //          low part
+  const float* ch;     // centre high part     (VVW: fo + SR; others: fo)
+  const float* cl;     //        low part
+  const float* l2Ih;   // log2 strength (incl. line weights and the 1/fo^2 of (f/fo)^2), hi
+  const float* l2Il;   //                                                               lo
+  const float* Eh;     // energy term multiplying LayerFam::cE, hi
+  const float* El;     //                                       lo
   const float* w1;     // per-line width parameters (family specific)
   const float* w2;
   const float* w3;
   const float* x1;     // per-line temperature exponents (VVW only)
   const float* x2;
   const float* x3;
-  const float* lnI32;  // float copy of lnI for the scale pre-pass
-  const float* E32;    // float copy of E
+  float l2Imax, Emin, Emax;   // family statistics for the strength scale
 };
 
 // Per (layer, family) scalars.
+//   alpha_fam(f) = fm * 2^fe * f^2 * sum_l S'_l shape_l(f)   [cm^-1]
+//   S'_l = 2^(l2I_l + cE * E_l - M2) <= 1, M2 an integer upper bound of the
+//   exponent over the family (from l2Imax, Emin, Emax), so no line pass is
+//   needed to scale float32 sums.
 struct LayerFam {
-  double fac;      // alpha_fam(f) = fac * f^2 * sum_l S'_l shape_l(f)   [cm^-1]
-  double M;        // log-strength offset: S'_l = exp(lnI_l + cE*E_l - M)
-  double cE;
+  float fm;        // prefactor mantissa
+  int fe;          // exponent incl. M2
+  float cEh, cEl;  // double-float log2 energy coefficient
+  float M2;        // integer-valued strength offset
   // width model (Ben-Reuven, per coefficient set s):
-  //   gamma = g0 + g1*w1 + g2*w2, zeta = z0 + z1*w1 + zg*gamma,
-  //   delta = dg*gamma + d0
-  // Gross: gamma = g1*w1 + g2*w2 + g3*w3 (set 0).
-  // VVW:  df = g1*w1*T^x1 + g2*w2*T^x2 + g3*w3*T^x3 with Theta exponents
-  //       (g1..g3 = partial pressures), logTheta in g0.
+  //   gamma = c0 + c1*w1 + c2*w2, zeta = c3 + c4*w1 + c5*gamma,
+  //   delta = c6*gamma + c7
+  // Gross: gamma = c1*w1 + c2*w2 + c3*w3 (set 0).
+  // VVW:  df = c1*w1*Th^x1 + c2*w2*Th^x2 + c3*w3*Th^x3, c0 = log2(Theta).
   float c[2][8];
 };
 
 // Per-layer parameters.
 struct LayerParams {
-  double P, T;
+  float P, T;
   LayerFam fam[NFAM];
-  double h2_cia;       // alpha_h2(f) = h2_cia * f^2
-  double h2o_cont;     // continuum part of alpha_h2o(f) = h2o_cont * f^2
-  double blendW;       // nh3_hs_sjs weight of sjs (0: hs only, 1: sjs only)
+  float h2_cia;        // alpha_h2(f) = h2_cia * f^2
+  float h2o_cont;      // continuum part of alpha_h2o(f) = h2o_cont * f^2
+  float blendW;        // nh3_hs_sjs weight of sjs (0: hs only, 1: sjs only)
   int use_hs, use_sjs; // which NH3 formalisms this layer evaluates
-  // nh3_sjs coefficient sets: [0] Joiner, [1] Spilker; each
-  // {GH2, GHe, GNH3, ZH2, ZHe, ZNH3, D} already multiplied by the partial
-  // pressures and (T0/T)^(2/3) where the formula does so.
-  double sjs[2][8];
+  // nh3_sjs coefficient sets [0] Joiner, [1] Spilker:
+  //   gamma = [0] + [1]*G0, zeta = [2] + [3]*G0, delta = [4]
+  float sjs[2][5];
+  float scale[NGAS];   // per-gas multipliers (1 when no scale is given)
 };
 
 struct AlphaConfig {
@@ -90,6 +97,16 @@ struct AlphaConfig {
   int use_h2, use_h2o, use_h2s, use_ph3;
   int h2state;         // 'e' or 'n'
   int units_db;        // 0: cm^-1, 1: dB/km (the nh3 clamp applies after units)
+};
+
+// Frequency slot plan: two slots per thread.
+struct SlotPlan {
+  const int* j;          // [nslot] frequency index, -1 = padding
+  const float2* F;       // [nslot] (hi, lo) of f^2
+  const float2* Fhs;     // [nslot] (hi, lo) of the nh3_hs frequency squared
+  const float2* f;       // [nslot] (hi, lo) of f
+  const float* wJ;       // [nslot] nh3_sjs Joiner weight (0 f<=26, 1 f>=34, linear between)
+  const int* set;        // [nslot] nh3_hs coefficient set (0: <=30 GHz, 1: >30 GHz)
 };
 
 // ---------------------------------------------------------------- helpers
@@ -110,20 +127,5 @@ __device__ __forceinline__ float rcp_approx(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
-
-// Compensated accumulator: running sum plus a plain partial over a block
-// of terms, folded in with Kahan's correction every few dozen terms.
-struct KahanAcc {
-  float s, c, part;
-  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; part = 0.f; }
-  __device__ __forceinline__ void flush() {
-    float y = part - c;
-    float t = s + y;
-    c = (t - s) - y;
-    s = t;
-    part = 0.f;
-  }
-  __device__ __forceinline__ float value() const { return s - c + part; }
-};
 
 }  // namespace rb

@@ -1,32 +1,31 @@
-// Ray path through the layered (ellipse-geoid) atmosphere: a float64
-// restatement of raypath.compute_ds / findEdge (raypath.py:60-273) and
-// Shape._calcEllipse (shape.py:223-274) for sm_103a.
+// Ray path through the layered (ellipse-geoid) atmosphere: a restatement of
+// raypath.compute_ds / findEdge (raypath.py:60-273) and Shape._calcEllipse
+// (shape.py:223-274) for sm_103a.
 //
-// One warp per ray.  findEdge's trial points (a 0.005 rNorm march along the
-// line of sight, raypath.py:62-87) are evaluated 32 at a time, one per lane,
-// and the first point inside the top shell is found with a ballot.  The
-// shell walk itself is a dependent chain and runs on lane 0.
-//
-// The walk follows the reference step by step:
-//   * the shell radii are the ellipse radius of shell `layer` at the current
-//     point's planetocentric latitude (rNow, rNext);
-//   * ds = -r.s -/+ sqrt((r.s)^2 + rNext^2 - rNow^2) (ingress / egress);
-//   * a negative discriminant on ingress is the tangent layer (chord -2 r.s,
-//     then egress); on egress it ends the path (raypath.py:191-209);
-//   * refraction only at the first step (nratio = nr[0]/nr[1]); afterwards
-//     nratio = 1 so the s-update reduces to s += dir*(c-|c|)*n with
-//     c = -dir s.n (zero unless the ray meets the local normal at more than
-//     90 degrees, where the reference's arcsin(sin t) folds the angle);
-//   * the path ends where the reference's `nr[layer + dir]` index check
-//     raises (Python negative indices wrap, so egress runs out at layer -1).
-// Latitude and longitude enter only through sin/cos, which are formed from
-// the vector components directly (lat = 0 keeps the reference's 1e-6 rad
-// substitution).
+// One warp per ray.
+//  * findEdge's trial points (a 0.005 rNorm march along the line of sight,
+//    raypath.py:62-87) are evaluated in float64, 32 at a time, one per lane;
+//    the first point inside the top shell is found with a ballot.
+//  * The edge point, the first normal and the one refraction at the top
+//    (nratio = nr[0]/nr[1]) are float64 on lane 0.
+//  * The shell walk is a dependent chain on lane 0 in float32 / double-float.
+//    After the first step the reference sets nratio = 1, so the direction s
+//    stays fixed (except the rare fold of arcsin(sin t) when the ray meets
+//    the local normal beyond 90 degrees, handled in float64).  The ray is
+//    r(S) = r0 + S s and the walk tracks w = u^2, u = r.s, as a double-float:
+//    each step of raypath.py:191-196 satisfies exactly
+//        u_{i+1}^2 = u_i^2 + D_i,   D_i = E_i^2 (R[next]^2 - R[cur]^2)
+//    (= rdots^2 + rNext^2 - rNow^2), E_i^2 = k^2 sin^2(lat) + cos^2(lat) at the
+//    current point.  So u_{i+1} = -/+ sqrt(w + D) (ingress / egress) and
+//    ds_i = u_{i+1} - u_i, with D in double-float from float64 radius
+//    differences.  Accumulating w instead of u keeps the along-ray coordinate
+//    exact to ~1e-14 over the whole path, which the tangent chord -2u needs.
+//  * disc = w + D < 0 on ingress -> tangent chord ds = -2u, then egress;
+//                      on egress  -> leave the atmosphere (raypath.py:197-209).
 #include "rb_args.cuh"
 #include <math_constants.h>
 
 namespace rb {
-
 
 __device__ __forceinline__ void rot_apply(const double* M, double x, double y, double z, double& ox,
                                           double& oy, double& oz) {
@@ -41,14 +40,17 @@ struct LatLng {
   double sl, cl, sg, cg;
 };
 
+constexpr double SIN_1EM6 = 9.9999999999983336e-07;   // sin(1e-6)
+constexpr double COS_1EM6 = 0.99999999999950007;      // cos(1e-6)
+
 __device__ __forceinline__ LatLng latlng_of(double x, double y, double z) {
   LatLng o;
   const double rho2 = x * x + z * z;
   const double rho = sqrt(rho2);
   const double rr = sqrt(rho2 + y * y);
   if (y == 0.0) {
-    o.sl = 9.9999999999983336e-07;   // sin(1e-6)
-    o.cl = 0.99999999999950007;      // cos(1e-6)
+    o.sl = SIN_1EM6;
+    o.cl = COS_1EM6;
   } else {
     o.sl = y / rr;
     o.cl = rho / rr;
@@ -63,9 +65,8 @@ __device__ __forceinline__ LatLng latlng_of(double x, double y, double z) {
   return o;
 }
 
-__device__ __forceinline__ double ellipse_factor(const LatLng& g, double k) {
-  // |[0, k a sin, a cos]| / a
-  return sqrt((k * g.sl) * (k * g.sl) + g.cl * g.cl);
+__device__ __forceinline__ double ellipse_factor2(const LatLng& g, double k) {
+  return (k * g.sl) * (k * g.sl) + g.cl * g.cl;   // (|[0, k a sin, a cos]| / a)^2
 }
 
 __device__ __forceinline__ void ellipse_normal(const LatLng& g, double k, double& nx, double& ny,
@@ -73,15 +74,73 @@ __device__ __forceinline__ void ellipse_normal(const LatLng& g, double k, double
   // rotY(lng, [0, a sin, b cos]/|.|)
   const double v1 = g.sl, v2 = k * g.cl;
   const double inv = 1.0 / sqrt(v1 * v1 + v2 * v2);
-  const double n1 = v1 * inv, n2 = v2 * inv;
-  nx = g.sg * n2;
-  ny = n1;
-  nz = g.cg * n2;
+  nx = g.sg * (v2 * inv);
+  ny = v1 * inv;
+  nz = g.cg * (v2 * inv);
 }
 
-__device__ __forceinline__ double layer_R(const double* R, int nL, int idx) {
-  return R[idx < 0 ? idx + nL : idx];
+__device__ __forceinline__ int wrap(int idx, int nL) { return idx < 0 ? idx + nL : idx; }
+
+// R[(c+1)%nL]^2 - R[c]^2 as a double-float (float64 product of the float64
+// difference and sum), R[(c+1)%nL] - R[c] and float copies of R and T.
+__global__ void rb_geom_prep_kernel(int nL, const double* R, const double* T, float2* dR2,
+                                    float* dR, float* R32, float* T32) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nL) return;
+  const int n = (c + 1 < nL) ? c + 1 : 0;
+  const double d = R[n] - R[c];
+  const double q = d * (R[n] + R[c]);
+  float h, l;
+  split_double(q, h, l);
+  dR2[c] = make_float2(h, l);
+  dR[c] = (float)d;
+  R32[c] = (float)R[c];
+  if (T) T32[c] = (float)T[c];
 }
+
+// ---------------- double-float helpers
+struct df {
+  float h, l;
+};
+__device__ __forceinline__ df df_make(double v) {
+  df r;
+  split_double(v, r.h, r.l);
+  return r;
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e += a.l + b.l;
+  df r;
+  r.h = s + e;
+  r.l = e - (r.h - s);
+  return r;
+}
+__device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
+// a * b for a double-float and a float
+__device__ __forceinline__ df df_mulf(df a, float b) {
+  const float p = a.h * b;
+  const float e = fmaf(a.h, b, -p) + a.l * b;
+  df r;
+  r.h = p + e;
+  r.l = e - (r.h - p);
+  return r;
+}
+// sqrt of a positive double-float: one Newton correction of sqrtf(hi)
+__device__ __forceinline__ df df_sqrt(df a) {
+  const float y = sqrtf(a.h);
+  if (y == 0.f) return {0.f, 0.f};
+  const float r = fmaf(-y, y, a.h) + a.l;
+  df o;
+  o.h = y;
+  o.l = r / (2.f * y);
+  const float t = o.h + o.l;
+  o.l = o.l - (t - o.h);
+  o.h = t;
+  return o;
+}
+__device__ __forceinline__ float df_val(df a) { return a.h + a.l; }
+__device__ __forceinline__ double df_d(df a) { return (double)a.h + (double)a.l; }
 
 __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
   const int ray = blockIdx.x;
@@ -91,7 +150,8 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
   const int nL = a.nL;
   const double rNorm = a.R[0];
   const double k = a.k;
-  double* ds_out = a.ds + (size_t)ray * a.max_seg;
+  double* ds_out = a.ds ? a.ds + (size_t)ray * a.max_seg : nullptr;
+  float* hds_out = a.hds ? a.hds + (size_t)ray * a.max_seg : nullptr;
   int* lay_out = a.layer + (size_t)ray * a.max_seg;
   double* r4_out = a.r4ds ? a.r4ds + (size_t)ray * a.max_seg : nullptr;
   double* ll_out = a.latlng ? a.latlng + (size_t)ray * (a.max_seg + 1) * 2 : nullptr;
@@ -121,7 +181,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
       rot_apply(a.rot, b0, b1, z, vx, vy, vz);
       const double r1 = sqrt(vx * vx + vy * vy + vz * vz) * rNorm;
       const LatLng g = latlng_of(vx, vy, vz);
-      const double r2 = rNorm * ellipse_factor(g, k);
+      const double r2 = rNorm * sqrt(ellipse_factor2(g, k));
       d = r1 - r2;
       h = r1 < r2;
     }
@@ -159,13 +219,11 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
   ex *= rNorm;
   ey *= rNorm;
   ez *= rNorm;
-  // ---------------- initial point on the top shell (raypath.py:130-160)
-  LatLng g = latlng_of(ex, ey, ez);
-  double E = ellipse_factor(g, k);
-  double rx = g.sg * (rNorm * g.cl), ry = k * rNorm * g.sl, rz = g.cg * (rNorm * g.cl);
+  // ---------------- initial point, normal and refraction (raypath.py:130-160)
+  const LatLng g0 = latlng_of(ex, ey, ez);
+  double r0x = g0.sg * (rNorm * g0.cl), r0y = k * rNorm * g0.sl, r0z = g0.cg * (rNorm * g0.cl);
   double nx, ny, nz;
-  ellipse_normal(g, k, nx, ny, nz);
-  double rNow = rNorm * E;
+  ellipse_normal(g0, k, nx, ny, nz);
   double sx, sy, sz;
   rot_apply(a.rot, 0.0, 0.0, -1.0, sx, sy, sz);
   {
@@ -178,74 +236,128 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
     sy = nratio * sy + cf * ny;
     sz = nratio * sz + cf * nz;
   }
-  const double mu = sqrt(1.0 - b0 * b0 - b1 * b1);
+  const float mu = (float)sqrt(1.0 - b0 * b0 - b1 * b1);
+  const float omk2 = (float)(1.0 - k * k);
+  // parametrisation r(S) = r0 + S s; S = u - u0
+  double u0 = r0x * sx + r0y * sy + r0z * sz;
+  df u = df_make(u0);
+  df mu0 = df_neg(u);
+  df w = df_make(u0 * u0);
+  float R0sq = (float)(r0x * r0x + r0y * r0y + r0z * r0z);
+  float twou0 = (float)(2.0 * u0);
+  float y0 = (float)r0y, syf = (float)sy;
+  // E^2 - 1 at the current point (step 0 uses the edge's latitude)
+  float em1 = (float)(ellipse_factor2(g0, k) - 1.0);
+  const float kf = (float)k;
+  const float em1_eq = (float)(ellipse_factor2(latlng_of(1.0, 0.0, 1.0), k) - 1.0);
+
   int layer = 0;
   int dir = 1;   // +1 ingress, -1 egress
   int nseg = 0;
   int code = 1;
   while (true) {
-    if (ll_out) {
-      ll_out[2 * nseg] = asin(g.sl) * 180.0 / CUDART_PI;
+    if (ll_out) {   // float64 reconstruction of the current point (drop-in output only)
+      const double S64 = df_d(u) - u0;
+      const LatLng g = nseg == 0 ? g0 : latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
+      ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
       ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
     }
-    double rNext = layer_R(a.R, nL, layer + dir) * E;
-    const double rdots = rx * sx + ry * sy + rz * sz;
-    const double disc = rdots * rdots + rNext * rNext - rNow * rNow;
+    const int j = dir > 0 ? layer : wrap(layer - 1, nL);
+    const float2 q2 = a.dR2[j];
+    df dr2 = {q2.x, q2.y};
+    if (dir < 0) dr2 = df_neg(dr2);                  // R[c-1]^2 - R[c]^2
+    const df D = df_add(dr2, df_mulf(dr2, em1));     // E^2 (R[next]^2 - R[cur]^2)
+    const df wn = df_add(w, D);
+    const bool neg = wn.h < 0.f || (wn.h == 0.f && wn.l < 0.f);
     bool tangent = false;
-    double step;
-    if (disc < 0.0) {
+    float step;
+    df un;
+    if (neg) {
       if (dir == 1) {
         tangent = true;
-        step = -2.0 * rdots;
-        if (step > rNorm) {
+        step = -2.f * df_val(u);
+        if ((double)step > rNorm) {
           code = 2;
           break;
         }
-        rNext = rNow;
+        un = df_neg(u);                              // egress starts at -u, w unchanged
       } else {
         code = 2;
         break;
       }
     } else {
-      const double sq = sqrt(disc);
-      step = (dir == 1) ? (-rdots - sq) : (-rdots + sq);
+      const df r = df_sqrt(wn);
+      un = dir == 1 ? df_neg(r) : r;
+      step = df_val(df_add(un, df_neg(u)));
+      w = wn;
     }
-    if (step < 0.0) {
+    if (step < 0.f) {
       code = 2;
       break;
     }
-    if (a.limb_sec) step = fabs(rNext - rNow) / mu;
+    if (a.limb_sec) {
+      // the secant step moves the point by |rNext - rNow| / mu instead
+      step = tangent ? 0.f : sqrtf(1.f + em1) * fabsf(a.dR[j]) / mu;
+      un = df_add(u, df{step, 0.f});
+      w = df_make(df_d(un) * df_d(un));
+    }
     if (nseg >= a.max_seg) {
       code = 3;
       break;
     }
-    ds_out[nseg] = step;
+    if (ds_out) ds_out[nseg] = (double)step;
+    if (hds_out) hds_out[nseg] = step * 0.5e5f;
     lay_out[nseg] = layer;
-    if (r4_out) r4_out[nseg] = rNow;
+    if (r4_out) r4_out[nseg] = (double)(a.R32[wrap(layer, nL)] * sqrtf(1.f + em1));
     ++nseg;
-    rx += step * sx;
-    ry += step * sy;
-    rz += step * sz;
-    g = latlng_of(rx, ry, rz);
-    E = ellipse_factor(g, k);
+    // advance along the ray
+    u = un;
+    const float S = df_val(df_add(u, mu0));
+    const float rr2 = fmaf(S, S + twou0, R0sq);
+    const float y = fmaf(S, syf, y0);
+    em1 = (y == 0.f) ? em1_eq : -omk2 * __fdividef(y * y, rr2);
     const int dv = tangent ? 0 : dir;
-    rNow = layer_R(a.R, nL, layer + dv) * E;
-    ellipse_normal(g, k, nx, ny, nz);
     layer += dv;
     if (tangent) {
-      dir = -1;      // t_inc = pi/2: next s-update is exactly zero
+      dir = -1;      // t_inc = pi/2: the next s-update is exactly zero
     } else {
-      const double c = -(double)dir * (sx * nx + sy * ny + sz * nz);
-      if (c > 1.0 || c < -1.0) {
-        sx = sy = sz = CUDART_NAN;     // numpy arccos -> nan
-      } else if (c < 0.0) {
-        const double u = (double)dir * 2.0 * c;
-        sx += u * nx;
-        sy += u * ny;
-        sz += u * nz;
+      // c = -dir s.n with n ~ [k x, y, k z]:  c < 0  <=>  dir (k u + (1-k) s_y y) > 0
+      const float un_f = df_val(u);
+      const float val = (float)dir * fmaf(kf, un_f, (1.f - kf) * syf * y);
+      const float tol = 1e-5f * (fabsf(kf * un_f) + fabsf((1.f - kf) * syf * y));
+      if (val > -tol) {   // possible fold: decide and apply in float64
+        const double S64 = df_d(u) - u0;
+        const double rx = r0x + S64 * sx, ry = r0y + S64 * sy, rz = r0z + S64 * sz;
+        const LatLng g = latlng_of(rx, ry, rz);
+        ellipse_normal(g, k, nx, ny, nz);
+        const double c = -(double)dir * (sx * nx + sy * ny + sz * nz);
+        bool moved = false;
+        if (c > 1.0 || c < -1.0) {
+          sx = sy = sz = CUDART_NAN;       // numpy arccos -> nan
+          moved = true;
+        } else if (c < 0.0) {
+          const double wgt = (double)dir * 2.0 * c;
+          sx += wgt * nx;
+          sy += wgt * ny;
+          sz += wgt * nz;
+          moved = true;
+        }
+        if (moved) {   // restart the parametrisation at this point
+          r0x = rx;
+          r0y = ry;
+          r0z = rz;
+          u0 = rx * sx + ry * sy + rz * sz;
+          u = df_make(u0);
+          mu0 = df_neg(u);
+          w = df_make(u0 * u0);
+          R0sq = (float)(rx * rx + ry * ry + rz * rz);
+          twou0 = (float)(2.0 * u0);
+          y0 = (float)ry;
+          syf = (float)sy;
+        }
       }
     }
-    // nr[layer] / nr[layer + dir] (raypath.py:253-264)
+    // nr[layer] / nr[layer + dir] index check (raypath.py:253-264)
     const int nxt = layer + dir;
     if (layer < -nL || layer >= nL || nxt < -nL || nxt >= nL) {
       code = 1;
@@ -253,11 +365,19 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
     }
   }
   if (ll_out && code != 3) {
-    ll_out[2 * nseg] = asin(g.sl) * 180.0 / CUDART_PI;
+    const double S64 = df_d(u) - u0;
+    const LatLng g = latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
+    ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
     ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
   }
   a.nseg[ray] = nseg;
   if (a.end_code) a.end_code[ray] = code;
+}
+
+cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
+                             float* R32, float* T32, cudaStream_t st) {
+  rb_geom_prep_kernel<<<(nL + 127) / 128, 128, 0, st>>>(nL, R, T, dR2, dR, R32, T32);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st) {

@@ -1,18 +1,26 @@
 // Brightness temperature along each ray: the trapezoidal optical-depth scan
 // of Brightness.single (brightness.py:53-117) for sm_103a.
 //
-// One thread per (ray, frequency); a CTA covers a tile of consecutive
-// frequencies of one ray, so the per-segment loads of ds / layer index /
-// temperature are warp-uniform and the absorption loads alpha[layer][f0..f31]
-// are one 128-byte line of the [nL][nf] float32 table (L2 resident).
-//
 // Per segment i (layers ii = layer4ds[i], ii1 = layer4ds[i+1], ds in cm):
 //   tau_{i+1} = tau_i + (a0 + a1) ds / 2                   double-float
 //   W_{i+1}   = a1 exp(-tau_{i+1})      or 2 a1 E2(tau_{i+1}) for 'disc'
 //   intW     += (W_{i+1} + W_i) ds / 2                      compensated fp32
 //   TbL      += (T1 W_{i+1} + T0 W_i) ds / 2                compensated fp32
-// and Tb = T_cmb if TbL < T_cmb else TbL / intW (brightness.py:107-117).
-// The last ds of the path is not used, as in the reference loop.
+// with W_0 = 0, and Tb = T_cmb if TbL < T_cmb else TbL / intW
+// (brightness.py:107-117).  The last ds of the path is not used, as in the
+// reference loop.
+//
+// Fast path (exp weighting): every ray's segments are cut into chunks that
+// are scanned in parallel with a local optical depth starting at 0; since
+// exp(-(tau_a + t)) = exp(-tau_a) exp(-t), chunk sums combine exactly as
+//   intW = sum_c exp(-tau_c) intW_c,  TbL = sum_c exp(-tau_c) TbL_c,
+// tau_c being the optical depth at the chunk's first point.  One CTA covers
+// (128 frequencies, one chunk, one ray); the chunk's ds / layer / T are
+// staged in shared memory so the loop's only global loads are the
+// alpha[layer][f0..f127] rows (coalesced, L2 resident).
+// Sequential path: one thread per (ray, frequency) over the whole path; used
+// for the E2 weighting of b = 'disc' and when per-segment profiles
+// (tau, W, TbL) are requested.
 #include "rb_args.cuh"
 #include <math_constants.h>
 
@@ -32,11 +40,10 @@ __device__ double expint2(double x) {
   if (x <= 1.0) {
     const double euler = 0.57721566490153286061;
     double sum = 0.0;
-    double term = x;   // (-x)^k / k!, starting at k = 1: -x ... built below
     double fact = -x;  // (-x)^1 / 1!
     for (int kk = 2; kk < 60; ++kk) {
       fact *= -x / kk;                 // (-x)^k / k!
-      term = fact / (kk - 1);
+      const double term = fact / (kk - 1);
       sum += term;
       if (fabs(term) < 1e-18 * fabs(sum) + 1e-300) break;
     }
@@ -60,7 +67,6 @@ __device__ double expint2(double x) {
   return h * exp(-x);
 }
 
-
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   const float y = v - c;
   const float t = s + y;
@@ -70,14 +76,15 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 
 __device__ __forceinline__ int wrap_layer(int l, int nL) { return l < 0 ? l + nL : l; }
 
-__global__ void __launch_bounds__(128) rb_tb_kernel(TbArgs a) {
+// ------------------------------------------------------------ sequential
+__global__ void __launch_bounds__(128) rb_tb_seq_kernel(TbArgs a) {
   const int ray = blockIdx.y;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (ray >= a.nb) return;
   const bool valid = f < a.nf;
   const int fi = valid ? f : 0;
   const int nseg = a.nseg[ray];
-  const double* ds = a.ds + (size_t)ray * a.max_seg;
+  const float* hds = a.hds + (size_t)ray * a.max_seg;
   const int* lay = a.layer + (size_t)ray * a.max_seg;
   const size_t pbase = ((size_t)ray * a.nf + fi) * a.max_seg;
   float th = 0.f, tl = 0.f;          // tau (double-float)
@@ -88,16 +95,14 @@ __global__ void __launch_bounds__(128) rb_tb_kernel(TbArgs a) {
     a.W[pbase] = 0.0;
     a.TbL[pbase] = 0.0;
   }
-  // layer indices follow Python semantics: negative values wrap
   int ii = nseg > 0 ? wrap_layer(lay[0], a.nL) : 0;
-  float T0 = nseg > 0 ? (float)a.T[ii] : 0.f;
+  float T0 = nseg > 0 ? a.T32[ii] : 0.f;
   float a0 = nseg > 0 ? a.alpha32[(size_t)ii * a.nf + fi] : 0.f;
   for (int i = 0; i + 1 < nseg; ++i) {
     const int ii1 = wrap_layer(lay[i + 1], a.nL);
-    const float d = (float)(ds[i] * 1.0e5);   // km -> cm
-    const float hd = 0.5f * d;
+    const float hd = hds[i];
     const float a1 = a.alpha32[(size_t)ii1 * a.nf + fi];
-    const float T1 = (float)a.T[ii1];
+    const float T1 = a.T32[ii1];
     const float dtau = (a0 + a1) * hd;
     float s, e;
     two_sum(th, dtau, s, e);
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(128) rb_tb_kernel(TbArgs a) {
     if (a.disc)
       W1 = (float)(2.0 * (double)a1 * expint2((double)th + (double)tl));
     else
-      W1 = a1 * __expf(-th);
+      W1 = a1 * __expf(-th) * (1.f - tl);
     kahan_add(iw, iwc, (W1 + W0) * hd);
     kahan_add(tb, tbc, fmaf(T1, W1, T0 * W0) * hd);
     if (valid && a.tau) {
@@ -124,17 +129,126 @@ __global__ void __launch_bounds__(128) rb_tb_kernel(TbArgs a) {
   if (!valid) return;
   const double TbL = (double)tb - (double)tbc;
   const double IW = (double)iw - (double)iwc;
-  a.Tb[(size_t)ray * a.nf + f] = (TbL < T_CMB) ? T_CMB : TbL / IW;
+  const double out = (TbL < T_CMB) ? T_CMB : TbL / IW;
+  a.Tb[(size_t)ray * a.nf + f] = out;
+  if (a.Tb32) a.Tb32[(size_t)ray * a.nf + f] = (float)out;
   if (a.intW) a.intW[(size_t)ray * a.nf + f] = IW;
 }
 
-// Weighted sum over rays (disc quadrature), one thread per frequency.
-__global__ void rb_disc_avg_kernel(int nb, int nf, const double* Tb, const double* w, double* out) {
+// ------------------------------------------------------------ chunked
+constexpr int TB_CHUNK = 128;
+
+__global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
+  const int ray = blockIdx.z;
+  const int ch = blockIdx.y;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nseg = a.nseg[ray];
+  const int nsteps = nseg - 1;                 // segments used by the scan
+  const int i0 = ch * TB_CHUNK;
+  float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
+  if (i0 >= nsteps) {                          // chunk past the end of this ray
+    if (f < a.nf) part[f] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const int n = min(TB_CHUNK, nsteps - i0);
+  __shared__ int s_off[TB_CHUNK + 1];
+  __shared__ float s_T[TB_CHUNK + 1];
+  __shared__ float s_hd[TB_CHUNK];
+  const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
+  const int* lay = a.layer + (size_t)ray * a.max_seg + i0;
+  for (int t = threadIdx.x; t <= n; t += blockDim.x) {
+    const int l = wrap_layer(lay[t], a.nL);
+    s_off[t] = l * a.nf;
+    s_T[t] = a.T32[l];
+    if (t < n) s_hd[t] = hds[t];
+  }
+  __syncthreads();
+  if (f >= a.nf) return;
+  const float* al = a.alpha32 + f;
+  float th = 0.f, tl = 0.f;
+  float a0 = al[s_off[0]];
+  // W at the chunk's first point relative to exp(-tau_start); W_0 = 0 on a path
+  float W0 = (i0 == 0) ? 0.f : a0;
+  float T0 = s_T[0];
+  float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
+  int i = 0;
+  for (; i + 4 <= n; i += 4) {
+    float an[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) an[k] = al[s_off[i + 1 + k]];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float hd = s_hd[i + k];
+      const float a1 = an[k];
+      const float T1 = s_T[i + 1 + k];
+      float s, e;
+      two_sum(th, (a0 + a1) * hd, s, e);
+      e += tl;
+      th = s + e;
+      tl = e - (th - s);
+      const float W1 = a1 * __expf(-th) * (1.f - tl);
+      kahan_add(iw, iwc, (W1 + W0) * hd);
+      kahan_add(tb, tbc, fmaf(T1, W1, T0 * W0) * hd);
+      W0 = W1;
+      T0 = T1;
+      a0 = a1;
+    }
+  }
+  for (; i < n; ++i) {
+    const float hd = s_hd[i];
+    const float a1 = al[s_off[i + 1]];
+    const float T1 = s_T[i + 1];
+    float s, e;
+    two_sum(th, (a0 + a1) * hd, s, e);
+    e += tl;
+    th = s + e;
+    tl = e - (th - s);
+    const float W1 = a1 * __expf(-th) * (1.f - tl);
+    kahan_add(iw, iwc, (W1 + W0) * hd);
+    kahan_add(tb, tbc, fmaf(T1, W1, T0 * W0) * hd);
+    W0 = W1;
+    T0 = T1;
+    a0 = a1;
+  }
+  part[f] = make_float4(th, tl, iw - iwc, tb - tbc);
+}
+
+// Combine chunk partials of each (ray, frequency) into Tb.
+__global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
+  const int ray = blockIdx.y;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= a.nf) return;
+  const float4* part = a.part + (size_t)ray * a.nchunk * a.nf + f;
+  const int nsteps = a.nseg[ray] - 1;
+  const int nc = nsteps > 0 ? (nsteps + TB_CHUNK - 1) / TB_CHUNK : 0;
+  float ph = 0.f, pl = 0.f;          // optical depth at the chunk start
+  float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
+  for (int c = 0; c < nc; ++c) {
+    const float4 p = part[(size_t)c * a.nf];
+    const float sc = __expf(-ph) * (1.f - pl);
+    kahan_add(iw, iwc, sc * p.z);
+    kahan_add(tb, tbc, sc * p.w);
+    float s, e;
+    two_sum(ph, p.x, s, e);
+    e += pl + p.y;
+    ph = s + e;
+    pl = e - (ph - s);
+  }
+  const float TbL = tb - tbc, IW = iw - iwc;
+  const float out = (TbL < (float)T_CMB) ? (float)T_CMB : TbL / IW;
+  a.Tb[(size_t)ray * a.nf + f] = (double)out;
+  if (a.Tb32) a.Tb32[(size_t)ray * a.nf + f] = out;
+  if (a.intW) a.intW[(size_t)ray * a.nf + f] = (double)IW;
+}
+
+// Weighted sum over rays (disc quadrature), one thread per frequency,
+// compensated float32 over the rays.
+__global__ void rb_disc_avg_kernel(int nb, int nf, const float* Tb32, const double* w, double* out) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
-  double s = 0.0;
-  for (int r = 0; r < nb; ++r) s += w[r] * Tb[(size_t)r * nf + f];
-  out[f] = s;
+  float s = 0.f, c = 0.f;
+  for (int r = 0; r < nb; ++r) kahan_add(s, c, (float)w[r] * Tb32[(size_t)r * nf + f]);
+  out[f] = (double)s - (double)c;
 }
 
 __global__ void rb_e2_kernel(int n, const double* x, double* out) {
@@ -142,16 +256,29 @@ __global__ void rb_e2_kernel(int n, const double* x, double* out) {
   if (i < n) out[i] = expint2(x[i]);
 }
 
-cudaError_t launch_tb(const TbArgs& a, cudaStream_t st) {
+int tb_nchunk(int max_seg) { return (max_seg + TB_CHUNK - 1) / TB_CHUNK; }
+
+cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st) {
   if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
   dim3 grid((a.nf + 127) / 128, a.nb);
-  rb_tb_kernel<<<grid, 128, 0, st>>>(a);
+  rb_tb_seq_kernel<<<grid, 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_disc_avg(int nb, int nf, const double* Tb, const double* w, double* out,
+cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
+  if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
+  dim3 grid((a.nf + 127) / 128, a.nchunk, a.nb);
+  rb_tb_chunk_kernel<<<grid, 128, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dim3 g2((a.nf + 127) / 128, a.nb);
+  rb_tb_combine_kernel<<<g2, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
                             cudaStream_t st) {
-  rb_disc_avg_kernel<<<(nf + 127) / 128, 128, 0, st>>>(nb, nf, Tb, w, out);
+  rb_disc_avg_kernel<<<(nf + 127) / 128, 128, 0, st>>>(nb, nf, Tb32, w, out);
   return cudaGetLastError();
 }
 
