@@ -22,6 +22,13 @@
 //    exact to ~1e-14 over the whole path, which the tangent chord -2u needs.
 //  * disc = w + D < 0 on ingress -> tangent chord ds = -2u, then egress;
 //                      on egress  -> leave the atmosphere (raypath.py:197-209).
+//  * Blocks of 32 steps run in parallel, one step per lane: with the E^2
+//    values at the steps' start points fixed, w after each step is a prefix
+//    sum of D over the lanes.  E^2 depends on the position only weakly, so a
+//    Jacobi iteration (E^2 guessed, points computed, E^2 re-evaluated) reaches
+//    the recurrence's fixed point bitwise in one or two rounds.  Steps with
+//    an event (tangent, exit, fold, end of layers) and blocks that do not
+//    settle within four rounds are taken sequentially.
 #include "rb_args.cuh"
 #include <math_constants.h>
 
@@ -201,12 +208,17 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
     d_last_lane31 = __shfl_sync(0xffffffffu, d, 31);
     z_last_lane31 = __shfl_sync(0xffffffffu, z, 31);
   }
-  if (lane != 0) return;
   if (hit < 0) {
-    a.nseg[ray] = 0;
-    if (a.end_code) a.end_code[ray] = 0;
+    if (lane == 0) {
+      a.nseg[ray] = 0;
+      if (a.end_code) a.end_code[ray] = 0;
+    }
     return;
   }
+  // From here every lane holds the same state (the float64 set-up is
+  // evaluated redundantly, which costs nothing extra per warp); lane 0
+  // writes the outputs of sequential steps, lane i those of the i-th step of
+  // a parallel block.
   double zQ;
   if (hit == 0) {
     zQ = z_hit;    // np.interp on a single point
@@ -250,13 +262,93 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
   float em1 = (float)(ellipse_factor2(g0, k) - 1.0);
   const float kf = (float)k;
   const float em1_eq = (float)(ellipse_factor2(latlng_of(1.0, 0.0, 1.0), k) - 1.0);
+  const unsigned FULL = 0xffffffffu;
 
   int layer = 0;
   int dir = 1;   // +1 ingress, -1 egress
   int nseg = 0;
   int code = 1;
-  while (true) {
-    if (ll_out) {   // float64 reconstruction of the current point (drop-in output only)
+  const bool par_ok = !a.limb_sec && !ll_out;
+  bool done = false;
+  while (!done) {
+    // nr[layer] / nr[layer + dir] index check (raypath.py:253-264) after the
+    // steps of a parallel block
+    if (layer < -nL || layer >= nL || layer + dir < -nL || layer + dir >= nL) {
+      code = 1;
+      break;
+    }
+    // ======== parallel block: up to 32 steps, one per lane
+    int taken = 0;
+    if (par_ok) {
+      const int c = layer + lane * dir;
+      const bool inrange = c >= -nL && c < nL && c + dir >= -nL && c + dir < nL;
+      df dr2 = {0.f, 0.f};
+      if (inrange) {
+        const float2 q2 = a.dR2[dir > 0 ? c : wrap(c - 1, nL)];
+        dr2 = dir > 0 ? df{q2.x, q2.y} : df{-q2.x, -q2.y};
+      }
+      float g = em1;            // E^2 - 1 at this lane's start point (guess)
+      df W = w, un = u;
+      float em1n = em1;
+      int first = 32;
+      bool conv = false;
+      for (int it = 0; it < 4 && !conv; ++it) {
+        const df D = df_add(dr2, df_mulf(dr2, g));
+        df v = D;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float h = __shfl_up_sync(FULL, v.h, o), l = __shfl_up_sync(FULL, v.l, o);
+          if (lane >= o) v = df_add(df{h, l}, v);
+        }
+        W = df_add(w, v);
+        const bool negl = W.h < 0.f || (W.h == 0.f && W.l < 0.f);
+        const df r = df_sqrt(negl ? df{0.f, 0.f} : W);
+        un = dir == 1 ? df_neg(r) : r;
+        const float S = df_val(df_add(un, mu0));
+        const float rr2 = fmaf(S, S + twou0, R0sq);
+        const float y = fmaf(S, syf, y0);
+        em1n = (y == 0.f) ? em1_eq : -omk2 * __fdividef(y * y, rr2);
+        // fold check at the new point (c < 0 <=> dir (k u + (1-k) s_y y) > 0)
+        const float uf = df_val(un);
+        const float val = (float)dir * fmaf(kf, uf, (1.f - kf) * syf * y);
+        const float tol = 1e-5f * (fabsf(kf * uf) + fabsf((1.f - kf) * syf * y));
+        const bool ev = !inrange || negl || val > -tol;
+        const unsigned evm = __ballot_sync(FULL, ev);
+        first = evm ? __ffs(evm) - 1 : 32;
+        float gn = __shfl_up_sync(FULL, em1n, 1);
+        if (lane == 0) gn = em1;
+        const unsigned diff = __ballot_sync(FULL, gn != g);
+        const unsigned below = first >= 32 ? FULL : ((1u << first) - 1u);
+        conv = (diff & below) == 0;
+        g = gn;
+      }
+      if (conv) {
+        taken = min(first, a.max_seg - nseg);
+        if (taken > 0) {
+          const float uph = __shfl_up_sync(FULL, un.h, 1), upl = __shfl_up_sync(FULL, un.l, 1);
+          const df uprev = lane == 0 ? u : df{uph, upl};
+          if (lane < taken) {
+            const float step = df_val(df_add(un, df_neg(uprev)));
+            if (ds_out) ds_out[nseg + lane] = (double)step;
+            if (hds_out) hds_out[nseg + lane] = step * 0.5e5f;
+            lay_out[nseg + lane] = c;
+            if (r4_out) r4_out[nseg + lane] = (double)(a.R32[wrap(c, nL)] * sqrtf(1.f + g));
+          }
+          const int src = taken - 1;
+          u.h = __shfl_sync(FULL, un.h, src);
+          u.l = __shfl_sync(FULL, un.l, src);
+          w.h = __shfl_sync(FULL, W.h, src);
+          w.l = __shfl_sync(FULL, W.l, src);
+          em1 = __shfl_sync(FULL, em1n, src);
+          layer += taken * dir;
+          nseg += taken;
+          continue;   // events at lane `taken` are handled on the next pass
+        }
+      }
+    }
+    // ======== one sequential step (tangent, exit, fold, end of path, or
+    //          a block that did not converge); identical on every lane
+    if (ll_out && lane == 0) {   // float64 reconstruction of the current point
       const double S64 = df_d(u) - u0;
       const LatLng g = nseg == 0 ? g0 : latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
       ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
@@ -305,10 +397,12 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
       code = 3;
       break;
     }
-    if (ds_out) ds_out[nseg] = (double)step;
-    if (hds_out) hds_out[nseg] = step * 0.5e5f;
-    lay_out[nseg] = layer;
-    if (r4_out) r4_out[nseg] = (double)(a.R32[wrap(layer, nL)] * sqrtf(1.f + em1));
+    if (lane == 0) {
+      if (ds_out) ds_out[nseg] = (double)step;
+      if (hds_out) hds_out[nseg] = step * 0.5e5f;
+      lay_out[nseg] = layer;
+      if (r4_out) r4_out[nseg] = (double)(a.R32[wrap(layer, nL)] * sqrtf(1.f + em1));
+    }
     ++nseg;
     // advance along the ray
     u = un;
@@ -364,14 +458,16 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
       break;
     }
   }
-  if (ll_out && code != 3) {
-    const double S64 = df_d(u) - u0;
-    const LatLng g = latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
-    ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
-    ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
+  if (lane == 0) {
+    if (ll_out && code != 3) {
+      const double S64 = df_d(u) - u0;
+      const LatLng g = latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
+      ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
+      ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
+    }
+    a.nseg[ray] = nseg;
+    if (a.end_code) a.end_code[ray] = code;
   }
-  a.nseg[ray] = nseg;
-  if (a.end_code) a.end_code[ray] = code;
 }
 
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
