@@ -175,6 +175,31 @@ int rb_phase_times(rb_handle* h, double* ms, int n);
  * kernel at the current clocks: the roofline denominator of the line sums. */
 int rb_probe_fp32_peak(rb_handle* h, double* tflops);
 
+/* Scratch limit of rb_brightness_noalloc: nb * ceil(max_seg / 128) * nf must
+ * not exceed this many float4 elements (8 MiB, held by every GPU that loads
+ * the library until the process exits). */
+#define RB_NOALLOC_SCRATCH_ELEMS 524288
+
+/* Brightness temperatures from device-resident inputs without allocating
+ * device memory.  No counterpart in the reference: it exists for callers
+ * that cannot call cudaMalloc -- applications that reserve all device
+ * memory up front, plugins running inside a framework that owns the
+ * allocator, real-time loops that forbid allocation (cudaMalloc/cudaFree can
+ * synchronise the device and take unbounded time).
+ * Every array is a device pointer on the calling thread's current device:
+ *   alpha32[nL][nf] absorption (float32, cm^-1), T[nL] K, nseg[nb],
+ *   ds[nb][max_seg] km, layer[nb][max_seg] (negative indices wrap as in
+ *   Python, out-of-range indices are clamped), Tb[nb][nf] output.
+ * The work is enqueued on `stream` (a cudaStream_t) and the call returns
+ * without synchronising.  Its scratch is one fixed file-scope device array
+ * shared by every call, so calls that overlap on the GPU race: serialise
+ * them.  The first call on a device looks up that array's address; make it
+ * before any stream capture.  Sizes beyond RB_NOALLOC_SCRATCH_ELEMS are
+ * rejected with RB_EINVAL. */
+int rb_brightness_noalloc(void* stream, int nL, int nf, const float* alpha32, const double* T,
+                          int nb, const int32_t* nseg, const double* ds, const int32_t* layer,
+                          int max_seg, double* Tb);
+
 /* E2(x) evaluated by the device routine used for b = 'disc' (test hook). */
 int rb_debug_e2(rb_handle* h, int n, const double* x, double* out);
 

@@ -127,6 +127,11 @@ struct rb_handle {
   DBuf d_probe;
 };
 
+namespace rb {
+// Lets other translation units of the library report through rb_last_error.
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace rb
+
 // launchers implemented in the kernel translation units
 namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
