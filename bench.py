@@ -48,6 +48,8 @@ def parse():
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-sample-s', type=float, default=20.0)
+    p.add_argument('--alpha-tiling', default='',
+                   help='line-sum tiling M,W,item_lines (default: automatic)')
     return p.parse_args()
 
 
@@ -279,6 +281,8 @@ def run_gpu(args, rank, world, local_rank):
     eng = _native.Engine(local_rank)
     catalog.upload(eng, wl.lines)
     eng.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    if args.alpha_tiling:
+        eng.set_alpha_tiling(*[int(v) for v in args.alpha_tiling.split(',')])
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
 

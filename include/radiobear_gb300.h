@@ -103,6 +103,14 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
 int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2s, int use_ph3,
                       int h2state);
 
+/* Tiling of the absorption line sums (no reference counterpart: the
+ * reference has no device decomposition).  M frequency slots per thread
+ * (2 or 4), W warps per CTA (1..4), item_lines lines per work item
+ * (multiple of 128).  Zeros select the automatic choice.  Takes effect at
+ * the next call with new frequencies or catalogues; the autotuner
+ * (radiobear_gb300.tune) drives it. */
+int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines);
+
 /* Absorption of nL layers at nf frequencies.
  *   P[nL] bar, T[nL] K, X[RB_NX][nL] mole fractions, freqs[nf] GHz.
  *   scale:      nullable, [nL][RB_NGAS] multipliers (number, per-layer list
@@ -171,8 +179,10 @@ int rb_last_launch_count(rb_handle* h);
 int rb_set_profiling(rb_handle* h, int on);
 int rb_phase_times(rb_handle* h, double* ms, int n);
 
-/* Float32 FMA throughput of the device (TFLOP/s), measured with a probe
- * kernel at the current clocks: the roofline denominator of the line sums. */
+/* Float32 FMA throughput of the device (TFLOP/s), measured with probe
+ * kernels (independent scalar FFMA chains and packed f32x2 FMA chains; the
+ * higher rate is returned) at the current clocks: the roofline denominator
+ * of the line sums. */
 int rb_probe_fp32_peak(rb_handle* h, double* tflops);
 
 /* Scratch limit of rb_brightness_noalloc: nb * ceil(max_seg / 128) * nf must

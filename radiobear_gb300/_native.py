@@ -38,7 +38,7 @@ FAMILY_COLUMNS = {
 EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set_lines',
            'rb_set_formalisms', 'rb_alpha', 'rb_raypath', 'rb_brightness', 'rb_forward',
            'rb_forward_device', 'rb_last_launch_count', 'rb_set_profiling', 'rb_phase_times',
-           'rb_probe_fp32_peak', 'rb_debug_e2')
+           'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling')
 
 _lib = None
 _lock = threading.Lock()
@@ -86,6 +86,7 @@ def load_library(path=None):
         lib.rb_set_profiling.argtypes = [_vp, c_int]
         lib.rb_phase_times.argtypes = [_vp, _d, c_int]
         lib.rb_probe_fp32_peak.argtypes = [_vp, _d]
+        lib.rb_set_alpha_tiling.argtypes = [_vp, c_int, c_int, c_int]
         for name in EXPORTS:
             getattr(lib, name).restype = getattr(lib, name).restype or c_int
         lib.rb_last_error.restype = ctypes.c_char_p
@@ -245,6 +246,12 @@ class Engine:
 
     def last_launch_count(self):
         return int(self.lib.rb_last_launch_count(self._h))
+
+    def set_alpha_tiling(self, M=0, W=0, item_lines=0):
+        """Line-sum tiling: M slots per thread, W warps per CTA, lines per work
+        item (zeros: automatic)."""
+        _check(self.lib, self.lib.rb_set_alpha_tiling(self._h, int(M), int(W), int(item_lines)),
+               'rb_set_alpha_tiling')
 
     def set_profiling(self, on=True):
         _check(self.lib, self.lib.rb_set_profiling(self._h, int(on)), 'rb_set_profiling')

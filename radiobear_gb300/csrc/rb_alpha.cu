@@ -1,21 +1,27 @@
 // Absorption coefficient of every (layer, frequency): the per-gas line sums
 // of radioBEAR's Jupiter formalisms, restated for sm_103a.
 //
-//   rb_layer_prep_kernel  one thread per layer: partial pressures, width /
-//                         shift / coupling coefficients and strength
-//                         prefactors (float32 with float64 only for the
-//                         temperature coefficient of the strengths).
-//   rb_alpha_kernel       one CTA per (layer, frequency tile), two frequency
-//                         slots per thread evaluated with packed f32x2
-//                         arithmetic.  Lines are staged in shared-memory
-//                         chunks: each thread builds one line's layer-
-//                         dependent record (duplicated into both halves of
-//                         a 64-bit pair, so the sweep loads operands ready
-//                         for f32x2), then every thread sweeps the chunk.
-//                         Sums are float32 with compensated (Kahan)
-//                         accumulation every 16 lines; the prefactor
-//                         (mantissa x 2^exponent), unit conversion, clamp,
-//                         blend and scaling are applied per slot at the end.
+//   rb_layer_prep_kernel     eight threads per layer: partial pressures,
+//                            width / shift / coupling coefficients and
+//                            strength prefactors (float32 with float64 only
+//                            for the temperature coefficient of the
+//                            strengths).
+//   rb_alpha_lines_kernel<M> persistent line sums.  Work items are (line
+//                            range of one family, layer, frequency tile),
+//                            taken from a global counter heaviest family
+//                            first.  A CTA stages the layer-dependent
+//                            records of 128 lines at a time in shared memory
+//                            (double-buffered, one barrier per chunk), lines
+//                            packed in pairs as f32x2; each thread sweeps
+//                            them for M frequency slots ("chains") with
+//                            packed f32x2 arithmetic, two line pairs sharing
+//                            one reciprocal, Kahan-compensated every 16
+//                            lines.  One float per (item, slot) goes to a
+//                            scratch table; the CTA finishing the last item
+//                            of a (layer, tile) assembles it: family sums,
+//                            prefactors (mantissa x 2^exponent), units,
+//                            clamp, blend and scaling; float32 total for the
+//                            brightness scan, optional float64 outputs.
 //
 // Numerics (per line l, frequency f, F = f^2):
 //   Ben-Reuven  S_l [(g-z) F + (g+z) K_l] / [(F - K_l)^2 + 4 F g^2],
@@ -24,14 +30,18 @@
 //   VVW         S_l df [1/((f-fo)^2+df^2) + 1/((f+fo)^2+df^2) - 2/(750^2+df^2)]
 //                                                         (h2o_bk.py:174-187)
 // with the common factor f^2 (and the 1/fo^2 of (f/fo)^2, folded into S_l)
-// taken out of the sum.  F - K is a double-float difference for lines whose
-// centre lies within [0.75 fmin, 1.3 fmax] of the warp's frequencies (there
-// float32 would cancel); elsewhere plain float32 is exact to a few ulp.
-// Pairs of lines share one reciprocal: n1/d1 + n2/d2 = (n1 d2 + n2 d1)/(d1 d2).
+// taken out of the sum.  For lines whose centre lies within [0.75 fmin,
+// 1.3 fmax] of a chain's 32 frequencies the denominator is formed from the
+// double-float difference F - K (float32 would cancel there); elsewhere it is
+// expanded as F (F + G4 - 2K) + K^2 (VVW: den1 den2 = F (F + 2(df^2 - fo^2))
+// + (fo^2 + df^2)^2), whose rounding error is at most ~18 ulp outside that
+// window, in two operations instead of five.
 // Strengths: S'_l = 2^(l2I_l + cE E_l - M2) with the exponent formed as a
 // double-float and split into integer and fractional parts before exp2.
 #include "rb_args.cuh"
 #include <math_constants.h>
+
+#include <algorithm>
 
 namespace rb {
 
@@ -68,23 +78,32 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
   return d;
 }
-__device__ __forceinline__ f2 rcp2(f2 v) { return pk(rcp_approx(lo2(v)), rcp_approx(hi2(v))); }
 __device__ __forceinline__ f2 dup(float a) { return pk(a, a); }
 
 // Kahan-compensated pair of sums; `part` collects a block of terms.
+// The running block sum is kept as two scalars (p0, p1) so the reciprocal
+// and the final multiply-add of each term need no repacking.
 struct Acc2 {
-  f2 s, c, part;
-  __device__ __forceinline__ void init() { s = c = part = 0ull; }
+  f2 s, c;
+  float p0, p1;
+  __device__ __forceinline__ void init() {
+    s = c = 0ull;
+    p0 = p1 = 0.f;
+  }
   __device__ __forceinline__ void flush() {
     const f2 mone = dup(-1.f);
-    const f2 y = fma2(c, mone, part);     // part - c
+    const f2 y = fma2(c, mone, pk(p0, p1));   // part - c
     const f2 t = add2(s, y);
-    c = fma2(y, mone, fma2(s, mone, t));  // (t - s) - y
+    c = fma2(y, mone, fma2(s, mone, t));     // (t - s) - y
     s = t;
-    part = 0ull;
+    p0 = p1 = 0.f;
   }
-  __device__ __forceinline__ float v0() const { return lo2(s) - lo2(c); }
-  __device__ __forceinline__ float v1() const { return hi2(s) - hi2(c); }
+  // p += N / D, both halves
+  __device__ __forceinline__ void add_div(f2 N, f2 D) {
+    p0 = fmaf(lo2(N), rcp_approx(lo2(D)), p0);
+    p1 = fmaf(hi2(N), rcp_approx(hi2(D)), p1);
+  }
+  __device__ __forceinline__ float value() const { return (lo2(s) - lo2(c)) + (hi2(s) - hi2(c)); }
 };
 
 // ------------------------------------------------------------------ constants
@@ -127,8 +146,24 @@ __device__ __forceinline__ void set_cE(LayerFam& F, double cE2) {
   F.cEl = (float)(cE2 - (double)F.cEh);
 }
 
-__global__ void __launch_bounds__(64) rb_layer_prep_kernel(PrepArgs a) {
-  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void zero_fam(LayerFam& F) {
+  F.fm = 0.f;
+  F.fe = 0;
+  F.cEh = F.cEl = 0.f;
+  F.M2 = 0.f;
+  for (int s = 0; s < 2; ++s)
+    for (int k = 0; k < 8; ++k) F.c[s][k] = 0.f;
+}
+
+// Eight threads per layer, one per part of the layer's parameters:
+//   0 shared scalars (P, T, NH3 formalism choice, scales, H2 CIA),
+//   1 NH3 inversion, 2 rotational, 3 nu2, 4 nh3_sjs, 5 H2S, 6 PH3, 7 H2O.
+constexpr int PREP_PARTS = 8;
+
+__global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = gid / PREP_PARTS, part = gid % PREP_PARTS;
+  if (gid == 0 && a.counter) *a.counter = 0;
   if (L >= a.nL) return;
   const int nL = a.nL;
   const double Pd = a.P[L], Td = a.T[L];
@@ -138,340 +173,179 @@ __global__ void __launch_bounds__(64) rb_layer_prep_kernel(PrepArgs a) {
   const float Pch4 = (float)(Pd * X[X_CH4 * nL + L]), Pnh3 = (float)(Pd * X[X_NH3 * nL + L]);
   const float Ph2o = (float)(Pd * X[X_H2O * nL + L]), Ph2s = (float)(Pd * X[X_H2S * nL + L]);
   const float Pph3 = (float)(Pd * X[X_PH3 * nL + L]);
-  LayerParams o;
-  o.P = P;
-  o.T = T;
-  for (int f = 0; f < NFAM; ++f) {
-    o.fam[f].fm = 0.f;
-    o.fam[f].fe = 0;
-    o.fam[f].cEh = o.fam[f].cEl = 0.f;
-    o.fam[f].M2 = 0.f;
-    for (int s = 0; s < 2; ++s)
-      for (int k = 0; k < 8; ++k) o.fam[f].c[s][k] = 0.f;
-  }
+  LayerParams& o = a.out[L];
   // strength temperature coefficients, log2 units, float64 (the only
   // float64 of the absorption path: 1/T - 1/T0 cancels near T0)
   const double invT = 1.0 / Td;
-  const double cE300 = -(invT - 1.0 / 300.0) * (19.858252418E-24 / 1.38E-23) * LOG2E;  // nh3_hs
-  const double cE296g = -(invT - 1.0 / 296.0) * 1.438396 * LOG2E;                      // sjs, h2s
-  const double cE300g = -(invT - 1.0 / 300.0) * 1.438396 * LOG2E;                      // ph3
-  const double cEh2o = (1.0 - 300.0 * invT) * LOG2E;                                   // h2o
   // NH3 formalism choice (nh3_hs_sjs.py:6-26)
-  o.use_hs = 0;
-  o.use_sjs = 0;
-  o.blendW = 0.f;
+  int use_hs = 0, use_sjs = 0;
+  float blendW = 0.f;
   const int mode = a.cfg.nh3_mode;
   if (mode == NH3_HS) {
-    o.use_hs = 1;
+    use_hs = 1;
   } else if (mode == NH3_SJS) {
-    o.use_sjs = 1;
-    o.blendW = 1.f;
+    use_sjs = 1;
+    blendW = 1.f;
   } else if (mode == NH3_HS_SJS) {
     if (Pd < 400.0) {
-      o.use_hs = 1;
+      use_hs = 1;
     } else if (Pd > 2000.0) {
-      o.use_sjs = 1;
-      o.blendW = 1.f;
+      use_sjs = 1;
+      blendW = 1.f;
     } else {
-      o.use_hs = 1;
-      o.use_sjs = 1;
-      o.blendW = (float)((Pd - 400.0) / (2000.0 - 400.0));
+      use_hs = 1;
+      use_sjs = 1;
+      blendW = (float)((Pd - 400.0) / (2000.0 - 400.0));
     }
   }
   const float Tdiv = 300.f / T;
   const float lTdiv = log2f(Tdiv);
   const float l295 = log2f(295.f / T);
   const float hs_base = HS_COEF * (Pnh3 / 300.f) * pw(lTdiv, 3.5f) * GHZ_INVCM;
-  {  // NH3 inversion (nh3_hs.py:137-229)
-    LayerFam& F = o.fam[FAM_NH3_INV];
-    for (int s = 0; s < 2; ++s) {
-      const float* c = INV_SET[s];
-      F.c[s][0] = c[0] * Ph2 * pw(lTdiv, c[3]) + c[1] * Phe * pw(lTdiv, c[4]);
-      F.c[s][1] = c[2] * Pnh3 * pw(l295, c[5]);
-      F.c[s][3] = c[6] * Ph2 * pw(lTdiv, c[9]) + c[7] * Phe * pw(lTdiv, c[10]);
-      F.c[s][4] = c[8] * Pnh3 * pw(l295, c[11]);
-      F.c[s][6] = c[12];
+  const double cE300 = -(invT - 1.0 / 300.0) * (19.858252418E-24 / 1.38E-23) * LOG2E;  // nh3_hs
+  LayerFam F;
+  zero_fam(F);
+  switch (part) {
+    case 0: {
+      o.P = P;
+      o.T = T;
+      o.use_hs = use_hs;
+      o.use_sjs = use_sjs;
+      o.blendW = blendW;
+      for (int g = 0; g < NGAS; ++g) o.scale[g] = a.scale ? (float)a.scale[(size_t)L * NGAS + g] : 1.f;
+      if (a.done)
+        for (int t = 0; t < a.ntile; ++t) a.done[(size_t)L * a.ntile + t] = 0;
+      // H2 CIA (h2_jj_ddb.py:7-38)
+      const float th = 273.f / T;
+      const float lth = log2f(th);
+      float pre;
+      if (a.cfg.h2state == 'n') {
+        pre = fminf(pw(log2f(T / 40.f), 2.5f), 1.f);
+      } else {
+        pre = fminf(pw(log2f(T / 55.f), 2.7f), 1.f);
+        pre = fminf(pre * pw(log2f(T / 120.f), 0.55f), 1.f);
+      }
+      o.h2_cia = 3.9522E-14f * Ph2 * pre *
+                 (Ph2 * pw(lth, 3.12f) + 1.382f * Phe * pw(lth, 2.24f) + 9.322f * Pch4 * pw(lth, 3.34f));
+      return;
     }
-    set_cE(F, cE300);
-    set_fac(F, hs_base * TWO_OVER_PI, scale_bound(a, FAM_NH3_INV, (float)cE300));
-  }
-  {  // NH3 rotational (nh3_hs.py:232-265)
-    LayerFam& F = o.fam[FAM_NH3_ROT];
-    F.c[0][1] = 0.2984f * Ph2 * pw(lTdiv, 0.8730f);
-    F.c[0][2] = 0.75f * Phe * pw(lTdiv, 0.66666667f);
-    F.c[0][3] = 3.1789f * Pnh3 * Tdiv;
-    set_cE(F, cE300);
-    set_fac(F, 2.4268f * hs_base * FOUR_OVER_PI, scale_bound(a, FAM_NH3_ROT, (float)cE300));
-  }
-  {  // NH3 nu2 (nh3_hs.py:269-302); per-line widths 1.4 / 0.68 / 9.5
-    LayerFam& F = o.fam[FAM_NH3_V2];
-    F.c[0][1] = Ph2 * pw(lTdiv, 0.73f);
-    F.c[0][2] = Phe * pw(lTdiv, 0.5716f);
-    F.c[0][3] = Pnh3 * Tdiv;
-    set_cE(F, cE300);
-    set_fac(F, 1.1206f * hs_base * FOUR_OVER_PI, scale_bound(a, FAM_NH3_V2, (float)cE300));
-  }
-  if (o.use_sjs) {  // NH3 sjs (nh3_sjs.py:37-124)
-    LayerFam& F = o.fam[FAM_NH3_SJS];
-    const float rexp = 8.79f * expf(-T / 83.0f);
-    const float GH2a = powf(expf(9.024f - T / 20.3f) - 0.9918f + Ph2, rexp);
-    float J[7] = {1.690f, 0.750f, 0.6f, 1.350f, 0.300f, 0.200f, -0.45f};
-    float S[7];
-    if (GH2a < 1e-12f) {
-      for (int k = 0; k < 7; ++k) S[k] = J[k];
-    } else {
-      const float g = 2.34f * (1.0f - 2.122f * expf(-T / 116.8f) / GH2a);
-      const double gd = g;   // the ZH2 polynomial cancels: evaluate in float64
-      S[0] = g;
-      S[1] = 0.46f + T / 3000.0f;
-      S[2] = 0.74f;
-      S[3] = (float)(5.7465 + gd * (-7.7644 + gd * (9.1931 + gd * (-5.6816 + gd * 1.2307))));
-      S[4] = 0.28f - T / 1750.0f;
-      S[5] = 0.50f;
-      S[6] = -0.45f;
+    case 1: {  // NH3 inversion (nh3_hs.py:137-229)
+      for (int s = 0; s < 2; ++s) {
+        const float* c = INV_SET[s];
+        F.c[s][0] = c[0] * Ph2 * pw(lTdiv, c[3]) + c[1] * Phe * pw(lTdiv, c[4]);
+        F.c[s][1] = c[2] * Pnh3 * pw(l295, c[5]);
+        F.c[s][3] = c[6] * Ph2 * pw(lTdiv, c[9]) + c[7] * Phe * pw(lTdiv, c[10]);
+        F.c[s][4] = c[8] * Pnh3 * pw(l295, c[11]);
+        F.c[s][6] = c[12];
+      }
+      set_cE(F, cE300);
+      set_fac(F, hs_base * TWO_OVER_PI, scale_bound(a, FAM_NH3_INV, (float)cE300));
+      o.fam[FAM_NH3_INV] = F;
+      return;
     }
-    const float tt = pw(log2f(296.f / T), 2.f / 3.f);
-    for (int s = 0; s < 2; ++s) {
-      const float* c = s == 0 ? J : S;
-      o.sjs[s][0] = tt * (c[0] * Ph2 + c[1] * Phe);
-      o.sjs[s][1] = tt * (c[2] * Pnh3);
-      o.sjs[s][2] = tt * (c[3] * Ph2 + c[4] * Phe);
-      o.sjs[s][3] = tt * (c[5] * Pnh3);
-      o.sjs[s][4] = c[6] * Pnh3;
+    case 2: {  // NH3 rotational (nh3_hs.py:232-265)
+      F.c[0][1] = 0.2984f * Ph2 * pw(lTdiv, 0.8730f);
+      F.c[0][2] = 0.75f * Phe * pw(lTdiv, 0.66666667f);
+      F.c[0][3] = 3.1789f * Pnh3 * Tdiv;
+      set_cE(F, cE300);
+      set_fac(F, 2.4268f * hs_base * FOUR_OVER_PI, scale_bound(a, FAM_NH3_ROT, (float)cE300));
+      o.fam[FAM_NH3_ROT] = F;
+      return;
     }
-    const float Pscale = 1.0f + P / 1.0E5f;
-    set_cE(F, cE296g);
-    set_fac(F, 7.244E+21f * (Pnh3 / 296.f) * pw(log2f(296.f / T), 3.5f) * Pscale * GHZ_INVCM * TWO_OVER_PI,
-            scale_bound(a, FAM_NH3_SJS, (float)cE296g));
-  } else {
-    for (int s = 0; s < 2; ++s)
-      for (int k = 0; k < 5; ++k) o.sjs[s][k] = 0.f;
-  }
-  {  // H2S (h2s_ddb.py:42-87)
-    LayerFam& F = o.fam[FAM_H2S];
-    const float l296 = log2f(296.f / T);
-    const float t7 = pw(l296, 0.7f);
-    F.c[0][0] = t7 * (1.960f * Ph2 + 1.200f * Phe);
-    F.c[0][1] = t7 * Ph2s;
-    F.c[0][5] = 1.f;                     // zeta = gamma
-    F.c[0][7] = 1.28f * Ph2s;            // delta
-    set_cE(F, cE296g);
-    set_fac(F, 7.244E+21f * (Ph2s / 296.f) * pw(l296, 3.5f) * GHZ_INVCM * TWO_OVER_PI,
-            scale_bound(a, FAM_H2S, (float)cE296g));
-  }
-  {  // PH3 (ph3_jh.py:64-108)
-    LayerFam& F = o.fam[FAM_PH3];
-    F.c[0][1] = pw(lTdiv, 2.f / 3.f) * (3.2930f * Ph2 + 1.6803f * Phe);
-    F.c[0][2] = Tdiv * 4.2157f * Pph3;
-    set_cE(F, cE300g);
-    set_fac(F, 7.244E+21f * (Pph3 / 300.f) * pw(lTdiv, 3.5f) * GHZ_INVCM * TWO_OVER_PI,
-            scale_bound(a, FAM_PH3, (float)cE300g));
-  }
-  {  // H2O lines (h2o_bk.py:80-99) and continuum (102-121)
-    LayerFam& F = o.fam[FAM_H2O];
-    const float Theta = Tdiv;
-    const float lTh = lTdiv;
-    const float density = (Ph2o / (8.314472e-5f * T)) * (0.997317f * 6.0221415e17f);
-    F.c[0][0] = lTh;
-    F.c[0][1] = Ph2o;
-    F.c[0][2] = Ph2;
-    F.c[0][3] = Phe;
-    set_cE(F, cEh2o);
-    set_fac(F, 4.342945e-4f * density * pw(lTh, 2.5f) / DB_PER_INVCM,
-            scale_bound(a, FAM_H2O, (float)cEh2o));
-    const float Cf_he = 1.0e6f * 1.03562010226e-10f, Cf_h2 = 1.0e6f * 5.07722009423e-11f;
-    const float th3 = Theta * Theta * Theta;
-    const float foreign = Cf_he * Phe * Ph2o * th3 + Cf_h2 * Ph2 * Ph2o * th3;
-    const float selfc = 3.1e-07f * pw(lTh, 12.f) * ((Ph2o * 1000.f) * (Ph2o * 1000.f));
-    o.h2o_cont = (4.342945f * foreign + 4.342945f * selfc) / DB_PER_INVCM;
-  }
-  {  // H2 CIA (h2_jj_ddb.py:7-38)
-    const float th = 273.f / T;
-    const float lth = log2f(th);
-    float pre;
-    if (a.cfg.h2state == 'n') {
-      pre = fminf(pw(log2f(T / 40.f), 2.5f), 1.f);
-    } else {
-      pre = fminf(pw(log2f(T / 55.f), 2.7f), 1.f);
-      pre = fminf(pre * pw(log2f(T / 120.f), 0.55f), 1.f);
+    case 3: {  // NH3 nu2 (nh3_hs.py:269-302); per-line widths 1.4 / 0.68 / 9.5
+      F.c[0][1] = Ph2 * pw(lTdiv, 0.73f);
+      F.c[0][2] = Phe * pw(lTdiv, 0.5716f);
+      F.c[0][3] = Pnh3 * Tdiv;
+      set_cE(F, cE300);
+      set_fac(F, 1.1206f * hs_base * FOUR_OVER_PI, scale_bound(a, FAM_NH3_V2, (float)cE300));
+      o.fam[FAM_NH3_V2] = F;
+      return;
     }
-    o.h2_cia = 3.9522E-14f * Ph2 * pre *
-               (Ph2 * pw(lth, 3.12f) + 1.382f * Phe * pw(lth, 2.24f) + 9.322f * Pch4 * pw(lth, 3.34f));
+    case 4: {  // NH3 sjs (nh3_sjs.py:37-124)
+      float sj[2][5] = {{0.f, 0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f, 0.f}};
+      if (use_sjs) {
+        const double cE296g = -(invT - 1.0 / 296.0) * 1.438396 * LOG2E;
+        const float rexp = 8.79f * expf(-T / 83.0f);
+        const float GH2a = powf(expf(9.024f - T / 20.3f) - 0.9918f + Ph2, rexp);
+        float J[7] = {1.690f, 0.750f, 0.6f, 1.350f, 0.300f, 0.200f, -0.45f};
+        float S[7];
+        if (GH2a < 1e-12f) {
+          for (int k = 0; k < 7; ++k) S[k] = J[k];
+        } else {
+          const float g = 2.34f * (1.0f - 2.122f * expf(-T / 116.8f) / GH2a);
+          const double gd = g;   // the ZH2 polynomial cancels: evaluate in float64
+          S[0] = g;
+          S[1] = 0.46f + T / 3000.0f;
+          S[2] = 0.74f;
+          S[3] = (float)(5.7465 + gd * (-7.7644 + gd * (9.1931 + gd * (-5.6816 + gd * 1.2307))));
+          S[4] = 0.28f - T / 1750.0f;
+          S[5] = 0.50f;
+          S[6] = -0.45f;
+        }
+        const float tt = pw(log2f(296.f / T), 2.f / 3.f);
+        for (int s = 0; s < 2; ++s) {
+          const float* c = s == 0 ? J : S;
+          sj[s][0] = tt * (c[0] * Ph2 + c[1] * Phe);
+          sj[s][1] = tt * (c[2] * Pnh3);
+          sj[s][2] = tt * (c[3] * Ph2 + c[4] * Phe);
+          sj[s][3] = tt * (c[5] * Pnh3);
+          sj[s][4] = c[6] * Pnh3;
+        }
+        const float Pscale = 1.0f + P / 1.0E5f;
+        set_cE(F, cE296g);
+        set_fac(F, 7.244E+21f * (Pnh3 / 296.f) * pw(log2f(296.f / T), 3.5f) * Pscale * GHZ_INVCM * TWO_OVER_PI,
+                scale_bound(a, FAM_NH3_SJS, (float)cE296g));
+      }
+      for (int s = 0; s < 2; ++s)
+        for (int k = 0; k < 5; ++k) o.sjs[s][k] = sj[s][k];
+      o.fam[FAM_NH3_SJS] = F;
+      return;
+    }
+    case 5: {  // H2S (h2s_ddb.py:42-87)
+      const double cE296g = -(invT - 1.0 / 296.0) * 1.438396 * LOG2E;
+      const float l296 = log2f(296.f / T);
+      const float t7 = pw(l296, 0.7f);
+      F.c[0][0] = t7 * (1.960f * Ph2 + 1.200f * Phe);
+      F.c[0][1] = t7 * Ph2s;
+      F.c[0][5] = 1.f;                     // zeta = gamma
+      F.c[0][7] = 1.28f * Ph2s;            // delta
+      set_cE(F, cE296g);
+      set_fac(F, 7.244E+21f * (Ph2s / 296.f) * pw(l296, 3.5f) * GHZ_INVCM * TWO_OVER_PI,
+              scale_bound(a, FAM_H2S, (float)cE296g));
+      o.fam[FAM_H2S] = F;
+      return;
+    }
+    case 6: {  // PH3 (ph3_jh.py:64-108)
+      const double cE300g = -(invT - 1.0 / 300.0) * 1.438396 * LOG2E;
+      F.c[0][1] = pw(lTdiv, 2.f / 3.f) * (3.2930f * Ph2 + 1.6803f * Phe);
+      F.c[0][2] = Tdiv * 4.2157f * Pph3;
+      set_cE(F, cE300g);
+      set_fac(F, 7.244E+21f * (Pph3 / 300.f) * pw(lTdiv, 3.5f) * GHZ_INVCM * TWO_OVER_PI,
+              scale_bound(a, FAM_PH3, (float)cE300g));
+      o.fam[FAM_PH3] = F;
+      return;
+    }
+    default: {  // H2O lines (h2o_bk.py:80-99) and continuum (102-121)
+      const double cEh2o = (1.0 - 300.0 * invT) * LOG2E;
+      const float Theta = Tdiv;
+      const float lTh = lTdiv;
+      const float density = (Ph2o / (8.314472e-5f * T)) * (0.997317f * 6.0221415e17f);
+      F.c[0][0] = lTh;
+      F.c[0][1] = Ph2o;
+      F.c[0][2] = Ph2;
+      F.c[0][3] = Phe;
+      set_cE(F, cEh2o);
+      set_fac(F, 4.342945e-4f * density * pw(lTh, 2.5f) / DB_PER_INVCM,
+              scale_bound(a, FAM_H2O, (float)cEh2o));
+      o.fam[FAM_H2O] = F;
+      const float Cf_he = 1.0e6f * 1.03562010226e-10f, Cf_h2 = 1.0e6f * 5.07722009423e-11f;
+      const float th3 = Theta * Theta * Theta;
+      const float foreign = Cf_he * Phe * Ph2o * th3 + Cf_h2 * Ph2 * Ph2o * th3;
+      const float selfc = 3.1e-07f * pw(lTh, 12.f) * ((Ph2o * 1000.f) * (Ph2o * 1000.f));
+      o.h2o_cont = (4.342945f * foreign + 4.342945f * selfc) / DB_PER_INVCM;
+      return;
+    }
   }
-  for (int g = 0; g < NGAS; ++g) o.scale[g] = a.scale ? (float)a.scale[(size_t)L * NGAS + g] : 1.f;
-  a.out[L] = o;
-}
-
-// ------------------------------------------------------------------ records
-constexpr int CHUNK = 128;      // lines per shared-memory chunk (= max threads per CTA)
-
-// S' = 2^(l2I + cE E - M2), exponent as a double-float, split before exp2
-__device__ __forceinline__ float line_strength(const LineTable& t, const LayerFam& F, int li) {
-  const float Eh = t.Eh[li], El = t.El[li];
-  const float ph = F.cEh * Eh;
-  const float pl = fmaf(F.cEh, Eh, -ph) + fmaf(F.cEh, El, F.cEl * Eh);
-  float s, e;
-  two_sum(t.l2Ih[li] - F.M2, ph, s, e);
-  const float lo = e + pl + t.l2Il[li];
-  const float ti = rintf(s);
-  const float tf = (s - ti) + lo;
-  if (ti < -140.f) return 0.f;
-  return ldexpf(exp2f(tf), (int)ti);
-}
-
-// Ben-Reuven record: {(-K,-K), (G4,G4)}, {(Na,Na), (Nb,Nb)}, and (-KL,-KL)
-__device__ __forceinline__ void br_record(const LineTable& t, const float* c, int li, float S,
-                                          ulonglong2* A, ulonglong2* B, f2* KL) {
-  const float w1 = t.w1[li];
-  const float w2 = t.w2[li];
-  const float g = c[0] + c[1] * w1 + c[2] * w2;
-  const float z = c[3] + c[4] * w1 + c[5] * g;
-  const float d = c[6] * g + c[7];
-  const float fo = t.ch[li];
-  const float small = fmaf(2.f * fo + d, d, (g - z) * (g + z));   // 2 fo d + d^2 + g^2 - z^2
-  float KH, e;
-  two_sum(t.c2h[li], small, KH, e);
-  const float kl = e + t.c2l[li];
-  *A = make_ulonglong2(dup(-KH), dup(4.f * g * g));
-  *B = make_ulonglong2(dup(S * (g - z)), dup(S * (g + z) * (KH + kl)));
-  *KL = dup(-kl);
-}
-
-// ------------------------------------------------------------------ sweeps
-template <bool PRECISE>
-__device__ __forceinline__ void br_pair(const ulonglong2 a1, const ulonglong2 b1, f2 k1,
-                                        const ulonglong2 a2, const ulonglong2 b2, f2 k2, f2 F,
-                                        f2 FL, f2& part) {
-  f2 d1 = add2(F, a1.x), d2 = add2(F, a2.x);
-  if (PRECISE) {
-    d1 = add2(d1, add2(FL, k1));
-    d2 = add2(d2, add2(FL, k2));
-  }
-  const f2 den1 = fma2(d1, d1, mul2(a1.y, F));
-  const f2 den2 = fma2(d2, d2, mul2(a2.y, F));
-  const f2 n1 = fma2(b1.x, F, b1.y);
-  const f2 n2 = fma2(b2.x, F, b2.y);
-  const f2 N = fma2(n1, den2, mul2(n2, den1));
-  part = fma2(N, rcp2(mul2(den1, den2)), part);
-}
-
-template <bool PRECISE>
-__device__ __forceinline__ void br_sweep(const ulonglong2* __restrict__ A,
-                                         const ulonglong2* __restrict__ B,
-                                         const f2* __restrict__ KL, int b, int e, f2 F, f2 FL,
-                                         Acc2& acc) {
-  int l = b;
-  for (; l + 16 <= e; l += 16) {
-#pragma unroll
-    for (int p = 0; p < 16; p += 2)
-      br_pair<PRECISE>(A[l + p], B[l + p], PRECISE ? KL[l + p] : 0ull, A[l + p + 1], B[l + p + 1],
-                       PRECISE ? KL[l + p + 1] : 0ull, F, FL, acc.part);
-    acc.flush();
-  }
-  for (; l + 1 < e; l += 2)
-    br_pair<PRECISE>(A[l], B[l], PRECISE ? KL[l] : 0ull, A[l + 1], B[l + 1],
-                     PRECISE ? KL[l + 1] : 0ull, F, FL, acc.part);
-  if (l < e) {
-    const ulonglong2 a1 = A[l], b1 = B[l];
-    f2 d1 = add2(F, a1.x);
-    if (PRECISE) d1 = add2(d1, add2(FL, KL[l]));
-    const f2 den1 = fma2(d1, d1, mul2(a1.y, F));
-    acc.part = fma2(fma2(b1.x, F, b1.y), rcp2(den1), acc.part);
-  }
-  acc.flush();
-}
-
-// Gross record: {(-K,-K), (G4,G4)}, {(Sg,Sg), (-KL,-KL)}
-template <bool PRECISE>
-__device__ __forceinline__ void gross_pair(const ulonglong2 a1, const ulonglong2 b1,
-                                           const ulonglong2 a2, const ulonglong2 b2, f2 F, f2 FL,
-                                           f2& part) {
-  f2 d1 = add2(F, a1.x), d2 = add2(F, a2.x);
-  if (PRECISE) {
-    d1 = add2(d1, add2(FL, b1.y));
-    d2 = add2(d2, add2(FL, b2.y));
-  }
-  const f2 den1 = fma2(d1, d1, mul2(a1.y, F));
-  const f2 den2 = fma2(d2, d2, mul2(a2.y, F));
-  const f2 N = fma2(b1.x, den2, mul2(b2.x, den1));
-  part = fma2(N, rcp2(mul2(den1, den2)), part);
-}
-
-template <bool PRECISE>
-__device__ __forceinline__ void gross_sweep(const ulonglong2* __restrict__ A,
-                                            const ulonglong2* __restrict__ B, int b, int e, f2 F,
-                                            f2 FL, Acc2& acc) {
-  int l = b;
-  for (; l + 16 <= e; l += 16) {
-#pragma unroll
-    for (int p = 0; p < 16; p += 2)
-      gross_pair<PRECISE>(A[l + p], B[l + p], A[l + p + 1], B[l + p + 1], F, FL, acc.part);
-    acc.flush();
-  }
-  for (; l + 1 < e; l += 2) gross_pair<PRECISE>(A[l], B[l], A[l + 1], B[l + 1], F, FL, acc.part);
-  if (l < e) {
-    const ulonglong2 a1 = A[l], b1 = B[l];
-    f2 d1 = add2(F, a1.x);
-    if (PRECISE) d1 = add2(d1, add2(FL, b1.y));
-    acc.part = fma2(b1.x, rcp2(fma2(d1, d1, mul2(a1.y, F))), acc.part);
-  }
-  acc.flush();
-}
-
-// VVW record: {(-ch,-ch), (ch,ch)}, {(df^2,df^2), (S df, S df)}, (-cl,-cl)
-__device__ __forceinline__ f2 vvw_term(const ulonglong2 a, const ulonglong2 b, f2 fq, f2 dn,
-                                       f2& den) {
-  const f2 den1 = fma2(dn, dn, b.x);
-  const f2 dp = add2(fq, a.y);
-  const f2 den2 = fma2(dp, dp, b.x);
-  den = mul2(den1, den2);
-  return mul2(b.y, add2(den1, den2));
-}
-
-template <bool PRECISE>
-__device__ __forceinline__ void vvw_pair(const ulonglong2 a1, const ulonglong2 b1, f2 c1,
-                                         const ulonglong2 a2, const ulonglong2 b2, f2 c2, f2 fq,
-                                         f2 fl, f2& part) {
-  f2 dm1 = add2(fq, a1.x), dm2 = add2(fq, a2.x);
-  if (PRECISE) {
-    dm1 = add2(dm1, add2(fl, c1));
-    dm2 = add2(dm2, add2(fl, c2));
-  }
-  f2 D1, D2;
-  const f2 n1 = vvw_term(a1, b1, fq, dm1, D1);
-  const f2 n2 = vvw_term(a2, b2, fq, dm2, D2);
-  part = fma2(fma2(n1, D2, mul2(n2, D1)), rcp2(mul2(D1, D2)), part);
-}
-
-template <bool PRECISE>
-__device__ __forceinline__ void vvw_sweep(const ulonglong2* __restrict__ A,
-                                          const ulonglong2* __restrict__ B,
-                                          const f2* __restrict__ CL, int b, int e, f2 fq, f2 fl,
-                                          Acc2& acc) {
-  int l = b;
-  for (; l + 16 <= e; l += 16) {
-#pragma unroll
-    for (int p = 0; p < 16; p += 2)
-      vvw_pair<PRECISE>(A[l + p], B[l + p], PRECISE ? CL[l + p] : 0ull, A[l + p + 1], B[l + p + 1],
-                        PRECISE ? CL[l + p + 1] : 0ull, fq, fl, acc.part);
-    acc.flush();
-  }
-  for (; l + 1 < e; l += 2)
-    vvw_pair<PRECISE>(A[l], B[l], PRECISE ? CL[l] : 0ull, A[l + 1], B[l + 1],
-                      PRECISE ? CL[l + 1] : 0ull, fq, fl, acc.part);
-  if (l < e) {
-    const ulonglong2 a1 = A[l], b1 = B[l];
-    f2 dm1 = add2(fq, a1.x);
-    if (PRECISE) dm1 = add2(dm1, add2(fl, CL[l]));
-    f2 D1;
-    const f2 n1 = vvw_term(a1, b1, fq, dm1, D1);
-    acc.part = fma2(n1, rcp2(D1), acc.part);
-  }
-  acc.flush();
-}
-
-__device__ __forceinline__ int2 clamp_range(int2 nr, int c0, int c1) {
-  return make_int2(max(c0, min(c1, nr.x)), max(c0, min(c1, nr.y)));
 }
 
 // Assemble one slot: per-gas absorption (T = float or double), scaled.
@@ -511,229 +385,649 @@ __device__ __forceinline__ void assemble(const LayerParams& lp, const AlphaConfi
   for (int k = 0; k < NGAS; ++k) g[k] *= (T)lp.scale[k];
 }
 
-// ------------------------------------------------------------------ kernel
-__global__ void __launch_bounds__(CHUNK) rb_alpha_kernel(AlphaArgs a) {
-  const int L = a.nL - 1 - blockIdx.x;           // deep (blend) layers first
-  const int tid = threadIdx.x;
-  const int nthr = blockDim.x;
-  const int warp = tid >> 5;
-  const int s0 = blockIdx.y * (2 * nthr) + 2 * tid;   // this thread's slot pair
-  __shared__ __align__(16) ulonglong2 sA[2][CHUNK];
-  __shared__ __align__(16) ulonglong2 sB[2][CHUNK];
-  __shared__ __align__(16) f2 sK[2][CHUNK];
-  __shared__ float s_red[CHUNK / 32];
-  const LayerParams& lp = a.lp[L];
-  const SlotPlan& P = a.sp;
-  const bool in0 = s0 < a.nslot;
-  const float2 one = make_float2(1.f, 0.f);
-  const float2 F0 = in0 ? P.F[s0] : one, F1 = in0 ? P.F[s0 + 1] : one;
-  const float2 H0 = in0 ? P.Fhs[s0] : one, H1 = in0 ? P.Fhs[s0 + 1] : one;
-  const float2 q0 = in0 ? P.f[s0] : one, q1 = in0 ? P.f[s0 + 1] : one;
-  const int set = in0 ? P.set[s0] : 0;           // both slots share the set
-  const f2 F = pk(F0.x, F1.x), FL = pk(F0.y, F1.y);
-  const f2 Fh = pk(H0.x, H1.x), FLh = pk(H0.y, H1.y);
-  const f2 fq = pk(q0.x, q1.x), fl = pk(q0.y, q1.y);
-  const int wglobal = blockIdx.y * (nthr >> 5) + warp;
-  const int2* nearw = a.near + (size_t)wglobal * NFAM;
-  const bool nh3_on = a.cfg.nh3_mode != NH3_OFF;
+// ------------------------------------------------------------------ records
+// A chunk holds the records of CH_LINES consecutive lines of one family for
+// one layer, as CH_QUADS quads of four lines.  Field f of quad q is a
+// ulonglong2 {P, Q}: P packs lines (4q, 4q+1) and Q lines (4q+2, 4q+3) as
+// f32x2, so one 16-byte broadcast load feeds every chain of a thread.
+//
+// Fields        0        1     2      3        4       5      6     7
+//   Ben-Reuven  G4-2K    K^2   S(g-z) S(g+z)K  -K_hi   -K_lo  G4    -
+//   Gross       G4-2K    K^2   S g    -        -K_hi   -K_lo  G4    -
+//   VVW         2(d2-c2) C^2   2h     2h C     -fo_hi  -fo_lo d2    h
+//   nh3_sjs     -K_hi    -K_lo G0     S
+// (G4 = 4 gamma^2; VVW: c2 = fo^2, d2 = df^2, C = c2 + d2, h = S df.)
+constexpr int CH_LINES = 128;
+constexpr int CH_QUADS = CH_LINES / 4;
+constexpr int NFIELD = 8;
 
-  Acc2 acc;
-  float r_inv[2] = {0.f, 0.f}, r_rot[2] = {0.f, 0.f}, r_v2[2] = {0.f, 0.f}, r_sjs[2] = {0.f, 0.f};
-  float r_h2o[2] = {0.f, 0.f}, r_h2s[2] = {0.f, 0.f}, r_ph3[2] = {0.f, 0.f};
-  float base_h2o = 0.f;
+struct Chunk {
+  ulonglong2 f[NFIELD][CH_QUADS];
+};
 
-  // ---------------- Ben-Reuven families with layer-level coefficients
-  for (int q = 0; q < 3; ++q) {
-    const int fam = q == 0 ? FAM_NH3_INV : (q == 1 ? FAM_H2S : FAM_PH3);
-    if (fam == FAM_NH3_INV && !(nh3_on && lp.use_hs)) continue;
-    if (fam == FAM_H2S && !a.cfg.use_h2s) continue;
-    if (fam == FAM_PH3 && !a.cfg.use_ph3) continue;
-    const LineTable& t = a.tab[fam];
-    if (t.n == 0) continue;
-    const LayerFam& LF = lp.fam[fam];
-    const bool two = fam == FAM_NH3_INV;
-    const int st = two ? set : 0;
-    const f2 Fx = two ? Fh : F, FLx = two ? FLh : FL;
-    const int2 nr = nearw[fam];
-    acc.init();
-    for (int c0 = 0; c0 < t.n; c0 += nthr) {
-      const int c1 = min(t.n, c0 + nthr);
-      const int li = c0 + tid;
-      if (li < c1) {
-        const float S = line_strength(t, LF, li);
-        br_record(t, LF.c[0], li, S, &sA[0][tid], &sB[0][tid], &sK[0][tid]);
-        if (two) br_record(t, LF.c[1], li, S, &sA[1][tid], &sB[1][tid], &sK[1][tid]);
-      }
-      __syncthreads();
-      const int2 rr = clamp_range(nr, c0, c1);
-      br_sweep<false>(sA[st], sB[st], sK[st], 0, rr.x - c0, Fx, FLx, acc);
-      br_sweep<true>(sA[st], sB[st], sK[st], rr.x - c0, rr.y - c0, Fx, FLx, acc);
-      br_sweep<false>(sA[st], sB[st], sK[st], rr.y - c0, c1 - c0, Fx, FLx, acc);
-      __syncthreads();
+enum Kind : int { K_BR = 0, K_GROSS = 1, K_VVW = 2, K_SJS = 3 };
+
+// S' = 2^(l2I + cE E - M2), exponent as a double-float, split before exp2
+__device__ __forceinline__ float line_strength(const LineTable& t, const LayerFam& F, int li) {
+  const float Eh = t.Eh[li], El = t.El[li];
+  const float ph = F.cEh * Eh;
+  const float pl = fmaf(F.cEh, Eh, -ph) + fmaf(F.cEh, El, F.cEl * Eh);
+  float s, e;
+  two_sum(t.l2Ih[li] - F.M2, ph, s, e);
+  const float lo = e + pl + t.l2Il[li];
+  const float ti = rintf(s);
+  const float tf = (s - ti) + lo;
+  if (ti < -140.f) return 0.f;
+  return ldexpf(exp2f(tf), (int)ti);
+}
+
+// Record of one line (fields above).  Padding lines get zero strength and a
+// denominator >= 3/4 for every F >= 0 (K = 1, G4 = 1), so they add exactly 0.
+template <int KIND>
+__device__ __forceinline__ void line_fields(const LineTable& t, const LayerFam& LF, int set, int li,
+                                            bool valid, float sjs_shift, float* v,
+                                            float& base_part) {
+  if (!valid) {
+    if (KIND == K_SJS) {
+      v[0] = -1e18f; v[1] = 0.f; v[2] = 0.f; v[3] = 0.f;
+    } else if (KIND == K_VVW) {
+      v[0] = 0.f; v[1] = 1.f; v[2] = 0.f; v[3] = 0.f; v[4] = 0.f; v[5] = 0.f; v[6] = 1.f; v[7] = 0.f;
+    } else {
+      v[0] = -1.f; v[1] = 1.f; v[2] = 0.f; v[3] = 0.f; v[4] = -1.f; v[5] = 0.f; v[6] = 1.f; v[7] = 0.f;
     }
-    float* r = fam == FAM_NH3_INV ? r_inv : (fam == FAM_H2S ? r_h2s : r_ph3);
-    r[0] = acc.v0();
-    r[1] = acc.v1();
+    return;
   }
-  // ---------------- Gross families (nh3_hs rotational, nu2)
-  if (nh3_on && lp.use_hs) {
-    for (int fam = FAM_NH3_ROT; fam <= FAM_NH3_V2; ++fam) {
-      const LineTable& t = a.tab[fam];
-      if (t.n == 0) continue;
-      const LayerFam& LF = lp.fam[fam];
-      const int2 nr = nearw[fam];
-      acc.init();
-      for (int c0 = 0; c0 < t.n; c0 += nthr) {
-        const int c1 = min(t.n, c0 + nthr);
-        const int li = c0 + tid;
-        if (li < c1) {
-          const float S = line_strength(t, LF, li);
-          const float g = LF.c[0][1] * t.w1[li] + LF.c[0][2] * t.w2[li] + LF.c[0][3] * t.w3[li];
-          sA[0][tid] = make_ulonglong2(dup(-t.c2h[li]), dup(4.f * g * g));
-          sB[0][tid] = make_ulonglong2(dup(S * g), dup(-t.c2l[li]));
-        }
-        __syncthreads();
-        const int2 rr = clamp_range(nr, c0, c1);
-        gross_sweep<false>(sA[0], sB[0], 0, rr.x - c0, Fh, FLh, acc);
-        gross_sweep<true>(sA[0], sB[0], rr.x - c0, rr.y - c0, Fh, FLh, acc);
-        gross_sweep<false>(sA[0], sB[0], rr.y - c0, c1 - c0, Fh, FLh, acc);
-        __syncthreads();
-      }
-      float* r = fam == FAM_NH3_ROT ? r_rot : r_v2;
-      r[0] = acc.v0();
-      r[1] = acc.v1();
-    }
-  }
-  // ---------------- nh3_sjs (frequency-dependent coefficients, all precise)
-  if (nh3_on && lp.use_sjs && a.tab[FAM_NH3_SJS].n > 0) {
-    const LineTable& t = a.tab[FAM_NH3_SJS];
-    const LayerFam& LF = lp.fam[FAM_NH3_SJS];
-    // coefficient set per slot (nh3_sjs.py:95-111): Spilker + (Joiner - Spilker) wJ
-    const float w0 = in0 ? P.wJ[s0] : 0.f, w1 = in0 ? P.wJ[s0 + 1] : 0.f;
-    float cf[2][4];
-    for (int k = 0; k < 4; ++k) {
-      cf[0][k] = fmaf(lp.sjs[0][k] - lp.sjs[1][k], w0, lp.sjs[1][k]);
-      cf[1][k] = fmaf(lp.sjs[0][k] - lp.sjs[1][k], w1, lp.sjs[1][k]);
-    }
-    const f2 A2 = pk(cf[0][0], cf[1][0]), B2 = pk(cf[0][1], cf[1][1]);
-    const f2 C2 = pk(cf[0][2], cf[1][2]), D2 = pk(cf[0][3], cf[1][3]);
-    const f2 mone = dup(-1.f), four = dup(4.f);
-    const float dl = lp.sjs[0][4];   // D is -0.45 in every set
-    acc.init();
-    for (int c0 = 0; c0 < t.n; c0 += nthr) {
-      const int c1 = min(t.n, c0 + nthr);
-      const int li = c0 + tid;
-      if (li < c1) {
-        const float S = line_strength(t, LF, li);
-        const float fo = t.ch[li];
-        float KH, e;
-        two_sum(t.c2h[li], (2.f * fo + dl) * dl, KH, e);
-        sA[0][tid] = make_ulonglong2(dup(KH), dup(e + t.c2l[li]));
-        sB[0][tid] = make_ulonglong2(dup(t.w1[li]), dup(S));
-      }
-      __syncthreads();
-      const int n = c1 - c0;
-      int cnt = 0;
-      for (int l = 0; l < n; ++l) {
-        const ulonglong2 ra = sA[0][l], rb = sB[0][l];
-        const f2 g = fma2(B2, rb.x, A2);
-        const f2 z = fma2(D2, rb.x, C2);
-        const f2 gm = fma2(z, mone, g);
-        const f2 gp = add2(g, z);
-        const f2 g2z2 = mul2(gm, gp);
-        const f2 d1 = fma2(g2z2, mone, add2(fma2(ra.x, mone, F), fma2(ra.y, mone, FL)));
-        const f2 den = fma2(d1, d1, mul2(mul2(four, F), mul2(g, g)));
-        const f2 num = fma2(gm, F, mul2(gp, add2(ra.x, g2z2)));
-        acc.part = fma2(mul2(rb.y, num), rcp2(den), acc.part);
-        if (++cnt == 16) {
-          acc.flush();
-          cnt = 0;
-        }
-      }
-      acc.flush();
-      __syncthreads();
-    }
-    r_sjs[0] = acc.v0();
-    r_sjs[1] = acc.v1();
-  }
-  // ---------------- H2O (VVW)
-  if (a.cfg.use_h2o && a.tab[FAM_H2O].n > 0) {
-    const LineTable& t = a.tab[FAM_H2O];
-    const LayerFam& LF = lp.fam[FAM_H2O];
-    const int2 nr = nearw[FAM_H2O];
+  const float S = line_strength(t, LF, li);
+  if (KIND == K_BR) {
+    const float* c = LF.c[set];
+    const float w1 = t.w1[li], w2 = t.w2[li];
+    const float g = c[0] + c[1] * w1 + c[2] * w2;
+    const float z = c[3] + c[4] * w1 + c[5] * g;
+    const float d = c[6] * g + c[7];
+    const float fo = t.ch[li];
+    const float small = fmaf(2.f * fo + d, d, (g - z) * (g + z));   // 2 fo d + d^2 + g^2 - z^2
+    float KH, e;
+    two_sum(t.c2h[li], small, KH, e);
+    const float kl = e + t.c2l[li];
+    const float G4 = 4.f * g * g;
+    v[0] = fmaf(-2.f, KH, G4) - 2.f * kl;
+    v[1] = fmaf(KH, KH, 2.f * KH * kl);
+    v[2] = S * (g - z);
+    v[3] = S * (g + z) * (KH + kl);
+    v[4] = -KH;
+    v[5] = -kl;
+    v[6] = G4;
+    v[7] = 0.f;
+  } else if (KIND == K_GROSS) {
+    const float g = LF.c[0][1] * t.w1[li] + LF.c[0][2] * t.w2[li] + LF.c[0][3] * t.w3[li];
+    const float KH = t.c2h[li], kl = t.c2l[li];
+    const float G4 = 4.f * g * g;
+    v[0] = fmaf(-2.f, KH, G4) - 2.f * kl;
+    v[1] = fmaf(KH, KH, 2.f * KH * kl);
+    v[2] = S * g;
+    v[3] = 0.f;
+    v[4] = -KH;
+    v[5] = -kl;
+    v[6] = G4;
+    v[7] = 0.f;
+  } else if (KIND == K_VVW) {
     const float l2T = LF.c[0][0];
-    acc.init();
-    for (int c0 = 0; c0 < t.n; c0 += nthr) {
-      const int c1 = min(t.n, c0 + nthr);
-      const int li = c0 + tid;
-      if (li < c1) {
-        const float S = line_strength(t, LF, li);
-        const float df = LF.c[0][1] * t.w1[li] * exp2f(t.x1[li] * l2T) +
-                         LF.c[0][2] * t.w2[li] * exp2f(t.x2[li] * l2T) +
-                         LF.c[0][3] * t.w3[li] * exp2f(t.x3[li] * l2T);
-        const float df2 = df * df;
-        const float Sd = S * df;
-        sA[0][tid] = make_ulonglong2(dup(-t.ch[li]), dup(t.ch[li]));
-        sB[0][tid] = make_ulonglong2(dup(df2), dup(Sd));
-        sK[0][tid] = dup(-t.cl[li]);
-        base_h2o += 2.f * Sd / (562500.f + df2);
-      }
-      __syncthreads();
-      const int2 rr = clamp_range(nr, c0, c1);
-      vvw_sweep<false>(sA[0], sB[0], sK[0], 0, rr.x - c0, fq, fl, acc);
-      vvw_sweep<true>(sA[0], sB[0], sK[0], rr.x - c0, rr.y - c0, fq, fl, acc);
-      vvw_sweep<false>(sA[0], sB[0], sK[0], rr.y - c0, c1 - c0, fq, fl, acc);
-      __syncthreads();
+    const float df = LF.c[0][1] * t.w1[li] * exp2f(t.x1[li] * l2T) +
+                     LF.c[0][2] * t.w2[li] * exp2f(t.x2[li] * l2T) +
+                     LF.c[0][3] * t.w3[li] * exp2f(t.x3[li] * l2T);
+    const float d2 = df * df;
+    const float h = S * df;
+    const float ch = t.ch[li], cl = t.cl[li];
+    const float c2 = fmaf(ch, ch, 2.f * ch * cl);
+    const float C = c2 + d2;
+    v[0] = 2.f * (d2 - c2);
+    v[1] = C * C;
+    v[2] = 2.f * h;
+    v[3] = 2.f * h * C;
+    v[4] = -ch;
+    v[5] = -cl;
+    v[6] = d2;
+    v[7] = h;
+    base_part += 2.f * h / (562500.f + d2);     // the -2 df / (750^2 + df^2) term (h2o_bk.py:183-185)
+  } else {  // K_SJS
+    const float fo = t.ch[li];
+    float KH, e;
+    two_sum(t.c2h[li], (2.f * fo + sjs_shift) * sjs_shift, KH, e);
+    v[0] = -KH;
+    v[1] = -(e + t.c2l[li]);
+    v[2] = t.w1[li];
+    v[3] = S;
+  }
+}
+
+// Build the records of lines [c0, c1) into `ck` (np = 2 * quads pairs).
+template <int KIND>
+__device__ __forceinline__ void build_chunk(Chunk& ck, const LineTable& t, const LayerFam& LF,
+                                            int set, int c0, int c1, float sjs_shift,
+                                            float& base_part) {
+  constexpr int NF = KIND == K_SJS ? 4 : NFIELD;
+  const int np = 2 * ((c1 - c0 + 3) >> 2);
+  f2* out = reinterpret_cast<f2*>(&ck);
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    const int la = c0 + 2 * p;
+    float va[NFIELD], vb[NFIELD];
+    line_fields<KIND>(t, LF, set, la, la < c1, sjs_shift, va, base_part);
+    line_fields<KIND>(t, LF, set, la + 1, la + 1 < c1, sjs_shift, vb, base_part);
+    const int q = p >> 1, h = p & 1;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) out[(f * CH_QUADS + q) * 2 + h] = pk(va[f], vb[f]);
+  }
+}
+
+// ------------------------------------------------------------------ sweeps
+// Two line pairs P, Q (packed halves) share one reciprocal per chain:
+// nP/dP + nQ/dQ = (nP dQ + nQ dP) / (dP dQ).
+//
+// Fast form, lines whose centre is outside [0.75 fmin, 1.3 fmax] of the
+// chain: den = F (F + (G4 - 2K)) + K^2, error <= ~18 ulp there.
+template <int KIND>
+__device__ __forceinline__ void eval_fast(f2 F, const ulonglong2& c1, const ulonglong2& c2,
+                                          const ulonglong2& a, const ulonglong2& b, Acc2& acc) {
+  const f2 dP = fma2(F, add2(F, c1.x), c2.x);
+  const f2 dQ = fma2(F, add2(F, c1.y), c2.y);
+  f2 N;
+  if (KIND == K_GROSS) {
+    N = fma2(a.x, dQ, mul2(a.y, dP));
+  } else {
+    const f2 nP = fma2(a.x, F, b.x);
+    const f2 nQ = fma2(a.y, F, b.y);
+    N = fma2(nP, dQ, mul2(nQ, dP));
+  }
+  acc.add_div(N, mul2(dP, dQ));
+}
+
+// Precise Ben-Reuven / Gross: den = ((F - K_hi) + (FL - K_lo))^2 + G4 F.
+template <int KIND>
+__device__ __forceinline__ void eval_precise(f2 F, f2 FL, const ulonglong2& a,
+                                             const ulonglong2& b, const ulonglong2& mKH,
+                                             const ulonglong2& mKL, const ulonglong2& G4,
+                                             Acc2& acc) {
+  const f2 eP = add2(add2(F, mKH.x), add2(FL, mKL.x));
+  const f2 eQ = add2(add2(F, mKH.y), add2(FL, mKL.y));
+  const f2 dP = fma2(eP, eP, mul2(G4.x, F));
+  const f2 dQ = fma2(eQ, eQ, mul2(G4.y, F));
+  f2 N;
+  if (KIND == K_GROSS) {
+    N = fma2(a.x, dQ, mul2(a.y, dP));
+  } else {
+    const f2 nP = fma2(a.x, F, b.x);
+    const f2 nQ = fma2(a.y, F, b.y);
+    N = fma2(nP, dQ, mul2(nQ, dP));
+  }
+  acc.add_div(N, mul2(dP, dQ));
+}
+
+// Precise VVW: den1 = ((f - fo_hi) + (fl - fo_lo))^2 + df^2, den2 = (f + fo)^2 + df^2,
+// line term h (den1 + den2) / (den1 den2).
+__device__ __forceinline__ void vvw_half(f2 fq, f2 fl, f2 mch, f2 mcl, f2 d2, f2 h, f2& n, f2& D) {
+  const f2 dm = add2(add2(fq, mch), add2(fl, mcl));
+  const f2 den1 = fma2(dm, dm, d2);
+  const f2 dp = fma2(mch, dup(-1.f), fq);
+  const f2 den2 = fma2(dp, dp, d2);
+  n = mul2(h, add2(den1, den2));
+  D = mul2(den1, den2);
+}
+
+__device__ __forceinline__ void eval_precise_vvw(f2 fq, f2 fl, const ulonglong2& mch,
+                                                 const ulonglong2& mcl, const ulonglong2& d2,
+                                                 const ulonglong2& h, Acc2& acc) {
+  f2 nP, DP, nQ, DQ;
+  vvw_half(fq, fl, mch.x, mcl.x, d2.x, h.x, nP, DP);
+  vvw_half(fq, fl, mch.y, mcl.y, d2.y, h.y, nQ, DQ);
+  acc.add_div(fma2(nP, DQ, mul2(nQ, DP)), mul2(DP, DQ));
+}
+
+// Per-thread frequency registers of one chain.
+struct ChainF {
+  f2 F, FL;     // f^2 as (hi, lo), both halves duplicated
+  f2 fq, fl;    // f as (hi, lo) (VVW precise path only)
+};
+
+// Records of one quad held in registers.
+struct QuadRec {
+  ulonglong2 c1, c2, a, b;          // fast fields 0..3
+  ulonglong2 mKH, mKL, G4, h;       // precise fields 4..7
+};
+
+template <int KIND, bool PREC>
+__device__ __forceinline__ void load_quad(const Chunk& ck, int q, QuadRec& r) {
+  if (!PREC || KIND != K_VVW) {   // the precise VVW path needs no fast fields
+    if (!PREC) {
+      r.c1 = ck.f[0][q];
+      r.c2 = ck.f[1][q];
     }
-    r_h2o[0] = acc.v0();
-    r_h2o[1] = acc.v1();
-    // block sum of the frequency-independent base term
-    float v = base_h2o;
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((tid & 31) == 0) s_red[warp] = v;
+    r.a = ck.f[2][q];
+    r.b = KIND == K_GROSS ? r.a : ck.f[3][q];
+  }
+  if (PREC) {
+    r.mKH = ck.f[4][q];
+    r.mKL = ck.f[5][q];
+    r.G4 = ck.f[6][q];
+    r.h = KIND == K_VVW ? ck.f[7][q] : r.G4;
+  }
+}
+
+template <int KIND, bool PREC>
+__device__ __forceinline__ void eval_tier(const QuadRec& r, const ChainF& c, Acc2& acc) {
+  if (!PREC) {
+    eval_fast<KIND>(c.F, r.c1, r.c2, r.a, r.b, acc);
+  } else if (KIND == K_VVW) {
+    eval_precise_vvw(c.fq, c.fl, r.mKH, r.mKL, r.G4, r.h, acc);
+  } else {
+    eval_precise<KIND>(c.F, c.FL, r.a, r.b, r.mKH, r.mKL, r.G4, acc);
+  }
+}
+
+// Quads [q0, q1) for all M chains at one precision tier.  Chains [0, KS)
+// read set-0 records (ck0), chains past the split read set-1 records (ck1);
+// with MIX, chain KS reads per lane from the set of its own slot.  Every
+// record load is shared by the chains of its set; Kahan flush every 32 lines
+// (all terms are positive, so a 16-term float32 block sum per lane is good
+// to ~1e-6 before compensation).
+template <int M, int KIND, bool PREC, int KS, bool MIX>
+__device__ __forceinline__ void run_tier(const Chunk& ck0, const Chunk& ck1, const Chunk& ckl,
+                                         int q0, int q1, const ChainF (&cf)[M], Acc2 (&acc)[M]) {
+  constexpr bool USE0 = KS > 0;
+  constexpr bool USE1 = KS + (MIX ? 1 : 0) < M;
+  int q = q0;
+  for (; q < q1;) {
+    const int qe = min(q1, q + 8);
+#pragma unroll 2
+    for (; q < qe; ++q) {
+      QuadRec r0, r1, rl;
+      if (USE0) load_quad<KIND, PREC>(ck0, q, r0);
+      if (USE1) load_quad<KIND, PREC>(ck1, q, r1);
+      if (MIX) load_quad<KIND, PREC>(ckl, q, rl);
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        if (k < KS)
+          eval_tier<KIND, PREC>(r0, cf[k], acc[k]);
+        else if (MIX && k == KS)
+          eval_tier<KIND, PREC>(rl, cf[k], acc[k]);
+        else
+          eval_tier<KIND, PREC>(r1, cf[k], acc[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < M; ++k) acc[k].flush();
+  }
+}
+
+// Set split of one warp -> one compiled variant (M = 2 or 4).
+template <int M, int KIND, bool PREC>
+__device__ __forceinline__ void run_split(int ks, bool mix, const Chunk& ck0, const Chunk& ck1,
+                                          const Chunk& ckl, int q0, int q1,
+                                          const ChainF (&cf)[M], Acc2 (&acc)[M]) {
+  if (KIND != K_BR || ks >= M) {
+    run_tier<M, KIND, PREC, M, false>(ck0, ck1, ckl, q0, q1, cf, acc);
+    return;
+  }
+  // inversion lines with set-1 chains in this warp
+  if (!mix) {
+    switch (ks) {
+      case 0: run_tier<M, KIND, PREC, 0, false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 1: run_tier<M, KIND, PREC, 1, false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 2: run_tier<M, KIND, PREC, (M > 2 ? 2 : 0), false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      default: run_tier<M, KIND, PREC, (M > 3 ? 3 : 0), false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+    }
+  } else {
+    switch (ks) {
+      case 0: run_tier<M, KIND, PREC, 0, true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 1: run_tier<M, KIND, PREC, 1, true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 2: run_tier<M, KIND, PREC, (M > 2 ? 2 : 0), true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      default: run_tier<M, KIND, PREC, (M > 3 ? 3 : 0), true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+    }
+  }
+}
+
+// One chunk: the quads where some chain of the warp sees a line within its
+// double-float window run at the precise tier for every chain, the rest at
+// the fast tier.
+template <int M, int KIND>
+__device__ __forceinline__ void sweep_chunk(const Chunk& ck0, const Chunk& ck1, const Chunk& ckl,
+                                            int c0, int c1, int ks, bool mix, const int (&na)[M],
+                                            const int (&nb)[M], const ChainF (&cf)[M],
+                                            Acc2 (&acc)[M]) {
+  const int nq = (c1 - c0 + 3) >> 2;
+  int qa = nq, qb = 0;   // hull of the chains' windows, in quads
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    if (na[k] < nb[k]) {
+      qa = min(qa, max((na[k] - c0) >> 2, 0));
+      qb = max(qb, min((nb[k] - c0 + 3) >> 2, nq));
+    }
+  }
+  if (qa >= qb) {
+    run_split<M, KIND, false>(ks, mix, ck0, ck1, ckl, 0, nq, cf, acc);
+    return;
+  }
+  if (qa > 0) run_split<M, KIND, false>(ks, mix, ck0, ck1, ckl, 0, qa, cf, acc);
+  run_split<M, KIND, true>(ks, mix, ck0, ck1, ckl, qa, qb, cf, acc);
+  if (qb < nq) run_split<M, KIND, false>(ks, mix, ck0, ck1, ckl, qb, nq, cf, acc);
+}
+
+__device__ __forceinline__ bool fam_is_hs(int fam) {
+  return fam == FAM_NH3_INV || fam == FAM_NH3_ROT || fam == FAM_NH3_V2;
+}
+
+// Whether a family contributes to a layer (the assembly kernel reads
+// exactly these).
+__device__ __forceinline__ bool fam_enabled(const AlphaArgs& a, const LayerParams& lp, int fam) {
+  const bool nh3 = a.cfg.nh3_mode != NH3_OFF;
+  switch (fam) {
+    case FAM_NH3_INV:
+    case FAM_NH3_ROT:
+    case FAM_NH3_V2: return nh3 && lp.use_hs;
+    case FAM_NH3_SJS: return nh3 && lp.use_sjs;
+    case FAM_H2O: return a.cfg.use_h2o;
+    case FAM_H2S: return a.cfg.use_h2s;
+    default: return a.cfg.use_ph3;
+  }
+}
+
+__device__ __forceinline__ size_t res_index(const AlphaArgs& a, int L, int tile, int t) {
+  return (((size_t)L * a.ntile + tile) * a.ntmpl + t) * a.spt;
+}
+
+// One item of a Ben-Reuven / Gross / VVW family: lines [l0, l1) of one
+// layer for all slots of one tile.  Records are double-buffered: chunk c+1
+// is built while chunk c is swept, one barrier per chunk.  Inversion items
+// build the records of each coefficient set the tile uses.
+template <int M, int KIND>
+__device__ __forceinline__ void lines_item(const AlphaArgs& a, Chunk (&buf)[2][2], float* s_red,
+                                           int L, int tile, int t, int fam, int l0, int l1) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool hsf = fam_is_hs(fam);
+  const LineTable& tab = a.tab[fam];
+  const LayerFam& LF = a.lp[L].fam[fam];
+  const ChainPlan* cp = a.chains + ((size_t)tile * a.W + warp) * M;
+  const int tflags = a.tile_flags[tile];
+  const bool inv = fam == FAM_NH3_INV;
+  const bool b0 = !inv || (tflags & CH_SET0), b1 = inv && (tflags & CH_SET1);
+  const int wsets = a.warp_sets[tile * a.W + warp];
+  const int ks = inv ? (wsets & 255) : M;
+  const bool mix = inv && (wsets & 256);
+  ChainF cf[M];
+  int na[M], nb[M], ls[M];
+  int lane_set = 0;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    ls[k] = 32 * cp[k].block + lane;
+    const int s = tile * a.spt + ls[k];
+    const float2 Fv = hsf ? a.sp.Fhs[s] : a.sp.F[s];
+    cf[k].F = dup(Fv.x);
+    cf[k].FL = dup(Fv.y);
+    if (KIND == K_VVW) {
+      const float2 fv = a.sp.f[s];
+      cf[k].fq = dup(fv.x);
+      cf[k].fl = dup(fv.y);
+    } else {
+      cf[k].fq = cf[k].fl = 0ull;
+    }
+    if (mix && k == ks) lane_set = a.sp.set[s];
+    const int2 nr = cp[k].near[fam];
+    na[k] = nr.x;
+    nb[k] = nr.y;
+  }
+  Acc2 acc[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) acc[k].init();
+  float base_part = 0.f;
+  const int nch = (l1 - l0 + CH_LINES - 1) / CH_LINES;
+  {
+    const int c1 = min(l1, l0 + CH_LINES);
+    if (b0) build_chunk<KIND>(buf[0][0], tab, LF, 0, l0, c1, 0.f, base_part);
+    if (b1) build_chunk<KIND>(buf[0][1], tab, LF, 1, l0, c1, 0.f, base_part);
+  }
+  __syncthreads();
+  for (int c = 0; c < nch; ++c) {
+    const int c0 = l0 + c * CH_LINES, c1 = min(l1, c0 + CH_LINES);
+    const int nbuf = (c + 1) & 1;
+    if (c + 1 < nch) {
+      const int n1 = min(l1, c1 + CH_LINES);
+      if (b0) build_chunk<KIND>(buf[nbuf][0], tab, LF, 0, c1, n1, 0.f, base_part);
+      if (b1) build_chunk<KIND>(buf[nbuf][1], tab, LF, 1, c1, n1, 0.f, base_part);
+    }
+    const Chunk& ck0 = buf[c & 1][0];
+    const Chunk& ck1 = buf[c & 1][1];
+    sweep_chunk<M, KIND>(ck0, ck1, lane_set ? ck1 : ck0, c0, c1, ks, mix, na, nb, cf, acc);
     __syncthreads();
-    float tot = 0.f;
-    for (int w = 0; w < (nthr >> 5); ++w) tot += s_red[w];
-    base_h2o = tot;
   }
-  if (!in0) return;
-  // ---------------- assemble both slots
-  const bool out64 = a.layers64 || a.gas64;
-  for (int h = 0; h < 2; ++h) {
-    const int j = P.j[s0 + h];
-    if (j < 0) continue;
-    const float2 Fs = h ? F1 : F0;
-    const float2 Hs = h ? H1 : H0;
-    float g32[NGAS];
-    assemble<float>(lp, a.cfg, Fs.x + Fs.y, Hs.x + Hs.y, set, r_inv[h], r_rot[h], r_v2[h],
-                    r_sjs[h], r_h2o[h], base_h2o, r_h2s[h], r_ph3[h], g32);
-    float tot = 0.f;
-    for (int k = 0; k < NGAS; ++k) tot += g32[k];
-    a.alpha32[(size_t)L * a.nf + j] = a.cfg.units_db ? tot / DB_PER_INVCM : tot;
-    if (out64) {
-      const double f = a.freqs[j], fh = a.freqs_hs[j];
-      double g64[NGAS];
-      assemble<double>(lp, a.cfg, f * f, fh * fh, set, r_inv[h], r_rot[h], r_v2[h], r_sjs[h],
-                       r_h2o[h], base_h2o, r_h2s[h], r_ph3[h], g64);
-      double t64 = 0.0;
-      for (int k = 0; k < NGAS; ++k) {
-        if (a.gas64) a.gas64[((size_t)L * a.nf + j) * NGAS + k] = g64[k];
-        t64 += g64[k];
-      }
-      if (a.layers64) a.layers64[(size_t)j * a.nL + L] = t64;
+  float* out = a.res + res_index(a, L, tile, t);
+#pragma unroll
+  for (int k = 0; k < M; ++k)
+    if (cp[k].flags & CH_VALID) out[ls[k]] = acc[k].value();
+  if (KIND == K_VVW) {
+    float v = base_part;
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (tid == 0) {
+      float tot = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_red[w];
+      a.base[((size_t)L * a.ntile + tile) * a.ntmpl + t] = tot;
     }
   }
+}
+
+// One nh3_sjs item (nh3_sjs.py:37-124): coefficients depend on frequency
+// (Spilker / Joiner blend per slot), every line takes the double-float path
+// and its own reciprocal; chains are swept one after another.
+template <int M>
+__device__ __forceinline__ void sjs_item(const AlphaArgs& a, Chunk (&buf)[2][2], int L, int tile,
+                                         int t, int l0, int l1) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const LineTable& tab = a.tab[FAM_NH3_SJS];
+  const LayerParams& lp = a.lp[L];
+  const LayerFam& LF = lp.fam[FAM_NH3_SJS];
+  const ChainPlan* cp = a.chains + ((size_t)tile * a.W + warp) * M;
+  const float shift = lp.sjs[0][4];   // delta = -0.45 P_NH3 in every set
+  float c0s[4], dcs[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    c0s[q] = lp.sjs[1][q];
+    dcs[q] = lp.sjs[0][q] - lp.sjs[1][q];
+  }
+  int ls[M];
+  unsigned am = 0;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    ls[k] = 32 * cp[k].block + lane;
+    if (cp[k].flags & CH_VALID) am |= 1u << k;
+  }
+  Acc2 acc[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) acc[k].init();
+  float unused = 0.f;
+  const f2 mone = dup(-1.f);
+  const int nch = (l1 - l0 + CH_LINES - 1) / CH_LINES;
+  build_chunk<K_SJS>(buf[0][0], tab, LF, 0, l0, min(l1, l0 + CH_LINES), shift, unused);
+  __syncthreads();
+  for (int c = 0; c < nch; ++c) {
+    const int c0 = l0 + c * CH_LINES, c1 = min(l1, c0 + CH_LINES);
+    if (c + 1 < nch)
+      build_chunk<K_SJS>(buf[(c + 1) & 1][0], tab, LF, 0, c1, min(l1, c1 + CH_LINES), shift, unused);
+    const Chunk& ck = buf[c & 1][0];
+    const int nq = (c1 - c0 + 3) >> 2;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      if (!((am >> k) & 1u)) continue;
+      const int s = tile * a.spt + ls[k];
+      const float wJ = a.sp.wJ[s];
+      const f2 A = dup(fmaf(dcs[0], wJ, c0s[0])), B = dup(fmaf(dcs[1], wJ, c0s[1]));
+      const f2 C = dup(fmaf(dcs[2], wJ, c0s[2])), D = dup(fmaf(dcs[3], wJ, c0s[3]));
+      const float2 Fv = a.sp.F[s];
+      const f2 F = dup(Fv.x), FL = dup(Fv.y), F4 = dup(4.f * Fv.x);
+      int cnt = 0;
+      for (int q = 0; q < nq; ++q) {
+        const ulonglong2 mKH = ck.f[0][q], mKL = ck.f[1][q], G0 = ck.f[2][q], S = ck.f[3][q];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const f2 kh = h ? mKH.y : mKH.x, kl = h ? mKL.y : mKL.x;
+          const f2 w = h ? G0.y : G0.x, st = h ? S.y : S.x;
+          const f2 g = fma2(B, w, A);
+          const f2 z = fma2(D, w, C);
+          const f2 gm = fma2(z, mone, g);
+          const f2 gp = add2(g, z);
+          const f2 g2z2 = mul2(gm, gp);
+          const f2 d1 = fma2(g2z2, mone, add2(add2(F, kh), add2(FL, kl)));
+          const f2 den = fma2(d1, d1, mul2(F4, mul2(g, g)));
+          const f2 num = fma2(gm, F, mul2(gp, fma2(kh, mone, g2z2)));
+          acc[k].add_div(mul2(st, num), den);
+        }
+        if (++cnt == 8) {
+          cnt = 0;
+          acc[k].flush();
+        }
+      }
+      acc[k].flush();
+    }
+    __syncthreads();
+  }
+  float* out = a.res + res_index(a, L, tile, t);
+#pragma unroll
+  for (int k = 0; k < M; ++k)
+    if ((am >> k) & 1u) out[ls[k]] = acc[k].value();
+}
+
+// ------------------------------------------------------------------ assembly
+// Sum of the items of one family for one slot (read through L2: the items
+// were written by other CTAs).
+__device__ __forceinline__ float fam_sum(const AlphaArgs& a, const float* r, int fam) {
+  float v = 0.f;
+#pragma unroll 4
+  for (int t = a.vbeg[fam]; t < a.vend[fam]; ++t) v += __ldcg(r + (size_t)t * a.spt);
+  return v;
+}
+
+// One slot of one layer: family sums -> per-gas absorption, scaled, float32
+// total for the brightness scan and the optional float64 outputs.
+__device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int tile, int ls) {
+  const int s = tile * a.spt + ls;
+  if (s >= a.nslot) return;
+  const int j = a.sp.j[s];
+  if (j < 0) return;
+  const LayerParams& lp = a.lp[L];
+  const float* r = a.res + res_index(a, L, tile, 0) + ls;
+  const int set = a.sp.set[s];
+  float inv = 0.f, rot = 0.f, v2 = 0.f, sjs = 0.f, h2o = 0.f, base = 0.f, h2s = 0.f, ph3 = 0.f;
+  if (fam_enabled(a, lp, FAM_NH3_INV)) {
+    inv = fam_sum(a, r, FAM_NH3_INV);
+    rot = fam_sum(a, r, FAM_NH3_ROT);
+    v2 = fam_sum(a, r, FAM_NH3_V2);
+  }
+  if (fam_enabled(a, lp, FAM_NH3_SJS)) sjs = fam_sum(a, r, FAM_NH3_SJS);
+  if (a.cfg.use_h2o) {
+    h2o = fam_sum(a, r, FAM_H2O);
+    const float* bs = a.base + ((size_t)L * a.ntile + tile) * a.ntmpl;
+    for (int t = a.vbeg[FAM_H2O]; t < a.vend[FAM_H2O]; ++t) base += __ldcg(bs + t);
+  }
+  if (a.cfg.use_h2s) h2s = fam_sum(a, r, FAM_H2S);
+  if (a.cfg.use_ph3) ph3 = fam_sum(a, r, FAM_PH3);
+  const float2 Fs = a.sp.F[s], Hs = a.sp.Fhs[s];
+  float g32[NGAS];
+  assemble<float>(lp, a.cfg, Fs.x + Fs.y, Hs.x + Hs.y, set, inv, rot, v2, sjs, h2o, base, h2s, ph3,
+                  g32);
+  float tot = 0.f;
+  for (int k = 0; k < NGAS; ++k) tot += g32[k];
+  a.alpha32[(size_t)L * a.nf + j] = a.cfg.units_db ? tot / DB_PER_INVCM : tot;
+  if (a.layers64 || a.gas64) {
+    const double f = a.freqs[j], fh = a.freqs_hs[j];
+    double g64[NGAS];
+    assemble<double>(lp, a.cfg, f * f, fh * fh, set, inv, rot, v2, sjs, h2o, base, h2s, ph3, g64);
+    double t64 = 0.0;
+    for (int k = 0; k < NGAS; ++k) {
+      if (a.gas64) a.gas64[((size_t)L * a.nf + j) * NGAS + k] = g64[k];
+      t64 += g64[k];
+    }
+    if (a.layers64) a.layers64[(size_t)j * a.nL + L] = t64;
+  }
+}
+
+// ------------------------------------------------------------------ kernels
+// Persistent line-sum kernel: every CTA takes items from a.counter until
+// none are left.  Item i -> template entry i / (nL ntile), then layers deep
+// to shallow, then tiles; template entries come heaviest family first.  The
+// CTA that finishes the last item of a (layer, tile) assembles it (counter
+// a.done after a memory fence; nothing waits on another CTA).
+template <int M>
+__global__ void __launch_bounds__(128, M >= 4 ? 4 : 6) rb_alpha_lines_kernel(AlphaArgs a) {
+  __shared__ __align__(16) Chunk buf[2][2];   // [double buffer][coefficient set]
+  __shared__ int s_item[2];
+  __shared__ int s_last;
+  __shared__ float s_red[4];
+  const int per = a.nL * a.ntile;
+  for (int it = 0;; ++it) {
+    if (threadIdx.x == 0) s_item[it & 1] = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int item = s_item[it & 1];
+    if (item >= a.nitems) break;
+    const int t = item / per, rem = item - t * per;
+    const int L = a.nL - 1 - rem / a.ntile, tile = rem % a.ntile;
+    const TmplEntry e = a.tmpl[t];
+    if (fam_enabled(a, a.lp[L], e.fam)) {
+      switch (e.fam) {
+        case FAM_NH3_INV:
+        case FAM_H2S:
+        case FAM_PH3: lines_item<M, K_BR>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
+        case FAM_NH3_ROT:
+        case FAM_NH3_V2: lines_item<M, K_GROSS>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
+        case FAM_H2O: lines_item<M, K_VVW>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
+        default: sjs_item<M>(a, buf, L, tile, t, e.l0, e.l1); break;
+      }
+    }
+    // the barrier orders every thread's result stores before thread 0's
+    // fence, which releases them at device scope with the counter update
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_last = atomicAdd(a.done + (size_t)L * a.ntile + tile, 1) == a.ntmpl - 1;
+      if (s_last) __threadfence();
+    }
+    __syncthreads();
+    if (s_last)
+      for (int ls = threadIdx.x; ls < a.spt; ls += blockDim.x) assemble_slot(a, L, tile, ls);
+  }
+}
+
+// Assembly alone, for a plan without line items (continua only).
+__global__ void __launch_bounds__(128) rb_alpha_assemble_kernel(AlphaArgs a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.nslot) return;
+  assemble_slot(a, blockIdx.y, s / a.spt, s % a.spt);
 }
 
 // ------------------------------------------------------------------ launch
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st) {
-  rb_layer_prep_kernel<<<(pa.nL + 63) / 64, 64, 0, st>>>(pa);
+  const int n = pa.nL * PREP_PARTS;
+  rb_layer_prep_kernel<<<(n + 255) / 256, 256, 0, st>>>(pa);
   return cudaGetLastError();
 }
 
-cudaError_t launch_alpha_lines(const AlphaArgs& aa, int block, int ntile, cudaStream_t st) {
-  dim3 grid(aa.nL, ntile);
-  rb_alpha_kernel<<<grid, block, 0, st>>>(aa);
+// Resident CTAs per SM of the line-sum kernel for M chains and W warps.
+int alpha_lines_occupancy(int M, int W) {
+  int n = 0;
+  cudaError_t e = cudaSuccess;
+  if (M == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rb_alpha_lines_kernel<4>, 32 * W, 0);
+  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rb_alpha_lines_kernel<2>, 32 * W, 0);
+  return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st) {
+  if (aa.nitems > 0) {
+    const int nb = std::max(1, std::min(nblocks, aa.nitems));
+    const int nthr = 32 * aa.W;
+    if (aa.M == 4) rb_alpha_lines_kernel<4><<<nb, nthr, 0, st>>>(aa);
+    else rb_alpha_lines_kernel<2><<<nb, nthr, 0, st>>>(aa);
+  } else {
+    dim3 grid((aa.nslot + 127) / 128, aa.nL);
+    rb_alpha_assemble_kernel<<<grid, 128, 0, st>>>(aa);
+  }
   return cudaGetLastError();
 }
 

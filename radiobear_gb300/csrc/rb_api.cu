@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -113,8 +114,12 @@ struct rb_handle {
   rb::AlphaConfig cfg{rb::NH3_HS_SJS, 1, 1, 1, 1, 'e', 0};
   // frequency plan
   std::vector<double> plan_f;
-  int plan_block = 0, plan_ntile = 0, plan_nslot = 0;
-  DBuf d_f, d_fhs, d_near, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset;
+  int plan_M = 0, plan_W = 0, plan_spt = 0, plan_ntile = 0, plan_nslot = 0, plan_ntmpl = 0;
+  int plan_grid = 0;
+  int plan_vbeg[rb::NFAM] = {}, plan_vend[rb::NFAM] = {};
+  int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
+  DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
+      d_res, d_base, d_done;
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
@@ -135,7 +140,8 @@ void set_last_error(const char* msg) { g_err = msg; }
 // launchers implemented in the kernel translation units
 namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
-cudaError_t launch_alpha_lines(const AlphaArgs& aa, int block, int ntile, cudaStream_t st);
+cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st);
+int alpha_lines_occupancy(int M, int W);
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
                              float* R32, float* T32, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
@@ -145,7 +151,7 @@ int tb_nchunk(int max_seg);
 cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
                             cudaStream_t st);
 cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st);
-cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, cudaStream_t st);
+cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, int packed, cudaStream_t st);
 }  // namespace rb
 
 namespace {
@@ -163,14 +169,20 @@ cudaError_t upload(DBuf& b, const T* src, size_t count, cudaStream_t st) {
   return cudaMemcpyAsync(b.p, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
 }
 
-// Frequency plan.
+// Frequency plan and line-sum work decomposition.
 //  * nh3_hs output order (nh3_hs.py:70-88): slot j evaluates nh3_hs at the
-//    j-th element of [freqs <= 30 GHz in order, freqs > 30 GHz in order];
-//  * slots: two per thread, the <=30 GHz block padded to an even length so
-//    no thread pair straddles the coefficient switch;
-//  * per warp (64 slots) and family, the index range of lines whose centre
-//    is within [0.75 fmin, 1.3 fmax] of the warp's frequencies (those take
-//    the double-float F - K path).
+//    j-th element of [freqs <= 30 GHz in order, freqs > 30 GHz in order] and
+//    takes coefficient set 1 when that frequency is above 30 GHz;
+//  * slot s = j, padded at the end to whole tiles of 32 M W slots; lane i of
+//    warp w owns slot 32 block(w, k) + i of its tile as chain k, the block
+//    partition chosen per tile to minimise the double-float work;
+//  * per chain and family, the index range of lines whose centre is within
+//    [0.75 fmin, 1.3 fmax] of the chain's frequencies (those take the
+//    double-float path);
+//  * template entries: each family's lines cut into items of item_lines,
+//    heaviest family first (nh3_sjs, inversion, h2o, rotational, nu2, h2s,
+//    ph3).  Inversion items build the records of both coefficient sets
+//    when the tile needs both.
 int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st) {
   if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
   for (int i = 0; i < nf; ++i)
@@ -185,23 +197,26 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
   const int n_lo = (int)fhs.size();
   for (int i = 0; i < nf; ++i)
     if (freqs[i] > 30.0) fhs.push_back(freqs[i]);
-  std::vector<int> slot_j;
-  for (int j = 0; j < n_lo; ++j) slot_j.push_back(j);
-  if (n_lo % 2) slot_j.push_back(-1);
-  for (int j = n_lo; j < nf; ++j) slot_j.push_back(j);
-  if (slot_j.size() % 2) slot_j.push_back(-1);
-  const int npair = (int)slot_j.size() / 2;
-  const int block = std::min(128, ((npair + 31) / 32) * 32);
-  const int ntile = (npair + block - 1) / block;
-  const int nslot = ntile * block * 2;
-  slot_j.resize(nslot, -1);
+  // tiling: forced by rb_set_alpha_tiling, else by the number of 32-slot blocks
+  int M = h->tile_M, W = h->tile_W;
+  if (M <= 0 || W <= 0) {
+    const int blocks = (nf + 31) / 32;
+    if (blocks >= 8) { M = 2; W = 4; }
+    else if (blocks >= 4) { M = 2; W = 2; }
+    else { M = 2; W = 1; }
+  }
+  const int spt = 32 * M * W;
+  const int ntile = (nf + spt - 1) / spt;
+  const int nslot = ntile * spt;
+  std::vector<int> slot_j(nslot, -1);
   std::vector<float2> sF(nslot), sFhs(nslot), sf(nslot);
   std::vector<float> swJ(nslot, 0.f);
   std::vector<int> sset(nslot, 0);
   for (int s = 0; s < nslot; ++s) {
-    const int j = slot_j[s];
-    const int jj = j >= 0 ? j : (s % 2 ? slot_j[s - 1] : -1);   // padding mirrors its partner
-    const double f = jj >= 0 ? freqs[jj] : 1.0, fh = jj >= 0 ? fhs[jj] : 1.0;
+    const int j = s < nf ? s : -1;
+    const int jj = j >= 0 ? j : nf - 1;   // padding repeats the last frequency
+    slot_j[s] = j;
+    const double f = freqs[jj], fh = fhs[jj];
     float a, b;
     rb::split_double(f * f, a, b);
     sF[s] = make_float2(a, b);
@@ -210,46 +225,193 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
     rb::split_double(f, a, b);
     sf[s] = make_float2(a, b);
     swJ[s] = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)((f - 26.0) / 8.0));
-    sset[s] = (jj >= n_lo) ? 1 : 0;
+    sset[s] = jj >= n_lo ? 1 : 0;
   }
-  for (int s = 0; s + 1 < nslot; s += 2) sset[s + 1] = sset[s] = std::max(sset[s], sset[s + 1]) *
-                                                                 (slot_j[s] >= 0 || slot_j[s + 1] >= 0);
-  const int nw = block / 32;
-  std::vector<int2> nearv((size_t)ntile * nw * rb::NFAM, make_int2(0, 0));
+  // per 32-slot block: set flags and the double-float line window of each family
+  const int nbk = M * W;
+  std::vector<rb::ChainPlan> blocks((size_t)ntile * nbk);
+  std::vector<int> tflags(ntile, 0);
   for (int t = 0; t < ntile; ++t)
-    for (int w = 0; w < nw; ++w) {
-      const int s0 = (t * block + w * 32) * 2, s1 = s0 + 64;
+    for (int bk = 0; bk < nbk; ++bk) {
+      rb::ChainPlan& c = blocks[(size_t)t * nbk + bk];
+      c = rb::ChainPlan{};
+      c.block = bk;
+      double lo = INFINITY, hi = -INFINITY, lo_h = INFINITY, hi_h = -INFINITY;
+      for (int i = 0; i < 32; ++i) {
+        const int s = t * spt + 32 * bk + i;
+        const int j = slot_j[s];
+        if (j < 0) continue;
+        c.flags |= rb::CH_VALID | (sset[s] ? rb::CH_SET1 : rb::CH_SET0);
+        lo = std::min(lo, freqs[j]);
+        hi = std::max(hi, freqs[j]);
+        lo_h = std::min(lo_h, fhs[j]);
+        hi_h = std::max(hi_h, fhs[j]);
+      }
+      tflags[t] |= c.flags;
       for (int fam = 0; fam < rb::NFAM; ++fam) {
+        c.near[fam] = make_int2(0, 0);
+        if (!(c.flags & rb::CH_VALID)) continue;
         const bool hs = fam == rb::FAM_NH3_INV || fam == rb::FAM_NH3_ROT || fam == rb::FAM_NH3_V2;
-        double lo = INFINITY, hi = -INFINITY;
-        for (int s = s0; s < s1; ++s) {
-          const int j = slot_j[s];
-          if (j < 0) continue;
-          const double v = hs ? fhs[j] : freqs[j];
-          lo = std::min(lo, v);
-          hi = std::max(hi, v);
-        }
-        if (!(lo <= hi)) continue;
-        const std::vector<double>& c = h->fam[fam].centre;
-        int a = (int)(std::lower_bound(c.begin(), c.end(), 0.75 * lo) - c.begin());
-        int b = (int)(std::upper_bound(c.begin(), c.end(), 1.3 * hi) - c.begin());
-        nearv[((size_t)t * nw + w) * rb::NFAM + fam] = make_int2(a, std::max(a, b));
+        const double l = hs ? lo_h : lo, u = hs ? hi_h : hi;
+        const std::vector<double>& cen = h->fam[fam].centre;
+        const int a = (int)(std::lower_bound(cen.begin(), cen.end(), 0.75 * l) - cen.begin());
+        const int b = (int)(std::upper_bound(cen.begin(), cen.end(), 1.3 * u) - cen.begin());
+        c.near[fam] = make_int2(a, std::max(a, b));
       }
     }
+  // Partition of each tile's blocks into W warps of M chains.  A warp runs
+  // the double-float tier over the hull of its chains' windows, so blocks
+  // whose windows overlap are grouped; the cost is the modelled packed-op
+  // count (fast / double-float per line quad and chain: Ben-Reuven 10 / 16,
+  // Gross 8 / 12, VVW 10 / 22), the objective half the sum and half W times
+  // the largest warp (warps of a CTA meet at a barrier every chunk).
+  auto group_cost = [&](int t, const std::vector<int>& g) {
+    static const int fams[6] = {rb::FAM_NH3_INV, rb::FAM_NH3_ROT, rb::FAM_NH3_V2,
+                                rb::FAM_H2O, rb::FAM_H2S, rb::FAM_PH3};
+    static const double cf[6] = {10, 8, 8, 10, 10, 10}, cp[6] = {16, 12, 12, 22, 16, 16};
+    double cost = 0.0;
+    for (int q = 0; q < 6; ++q) {
+      const int n = h->fam[fams[q]].n;
+      if (n == 0) continue;
+      int lo = n, hi = 0;
+      for (int bk : g) {
+        const int2 r = blocks[(size_t)t * nbk + bk].near[fams[q]];
+        if (r.x < r.y) {
+          lo = std::min(lo, r.x);
+          hi = std::max(hi, r.y);
+        }
+      }
+      const int hull = std::max(0, hi - lo);
+      cost += (double)g.size() * ((n - hull) * cf[q] + hull * cp[q]);
+    }
+    return cost;
+  };
+  std::vector<rb::ChainPlan> chains((size_t)ntile * W * M);
+  for (int t = 0; t < ntile; ++t) {
+    std::vector<std::vector<int>> best(W, std::vector<int>(M));
+    for (int w = 0; w < W; ++w)
+      for (int k = 0; k < M; ++k) best[w][k] = k * W + w;   // default: interleaved
+    if (W > 1 && nbk <= 8) {
+      double best_obj = INFINITY;
+      std::vector<std::vector<int>> cur;
+      std::vector<int> used(nbk, 0);
+      std::function<void()> rec = [&]() {
+        int first = -1;
+        for (int b = 0; b < nbk; ++b)
+          if (!used[b]) { first = b; break; }
+        if (first < 0) {
+          double sum = 0.0, mx = 0.0;
+          for (auto& g : cur) {
+            const double c = group_cost(t, g);
+            sum += c;
+            mx = std::max(mx, c);
+          }
+          const double obj = 0.5 * sum + 0.5 * W * mx;
+          if (obj < best_obj - 1e-9) {
+            best_obj = obj;
+            best = cur;
+          }
+          return;
+        }
+        // groups are built from the lowest unused block upward (each
+        // unordered partition is visited once)
+        std::vector<int> g{first};
+        used[first] = 1;
+        std::function<void(int)> pick = [&](int from) {
+          if ((int)g.size() == M) {
+            cur.push_back(g);
+            rec();
+            cur.pop_back();
+            return;
+          }
+          for (int b = from; b < nbk; ++b) {
+            if (used[b]) continue;
+            used[b] = 1;
+            g.push_back(b);
+            pick(b + 1);
+            g.pop_back();
+            used[b] = 0;
+          }
+        };
+        pick(first + 1);
+        used[first] = 0;
+      };
+      rec();
+    }
+    for (int w = 0; w < W; ++w) {
+      std::sort(best[w].begin(), best[w].end());
+      for (int k = 0; k < M; ++k) chains[((size_t)t * W + w) * M + k] = blocks[(size_t)t * nbk + best[w][k]];
+    }
+  }
+  // per warp: chains [0, KS) take inversion set 0, chain KS may mix both
+  // sets, the rest take set 1 (slots are in frequency order, so the set is
+  // monotone in the chain index); chains without a valid slot follow the
+  // set-1 records when the tile builds them, else the set-0 records.
+  std::vector<int> wsets((size_t)ntile * W, M);
+  for (int t = 0; t < ntile; ++t)
+    for (int w = 0; w < W; ++w) {
+      int ks = 0;
+      bool mix = false;
+      for (int k = 0; k < M; ++k) {
+        const int f = chains[((size_t)t * W + w) * M + k].flags;
+        const bool set0_only = (f & rb::CH_VALID) ? !(f & rb::CH_SET1) : !(tflags[t] & rb::CH_SET1);
+        if (set0_only && ks == k) {
+          ++ks;
+        } else if (ks == k && (f & rb::CH_SET0) && (f & rb::CH_SET1)) {
+          mix = true;
+        }
+      }
+      for (int k = ks + (mix ? 1 : 0); k < M; ++k) {   // the rest must take set 1
+        const int f = chains[((size_t)t * W + w) * M + k].flags;
+        if ((f & rb::CH_VALID) && (f & rb::CH_SET0))
+          return fail(RB_ESTATE, "frequency plan: coefficient sets not monotone in a warp");
+      }
+      wsets[(size_t)t * W + w] = ks | (mix ? 256 : 0);
+    }
+  // template entries, heaviest family first
+  const int order[rb::NFAM] = {rb::FAM_NH3_SJS, rb::FAM_NH3_INV, rb::FAM_H2O, rb::FAM_NH3_ROT,
+                               rb::FAM_NH3_V2,  rb::FAM_H2S,     rb::FAM_PH3};
+  // Lines per item scale with the per-line cost so items take similar time:
+  // nh3_sjs (frequency-dependent widths, double-float everywhere) half the
+  // base, the inversion lines (mostly double-float near 18-26 GHz) the
+  // base, the others twice the base.
+  const int base_lines = std::max(128, (h->item_lines > 0 ? h->item_lines : 1024) / 128 * 128);
+  std::vector<rb::TmplEntry> tmpl;
+  for (int v = 0; v < rb::NFAM; ++v) {
+    const int fam = order[v];
+    const int n = h->fam[fam].n;
+    const int lines = fam == rb::FAM_NH3_SJS   ? std::max(128, base_lines / 2 / 128 * 128)
+                      : fam == rb::FAM_NH3_INV ? base_lines
+                                               : 2 * base_lines;
+    h->plan_vbeg[fam] = (int)tmpl.size();
+    for (int l0 = 0; l0 < n; l0 += lines) tmpl.push_back(rb::TmplEntry{fam, l0, std::min(n, l0 + lines), 0});
+    h->plan_vend[fam] = (int)tmpl.size();
+  }
+  int dev_sms = 0;
+  RB_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device));
+  const int occ = std::max(1, rb::alpha_lines_occupancy(M, W));
   RB_CUDA(upload(h->d_f, freqs, nf, st));
   RB_CUDA(upload(h->d_fhs, fhs.data(), nf, st));
-  RB_CUDA(upload(h->d_near, nearv.data(), nearv.size(), st));
+  RB_CUDA(upload(h->d_chains, chains.data(), chains.size(), st));
+  RB_CUDA(upload(h->d_tflags, tflags.data(), tflags.size(), st));
+  RB_CUDA(upload(h->d_wsets, wsets.data(), wsets.size(), st));
+  RB_CUDA(upload(h->d_tmpl, tmpl.data(), tmpl.size(), st));
   RB_CUDA(upload(h->d_sj, slot_j.data(), slot_j.size(), st));
   RB_CUDA(upload(h->d_sF, sF.data(), sF.size(), st));
   RB_CUDA(upload(h->d_sFhs, sFhs.data(), sFhs.size(), st));
   RB_CUDA(upload(h->d_sf, sf.data(), sf.size(), st));
   RB_CUDA(upload(h->d_swJ, swJ.data(), swJ.size(), st));
   RB_CUDA(upload(h->d_sset, sset.data(), sset.size(), st));
+  RB_CUDA(h->d_counter.ensure(sizeof(int)));
   RB_CUDA(cudaStreamSynchronize(st));
   h->plan_f.assign(freqs, freqs + nf);
-  h->plan_block = block;
+  h->plan_M = M;
+  h->plan_W = W;
+  h->plan_spt = spt;
   h->plan_ntile = ntile;
   h->plan_nslot = nslot;
+  h->plan_ntmpl = (int)tmpl.size();
+  h->plan_grid = dev_sms * occ;
   return RB_OK;
 }
 
@@ -284,21 +446,44 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
     pa.nlines[f] = h->fam[f].n;
   }
   pa.out = h->d_lp.as<rb::LayerParams>();
+  pa.counter = h->d_counter.as<int>();
   rb::AlphaArgs aa{};
   aa.nL = nL;
   aa.nf = nf;
   aa.nslot = h->plan_nslot;
+  aa.M = h->plan_M;
+  aa.W = h->plan_W;
+  aa.spt = h->plan_spt;
+  aa.ntile = h->plan_ntile;
   aa.sp.j = h->d_sj.as<int>();
   aa.sp.F = h->d_sF.as<float2>();
   aa.sp.Fhs = h->d_sFhs.as<float2>();
   aa.sp.f = h->d_sf.as<float2>();
   aa.sp.wJ = h->d_swJ.as<float>();
   aa.sp.set = h->d_sset.as<int>();
+  aa.chains = h->d_chains.as<rb::ChainPlan>();
+  aa.tile_flags = h->d_tflags.as<int>();
+  aa.warp_sets = h->d_wsets.as<int>();
+  aa.tmpl = h->d_tmpl.as<rb::TmplEntry>();
+  aa.ntmpl = h->plan_ntmpl;
+  for (int v = 0; v < rb::NFAM; ++v) {
+    aa.vbeg[v] = h->plan_vbeg[v];
+    aa.vend[v] = h->plan_vend[v];
+  }
+  aa.nitems = aa.ntmpl * nL * aa.ntile;
+  aa.counter = h->d_counter.as<int>();
+  RB_CUDA(h->d_res.ensure(sizeof(float) * std::max<size_t>(1, (size_t)nL * aa.ntile * aa.ntmpl * aa.spt)));
+  RB_CUDA(h->d_base.ensure(sizeof(float) * std::max<size_t>(1, (size_t)nL * aa.ntile * aa.ntmpl)));
+  RB_CUDA(h->d_done.ensure(sizeof(int) * (size_t)nL * aa.ntile));
+  aa.done = h->d_done.as<int>();
+  pa.done = aa.done;
+  pa.ntile = aa.ntile;
+  aa.res = h->d_res.as<float>();
+  aa.base = h->d_base.as<float>();
   aa.freqs = h->d_f.as<double>();
   aa.freqs_hs = h->d_fhs.as<double>();
   aa.lp = h->d_lp.as<rb::LayerParams>();
   for (int f = 0; f < rb::NFAM; ++f) aa.tab[f] = h->fam[f].table();
-  aa.near = h->d_near.as<int2>();
   aa.cfg = pa.cfg;
   aa.alpha32 = h->d_a32.as<float>();
   aa.layers64 = d_layers64;
@@ -306,7 +491,7 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[0], st));
   RB_CUDA(rb::launch_prep(pa, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[1], st));
-  RB_CUDA(rb::launch_alpha_lines(aa, h->plan_block, h->plan_ntile, st));
+  RB_CUDA(rb::launch_alpha_lines(aa, h->plan_grid, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[2], st));
   h->launches += 2;
   return RB_OK;
@@ -421,7 +606,10 @@ int rb_destroy(rb_handle* h) {
   for (DBuf* b : {&h->d_sj, &h->d_sF, &h->d_sFhs, &h->d_sf, &h->d_swJ, &h->d_sset, &h->d_dR,
                   &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part})
     b->release();
-  for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_near, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
+  for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
+                  &h->d_done})
+    b->release();
+  for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
                   &h->d_ds, &h->d_layer, &h->d_r4, &h->d_ll, &h->d_end, &h->d_Tb, &h->d_avg,
                   &h->d_iw, &h->d_tau, &h->d_W, &h->d_tbl, &h->d_x})
@@ -563,6 +751,19 @@ int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2
   h->cfg.use_h2s = use_h2s != 0;
   h->cfg.use_ph3 = use_ph3 != 0;
   h->cfg.h2state = h2state;
+  return RB_OK;
+}
+
+int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!(M == 0 || M == 2 || M == 4)) return fail(RB_EINVAL, "M must be 0, 2 or 4");
+  if (W < 0 || W > 4) return fail(RB_EINVAL, "W must be in 0..4");
+  if ((M == 0) != (W == 0)) return fail(RB_EINVAL, "M and W are set together");
+  if (item_lines < 0 || item_lines % 128) return fail(RB_EINVAL, "item_lines must be a multiple of 128");
+  h->tile_M = M;
+  h->tile_W = W;
+  h->item_lines = item_lines;
+  h->plan_f.clear();
   return RB_OK;
 }
 
@@ -902,20 +1103,24 @@ int rb_probe_fp32_peak(rb_handle* h, double* tflops) {
   RB_CUDA(cudaEventCreate(&e0));
   RB_CUDA(cudaEventCreate(&e1));
   const int blocks = sms * 8, iters = 1 << 14;
-  float best = 1e30f;
-  for (int rep = 0; rep < 4; ++rep) {
-    RB_CUDA(cudaEventRecord(e0, h->st));
-    RB_CUDA(rb::launch_fp32_probe(blocks, iters, h->d_probe.as<float>(), h->st));
-    RB_CUDA(cudaEventRecord(e1, h->st));
-    RB_CUDA(cudaEventSynchronize(e1));
-    float ms = 0;
-    RB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    if (rep > 0) best = std::min(best, ms);
+  double best_tf = 0.0;
+  for (int packed = 0; packed < 2; ++packed) {
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      RB_CUDA(cudaEventRecord(e0, h->st));
+      RB_CUDA(rb::launch_fp32_probe(blocks, iters, h->d_probe.as<float>(), packed, h->st));
+      RB_CUDA(cudaEventRecord(e1, h->st));
+      RB_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      RB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) best = std::min(best, ms);
+    }
+    const double flops = 2.0 * 8.0 * (packed ? 2.0 : 1.0) * (double)iters * blocks * 256.0;
+    best_tf = std::max(best_tf, flops / (best * 1e-3) / 1e12);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
-  *tflops = flops / (best * 1e-3) / 1e12;
+  *tflops = best_tf;
   return RB_OK;
 }
 

@@ -15,16 +15,58 @@ struct PrepArgs {
   float l2Imax[NFAM], Emin[NFAM], Emax[NFAM];
   int nlines[NFAM];
   LayerParams* out;
+  int* counter;          // line-sum work counter to reset (or null)
+  int* done;             // [nL][ntile] finished-item counters to reset (or null)
+  int ntile;
+};
+
+// Line-sum work decomposition.
+//
+// Frequencies are planned into slots, tiles of spt = 32 * M * W slots cut
+// into blocks of 32 consecutive slots.  In a tile, lane i of warp w holds M
+// "chains"; chain k owns slot 32 * block(w, k) + i, so the 32 lanes of one
+// chain cover 32 consecutive slots (one precision decision per chain).  The
+// planner picks the partition of blocks into warps (ascending within a
+// warp) that minimises the double-float work.  Slot order is frequency
+// order, so the nh3_hs coefficient set (0 up to 30 GHz, 1 above) is
+// monotone in k: per warp, chains [0, KS) take set 0, chain KS may mix both
+// sets lane by lane, the rest take set 1.
+//
+// The lines of every family are cut into items of at most item_lines lines;
+// template entry t = (family, l0, l1).  The persistent kernel takes items
+// from a global counter in the order (template entry, layer deep to
+// shallow, tile); each item writes one float per slot of its tile into
+// res[layer][tile][t][slot], and the assembly kernel sums those per family.
+struct ChainPlan {
+  int flags;              // CH_VALID | CH_SET0 | CH_SET1
+  int block;              // 32-slot block of the tile owned by this chain
+  int2 near[NFAM];        // line index range taking the double-float path
+};
+constexpr int CH_VALID = 1, CH_SET0 = 2, CH_SET1 = 4;
+
+struct TmplEntry {
+  int fam, l0, l1, pad;
 };
 
 struct AlphaArgs {
   int nL, nf, nslot;
+  int M, W, spt, ntile;     // chains per thread, warps per CTA, slots per tile, tiles
   SlotPlan sp;
+  const ChainPlan* chains;  // [ntile][W][M]
+  const int* tile_flags;    // [ntile] OR of the tile's chain flags
+  const int* warp_sets;     // [ntile][W] KS | (mixed chain KS ? 256 : 0)
+  const TmplEntry* tmpl;    // [ntmpl], grouped by family
+  int ntmpl;
+  int vbeg[NFAM], vend[NFAM];  // template range of each family
+  int nitems;               // ntmpl * nL * ntile
+  int* counter;             // work counter, zeroed by rb_layer_prep_kernel
+  float* res;               // [nL][ntile][ntmpl][spt] per-item line sums
+  float* base;              // [nL][ntile][ntmpl] h2o frequency-independent term per item
+  int* done;                // [nL][ntile] finished items, zeroed by rb_layer_prep_kernel
   const double* freqs;      // [nf] (float64 outputs only)
   const double* freqs_hs;   // [nf] frequency evaluated by nh3_hs in slot j
   const LayerParams* lp;
   LineTable tab[NFAM];
-  const int2* near;         // [nwarps total][NFAM] line index ranges
   AlphaConfig cfg;
   float* alpha32;           // [nL][nf] total, cm^-1 (brightness input)
   double* layers64;         // [nf][nL] total, units of cfg (or null)

@@ -7,8 +7,8 @@
 //     digits;
 //   * per-layer scalars (width coefficients, strength prefactors as
 //     mantissa x 2^exponent) live in an array of LayerParams, one per layer;
-//   * frequencies are planned into "slots": two slots per thread, padded so
-//     a thread's pair never straddles the nh3_hs 30 GHz coefficient switch;
+//   * frequencies are planned into "slots", tiles of 32 * M * W slots (M
+//     slots per thread, W warps per CTA), padded at the end of the last tile;
 //   * absorption for the brightness scan is float32 [nL][nf] (frequency
 //     contiguous, so a warp reading 32 frequencies of one layer is one
 //     128-byte transaction).
@@ -99,7 +99,7 @@ struct AlphaConfig {
   int units_db;        // 0: cm^-1, 1: dB/km (the nh3 clamp applies after units)
 };
 
-// Frequency slot plan: two slots per thread.
+// Frequency slot plan (see AlphaArgs for the slot -> thread mapping).
 struct SlotPlan {
   const int* j;          // [nslot] frequency index, -1 = padding
   const float2* F;       // [nslot] (hi, lo) of f^2

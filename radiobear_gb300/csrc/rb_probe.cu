@@ -18,8 +18,43 @@ __global__ void __launch_bounds__(256) rb_fp32_probe_kernel(int iters, float see
   if (s == 1234.5f) sink[threadIdx.x] = s;   // keeps the chains live
 }
 
-cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, cudaStream_t st) {
-  rb_fp32_probe_kernel<<<blocks, 256, 0, st>>>(iters, 0.5f, sink);
+// The same chains as packed f32x2 FMAs (two float32 FMAs per instruction),
+// in case the packed form reaches a higher rate than scalar FFMA.
+__device__ __forceinline__ unsigned long long probe_fma2(unsigned long long a, unsigned long long b,
+                                                         unsigned long long c) {
+  unsigned long long d;
+  asm volatile("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+__device__ __forceinline__ unsigned long long probe_pk(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+__global__ void __launch_bounds__(256) rb_fp32x2_probe_kernel(int iters, float seed, float* sink) {
+  const float s0 = seed + threadIdx.x;
+  unsigned long long a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = probe_pk(s0 + k, s0 + k + 0.5f);
+  const unsigned long long m = probe_pk(0.9999999f, 0.9999999f), c = probe_pk(1e-7f, 1e-7f);
+#pragma unroll 4
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = probe_fma2(a[k], m, c);
+  }
+  unsigned long long x = a[0];
+#pragma unroll
+  for (int k = 1; k < 8; ++k) x ^= a[k];
+  if (x == 0x0123456789abcdefull) sink[threadIdx.x] = 1.f;   // keeps the chains live
+}
+
+cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, int packed, cudaStream_t st) {
+  if (packed)
+    rb_fp32x2_probe_kernel<<<blocks, 256, 0, st>>>(iters, 0.5f, sink);
+  else
+    rb_fp32_probe_kernel<<<blocks, 256, 0, st>>>(iters, 0.5f, sink);
   return cudaGetLastError();
 }
 

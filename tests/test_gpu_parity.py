@@ -89,6 +89,40 @@ def test_alpha_c1_layers_with_blend(engine):
     assert _rel(lay, tot) < ALPHA_RTOL
 
 
+@pytest.mark.parametrize('tiling', [(2, 1, 128), (2, 2, 256), (2, 4, 512), (4, 1, 128),
+                                    (4, 2, 512), (4, 4, 1024)])
+def test_alpha_c1_tilings(engine, tiling):
+    """Every line-sum tiling (slots per thread, warps per CTA, lines per
+    work item) gives the same absorption within the contract."""
+    M, W, lines = tiling
+    z = G.load('c1_alpha')
+    wl = G.c1_workload()
+    _load(engine, wl.lines)
+    g = G.gas_table(z)[:, z['layers']]
+    engine.set_alpha_tiling(M, W, lines)
+    try:
+        lay, gas = engine.alpha(g[G.C['P']], g[G.C['T']], _X(g), z['freqs'], per_gas=True)
+    finally:
+        engine.set_alpha_tiling(0, 0, 0)
+    err = _per_gas_err(gas, z['alpha_gas'], z['ordered_constituents'])
+    print('c1 tiling', tiling, 'per-gas rel err', err)
+    assert max(err.values()) < ALPHA_RTOL
+
+
+@pytest.mark.parametrize('tiling', [(2, 1, 128), (4, 2, 128)])
+def test_alpha_benchmark_tilings(engine, tiling):
+    z = G.load('benchmark')
+    _load(engine, G.benchmark_lines())
+    g = G.gas_table(z)
+    engine.set_alpha_tiling(*tiling)
+    try:
+        lay, gas = engine.alpha(g[G.C['P']], g[G.C['T']], _X(g), z['freqs'], per_gas=True)
+    finally:
+        engine.set_alpha_tiling(0, 0, 0)
+    err = _per_gas_err(gas, z['alpha_gas'], z['ordered_constituents'])
+    assert max(err.values()) < ALPHA_RTOL
+
+
 def test_raypaths_c0(engine):
     z = G.load('c0')
     out = engine.raypath(z['prop_R'], z['prop_N'], z['rays_b'], G.REQ, G.RPOL)
