@@ -168,6 +168,30 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
                       const double* b, const double* weights, int disc, double* Tb_out,
                       double* Tb_avg);
 
+/* Adjoint of the forward model (no reference counterpart: radioBEAR has
+ * no derivatives).  Runs the forward (exp weighting) and returns Tb, the
+ * weighted average (when weights are given) and the gradient of
+ *   loss = sum_f grad[f] Tb_avg[f]           (weights given, grad [nf])
+ *   loss = sum_{b,f} grad[b][f] Tb[b][f]     (no weights, grad [nb][nf])
+ * with respect to each layer's T (K), P (bar) and ln X of NH3, H2O, H2S:
+ * dT[nL], dP[nL], dlnX[3][nL] (rows NH3, H2O, H2S).  The ray paths are
+ * held fixed (they depend on R and N only); alpha is recomputed with its
+ * layer derivatives instead of being stored. */
+int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const double* X,
+               const double* R, const double* N, int nf, const double* freqs, const double* scale,
+               double Req, double Rpol, double orient0, double orient1, int gtype, int limb, int nb,
+               const double* b, const double* weights, const double* grad, double* Tb_out,
+               double* Tb_avg, double* dT, double* dP, double* dlnX);
+
+/* Device-pointer variant of rb_adjoint (freqs on the host), enqueued on
+ * `stream`; Tb_out and Tb_avg may be null. */
+int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
+                      const double* X, const double* R, const double* N, int nf,
+                      const double* freqs_host, const double* scale, double Req, double Rpol,
+                      double orient0, double orient1, int gtype, int limb, int nb, const double* b,
+                      const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
+                      double* dT, double* dP, double* dlnX);
+
 /* Number of this library's kernel launches made by the last rb_forward /
  * rb_forward_device call (for launch accounting). */
 int rb_last_launch_count(rb_handle* h);

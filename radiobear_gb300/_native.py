@@ -38,7 +38,8 @@ FAMILY_COLUMNS = {
 EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set_lines',
            'rb_set_formalisms', 'rb_alpha', 'rb_raypath', 'rb_brightness', 'rb_forward',
            'rb_forward_device', 'rb_last_launch_count', 'rb_set_profiling', 'rb_phase_times',
-           'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling')
+           'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
+           'rb_adjoint_device')
 
 _lib = None
 _lock = threading.Lock()
@@ -87,6 +88,12 @@ def load_library(path=None):
         lib.rb_phase_times.argtypes = [_vp, _d, c_int]
         lib.rb_probe_fp32_peak.argtypes = [_vp, _d]
         lib.rb_set_alpha_tiling.argtypes = [_vp, c_int, c_int, c_int]
+        lib.rb_adjoint.argtypes = [_vp, c_int, _d, _d, _d, _d, _d, c_int, _d, _d, c_double, c_double,
+                                   c_double, c_double, c_int, c_int, c_int, _d, _d, _d, _d, _d, _d,
+                                   _d, _d]
+        lib.rb_adjoint_device.argtypes = [_vp, _vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _d, _vp,
+                                          c_double, c_double, c_double, c_double, c_int, c_int,
+                                          c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
         for name in EXPORTS:
             getattr(lib, name).restype = getattr(lib, name).restype or c_int
         lib.rb_last_error.restype = ctypes.c_char_p
@@ -243,6 +250,49 @@ class Engine:
             vp(scale), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]),
             GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), 0, vp(Tb_out), vp(Tb_avg))
         _check(self.lib, rc, 'rb_forward_device')
+
+    def adjoint(self, P, T, X, R, N, freqs, b, Req, Rpol, grad, weights=None,
+                orientation=(0.0, 0.0), gtype='ellipse', limb='shape', scale=None):
+        """Forward Tb and the gradient of sum(grad * Tb_avg) (weights given,
+        grad [nf]) or sum(grad * Tb) (grad [nb, nf]) with respect to each
+        layer's T, P and ln X of NH3, H2O, H2S.  Returns dict(Tb, Tb_avg, dT,
+        dP, dlnX [3, nL])."""
+        P, T, X, R, N, f = (_f64(v) for v in (P, T, X, R, N, freqs))
+        b = _f64(np.atleast_2d(b))
+        nL, nf, nb = P.size, f.size, b.shape[0]
+        w = None if weights is None else _f64(weights)
+        g = _f64(grad)
+        want = (nf,) if w is not None else (nb, nf)
+        if g.shape != want:
+            raise ValueError('grad must have shape {}'.format(want))
+        sc = None if scale is None else _f64(scale)
+        Tb = np.empty((nb, nf))
+        avg = np.empty(nf) if w is not None else None
+        dT, dP, dlnX = np.empty(nL), np.empty(nL), np.empty((3, nL))
+        rc = self.lib.rb_adjoint(self._h, nL, _ptr(P), _ptr(T), _ptr(X), _ptr(R), _ptr(N), nf,
+                                 _ptr(f), _ptr(sc), float(Req), float(Rpol), float(orientation[0]),
+                                 float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _ptr(b),
+                                 _ptr(w), _ptr(g), _ptr(Tb), _ptr(avg), _ptr(dT), _ptr(dP),
+                                 _ptr(dlnX))
+        _check(self.lib, rc, 'rb_adjoint')
+        return dict(Tb=Tb, Tb_avg=avg, dT=dT, dP=dP, dlnX=dlnX)
+
+    def adjoint_device(self, stream, nL, nb, P, T, X, R, N, freqs_host, b, Req, Rpol, grad, dT,
+                       dP, dlnX, weights=None, Tb_out=None, Tb_avg=None, orientation=(0.0, 0.0),
+                       gtype='ellipse', limb='shape', scale=None):
+        """Device-pointer variant of :meth:`adjoint` (integer device
+        addresses, enqueued on ``stream``)."""
+        f = _f64(freqs_host)
+
+        def vp(x):
+            return None if x is None else _vp(int(x))
+
+        rc = self.lib.rb_adjoint_device(
+            self._h, _vp(int(stream)), int(nL), vp(P), vp(T), vp(X), vp(R), vp(N), f.size, _ptr(f),
+            vp(scale), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]),
+            GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), vp(grad), vp(Tb_out),
+            vp(Tb_avg), vp(dT), vp(dP), vp(dlnX))
+        _check(self.lib, rc, 'rb_adjoint_device')
 
     def last_launch_count(self):
         return int(self.lib.rb_last_launch_count(self._h))

@@ -1,0 +1,800 @@
+// Adjoint of the forward model: dTb/dT, dTb/dP and dTb/dln X (NH3, H2O,
+// H2S) per layer, for the exp-weighted brightness of every ray (or their
+// quadrature average).  The ray paths are held fixed (they depend on the
+// layer radii and refractive indices, inputs of their own).
+//
+//   rb_tb_adjoint_kernel    one thread per (ray, frequency): the forward
+//                           scan of Brightness.single (brightness.py:53-117)
+//                           in float64, then the reverse sweep with the
+//                           optical depth recomputed backwards,
+//                             dTb/dW_i  = c_i (T_i - Tb) / intW,
+//                             dTb/da_k  = w_k E_k + d_{k-1}/2 Lam_k + d_k/2 Lam_{k+1},
+//                             Lam_k     = sum_{i>=k} dTb/dW_i (-a_i E_i),
+//                           (c_i the trapezoid node weight, E = exp(-tau));
+//                           writes g dTb/dalpha and g W c / intW (the
+//                           source-temperature term) per visited layer.
+//   rb_adjoint_reduce_kernel sums those over rays (fixed order).
+//   rb_layer_tan_kernel     eight threads per layer: the layer coefficients
+//                           of the absorption (widths, couplings, strength
+//                           prefactors, continua) in dual numbers, giving
+//                           their derivatives with respect to the layer's
+//                           T, P, ln X_NH3, ln X_H2O, ln X_H2S.
+//   rb_alpha_jvp_kernel     one CTA per (layer, 128 frequencies): alpha is
+//                           recomputed line by line together with its
+//                           derivatives with respect to the five layer
+//                           parameters (each family depends on T, P and its
+//                           own abundance), contracted with dTb/dalpha of
+//                           the layer and reduced over the frequencies.
+//   rb_adjoint_final_kernel adds the source-temperature term and writes
+//                           dTb/dT, dTb/dP, dTb/dln X.
+#include "rb_args.cuh"
+#include <math_constants.h>
+
+namespace rb {
+
+constexpr double T_CMB_ADJ = 2.725;   // utils.py:77
+constexpr double LN2 = 0.69314718055994531;
+constexpr double LOG2E_D = 1.4426950408889634;
+
+__device__ __forceinline__ int wrap_l(int l, int nL) {
+  l = l < 0 ? l + nL : l;
+  return l < 0 ? 0 : (l >= nL ? nL - 1 : l);
+}
+
+// ------------------------------------------------------------------ scan adjoint
+__global__ void __launch_bounds__(128) rb_tb_adjoint_kernel(TbAdjArgs a) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = idx / a.nf, j = idx - b * a.nf;
+  if (b >= a.nb) return;
+  const int n = min(max(a.nseg[b], 0), a.max_seg);
+  const double gb = a.weights ? a.weights[b] * a.grad[j] : a.grad[(size_t)b * a.nf + j];
+  if (n < 2 || gb == 0.0) return;
+  const float* hd = a.hds + (size_t)b * a.max_seg;
+  const int* lay = a.layer + (size_t)b * a.max_seg;
+  const int nL = a.nL, nf = a.nf;
+  auto alp = [&](int i) { return (double)a.alpha32[(size_t)wrap_l(lay[i], nL) * nf + j]; };
+  const int N = n - 1;
+  // forward scan
+  double tau = 0.0, IW = 0.0, TL = 0.0, Wp = 0.0;
+  double ap = alp(0), Tp = a.T[wrap_l(lay[0], nL)];
+  for (int i = 0; i < N; ++i) {
+    const double d = 2.0 * (double)hd[i];
+    const double a1 = alp(i + 1), T1 = a.T[wrap_l(lay[i + 1], nL)];
+    tau += (ap + a1) * d * 0.5;
+    const double W1 = a1 * (double)__expf(-(float)tau);
+    IW += (Wp + W1) * d * 0.5;
+    TL += (Tp * Wp + T1 * W1) * d * 0.5;
+    Wp = W1;
+    ap = a1;
+    Tp = T1;
+  }
+  if (TL < T_CMB_ADJ || !(IW > 0.0)) return;   // clamped to T_cmb: no gradient
+  const double Tb = TL / IW, rIW = 1.0 / IW;
+  double* ga = a.ga + ((size_t)b * nf + j) * nL;
+  double* gs = a.gs + ((size_t)b * nf + j) * nL;
+  double Lnext = 0.0;          // Lam_{i+1}
+  double ti = tau;             // tau_N
+  double ai = alp(N);
+  for (int i = N; i >= 0; --i) {
+    const int Li = wrap_l(lay[i], nL);
+    const double Ti = a.T[Li];
+    const double dprev = i >= 1 ? 2.0 * (double)hd[i - 1] : 0.0;
+    const double dcur = i < N ? 2.0 * (double)hd[i] : 0.0;
+    const double ci = 0.5 * (dprev + dcur);
+    const double Ei = i >= 1 ? (double)__expf(-(float)ti) : 0.0;
+    const double wi = ci * (Ti - Tb) * rIW;
+    const double Wi = ai * Ei;
+    const double Li_ = Lnext - wi * ai * Ei;   // Lam_i (lambda_0 = 0 since E_0 = 0 here)
+    const double gA = (i >= 1 ? wi * Ei + 0.5 * dprev * Li_ : 0.0) + 0.5 * dcur * Lnext;
+    ga[Li] += gb * gA;
+    gs[Li] += gb * Wi * ci * rIW;
+    if (i >= 1) {
+      const double am = alp(i - 1);
+      ti -= (am + ai) * dprev * 0.5;
+      ai = am;
+    }
+    Lnext = Li_;
+  }
+}
+
+// galpha[L][j] = sum_b ga[b][j][L];  gsrc[L] = sum_b sum_j gs[b][j][L]
+__global__ void __launch_bounds__(128) rb_adjoint_reduce_kernel(TbAdjArgs a, double* galpha,
+                                                                double* gsrc) {
+  const int L = blockIdx.x;
+  const int nL = a.nL, nf = a.nf;
+  double src = 0.0;
+  for (int j = threadIdx.x; j < nf; j += blockDim.x) {
+    double g = 0.0;
+    for (int b = 0; b < a.nb; ++b) {
+      g += a.ga[((size_t)b * nf + j) * nL + L];
+      src += a.gs[((size_t)b * nf + j) * nL + L];
+    }
+    galpha[(size_t)L * nf + j] = g;
+  }
+  __shared__ double s[4];
+  for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(0xffffffffu, src, o);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = src;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+    gsrc[L] = t;
+  }
+}
+
+// ------------------------------------------------------------------ dual numbers
+// Value and derivatives with respect to the five layer parameters
+// (T, P, ln X_NH3, ln X_H2O, ln X_H2S), float64.
+struct D5 {
+  double v, d[NTH];
+};
+
+__device__ __forceinline__ D5 dc(double v) {
+  D5 r;
+  r.v = v;
+  for (int k = 0; k < NTH; ++k) r.d[k] = 0.0;
+  return r;
+}
+__device__ __forceinline__ D5 operator+(const D5& a, const D5& b) {
+  D5 r;
+  r.v = a.v + b.v;
+  for (int k = 0; k < NTH; ++k) r.d[k] = a.d[k] + b.d[k];
+  return r;
+}
+__device__ __forceinline__ D5 operator-(const D5& a, const D5& b) {
+  D5 r;
+  r.v = a.v - b.v;
+  for (int k = 0; k < NTH; ++k) r.d[k] = a.d[k] - b.d[k];
+  return r;
+}
+__device__ __forceinline__ D5 operator*(const D5& a, const D5& b) {
+  D5 r;
+  r.v = a.v * b.v;
+  for (int k = 0; k < NTH; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return r;
+}
+__device__ __forceinline__ D5 operator/(const D5& a, const D5& b) {
+  D5 r;
+  r.v = a.v / b.v;
+  for (int k = 0; k < NTH; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
+  return r;
+}
+__device__ __forceinline__ D5 operator*(double s, const D5& a) {
+  D5 r;
+  r.v = s * a.v;
+  for (int k = 0; k < NTH; ++k) r.d[k] = s * a.d[k];
+  return r;
+}
+__device__ __forceinline__ D5 operator+(const D5& a, double s) {
+  D5 r = a;
+  r.v += s;
+  return r;
+}
+__device__ __forceinline__ D5 chain(const D5& a, double fv, double dfdx) {
+  D5 r;
+  r.v = fv;
+  for (int k = 0; k < NTH; ++k) r.d[k] = dfdx * a.d[k];
+  return r;
+}
+__device__ __forceinline__ D5 dlog2(const D5& a) { return chain(a, log2(a.v), LOG2E_D / a.v); }
+__device__ __forceinline__ D5 dexp2(const D5& a) {
+  const double e = exp2(a.v);
+  return chain(a, e, LN2 * e);
+}
+__device__ __forceinline__ D5 dexp(const D5& a) {
+  const double e = exp(a.v);
+  return chain(a, e, e);
+}
+// 2^(e lg2x), the prep kernel's pw()
+__device__ __forceinline__ D5 dpw(const D5& lg2x, double e) { return dexp2(e * lg2x); }
+__device__ __forceinline__ D5 dmin1(const D5& a) { return a.v < 1.0 ? a : dc(1.0); }
+
+__device__ __forceinline__ void store_tan(FamTan& o, int s, int k, const D5& v) {
+  for (int q = 0; q < NTH; ++q) o.dc[s][k][q] = (float)v.d[q];
+}
+__device__ __forceinline__ void store_pref(FamTan& o, const D5& pref) {
+  for (int q = 0; q < NTH; ++q) o.dlnpref[q] = pref.v != 0.0 ? (float)(pref.d[q] / pref.v) : 0.f;
+}
+__device__ __forceinline__ void zero_tan(FamTan& o) {
+  for (int s = 0; s < 2; ++s)
+    for (int k = 0; k < 8; ++k)
+      for (int q = 0; q < NTH; ++q) o.dc[s][k][q] = 0.f;
+  for (int q = 0; q < NTH; ++q) o.dlnpref[q] = 0.f;
+  o.dcE = 0.f;
+}
+
+// Inversion coefficient sets (nh3_hs.py:139-168), as in the prep kernel.
+__device__ constexpr double INV_SET_D[2][13] = {
+    {1.640, 0.75, 0.852, 0.7756, 0.666, 1.0, 1.262, 0.3, 0.5296, 0.7964, 0.667, 1.554, -0.0498},
+    {1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152, 0.8873, 0.8994, 0.66666667,
+     -0.0627}};
+
+// Derivatives of the layer coefficients, eight threads per layer (the parts
+// of rb_layer_prep_kernel: 0 shared, 1 inversion, 2 rotational, 3 nu2,
+// 4 nh3_sjs, 5 H2S, 6 PH3, 7 H2O).
+__global__ void __launch_bounds__(256) rb_layer_tan_kernel(TanArgs a) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = gid / 8, part = gid % 8;
+  if (L >= a.nL) return;
+  const int nL = a.nL;
+  const double Pd = a.P[L], Td = a.T[L];
+  const double* X = a.X;
+  D5 T = dc(Td), P = dc(Pd);
+  T.d[0] = 1.0;
+  P.d[1] = 1.0;
+  auto pp = [&](int row, int th) {   // partial pressure P X, d/dln X on tangent th
+    const double x = X[row * nL + L];
+    D5 r = x * P;
+    if (th >= 0) r.d[th] = Pd * x;
+    return r;
+  };
+  const D5 Ph2 = pp(X_H2, -1), Phe = pp(X_HE, -1), Pch4 = pp(X_CH4, -1);
+  const D5 Pnh3 = pp(X_NH3, TH_XNH3), Ph2o = pp(X_H2O, TH_XH2O), Ph2s = pp(X_H2S, TH_XH2S);
+  const D5 Pph3 = pp(X_PH3, -1);
+  LayerTan& o = a.out[L];
+  const D5 Tdiv = dc(300.0) / T;
+  const D5 lTdiv = dlog2(Tdiv);
+  const D5 l295 = dlog2(dc(295.0) / T);
+  const double GHZ = 29.9792458, TWO_PI = 0.63661977236758134, FOUR_PI = 1.2732395447351627;
+  const double HS = 1.0E6 * 6.02297E23 / 8.31432E7;
+  const D5 hs_base = HS * GHZ * ((1.0 / 300.0) * Pnh3 * dpw(lTdiv, 3.5));
+  const double invT2 = 1.0 / (Td * Td);
+  FamTan F;
+  zero_tan(F);
+  switch (part) {
+    case 0: {
+      // blend weight of nh3_hs_sjs (nh3_hs_sjs.py:6-26)
+      o.dblendW_dP = (a.nh3_mode == NH3_HS_SJS && Pd >= 400.0 && Pd <= 2000.0) ? (float)(1.0 / 1600.0) : 0.f;
+      const D5 th = dc(273.0) / T;
+      const D5 lth = dlog2(th);
+      D5 pre;
+      if (a.h2state == 'n') {
+        pre = dmin1(dpw(dlog2(T / dc(40.0)), 2.5));
+      } else {
+        pre = dmin1(dpw(dlog2(T / dc(55.0)), 2.7));
+        pre = dmin1(pre * dpw(dlog2(T / dc(120.0)), 0.55));
+      }
+      const D5 cia = 3.9522E-14 * (Ph2 * pre *
+                                   (Ph2 * dpw(lth, 3.12) + 1.382 * (Phe * dpw(lth, 2.24)) +
+                                    9.322 * (Pch4 * dpw(lth, 3.34))));
+      for (int q = 0; q < NTH; ++q) o.dh2_cia[q] = (float)cia.d[q];
+      return;
+    }
+    case 1: {
+      for (int s = 0; s < 2; ++s) {
+        const double* c = INV_SET_D[s];
+        store_tan(F, s, 0, c[0] * (Ph2 * dpw(lTdiv, c[3])) + c[1] * (Phe * dpw(lTdiv, c[4])));
+        store_tan(F, s, 1, c[2] * (Pnh3 * dpw(l295, c[5])));
+        store_tan(F, s, 3, c[6] * (Ph2 * dpw(lTdiv, c[9])) + c[7] * (Phe * dpw(lTdiv, c[10])));
+        store_tan(F, s, 4, c[8] * (Pnh3 * dpw(l295, c[11])));
+      }
+      store_pref(F, TWO_PI * hs_base);
+      F.dcE = (float)(19.858252418E-24 / 1.38E-23 * LOG2E_D * invT2);
+      o.fam[FAM_NH3_INV] = F;
+      return;
+    }
+    case 2: {
+      store_tan(F, 0, 1, 0.2984 * (Ph2 * dpw(lTdiv, 0.8730)));
+      store_tan(F, 0, 2, 0.75 * (Phe * dpw(lTdiv, 0.66666667)));
+      store_tan(F, 0, 3, 3.1789 * (Pnh3 * Tdiv));
+      store_pref(F, (2.4268 * FOUR_PI) * hs_base);
+      F.dcE = (float)(19.858252418E-24 / 1.38E-23 * LOG2E_D * invT2);
+      o.fam[FAM_NH3_ROT] = F;
+      return;
+    }
+    case 3: {
+      store_tan(F, 0, 1, Ph2 * dpw(lTdiv, 0.73));
+      store_tan(F, 0, 2, Phe * dpw(lTdiv, 0.5716));
+      store_tan(F, 0, 3, Pnh3 * Tdiv);
+      store_pref(F, (1.1206 * FOUR_PI) * hs_base);
+      F.dcE = (float)(19.858252418E-24 / 1.38E-23 * LOG2E_D * invT2);
+      o.fam[FAM_NH3_V2] = F;
+      return;
+    }
+    case 4: {
+      for (int s = 0; s < 2; ++s)
+        for (int k = 0; k < 5; ++k)
+          for (int q = 0; q < NTH; ++q) o.dsjs[s][k][q] = 0.f;
+      const bool use_sjs = a.nh3_mode == NH3_SJS || (a.nh3_mode == NH3_HS_SJS && Pd >= 400.0);
+      if (use_sjs) {
+        const D5 rexp = 8.79 * dexp((-1.0 / 83.0) * T);
+        const D5 base = dexp(dc(9.024) - (1.0 / 20.3) * T) + (-0.9918) + Ph2;
+        const D5 GH2a = dexp2(rexp * dlog2(base));
+        const double J[7] = {1.690, 0.750, 0.6, 1.350, 0.300, 0.200, -0.45};
+        D5 S[7];
+        if (GH2a.v < 1e-12) {
+          for (int k = 0; k < 7; ++k) S[k] = dc(J[k]);
+        } else {
+          const D5 g = 2.34 * (dc(1.0) - 2.122 * (dexp((-1.0 / 116.8) * T) / GH2a));
+          S[0] = g;
+          S[1] = dc(0.46) + (1.0 / 3000.0) * T;
+          S[2] = dc(0.74);
+          S[3] = dc(5.7465) + g * (dc(-7.7644) + g * (dc(9.1931) + g * (dc(-5.6816) + 1.2307 * g)));
+          S[4] = dc(0.28) - (1.0 / 1750.0) * T;
+          S[5] = dc(0.50);
+          S[6] = dc(-0.45);
+        }
+        const D5 l296 = dlog2(dc(296.0) / T);
+        const D5 tt = dpw(l296, 2.0 / 3.0);
+        for (int s = 0; s < 2; ++s) {
+          D5 c[7];
+          for (int k = 0; k < 7; ++k) c[k] = s == 0 ? dc(J[k]) : S[k];
+          const D5 v[5] = {tt * (c[0] * Ph2 + c[1] * Phe), tt * (c[2] * Pnh3),
+                           tt * (c[3] * Ph2 + c[4] * Phe), tt * (c[5] * Pnh3), c[6] * Pnh3};
+          for (int k = 0; k < 5; ++k)
+            for (int q = 0; q < NTH; ++q) o.dsjs[s][k][q] = (float)v[k].d[q];
+        }
+        const D5 Pscale = dc(1.0) + 1.0E-5 * P;
+        store_pref(F, (7.244E+21 * GHZ * TWO_PI / 296.0) * (Pnh3 * dpw(l296, 3.5) * Pscale));
+        F.dcE = (float)(1.438396 * LOG2E_D * invT2);
+      }
+      o.fam[FAM_NH3_SJS] = F;
+      return;
+    }
+    case 5: {
+      const D5 l296 = dlog2(dc(296.0) / T);
+      const D5 t7 = dpw(l296, 0.7);
+      store_tan(F, 0, 0, t7 * (1.960 * Ph2 + 1.200 * Phe));
+      store_tan(F, 0, 1, t7 * Ph2s);
+      store_tan(F, 0, 7, 1.28 * Ph2s);
+      store_pref(F, (7.244E+21 * GHZ * TWO_PI / 296.0) * (Ph2s * dpw(l296, 3.5)));
+      F.dcE = (float)(1.438396 * LOG2E_D * invT2);
+      o.fam[FAM_H2S] = F;
+      return;
+    }
+    case 6: {
+      store_tan(F, 0, 1, dpw(lTdiv, 2.0 / 3.0) * (3.2930 * Ph2 + 1.6803 * Phe));
+      store_tan(F, 0, 2, 4.2157 * (Tdiv * Pph3));
+      store_pref(F, (7.244E+21 * GHZ * TWO_PI / 300.0) * (Pph3 * dpw(lTdiv, 3.5)));
+      F.dcE = (float)(1.438396 * LOG2E_D * invT2);
+      o.fam[FAM_PH3] = F;
+      return;
+    }
+    default: {
+      store_tan(F, 0, 0, lTdiv);
+      store_tan(F, 0, 1, Ph2o);
+      store_tan(F, 0, 2, Ph2);
+      store_tan(F, 0, 3, Phe);
+      const D5 density = (0.997317 * 6.0221415e17 / 8.314472e-5) * (Ph2o / T);
+      store_pref(F, (4.342945e-4 / 434294.5) * (density * dpw(lTdiv, 2.5)));
+      F.dcE = (float)(300.0 * LOG2E_D * invT2);
+      o.fam[FAM_H2O] = F;
+      const double Cf_he = 1.0e6 * 1.03562010226e-10, Cf_h2 = 1.0e6 * 5.07722009423e-11;
+      const D5 th3 = Tdiv * Tdiv * Tdiv;
+      const D5 foreign = Cf_he * (Phe * Ph2o * th3) + Cf_h2 * (Ph2 * Ph2o * th3);
+      const D5 selfc = 3.1e-07 * (dpw(lTdiv, 12.0) * (1.0e6 * (Ph2o * Ph2o)));
+      const D5 cont = (4.342945 / 434294.5) * (foreign + selfc);
+      for (int q = 0; q < NTH; ++q) o.dh2o_cont[q] = (float)cont.d[q];
+      return;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ alpha JVP
+// Records of one line, float: value fields and derivatives along the
+// family's three tangents (T, P, ln X of its own gas).
+constexpr int JV_CHUNK = 64;
+constexpr int JV_NREC = 16;
+
+struct JvpShared {
+  float rec[2][JV_NREC][JV_CHUNK];   // [coefficient set][field][line]
+  double red[4][NTH + 1];
+};
+
+// Compensated float sum.
+struct KSum {
+  float s, c;
+  __device__ __forceinline__ void init() { s = c = 0.f; }
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ float val() const { return s - c; }
+};
+
+// Family tangent slots: T, P and the family's own abundance.
+__device__ __forceinline__ int fam_xtan(int fam) {
+  switch (fam) {
+    case FAM_H2O: return TH_XH2O;
+    case FAM_H2S: return TH_XH2S;
+    case FAM_PH3: return -1;
+    default: return TH_XNH3;
+  }
+}
+
+__device__ __forceinline__ float tan3(const float* d5, int q, int xt) {
+  return q == 0 ? d5[TH_T] : (q == 1 ? d5[TH_P] : (xt >= 0 ? d5[xt] : 0.f));
+}
+
+__device__ __forceinline__ float strength(const LineTable& t, const LayerFam& F, int li) {
+  const float Eh = t.Eh[li], El = t.El[li];
+  const float ph = F.cEh * Eh;
+  const float pl = fmaf(F.cEh, Eh, -ph) + fmaf(F.cEh, El, F.cEl * Eh);
+  float s, e;
+  two_sum(t.l2Ih[li] - F.M2, ph, s, e);
+  const float lo = e + pl + t.l2Il[li];
+  const float ti = rintf(s);
+  const float tf = (s - ti) + lo;
+  if (ti < -140.f) return 0.f;
+  return ldexpf(exp2f(tf), (int)ti);
+}
+
+// Ben-Reuven record, fields: 0 g, 1 z, 2 KH, 3 KL, 4 S, 5 dlnS/dT,
+// 6..8 dg, 9..11 dz, 12..14 dK.
+__device__ void jv_br_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int set,
+                             int li, int xt, float* r, int stride) {
+  const float* c = LF.c[set];
+  const float w1 = t.w1[li], w2 = t.w2[li];
+  const float g = c[0] + c[1] * w1 + c[2] * w2;
+  const float z = c[3] + c[4] * w1 + c[5] * g;
+  const float d = c[6] * g + c[7];
+  const float fo = t.ch[li];
+  float KH, e;
+  two_sum(t.c2h[li], fmaf(2.f * fo + d, d, (g - z) * (g + z)), KH, e);
+  const float KL = e + t.c2l[li];
+  r[0 * stride] = g;
+  r[1 * stride] = z;
+  r[2 * stride] = KH;
+  r[3 * stride] = KL;
+  r[4 * stride] = strength(t, LF, li);
+  r[5 * stride] = (float)LN2 * (t.Eh[li] + t.El[li]) * FT.dcE;
+  for (int q = 0; q < 3; ++q) {
+    auto dcq = [&](int k) { return tan3(FT.dc[set][k], q, xt); };
+    const float dg = dcq(0) + dcq(1) * w1 + dcq(2) * w2;
+    const float dz = dcq(3) + dcq(4) * w1 + dcq(5) * g + c[5] * dg;
+    const float dd = dcq(6) * g + c[6] * dg + dcq(7);
+    r[(6 + q) * stride] = dg;
+    r[(9 + q) * stride] = dz;
+    r[(12 + q) * stride] = 2.f * (fo + d) * dd + 2.f * g * dg - 2.f * z * dz;
+  }
+}
+
+// Gross record: 0 g, 2 KH, 3 KL, 4 S, 5 dlnS/dT, 6..8 dg.
+__device__ void jv_gross_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int li,
+                                int xt, float* r, int stride) {
+  const float g = LF.c[0][1] * t.w1[li] + LF.c[0][2] * t.w2[li] + LF.c[0][3] * t.w3[li];
+  r[0 * stride] = g;
+  r[2 * stride] = t.c2h[li];
+  r[3 * stride] = t.c2l[li];
+  r[4 * stride] = strength(t, LF, li);
+  r[5 * stride] = (float)LN2 * (t.Eh[li] + t.El[li]) * FT.dcE;
+  for (int q = 0; q < 3; ++q)
+    r[(6 + q) * stride] = tan3(FT.dc[0][1], q, xt) * t.w1[li] + tan3(FT.dc[0][2], q, xt) * t.w2[li] +
+                          tan3(FT.dc[0][3], q, xt) * t.w3[li];
+}
+
+// VVW record: 0 df, 2 fo_hi, 3 fo_lo, 4 S, 5 dlnS/dT, 6..8 d(df).
+__device__ void jv_vvw_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int li,
+                              int xt, float* r, int stride, float* base, float* dbase) {
+  const float l2T = LF.c[0][0];
+  const float e1 = exp2f(t.x1[li] * l2T), e2 = exp2f(t.x2[li] * l2T), e3 = exp2f(t.x3[li] * l2T);
+  const float df = LF.c[0][1] * t.w1[li] * e1 + LF.c[0][2] * t.w2[li] * e2 + LF.c[0][3] * t.w3[li] * e3;
+  const float S = strength(t, LF, li);
+  const float dlnS = (float)LN2 * (t.Eh[li] + t.El[li]) * FT.dcE;
+  r[0 * stride] = df;
+  r[2 * stride] = t.ch[li];
+  r[3 * stride] = t.cl[li];
+  r[4 * stride] = S;
+  r[5 * stride] = dlnS;
+  const float h = S * df, den = 562500.f + df * df;
+  *base += 2.f * h / den;
+  for (int q = 0; q < 3; ++q) {
+    const float dl2T = tan3(FT.dc[0][0], q, xt);
+    const float ddf = tan3(FT.dc[0][1], q, xt) * t.w1[li] * e1 + tan3(FT.dc[0][2], q, xt) * t.w2[li] * e2 +
+                      tan3(FT.dc[0][3], q, xt) * t.w3[li] * e3 +
+                      (float)LN2 * dl2T *
+                          (LF.c[0][1] * t.w1[li] * e1 * t.x1[li] + LF.c[0][2] * t.w2[li] * e2 * t.x2[li] +
+                           LF.c[0][3] * t.w3[li] * e3 * t.x3[li]);
+    r[(6 + q) * stride] = ddf;
+    const float dh = (q == 0 ? h * dlnS : 0.f) + S * ddf;
+    dbase[q] += 2.f * dh / den - 2.f * h * 2.f * df * ddf / (den * den);
+  }
+}
+
+// nh3_sjs record: 2 KH0, 3 KL0 ((fo + shift)^2), 4 S, 5 dlnS/dT, 6 G0, 9..11 dK0.
+__device__ void jv_sjs_record(const LineTable& t, const LayerFam& LF, const FamTan& FT,
+                              const LayerTan& LT, float shift, int li, float* r, int stride) {
+  const float fo = t.ch[li];
+  float KH, e;
+  two_sum(t.c2h[li], (2.f * fo + shift) * shift, KH, e);
+  r[2 * stride] = KH;
+  r[3 * stride] = e + t.c2l[li];
+  r[4 * stride] = strength(t, LF, li);
+  r[5 * stride] = (float)LN2 * (t.Eh[li] + t.El[li]) * FT.dcE;
+  r[6 * stride] = t.w1[li];
+  for (int q = 0; q < 3; ++q) r[(9 + q) * stride] = 2.f * (fo + shift) * tan3(LT.dsjs[0][4], q, TH_XNH3);
+}
+
+// Ben-Reuven term and its three derivatives.
+__device__ __forceinline__ void br_eval(float F, float FL, float g, float z, float KH, float KL,
+                                        float S, float dlnS, const float* dg, const float* dz,
+                                        const float* dK, KSum& val, KSum* der) {
+  const float e = (F - KH) + (FL - KL);
+  const float K = KH + KL;
+  const float den = fmaf(e, e, 4.f * F * g * g);
+  const float r = 1.f / den;
+  const float gp = g + z, gm = g - z;
+  const float n = fmaf(gm, F, gp * K);
+  const float t = S * n * r;
+  val.add(t);
+  for (int q = 0; q < 3; ++q) {
+    const float dn = (dg[q] - dz[q]) * F + (dg[q] + dz[q]) * K + gp * dK[q];
+    const float dden = -2.f * e * dK[q] + 8.f * F * g * dg[q];
+    der[q].add((q == 0 ? t * dlnS : 0.f) + S * (dn - n * r * dden) * r);
+  }
+}
+
+__global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
+  __shared__ JvpShared sh;
+  const int L = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int j = blockIdx.y * blockDim.x + tid;
+  const bool on = j < a.nf;
+  const LayerParams& lp = a.lp[L];
+  const LayerTan& LT = a.lt[L];
+  // this thread's frequency
+  const double f = on ? a.freqs[j] : 1.0, fh = on ? a.freqs_hs[j] : 1.0;
+  float F, FL, Fh, FhL, fq, fql;
+  split_double(f * f, F, FL);
+  split_double(fh * fh, Fh, FhL);
+  split_double(f, fq, fql);
+  const int set = fh > 30.0 ? 1 : 0;
+  const float wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)((f - 26.0) / 8.0));
+  const bool nh3 = a.cfg.nh3_mode != NH3_OFF;
+  // per family: value sum and three derivative sums
+  float fv[NFAM], fd[NFAM][3];
+  float base = 0.f, dbase[3] = {0.f, 0.f, 0.f};
+  for (int fam = 0; fam < NFAM; ++fam) {
+    fv[fam] = 0.f;
+    fd[fam][0] = fd[fam][1] = fd[fam][2] = 0.f;
+    bool en;
+    switch (fam) {
+      case FAM_NH3_INV:
+      case FAM_NH3_ROT:
+      case FAM_NH3_V2: en = nh3 && lp.use_hs; break;
+      case FAM_NH3_SJS: en = nh3 && lp.use_sjs; break;
+      case FAM_H2O: en = a.cfg.use_h2o; break;
+      case FAM_H2S: en = a.cfg.use_h2s; break;
+      default: en = a.cfg.use_ph3; break;
+    }
+    const LineTable& t = a.tab[fam];
+    if (!en || t.n == 0) continue;
+    const LayerFam& LF = lp.fam[fam];
+    const FamTan& FT = LT.fam[fam];
+    const int xt = fam_xtan(fam);
+    const bool two = fam == FAM_NH3_INV;
+    const bool hsf = fam == FAM_NH3_INV || fam == FAM_NH3_ROT || fam == FAM_NH3_V2;
+    const float Fx = hsf ? Fh : F, FLx = hsf ? FhL : FL;
+    // nh3_sjs per-frequency coefficients and their derivatives
+    float A = 0.f, B = 0.f, C = 0.f, D = 0.f, dA[3] = {0, 0, 0}, dB[3] = {0, 0, 0}, dC[3] = {0, 0, 0},
+          dD[3] = {0, 0, 0};
+    if (fam == FAM_NH3_SJS) {
+      auto lerp = [&](float j0, float s0) { return fmaf(j0 - s0, wJ, s0); };
+      A = lerp(lp.sjs[0][0], lp.sjs[1][0]);
+      B = lerp(lp.sjs[0][1], lp.sjs[1][1]);
+      C = lerp(lp.sjs[0][2], lp.sjs[1][2]);
+      D = lerp(lp.sjs[0][3], lp.sjs[1][3]);
+      for (int q = 0; q < 3; ++q) {
+        dA[q] = lerp(tan3(LT.dsjs[0][0], q, xt), tan3(LT.dsjs[1][0], q, xt));
+        dB[q] = lerp(tan3(LT.dsjs[0][1], q, xt), tan3(LT.dsjs[1][1], q, xt));
+        dC[q] = lerp(tan3(LT.dsjs[0][2], q, xt), tan3(LT.dsjs[1][2], q, xt));
+        dD[q] = lerp(tan3(LT.dsjs[0][3], q, xt), tan3(LT.dsjs[1][3], q, xt));
+      }
+    }
+    KSum val, der[3];
+    val.init();
+    for (int q = 0; q < 3; ++q) der[q].init();
+    for (int c0 = 0; c0 < t.n; c0 += JV_CHUNK) {
+      const int nc = min(JV_CHUNK, t.n - c0);
+      for (int i = tid; i < nc; i += blockDim.x) {
+        const int li = c0 + i;
+        if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
+          jv_br_record(t, LF, FT, 0, li, xt, &sh.rec[0][0][i], JV_CHUNK);
+          if (two) jv_br_record(t, LF, FT, 1, li, xt, &sh.rec[1][0][i], JV_CHUNK);
+        } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
+          jv_gross_record(t, LF, FT, li, xt, &sh.rec[0][0][i], JV_CHUNK);
+        } else if (fam == FAM_H2O) {
+          jv_vvw_record(t, LF, FT, li, xt, &sh.rec[0][0][i], JV_CHUNK, &base, dbase);
+        } else {
+          jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, &sh.rec[0][0][i], JV_CHUNK);
+        }
+      }
+      __syncthreads();
+      if (on) {
+        const float(*R)[JV_CHUNK] = sh.rec[two ? set : 0];
+        for (int i = 0; i < nc; ++i) {
+          if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
+            const float dg[3] = {R[6][i], R[7][i], R[8][i]};
+            const float dz[3] = {R[9][i], R[10][i], R[11][i]};
+            const float dK[3] = {R[12][i], R[13][i], R[14][i]};
+            br_eval(Fx, FLx, R[0][i], R[1][i], R[2][i], R[3][i], R[4][i], R[5][i], dg, dz, dK, val,
+                    der);
+          } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
+            const float g = R[0][i], S = R[4][i];
+            const float e = (Fx - R[2][i]) + (FLx - R[3][i]);
+            const float den = fmaf(e, e, 4.f * Fx * g * g);
+            const float r = 1.f / den;
+            const float tt = S * g * r;
+            val.add(tt);
+            for (int q = 0; q < 3; ++q) {
+              const float dg = R[6 + q][i];
+              der[q].add((q == 0 ? tt * R[5][i] : 0.f) + S * (dg - g * r * 8.f * Fx * g * dg) * r);
+            }
+          } else if (fam == FAM_H2O) {
+            const float df = R[0][i], S = R[4][i];
+            const float dm = (fq - R[2][i]) + (fql - R[3][i]);
+            const float dp = fq + R[2][i];
+            const float d1 = fmaf(dm, dm, df * df), d2 = fmaf(dp, dp, df * df);
+            const float r1 = 1.f / d1, r2 = 1.f / d2;
+            const float h = S * df, u = r1 + r2;
+            val.add(h * u);
+            for (int q = 0; q < 3; ++q) {
+              const float ddf = R[6 + q][i];
+              const float dh = (q == 0 ? h * R[5][i] : 0.f) + S * ddf;
+              der[q].add(dh * u - h * 2.f * df * ddf * (r1 * r1 + r2 * r2));
+            }
+          } else {   // nh3_sjs
+            const float G0 = R[6][i], S = R[4][i];
+            const float g = fmaf(B, G0, A), z = fmaf(D, G0, C);
+            const float g2z2 = (g - z) * (g + z);
+            float dg[3], dz[3], dK[3];
+            for (int q = 0; q < 3; ++q) {
+              dg[q] = fmaf(dB[q], G0, dA[q]);
+              dz[q] = fmaf(dD[q], G0, dC[q]);
+              dK[q] = R[9 + q][i] + 2.f * g * dg[q] - 2.f * z * dz[q];
+            }
+            float KH, e;
+            two_sum(R[2][i], g2z2, KH, e);
+            br_eval(Fx, FLx, g, z, KH, e + R[3][i], S, R[5][i], dg, dz, dK, val, der);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    fv[fam] = val.val();
+    for (int q = 0; q < 3; ++q) fd[fam][q] = der[q].val();
+  }
+  // h2o base term summed over the CTA (every thread built some lines)
+  {
+    float v[4] = {base, dbase[0], dbase[1], dbase[2]};
+    for (int k = 0; k < 4; ++k)
+      for (int o = 16; o; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    __shared__ float s_b[4][4];
+    if ((tid & 31) == 0)
+      for (int k = 0; k < 4; ++k) s_b[tid >> 5][k] = v[k];
+    __syncthreads();
+    base = dbase[0] = dbase[1] = dbase[2] = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      base += s_b[w][0];
+      dbase[0] += s_b[w][1];
+      dbase[1] += s_b[w][2];
+      dbase[2] += s_b[w][3];
+    }
+  }
+  // assemble dalpha/dtheta (cm^-1) in float64 and contract with dTb/dalpha
+  double g5[NTH] = {0, 0, 0, 0, 0};
+  if (on) {
+    const double gal = a.galpha[(size_t)L * a.nf + j];
+    const double Fd = f * f, Fhd = fh * fh;
+    auto pref = [&](int fam) { return ldexp((double)lp.fam[fam].fm, lp.fam[fam].fe); };
+    // d(pref * S) / dtheta for a family with tangent triple (T, P, X_own)
+    double dal[NTH] = {0, 0, 0, 0, 0};
+    auto add_fam = [&](int fam, double mult, double s, const float* ds, double* out) {
+      const FamTan& FT = LT.fam[fam];
+      const double p = pref(fam) * mult;
+      const int xt = fam_xtan(fam);
+      out[TH_T] += p * ((double)FT.dlnpref[TH_T] * s + ds[0]);
+      out[TH_P] += p * ((double)FT.dlnpref[TH_P] * s + ds[1]);
+      for (int q = 2; q < NTH; ++q) {
+        const double dx = (q == xt) ? ds[2] : 0.0;
+        out[q] += p * ((double)FT.dlnpref[q] * s + dx);
+      }
+    };
+    // H2 CIA
+    if (a.cfg.use_h2)
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2] * (double)LT.dh2_cia[q] * Fd;
+    // H2O lines and continuum
+    if (a.cfg.use_h2o) {
+      double d[NTH] = {0, 0, 0, 0, 0};
+      const float ds[3] = {fd[FAM_H2O][0] - dbase[0], fd[FAM_H2O][1] - dbase[1], fd[FAM_H2O][2] - dbase[2]};
+      add_fam(FAM_H2O, 1.0, (double)fv[FAM_H2O] - base, ds, d);
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2O] * (d[q] + (double)LT.dh2o_cont[q]) * Fd;
+    }
+    if (a.cfg.use_h2s) {
+      double d[NTH] = {0, 0, 0, 0, 0};
+      add_fam(FAM_H2S, 1.0, fv[FAM_H2S], fd[FAM_H2S], d);
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2S] * d[q] * Fd;
+    }
+    if (a.cfg.use_ph3) {
+      double d[NTH] = {0, 0, 0, 0, 0};
+      add_fam(FAM_PH3, 1.0, fv[FAM_PH3], fd[FAM_PH3], d);
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_PH3] * d[q] * Fd;
+    }
+    if (nh3) {
+      double hs = 0.0, dhs[NTH] = {0, 0, 0, 0, 0}, sj = 0.0, dsj[NTH] = {0, 0, 0, 0, 0};
+      const double INVC[2] = {0.9301, 0.9862};
+      if (lp.use_hs) {
+        hs = Fhd * (pref(FAM_NH3_INV) * INVC[set] * fv[FAM_NH3_INV] +
+                    pref(FAM_NH3_ROT) * fv[FAM_NH3_ROT] + pref(FAM_NH3_V2) * fv[FAM_NH3_V2]);
+        add_fam(FAM_NH3_INV, INVC[set], fv[FAM_NH3_INV], fd[FAM_NH3_INV], dhs);
+        add_fam(FAM_NH3_ROT, 1.0, fv[FAM_NH3_ROT], fd[FAM_NH3_ROT], dhs);
+        add_fam(FAM_NH3_V2, 1.0, fv[FAM_NH3_V2], fd[FAM_NH3_V2], dhs);
+        for (int q = 0; q < NTH; ++q) dhs[q] *= Fhd;
+        if (hs < 0.0) {   // clamped to 1e-8 (nh3_hs.py:311-312): no derivative
+          hs = 1.0e-8;
+          for (int q = 0; q < NTH; ++q) dhs[q] = 0.0;
+        }
+      }
+      if (lp.use_sjs) {
+        sj = Fd * pref(FAM_NH3_SJS) * fv[FAM_NH3_SJS];
+        add_fam(FAM_NH3_SJS, 1.0, fv[FAM_NH3_SJS], fd[FAM_NH3_SJS], dsj);
+        for (int q = 0; q < NTH; ++q) dsj[q] *= Fd;
+      }
+      double dn[NTH];
+      if (lp.use_hs && lp.use_sjs) {
+        const double W = lp.blendW;
+        for (int q = 0; q < NTH; ++q) dn[q] = W * dsj[q] + (1.0 - W) * dhs[q];
+        dn[TH_P] += (double)LT.dblendW_dP * (sj - hs);
+      } else {
+        for (int q = 0; q < NTH; ++q) dn[q] = lp.use_hs ? dhs[q] : dsj[q];
+      }
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_NH3] * dn[q];
+    }
+    for (int q = 0; q < NTH; ++q) g5[q] = gal * dal[q];
+  }
+  // reduce over the CTA's frequencies
+  for (int q = 0; q < NTH; ++q)
+    for (int o = 16; o; o >>= 1) g5[q] += __shfl_xor_sync(0xffffffffu, g5[q], o);
+  if ((tid & 31) == 0)
+    for (int q = 0; q < NTH; ++q) sh.red[tid >> 5][q] = g5[q];
+  __syncthreads();
+  if (tid == 0) {
+    for (int q = 0; q < NTH; ++q) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh.red[w][q];
+      a.part[((size_t)L * gridDim.y + blockIdx.y) * NTH + q] = s;
+    }
+  }
+}
+
+// dT = sum of tiles + source term; dP; dln X for NH3, H2O, H2S.
+__global__ void rb_adjoint_final_kernel(int nL, int ntile, const double* part, const double* gsrc,
+                                        double* dT, double* dP, double* dlnX) {
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nL) return;
+  double s[NTH] = {0, 0, 0, 0, 0};
+  for (int t = 0; t < ntile; ++t)
+    for (int q = 0; q < NTH; ++q) s[q] += part[((size_t)L * ntile + t) * NTH + q];
+  dT[L] = s[TH_T] + gsrc[L];
+  dP[L] = s[TH_P];
+  dlnX[L] = s[TH_XNH3];
+  dlnX[nL + L] = s[TH_XH2O];
+  dlnX[2 * nL + L] = s[TH_XH2S];
+}
+
+// ------------------------------------------------------------------ launch
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
+                           double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st) {
+  const size_t nbuf = (size_t)ta.nb * ta.nf * ta.nL;
+  cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(double) * nbuf, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * nbuf, st);
+  if (e != cudaSuccess) return e;
+  const int nt = ta.nb * ta.nf;
+  if (nt > 0) rb_tb_adjoint_kernel<<<(nt + 127) / 128, 128, 0, st>>>(ta);
+  rb_adjoint_reduce_kernel<<<ta.nL, 128, 0, st>>>(ta, galpha, gsrc);
+  rb_layer_tan_kernel<<<(tn.nL * 8 + 255) / 256, 256, 0, st>>>(tn);
+  const int block = jv.nf >= 128 ? 128 : ((jv.nf + 31) / 32) * 32;
+  dim3 grid(jv.nL, (jv.nf + block - 1) / block);
+  rb_alpha_jvp_kernel<<<grid, block, 0, st>>>(jv);
+  rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(jv.nL, grid.y, jv.part, gsrc, dT, dP, dlnX);
+  return cudaGetLastError();
+}
+
+int adjoint_tiles(int nf) {
+  const int block = nf >= 128 ? 128 : ((nf + 31) / 32) * 32;
+  return (nf + block - 1) / block;
+}
+
+}  // namespace rb

@@ -120,6 +120,8 @@ struct rb_handle {
   int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
   DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base, d_done;
+  // adjoint workspaces
+  DBuf d_ga, d_gs, d_galpha, d_gsrc, d_lt, d_jpart, d_grad, d_dth;
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
@@ -142,6 +144,9 @@ namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
 cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st);
 int alpha_lines_occupancy(int M, int W);
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
+                           double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st);
+int adjoint_tiles(int nf);
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
                              float* R32, float* T32, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
@@ -607,7 +612,8 @@ int rb_destroy(rb_handle* h) {
                   &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part})
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
-                  &h->d_done})
+                  &h->d_done, &h->d_ga, &h->d_gs, &h->d_galpha, &h->d_gsrc, &h->d_lt, &h->d_jpart,
+                  &h->d_grad, &h->d_dth})
     b->release();
   for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
@@ -1065,6 +1071,139 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
   return forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
                       nb, b, weights, disc, Tb_out, Tb_avg, nullptr);
+}
+
+// Forward (recomputed) then the adjoint sweep: galpha from the scan adjoint,
+// alpha recomputed with its layer derivatives and contracted.
+int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
+                      const double* X, const double* R, const double* N, int nf,
+                      const double* freqs_host, const double* scale, double Req, double Rpol,
+                      double orient0, double orient1, int gtype, int limb, int nb, const double* b,
+                      const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
+                      double* dT, double* dP, double* dlnX) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs_host || !grad || !dT || !dP || !dlnX ||
+      (nb > 0 && !b))
+    return fail(RB_EINVAL, "null array");
+  if (nL < 2 || nb < 1) return fail(RB_EINVAL, "bad sizes");
+  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
+  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
+  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
+  RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
+  double* dTb = Tb_out ? Tb_out : h->d_Tb.as<double>();
+  double* davg = Tb_avg ? Tb_avg : (weights ? h->d_avg.as<double>() : nullptr);
+  if ((rc = forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
+                         nb, b, weights, 0, dTb, davg, nullptr)))
+    return rc;
+  const int launches = h->launches;
+  const int max_seg = 2 * nL + 4;
+  const size_t nbuf = (size_t)nb * nf * nL;
+  const int ntile = rb::adjoint_tiles(nf);
+  RB_CUDA(h->d_ga.ensure(sizeof(double) * nbuf));
+  RB_CUDA(h->d_gs.ensure(sizeof(double) * nbuf));
+  RB_CUDA(h->d_galpha.ensure(sizeof(double) * (size_t)nL * nf));
+  RB_CUDA(h->d_gsrc.ensure(sizeof(double) * nL));
+  RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
+  RB_CUDA(h->d_jpart.ensure(sizeof(double) * (size_t)nL * ntile * rb::NTH));
+  rb::TbAdjArgs ta{};
+  ta.nL = nL;
+  ta.nf = nf;
+  ta.nb = nb;
+  ta.max_seg = max_seg;
+  ta.alpha32 = h->d_a32.as<float>();
+  ta.T = T;
+  ta.nseg = h->d_nseg.as<int>();
+  ta.hds = h->d_hds.as<float>();
+  ta.layer = h->d_layer.as<int>();
+  ta.weights = weights;
+  ta.grad = grad;
+  ta.ga = h->d_ga.as<double>();
+  ta.gs = h->d_gs.as<double>();
+  rb::TanArgs tn{};
+  tn.nL = nL;
+  tn.P = P;
+  tn.T = T;
+  tn.X = X;
+  tn.nh3_mode = h->cfg.nh3_mode;
+  tn.h2state = h->cfg.h2state;
+  tn.out = h->d_lt.as<rb::LayerTan>();
+  rb::JvpArgs jv{};
+  jv.nL = nL;
+  jv.nf = nf;
+  jv.freqs = h->d_f.as<double>();
+  jv.freqs_hs = h->d_fhs.as<double>();
+  jv.lp = h->d_lp.as<rb::LayerParams>();
+  jv.lt = h->d_lt.as<rb::LayerTan>();
+  for (int f = 0; f < rb::NFAM; ++f) jv.tab[f] = h->fam[f].table();
+  jv.cfg = h->cfg;
+  jv.cfg.units_db = 0;
+  jv.galpha = h->d_galpha.as<double>();
+  jv.part = h->d_jpart.as<double>();
+  RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_galpha.as<double>(), h->d_gsrc.as<double>(), dT, dP,
+                             dlnX, st));
+  h->launches = launches + 5;
+  return RB_OK;
+}
+
+int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const double* X,
+               const double* R, const double* N, int nf, const double* freqs, const double* scale,
+               double Req, double Rpol, double orient0, double orient1, int gtype, int limb, int nb,
+               const double* b, const double* weights, const double* grad, double* Tb_out,
+               double* Tb_avg, double* dT, double* dP, double* dlnX) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs || !grad || !dT || !dP || !dlnX || (nb > 0 && !b))
+    return fail(RB_EINVAL, "null array");
+  int rc = validate_atm(nL, P, T, X);
+  if (rc) return rc;
+  if ((rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b))) return rc;
+  if (nb < 1) return fail(RB_EINVAL, "nb must be >= 1");
+  if (weights && !finite_all(weights, nb)) return fail(RB_EINVAL, "weights not finite");
+  if (!finite_all(grad, weights ? (size_t)nf : (size_t)nb * nf)) return fail(RB_EINVAL, "grad not finite");
+  if (scale && !finite_all(scale, (size_t)nL * rb::NGAS)) return fail(RB_EINVAL, "scale not finite");
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  RB_CUDA(upload(h->d_P, P, nL, st));
+  RB_CUDA(upload(h->d_T, T, nL, st));
+  RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
+  RB_CUDA(upload(h->d_R, R, nL, st));
+  RB_CUDA(upload(h->d_N, N, nL, st));
+  RB_CUDA(upload(h->d_b, b, 2 * (size_t)nb, st));
+  RB_CUDA(upload(h->d_grad, grad, weights ? (size_t)nf : (size_t)nb * nf, st));
+  const double* dscale = nullptr;
+  if (scale) {
+    RB_CUDA(upload(h->d_scale, scale, (size_t)nL * rb::NGAS, st));
+    dscale = h->d_scale.as<double>();
+  }
+  const double* dw = nullptr;
+  if (weights) {
+    RB_CUDA(upload(h->d_w, weights, nb, st));
+    dw = h->d_w.as<double>();
+  }
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
+  RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
+  RB_CUDA(h->d_dth.ensure(sizeof(double) * 5 * (size_t)nL));
+  double* dd = h->d_dth.as<double>();
+  if ((rc = rb_adjoint_device(h, st, nL, h->d_P.as<double>(), h->d_T.as<double>(),
+                              h->d_X.as<double>(), h->d_R.as<double>(), h->d_N.as<double>(), nf,
+                              freqs, dscale, Req, Rpol, orient0, orient1, gtype, limb, nb,
+                              h->d_b.as<double>(), dw, h->d_grad.as<double>(), h->d_Tb.as<double>(),
+                              dw ? h->d_avg.as<double>() : nullptr, dd, dd + nL, dd + 2 * (size_t)nL)))
+    return rc;
+  if (Tb_out)
+    RB_CUDA(cudaMemcpyAsync(Tb_out, h->d_Tb.p, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
+  if (Tb_avg && dw)
+    RB_CUDA(cudaMemcpyAsync(Tb_avg, h->d_avg.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaMemcpyAsync(dT, dd, sizeof(double) * nL, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaMemcpyAsync(dP, dd + nL, sizeof(double) * nL, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaMemcpyAsync(dlnX, dd + 2 * (size_t)nL, sizeof(double) * 3 * nL, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
 }
 
 int rb_last_launch_count(rb_handle* h) { return h ? h->launches : 0; }

@@ -114,4 +114,60 @@ struct TbArgs {
   float4* part;           // [nb][nchunk][nf] {dtau_hi, dtau_lo, intW, TbL} per chunk
 };
 
+// ---------------------------------------------------------------- adjoint
+// Tangent directions of one layer's parameters.
+constexpr int NTH = 5;
+enum Tangent : int { TH_T = 0, TH_P = 1, TH_XNH3 = 2, TH_XH2O = 3, TH_XH2S = 4 };
+
+// Derivatives of one family's layer coefficients (LayerFam) along the five
+// tangents: dc for c[s][k], dlnpref for the log of the strength prefactor
+// fm 2^fe, dcE = d cE / dT (log2 units per K).
+struct FamTan {
+  float dc[2][8][NTH];
+  float dlnpref[NTH];
+  float dcE;
+};
+
+struct LayerTan {
+  FamTan fam[NFAM];
+  float dsjs[2][5][NTH];   // nh3_sjs coefficient sets
+  float dh2_cia[NTH];
+  float dh2o_cont[NTH];
+  float dblendW_dP;        // nh3_hs_sjs blend weight, per bar
+};
+
+struct TanArgs {
+  int nL;
+  const double* P;
+  const double* T;
+  const double* X;
+  int nh3_mode, h2state;
+  LayerTan* out;
+};
+
+struct TbAdjArgs {
+  int nL, nf, nb, max_seg;
+  const float* alpha32;   // [nL][nf] cm^-1 (forward absorption)
+  const double* T;        // [nL]
+  const int* nseg;        // [nb]
+  const float* hds;       // [nb][max_seg] ds/2 in cm
+  const int* layer;       // [nb][max_seg]
+  const double* weights;  // [nb] or null
+  const double* grad;     // [nf] (with weights: d loss / d Tb_avg) or [nb][nf]
+  double* ga;             // [nb][nf][nL] g dTb/dalpha
+  double* gs;             // [nb][nf][nL] g dTb/dT through the source term
+};
+
+struct JvpArgs {
+  int nL, nf;
+  const double* freqs;
+  const double* freqs_hs;
+  const LayerParams* lp;
+  const LayerTan* lt;
+  LineTable tab[NFAM];
+  AlphaConfig cfg;
+  const double* galpha;   // [nL][nf] d loss / d alpha
+  double* part;           // [nL][ntile][NTH]
+};
+
 }  // namespace rb

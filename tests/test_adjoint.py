@@ -1,0 +1,156 @@
+"""Adjoint: dTb/dT, dTb/dP and dTb/dln X per layer.
+
+The reference has no derivatives ("parity unpinned" for gradients); the
+gradient of loss = sum_f g_f Tb_avg(f) is pinned by central finite
+differences (step 1e-4) of the float64 oracle forward model, along random
+perturbations of the layer parameters (T Gaussian 5 K, ln X Gaussian 0.3
+dex correlated over 5 layers, P Gaussian 1 %) and along single layer
+parameters.  The scan's reverse sweep is checked on CPU against finite
+differences of the oracle's brightness scan.
+"""
+import numpy as np
+import pytest
+
+from oracle import adjoint as A
+from oracle import oracle as O
+from radiobear_gb300 import synth
+from tests import goldio as G
+
+LP = {k: i for i, k in enumerate(synth.PROPERTY_COLUMNS)}
+C = G.C
+
+# Directional derivatives: float32 absorption and float32 tangent sums
+# against float64 finite differences.
+DIR_RTOL = 3e-3
+LAYER_RTOL = 1e-2
+
+
+def small_case(nL=40, Pmax=700.0, nrays=3):
+    gas = synth.make_gas_table(nL, 1.0e-2, Pmax)
+    prop = synth.compute_properties(gas)
+    freqs = np.array([1.4, 5.0, 12.0, 22.2, 24.0, 33.0, 44.0, 60.0])
+    b, w = synth.gauss_legendre_disc(nrays)
+    return gas, prop[LP['R']], prop[LP['N']], freqs, b, w, G.c0_lines()
+
+
+def random_direction(rng, gas):
+    nL = gas.shape[1]
+    k = np.ones(5) / 5.0
+
+    def corr(sigma):
+        return np.convolve(rng.normal(0.0, sigma, nL + 4), k, mode='valid') * np.sqrt(5.0)
+
+    dex = 0.3 * np.log(10.0)
+    return dict(T=rng.normal(0.0, 5.0, nL), P=0.01 * gas[C['P']] * rng.normal(0.0, 1.0, nL),
+                NH3=corr(dex), H2O=corr(dex), H2S=corr(dex))
+
+
+def dot(grad, direction):
+    return (np.dot(grad['dT'], direction['T']) + np.dot(grad['dP'], direction['P']) +
+            np.dot(grad['dlnX'][0], direction['NH3']) + np.dot(grad['dlnX'][1], direction['H2O']) +
+            np.dot(grad['dlnX'][2], direction['H2S']))
+
+
+def test_brightness_vjp_matches_finite_differences():
+    """CPU: the reverse sweep of the scan against central differences."""
+    z = G.load('c0')
+    g = G.gas_table(z)
+    nL = g.shape[1]
+    rng = np.random.default_rng(7)
+    alpha = z['alpha_layers']
+    T = g[C['T']]
+    ds = z['ray0_ds']
+    lay = z['ray0_layer']
+    nf = alpha.shape[0]
+    gTb = rng.normal(size=nf)
+    ga, gT = A.brightness_vjp(ds, lay, alpha, T, gTb)
+
+    def loss(al, TT):
+        tb, _, _, _ = O.brightness(ds, lay, al, TT)
+        return float(np.dot(gTb, tb))
+
+    for (f, L) in [(0, 10), (3, 60), (7, 120), (12, 180), (20, nL - 1)]:
+        h = 1e-5 * np.max(alpha[f])
+        ap, am = alpha.copy(), alpha.copy()
+        ap[f, L] += h
+        am[f, L] -= h
+        fd = (loss(ap, T) - loss(am, T)) / (2 * h)
+        assert abs(ga[f, L] - fd) <= 2e-6 * abs(fd) + 1e-7 * np.max(np.abs(ga[f])), (f, L, ga[f, L], fd)
+    # source term: T enters only through the weighting of the emission
+    for L in (5, 50, 150):
+        Tp, Tm = T.copy(), T.copy()
+        Tp[L] += 1e-3
+        Tm[L] -= 1e-3
+        fd = (loss(alpha, Tp) - loss(alpha, Tm)) / 2e-3
+        assert abs(gT[L] - fd) <= 1e-6 * abs(fd) + 1e-7 * np.max(np.abs(gT)), (L, gT[L], fd)
+
+
+@pytest.fixture(scope='module')
+def engine():
+    from radiobear_gb300 import _native
+    e = _native.Engine(0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope='module')
+def case():
+    return small_case()
+
+
+def _run(engine, case, grad):
+    from radiobear_gb300 import catalog
+    from radiobear_gb300._native import x_matrix
+    gas, R, N, freqs, b, w, lines = case
+    catalog.upload(engine, lines)
+    engine.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    return engine.adjoint(gas[C['P']], gas[C['T']], x_matrix(gas, C), R, N, freqs, b, G.REQ,
+                          G.RPOL, grad, weights=w)
+
+
+@pytest.mark.gpu
+def test_adjoint_forward_matches_oracle(engine, case):
+    gas, R, N, freqs, b, w, lines = case
+    grad = np.ones(freqs.size)
+    out = _run(engine, case, grad)
+    tbs, _, avg = O.forward(gas, C, R, N, freqs, b, lines, G.REQ, G.RPOL, weights=w)
+    assert np.max(np.abs(out['Tb'] - tbs)) < 1e-3
+    assert np.max(np.abs(out['Tb_avg'] - avg)) < 1e-3
+
+
+@pytest.mark.gpu
+def test_adjoint_directional_derivatives(engine, case):
+    """32 random perturbations: <gradient, direction> against central
+    differences of the float64 oracle."""
+    gas, R, N, freqs, b, w, lines = case
+    rng = np.random.default_rng(3)
+    grad = rng.normal(size=freqs.size)
+    out = _run(engine, case, grad)
+    errs = []
+    for k in range(32):
+        d = random_direction(rng, gas)
+        fd = A.directional_fd(gas, C, R, N, freqs, b, lines, G.REQ, G.RPOL, w, grad, d, h=1e-4)
+        ad = dot(out, d)
+        errs.append(abs(ad - fd) / max(abs(fd), 1e-9))
+        assert abs(ad - fd) <= DIR_RTOL * abs(fd) + 1e-7, (k, ad, fd)
+    print('directional rel err max', max(errs))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('param', ['T', 'P', 'NH3', 'H2O', 'H2S'])
+def test_adjoint_single_layers(engine, case, param):
+    gas, R, N, freqs, b, w, lines = case
+    nL = gas.shape[1]
+    rng = np.random.default_rng(11)
+    grad = rng.normal(size=freqs.size)
+    out = _run(engine, case, grad)
+    key = {'T': out['dT'], 'P': out['dP'], 'NH3': out['dlnX'][0], 'H2O': out['dlnX'][1],
+           'H2S': out['dlnX'][2]}[param]
+    scale = np.max(np.abs(key)) + 1e-30
+    for L in (3, 15, 27, nL - 3, nL - 1):
+        v = np.zeros(nL)
+        v[L] = 1.0 if param != 'P' else gas[C['P'], L] * 1e-2
+        fd = A.directional_fd(gas, C, R, N, freqs, b, lines, G.REQ, G.RPOL, w, grad, {param: v},
+                              h=1e-4 if param != 'T' else 1e-3)
+        ad = key[L] * v[L]
+        assert abs(ad - fd) <= LAYER_RTOL * abs(fd) + 1e-4 * scale * abs(v[L]), (param, L, ad, fd)
