@@ -72,6 +72,79 @@ def workload_arrays(wl):
                 b=np.ascontiguousarray(wl.b), w=np.ascontiguousarray(wl.weights), C=C)
 
 
+GRAD_WORKLOAD = ('C3 differentiable forward model: 1000 layers (1e-3..500 bar) x 64 freqs '
+                 '(1..50 GHz log) x 16 Gauss-Legendre disc rays; forward Tb_avg + adjoint '
+                 'dTb/dT, dTb/dP, dTb/dlnX(NH3, H2O, H2S) per layer')
+
+
+def measure_gradients(args, dev, stream, flush):
+    """Spectra + gradients per second on the C3 workload: each step runs
+    rb_adjoint_device (forward, then the adjoint with alpha recomputed)
+    on device-resident inputs; e2e through rb_adjoint with host buffers."""
+    import torch
+    from radiobear_gb300 import _native, catalog, synth
+    from tests import goldio
+    cats = goldio.real_catalogues()
+    wl = synth.make_workload(3, real=cats)
+    wl['lines']['ph3wgt'] = cats['ph3wgt']
+    a = workload_arrays(wl)
+    nL, nf, nb = a['P'].size, a['freqs'].size, a['b'].shape[0]
+    eng = _native.Engine(dev.index or 0)
+    catalog.upload(eng, wl.lines)
+    eng.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+
+    def dt(x):
+        return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)
+
+    dP, dT, dX, dR, dN, db, dw = (dt(a[k]) for k in ('P', 'T', 'X', 'R', 'N', 'b', 'w'))
+    g = dt(np.random.default_rng(3).normal(size=nf))
+    gT, gP, gX = (torch.empty(n, dtype=torch.float64, device=dev) for n in (nL, nL, 3 * nL))
+    avg = torch.empty(nf, dtype=torch.float64, device=dev)
+    sp = stream.cuda_stream
+
+    def step():
+        eng.adjoint_device(sp, nL, nb, dP.data_ptr(), dT.data_ptr(), dX.data_ptr(), dR.data_ptr(),
+                           dN.data_ptr(), a['freqs'], db.data_ptr(), 71492.0, 66854.0,
+                           g.data_ptr(), gT.data_ptr(), gP.data_ptr(), gX.data_ptr(),
+                           weights=dw.data_ptr(), Tb_avg=avg.data_ptr())
+
+    step()
+    torch.cuda.synchronize()
+    launches = eng.last_launch_count()
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    n = max(10, min(args.steps, 50))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    torch.cuda.synchronize()
+    for i in range(n):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
+    host = {k: np.ascontiguousarray(a[k]) for k in ('P', 'T', 'X', 'R', 'N', 'b', 'w')}
+    gh = g.cpu().numpy()
+    e2e = []
+    for i in range(args.warmup + 10):
+        t0 = time.perf_counter()
+        out = eng.adjoint(host['P'], host['T'], host['X'], host['R'], host['N'], a['freqs'], host['b'],
+                          71492.0, 66854.0, gh, weights=host['w'])
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    h2d = sum(v.nbytes for v in host.values()) + gh.nbytes + a['freqs'].nbytes
+    d2h = out['dT'].nbytes + out['dP'].nbytes + out['dlnX'].nbytes + out['Tb'].nbytes + out['Tb_avg'].nbytes
+    eng.close()
+    return dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second',
+                value=1e3 / ms, unit='spectra+gradients/s', ms_per_step=ms, steps=n,
+                config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb),
+                gpu_launches_per_step=int(launches),
+                e2e=dict(value=1.0 / float(np.mean(e2e)), unit='spectra+gradients/s',
+                         h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
+                         api='rb_adjoint (C ABI, host buffers)'))
+
+
 def alpha_flops(wl):
     """Algorithmic FLOPs of one absorption launch: per (layer, line, freq)
     Ben-Reuven 10, Gross 8, VVW 12 (FMA = 2); blend layers add the nh3_sjs
@@ -361,6 +434,7 @@ def run_gpu(args, rank, world, local_rank):
     h2d = sum(host[k].nbytes for k in host) + a['freqs'].nbytes
     d2h = out['Tb_avg'].nbytes
 
+    grads = measure_gradients(args, dev, stream, flush)
     if rank != 0:
         return
     # roofline of the dominant kernel (absorption) and of the Tb scan
@@ -392,7 +466,7 @@ def run_gpu(args, rank, world, local_rank):
                            unit='GB/s', frac=(scan_gbs / hbm) if hbm else None,
                            algorithmic_bytes_per_launch=sbytes,
                            peak_source='MEASURED_PEAKS.json hbm_gbs (of measured)'),
-        phase_ms=ph, clocks=clocks)
+        phase_ms=ph, clocks=clocks, gradients=grads)
     if pool is not None:
         try:
             line['cpu_baseline'] = cpu_baseline(wl, args.cpu_sample_s, pool, cores)

@@ -154,3 +154,37 @@ def test_adjoint_single_layers(engine, case, param):
                               h=1e-4 if param != 'T' else 1e-3)
         ad = key[L] * v[L]
         assert abs(ad - fd) <= LAYER_RTOL * abs(fd) + 1e-4 * scale * abs(v[L]), (param, L, ad, fd)
+
+
+@pytest.mark.gpu
+def test_autograd_function(engine, case):
+    """torch.autograd through TbFunction: forward equals rb_forward, the
+    gradient equals rb_adjoint and a finite difference of the oracle."""
+    import torch
+    from radiobear_gb300 import catalog
+    from radiobear_gb300._native import x_matrix
+    from radiobear_gb300.autograd import TbModel
+    gas, R, N, freqs, b, w, lines = case
+    catalog.upload(engine, lines)
+    engine.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    X = x_matrix(gas, C)
+    model = TbModel(engine, R, N, freqs, b, w, X, G.REQ, G.RPOL)
+    dev = torch.device('cuda')
+    T = torch.tensor(gas[C['T']], dtype=torch.float64, device=dev, requires_grad=True)
+    P = torch.tensor(gas[C['P']], dtype=torch.float64, device=dev, requires_grad=True)
+    lnX = torch.tensor(np.log(np.stack([gas[C['NH3']], gas[C['H2O']], gas[C['H2S']]])),
+                       dtype=torch.float64, device=dev, requires_grad=True)
+    rng = np.random.default_rng(5)
+    gw = rng.normal(size=freqs.size)
+    avg = model(T, P, lnX)
+    loss = (avg * torch.tensor(gw, dtype=torch.float64, device=dev)).sum()
+    loss.backward()
+    ref = _run(engine, case, gw)
+    np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(T.grad.cpu().numpy(), ref['dT'], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(P.grad.cpu().numpy(), ref['dP'], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(lnX.grad.cpu().numpy(), ref['dlnX'], rtol=1e-12, atol=0)
+    d = random_direction(rng, gas)
+    fd = A.directional_fd(gas, C, R, N, freqs, b, lines, G.REQ, G.RPOL, w, gw, d, h=1e-4)
+    ad = dot(dict(dT=T.grad.cpu().numpy(), dP=P.grad.cpu().numpy(), dlnX=lnX.grad.cpu().numpy()), d)
+    assert abs(ad - fd) <= DIR_RTOL * abs(fd) + 1e-7
