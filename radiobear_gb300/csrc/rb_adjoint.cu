@@ -3,15 +3,15 @@
 // quadrature average).  The ray paths are held fixed (they depend on the
 // layer radii and refractive indices, inputs of their own).
 //
-//   rb_tb_adjoint_kernel    one thread per (ray, frequency): the forward
-//                           scan of Brightness.single (brightness.py:53-117)
-//                           in float64, then the reverse sweep with the
-//                           optical depth recomputed backwards,
+//   rb_tb_adj_lambda_kernel, rb_tb_adj_grad_kernel
+//                           reverse sweep of the scan of Brightness.single
+//                           (brightness.py:53-117), chunk-parallel like the
+//                           forward scan, with
 //                             dTb/dW_i  = c_i (T_i - Tb) / intW,
 //                             dTb/da_k  = w_k E_k + d_{k-1}/2 Lam_k + d_k/2 Lam_{k+1},
 //                             Lam_k     = sum_{i>=k} dTb/dW_i (-a_i E_i),
 //                           (c_i the trapezoid node weight, E = exp(-tau));
-//                           writes g dTb/dalpha and g W c / intW (the
+//                           adds g dTb/dalpha and g W c / intW (the
 //                           source-temperature term) per visited layer.
 //   rb_adjoint_reduce_kernel sums those over rays (fixed order).
 //   rb_layer_tan_kernel     eight threads per layer: the layer coefficients
@@ -19,7 +19,7 @@
 //                           prefactors, continua) in dual numbers, giving
 //                           their derivatives with respect to the layer's
 //                           T, P, ln X_NH3, ln X_H2O, ln X_H2S.
-//   rb_alpha_jvp_kernel     one CTA per (layer, 128 frequencies): alpha is
+//   rb_alpha_jvp_kernel     one CTA per (layer, 64 frequencies): alpha is
 //                           recomputed line by line together with its
 //                           derivatives with respect to the five layer
 //                           parameters (each family depends on T, P and its
@@ -42,74 +42,219 @@ __device__ __forceinline__ int wrap_l(int l, int nL) {
 }
 
 // ------------------------------------------------------------------ scan adjoint
-__global__ void __launch_bounds__(128) rb_tb_adjoint_kernel(TbAdjArgs a) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int b = idx / a.nf, j = idx - b * a.nf;
-  if (b >= a.nb) return;
-  const int n = min(max(a.nseg[b], 0), a.max_seg);
-  const double gb = a.weights ? a.weights[b] * a.grad[j] : a.grad[(size_t)b * a.nf + j];
-  if (n < 2 || gb == 0.0) return;
+// The forward's chunk partials (rb_tb_chunk_kernel: per ray, chunk of
+// ADJ_CHUNK segments and frequency, the chunk's optical depth as a
+// double-float and its intW / TbL from a local optical depth of 0) give the
+// optical depth at every chunk start and Tb; the reverse sweep then runs
+// chunk by chunk in parallel:
+//   rb_tb_adj_lambda_kernel  S_c = sum over the chunk's nodes of
+//                            dTb/dtau_k = -w_k a_k E_k
+//   rb_tb_adj_grad_kernel    Lam after the chunk = sum of S over later
+//                            chunks, then the chunk's nodes in reverse.
+constexpr int ADJ_CHUNK = 128;   // = the forward scan's chunk (rb_tb.cu)
+
+struct ChunkState {
+  double tau_c;    // optical depth at this chunk's first node
+  float Tb, rIW;
+  bool live;       // TbL >= T_cmb (else Tb is clamped and has no gradient)
+};
+
+// Combine of the forward's partials (the arithmetic of rb_tb_combine_kernel).
+__device__ __forceinline__ ChunkState adj_combine(const TbAdjArgs& a, int b, int c, int f, int nc) {
+  const float4* part = a.part + (size_t)b * a.nchunk * a.nf + f;
+  float ph = 0.f, pl = 0.f;
+  float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
+  ChunkState st;
+  st.tau_c = 0.0;
+  for (int k = 0; k < nc; ++k) {
+    if (k == c) st.tau_c = (double)ph + (double)pl;
+    const float4 p = part[(size_t)k * a.nf];
+    const float sc = __expf(-ph) * (1.f - pl);
+    float y = sc * p.z - iwc, t = iw + y;
+    iwc = (t - iw) - y;
+    iw = t;
+    y = sc * p.w - tbc;
+    t = tb + y;
+    tbc = (t - tb) - y;
+    tb = t;
+    float s, e;
+    two_sum(ph, p.x, s, e);
+    e += pl + p.y;
+    ph = s + e;
+    pl = e - (ph - s);
+  }
+  const float TbL = tb - tbc, IW = iw - iwc;
+  st.live = !(TbL < (float)T_CMB_ADJ) && IW > 0.f;
+  st.Tb = st.live ? TbL / IW : (float)T_CMB_ADJ;
+  st.rIW = st.live ? 1.f / IW : 0.f;
+  return st;
+}
+
+// The chunk's path nodes staged in shared memory (layer offsets, T,
+// half-lengths), so the loops' only global loads are the coalesced
+// alpha[layer][f] rows.
+struct AdjStage {
+  int off[ADJ_CHUNK + 1];
+  int lay[ADJ_CHUNK + 1];
+  float T[ADJ_CHUNK + 1];
+  float hd[ADJ_CHUNK + 1];
+};
+
+__device__ __forceinline__ void adj_stage(const TbAdjArgs& a, AdjStage& sg, int b, int i0, int ns,
+                                          int N) {
   const float* hd = a.hds + (size_t)b * a.max_seg;
   const int* lay = a.layer + (size_t)b * a.max_seg;
-  const int nL = a.nL, nf = a.nf;
-  auto alp = [&](int i) { return (double)a.alpha32[(size_t)wrap_l(lay[i], nL) * nf + j]; };
-  const int N = n - 1;
-  // forward scan
-  double tau = 0.0, IW = 0.0, TL = 0.0, Wp = 0.0;
-  double ap = alp(0), Tp = a.T[wrap_l(lay[0], nL)];
-  for (int i = 0; i < N; ++i) {
-    const double d = 2.0 * (double)hd[i];
-    const double a1 = alp(i + 1), T1 = a.T[wrap_l(lay[i + 1], nL)];
-    tau += (ap + a1) * d * 0.5;
-    const double W1 = a1 * (double)__expf(-(float)tau);
-    IW += (Wp + W1) * d * 0.5;
-    TL += (Tp * Wp + T1 * W1) * d * 0.5;
-    Wp = W1;
-    ap = a1;
-    Tp = T1;
-  }
-  if (TL < T_CMB_ADJ || !(IW > 0.0)) return;   // clamped to T_cmb: no gradient
-  const double Tb = TL / IW, rIW = 1.0 / IW;
-  double* ga = a.ga + ((size_t)b * nf + j) * nL;
-  double* gs = a.gs + ((size_t)b * nf + j) * nL;
-  double Lnext = 0.0;          // Lam_{i+1}
-  double ti = tau;             // tau_N
-  double ai = alp(N);
-  for (int i = N; i >= 0; --i) {
-    const int Li = wrap_l(lay[i], nL);
-    const double Ti = a.T[Li];
-    const double dprev = i >= 1 ? 2.0 * (double)hd[i - 1] : 0.0;
-    const double dcur = i < N ? 2.0 * (double)hd[i] : 0.0;
-    const double ci = 0.5 * (dprev + dcur);
-    const double Ei = i >= 1 ? (double)__expf(-(float)ti) : 0.0;
-    const double wi = ci * (Ti - Tb) * rIW;
-    const double Wi = ai * Ei;
-    const double Li_ = Lnext - wi * ai * Ei;   // Lam_i (lambda_0 = 0 since E_0 = 0 here)
-    const double gA = (i >= 1 ? wi * Ei + 0.5 * dprev * Li_ : 0.0) + 0.5 * dcur * Lnext;
-    ga[Li] += gb * gA;
-    gs[Li] += gb * Wi * ci * rIW;
-    if (i >= 1) {
-      const double am = alp(i - 1);
-      ti -= (am + ai) * dprev * 0.5;
-      ai = am;
-    }
-    Lnext = Li_;
+  for (int t = threadIdx.x; t <= ns; t += blockDim.x) {
+    const int L = wrap_l(lay[i0 + t], a.nL);
+    sg.lay[t] = L;
+    sg.off[t] = L * a.nf;
+    sg.T[t] = (float)a.T[L];
+    sg.hd[t] = (i0 + t < N) ? hd[i0 + t] : 0.f;
   }
 }
 
-// galpha[L][j] = sum_b ga[b][j][L];  gsrc[L] = sum_b sum_j gs[b][j][L]
+__global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
+  __shared__ AdjStage sg;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y, b = blockIdx.z;
+  const int n = min(max(a.nseg[b], 0), a.max_seg);
+  const int N = n - 1;
+  const int nc = N > 0 ? (N + ADJ_CHUNK - 1) / ADJ_CHUNK : 0;
+  const int i0 = c * ADJ_CHUNK;
+  if (c >= nc) {
+    if (f < a.nf) a.S[((size_t)b * a.nchunk + c) * a.nf + f] = 0.f;
+    return;
+  }
+  const int ns = min(ADJ_CHUNK, N - i0);
+  adj_stage(a, sg, b, i0, ns, N);
+  __syncthreads();
+  if (f >= a.nf) return;
+  float* S = a.S + ((size_t)b * a.nchunk + c) * a.nf + f;
+  const ChunkState st = adj_combine(a, b, c, f, nc);
+  if (!st.live) {
+    *S = 0.f;
+    return;
+  }
+  const float* al = a.alpha32 + f;
+  double tl = 0.0, lam = 0.0;
+  float a0 = al[sg.off[0]];
+  for (int s = 0; s < ns; ++s) {
+    const float ak = al[sg.off[s + 1]];
+    const float d = 2.f * sg.hd[s];
+    tl += (double)((a0 + ak) * d * 0.5f);
+    const float dk = 2.f * sg.hd[s + 1];
+    const float ck = 0.5f * (d + dk);
+    const float Ek = __expf(-(float)tl);
+    const float wk = ck * (sg.T[s + 1] - st.Tb) * st.rIW;
+    lam -= (double)(wk * ak * Ek);
+    a0 = ak;
+  }
+  *S = (float)(exp(-st.tau_c) * lam);
+}
+
+__global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
+  __shared__ AdjStage sg;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y, b = blockIdx.z;
+  const int n = min(max(a.nseg[b], 0), a.max_seg);
+  const int N = n - 1;
+  const int nc = N > 0 ? (N + ADJ_CHUNK - 1) / ADJ_CHUNK : 0;
+  if (c >= nc) return;
+  const int i0 = c * ADJ_CHUNK;
+  const int ns = min(ADJ_CHUNK, N - i0);
+  adj_stage(a, sg, b, i0, ns, N);
+  __syncthreads();
+  if (f >= a.nf) return;
+  const int nf = a.nf;
+  // per node: g dTb/dalpha and g dTb/dT (source term), [nb][max_seg][nf]
+  double* gn = a.ga + (size_t)b * a.max_seg * nf + f;
+  double* sn = a.gs + (size_t)b * a.max_seg * nf + f;
+  const double gb = a.weights ? a.weights[b] * a.grad[f] : a.grad[(size_t)b * a.nf + f];
+  const ChunkState st = adj_combine(a, b, c, f, nc);
+  if (gb == 0.0 || !st.live) {
+    for (int k = (c == 0 ? 0 : i0 + 1); k <= i0 + ns; ++k) {
+      gn[(size_t)k * nf] = 0.0;
+      sn[(size_t)k * nf] = 0.0;
+    }
+    return;
+  }
+  const float* S = a.S + (size_t)b * a.nchunk * a.nf + f;
+  double Lnext = 0.0;    // Lam of the node after this chunk's last node
+  for (int k = c + 1; k < nc; ++k) Lnext += (double)S[(size_t)k * a.nf];
+  const float* al = a.alpha32 + f;
+  // local optical depth at the chunk's last node
+  double tl = 0.0;
+  {
+    float ap = al[sg.off[0]];
+    for (int s = 0; s < ns; ++s) {
+      const float ak = al[sg.off[s + 1]];
+      tl += (double)((ap + ak) * (2.f * sg.hd[s]) * 0.5f);
+      ap = ak;
+    }
+  }
+  const double Ec = exp(-st.tau_c);
+  // nodes i0+ns .. i0+1 in reverse (node i0 belongs to the previous chunk,
+  // except node 0, which chunk 0 handles last)
+  float ak = al[sg.off[ns]];
+  for (int t = ns; t > 0; --t) {
+    const int k = i0 + t;
+    const float dprev = 2.f * sg.hd[t - 1];
+    const float dcur = 2.f * sg.hd[t];
+    const float ck = 0.5f * (dprev + dcur);
+    const double Ek = Ec * (double)__expf(-(float)tl);
+    const double wk = (double)(ck * (sg.T[t] - st.Tb) * st.rIW);
+    const double Lk_ = Lnext - wk * (double)ak * Ek;
+    gn[(size_t)k * nf] = gb * (wk * Ek + 0.5 * (double)dprev * Lk_ + 0.5 * (double)dcur * Lnext);
+    sn[(size_t)k * nf] = gb * (double)ak * Ek * (double)ck * (double)st.rIW;
+    const float am = al[sg.off[t - 1]];
+    tl -= (double)((am + ak) * dprev * 0.5f);
+    ak = am;
+    Lnext = Lk_;
+  }
+  if (c == 0) {   // node 0: W_0 = 0, only the segment term
+    gn[0] = gb * 0.5 * (double)(2.f * sg.hd[0]) * Lnext;
+    sn[0] = 0.0;
+  }
+}
+
+// Inverse of the paths: first and last node of each ray at each layer (a
+// path visits a layer at most twice: down to the tangent point and back).
+__global__ void rb_ray_inverse_kernel(TbAdjArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+  const int n = min(max(a.nseg[b], 0), a.max_seg);
+  if (k >= n || n < 2) return;
+  const int L = wrap_l(a.layer[(size_t)b * a.max_seg + k], a.nL);
+  atomicMin(&a.inv[((size_t)b * a.nL + L) * 2 + 0], k);
+  atomicMax(&a.inv[((size_t)b * a.nL + L) * 2 + 1], k);
+}
+
+__global__ void rb_ray_inverse_init_kernel(int n, int2* inv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) inv[i] = make_int2(0x7fffffff, -1);
+}
+
+// galpha[L][f] = sum over rays and the (at most two) nodes at layer L of
+// the node values; gsrc[L] likewise summed over frequencies.  Fixed order.
 __global__ void __launch_bounds__(128) rb_adjoint_reduce_kernel(TbAdjArgs a, double* galpha,
                                                                 double* gsrc) {
   const int L = blockIdx.x;
   const int nL = a.nL, nf = a.nf;
   double src = 0.0;
-  for (int j = threadIdx.x; j < nf; j += blockDim.x) {
+  for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double g = 0.0;
     for (int b = 0; b < a.nb; ++b) {
-      g += a.ga[((size_t)b * nf + j) * nL + L];
-      src += a.gs[((size_t)b * nf + j) * nL + L];
+      const int k1 = a.inv[((size_t)b * nL + L) * 2 + 0], k2 = a.inv[((size_t)b * nL + L) * 2 + 1];
+      if (k2 < 0) continue;
+      const double* gn = a.ga + (size_t)b * a.max_seg * nf + f;
+      const double* sn = a.gs + (size_t)b * a.max_seg * nf + f;
+      g += gn[(size_t)k1 * nf];
+      src += sn[(size_t)k1 * nf];
+      if (k2 != k1) {
+        g += gn[(size_t)k2 * nf];
+        src += sn[(size_t)k2 * nf];
+      }
     }
-    galpha[(size_t)L * nf + j] = g;
+    galpha[(size_t)L * nf + f] = g;
   }
   __shared__ double s[4];
   for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(0xffffffffu, src, o);
@@ -124,15 +269,16 @@ __global__ void __launch_bounds__(128) rb_adjoint_reduce_kernel(TbAdjArgs a, dou
 
 // ------------------------------------------------------------------ dual numbers
 // Value and derivatives with respect to the five layer parameters
-// (T, P, ln X_NH3, ln X_H2O, ln X_H2S), float64.
+// (T, P, ln X_NH3, ln X_H2O, ln X_H2S), float32 (the derivatives feed a
+// gradient, not the forward values).
 struct D5 {
-  double v, d[NTH];
+  float v, d[NTH];
 };
 
-__device__ __forceinline__ D5 dc(double v) {
+__device__ __forceinline__ D5 dc(float v) {
   D5 r;
   r.v = v;
-  for (int k = 0; k < NTH; ++k) r.d[k] = 0.0;
+  for (int k = 0; k < NTH; ++k) r.d[k] = 0.f;
   return r;
 }
 __device__ __forceinline__ D5 operator+(const D5& a, const D5& b) {
@@ -159,41 +305,41 @@ __device__ __forceinline__ D5 operator/(const D5& a, const D5& b) {
   for (int k = 0; k < NTH; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
   return r;
 }
-__device__ __forceinline__ D5 operator*(double s, const D5& a) {
+__device__ __forceinline__ D5 operator*(float s, const D5& a) {
   D5 r;
   r.v = s * a.v;
   for (int k = 0; k < NTH; ++k) r.d[k] = s * a.d[k];
   return r;
 }
-__device__ __forceinline__ D5 operator+(const D5& a, double s) {
+__device__ __forceinline__ D5 operator+(const D5& a, float s) {
   D5 r = a;
   r.v += s;
   return r;
 }
-__device__ __forceinline__ D5 chain(const D5& a, double fv, double dfdx) {
+__device__ __forceinline__ D5 chain(const D5& a, float fv, float dfdx) {
   D5 r;
   r.v = fv;
   for (int k = 0; k < NTH; ++k) r.d[k] = dfdx * a.d[k];
   return r;
 }
-__device__ __forceinline__ D5 dlog2(const D5& a) { return chain(a, log2(a.v), LOG2E_D / a.v); }
+__device__ __forceinline__ D5 dlog2(const D5& a) { return chain(a, log2f(a.v), (float)LOG2E_D / a.v); }
 __device__ __forceinline__ D5 dexp2(const D5& a) {
-  const double e = exp2(a.v);
-  return chain(a, e, LN2 * e);
+  const float e = exp2f(a.v);
+  return chain(a, e, (float)LN2 * e);
 }
 __device__ __forceinline__ D5 dexp(const D5& a) {
-  const double e = exp(a.v);
+  const float e = expf(a.v);
   return chain(a, e, e);
 }
 // 2^(e lg2x), the prep kernel's pw()
-__device__ __forceinline__ D5 dpw(const D5& lg2x, double e) { return dexp2(e * lg2x); }
-__device__ __forceinline__ D5 dmin1(const D5& a) { return a.v < 1.0 ? a : dc(1.0); }
+__device__ __forceinline__ D5 dpw(const D5& lg2x, float e) { return dexp2(e * lg2x); }
+__device__ __forceinline__ D5 dmin1(const D5& a) { return a.v < 1.f ? a : dc(1.f); }
 
 __device__ __forceinline__ void store_tan(FamTan& o, int s, int k, const D5& v) {
   for (int q = 0; q < NTH; ++q) o.dc[s][k][q] = (float)v.d[q];
 }
 __device__ __forceinline__ void store_pref(FamTan& o, const D5& pref) {
-  for (int q = 0; q < NTH; ++q) o.dlnpref[q] = pref.v != 0.0 ? (float)(pref.d[q] / pref.v) : 0.f;
+  for (int q = 0; q < NTH; ++q) o.dlnpref[q] = pref.v != 0.f ? pref.d[q] / pref.v : 0.f;
 }
 __device__ __forceinline__ void zero_tan(FamTan& o) {
   for (int s = 0; s < 2; ++s)
@@ -204,7 +350,7 @@ __device__ __forceinline__ void zero_tan(FamTan& o) {
 }
 
 // Inversion coefficient sets (nh3_hs.py:139-168), as in the prep kernel.
-__device__ constexpr double INV_SET_D[2][13] = {
+__device__ constexpr float INV_SET_D[2][13] = {
     {1.640, 0.75, 0.852, 0.7756, 0.666, 1.0, 1.262, 0.3, 0.5296, 0.7964, 0.667, 1.554, -0.0498},
     {1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152, 0.8873, 0.8994, 0.66666667,
      -0.0627}};
@@ -262,7 +408,7 @@ __global__ void __launch_bounds__(256) rb_layer_tan_kernel(TanArgs a) {
     }
     case 1: {
       for (int s = 0; s < 2; ++s) {
-        const double* c = INV_SET_D[s];
+        const float* c = INV_SET_D[s];
         store_tan(F, s, 0, c[0] * (Ph2 * dpw(lTdiv, c[3])) + c[1] * (Phe * dpw(lTdiv, c[4])));
         store_tan(F, s, 1, c[2] * (Pnh3 * dpw(l295, c[5])));
         store_tan(F, s, 3, c[6] * (Ph2 * dpw(lTdiv, c[9])) + c[7] * (Phe * dpw(lTdiv, c[10])));
@@ -378,7 +524,7 @@ constexpr int JV_NREC = 16;
 
 struct JvpShared {
   float rec[2][JV_NREC][JV_CHUNK];   // [coefficient set][field][line]
-  double red[4][NTH + 1];
+  double red[8][NTH + 1];
 };
 
 // Compensated float sum.
@@ -514,7 +660,7 @@ __device__ __forceinline__ void br_eval(float F, float FL, float g, float z, flo
   const float e = (F - KH) + (FL - KL);
   const float K = KH + KL;
   const float den = fmaf(e, e, 4.f * F * g * g);
-  const float r = 1.f / den;
+  const float r = rcp_approx(den);
   const float gp = g + z, gm = g - z;
   const float n = fmaf(gm, F, gp * K);
   const float t = S * n * r;
@@ -526,11 +672,17 @@ __device__ __forceinline__ void br_eval(float F, float FL, float g, float z, flo
   }
 }
 
-__global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
+// Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
+// sweeps lines g, g + NG, ... of every chunk and the groups' sums are added
+// per family.
+__global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
   __shared__ JvpShared sh;
+  __shared__ float s_grp[256][4];
   const int L = blockIdx.x;
   const int tid = threadIdx.x;
-  const int j = blockIdx.y * blockDim.x + tid;
+  const int FTL = a.ft, NG = blockDim.x / a.ft;
+  const int fi = tid % FTL, grp = tid / FTL;
+  const int j = blockIdx.y * FTL + fi;
   const bool on = j < a.nf;
   const LayerParams& lp = a.lp[L];
   const LayerTan& LT = a.lt[L];
@@ -604,7 +756,7 @@ __global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
       __syncthreads();
       if (on) {
         const float(*R)[JV_CHUNK] = sh.rec[two ? set : 0];
-        for (int i = 0; i < nc; ++i) {
+        for (int i = grp; i < nc; i += NG) {
           if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
             const float dg[3] = {R[6][i], R[7][i], R[8][i]};
             const float dz[3] = {R[9][i], R[10][i], R[11][i]};
@@ -615,7 +767,7 @@ __global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
             const float g = R[0][i], S = R[4][i];
             const float e = (Fx - R[2][i]) + (FLx - R[3][i]);
             const float den = fmaf(e, e, 4.f * Fx * g * g);
-            const float r = 1.f / den;
+            const float r = rcp_approx(den);
             const float tt = S * g * r;
             val.add(tt);
             for (int q = 0; q < 3; ++q) {
@@ -627,7 +779,7 @@ __global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
             const float dm = (fq - R[2][i]) + (fql - R[3][i]);
             const float dp = fq + R[2][i];
             const float d1 = fmaf(dm, dm, df * df), d2 = fmaf(dp, dp, df * df);
-            const float r1 = 1.f / d1, r2 = 1.f / d2;
+            const float r1 = rcp_approx(d1), r2 = rcp_approx(d2);
             const float h = S * df, u = r1 + r2;
             val.add(h * u);
             for (int q = 0; q < 3; ++q) {
@@ -653,15 +805,25 @@ __global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
       }
       __syncthreads();
     }
-    fv[fam] = val.val();
-    for (int q = 0; q < 3; ++q) fd[fam][q] = der[q].val();
+    // add the line groups' sums
+    s_grp[tid][0] = val.val();
+    for (int q = 0; q < 3; ++q) s_grp[tid][1 + q] = der[q].val();
+    __syncthreads();
+    if (grp == 0) {
+      float v4[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int gg = 0; gg < NG; ++gg)
+        for (int q = 0; q < 4; ++q) v4[q] += s_grp[gg * FTL + fi][q];
+      fv[fam] = v4[0];
+      for (int q = 0; q < 3; ++q) fd[fam][q] = v4[1 + q];
+    }
+    __syncthreads();
   }
   // h2o base term summed over the CTA (every thread built some lines)
   {
     float v[4] = {base, dbase[0], dbase[1], dbase[2]};
     for (int k = 0; k < 4; ++k)
       for (int o = 16; o; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-    __shared__ float s_b[4][4];
+    __shared__ float s_b[8][4];
     if ((tid & 31) == 0)
       for (int k = 0; k < 4; ++k) s_b[tid >> 5][k] = v[k];
     __syncthreads();
@@ -675,7 +837,7 @@ __global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
   }
   // assemble dalpha/dtheta (cm^-1) in float64 and contract with dTb/dalpha
   double g5[NTH] = {0, 0, 0, 0, 0};
-  if (on) {
+  if (on && grp == 0) {
     const double gal = a.galpha[(size_t)L * a.nf + j];
     const double Fd = f * f, Fhd = fh * fh;
     auto pref = [&](int fam) { return ldexp((double)lp.fam[fam].fm, lp.fam[fam].fe); };
@@ -749,6 +911,7 @@ __global__ void __launch_bounds__(128) rb_alpha_jvp_kernel(JvpArgs a) {
     for (int o = 16; o; o >>= 1) g5[q] += __shfl_xor_sync(0xffffffffu, g5[q], o);
   if ((tid & 31) == 0)
     for (int q = 0; q < NTH; ++q) sh.red[tid >> 5][q] = g5[q];
+  // (sh.red holds up to 8 warps)
   __syncthreads();
   if (tid == 0) {
     for (int q = 0; q < NTH; ++q) {
@@ -777,24 +940,26 @@ __global__ void rb_adjoint_final_kernel(int nL, int ntile, const double* part, c
 // ------------------------------------------------------------------ launch
 cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st) {
-  const size_t nbuf = (size_t)ta.nb * ta.nf * ta.nL;
-  cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(double) * nbuf, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * nbuf, st);
-  if (e != cudaSuccess) return e;
-  const int nt = ta.nb * ta.nf;
-  if (nt > 0) rb_tb_adjoint_kernel<<<(nt + 127) / 128, 128, 0, st>>>(ta);
+  if (ta.nb > 0) {
+    const int ninv = ta.nb * ta.nL;
+    rb_ray_inverse_init_kernel<<<(ninv + 255) / 256, 256, 0, st>>>(ninv, reinterpret_cast<int2*>(ta.inv));
+    rb_ray_inverse_kernel<<<dim3((ta.max_seg + 127) / 128, ta.nb), 128, 0, st>>>(ta);
+    const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
+    dim3 grid((ta.nf + blk - 1) / blk, ta.nchunk, ta.nb);
+    rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);
+    rb_tb_adj_grad_kernel<<<grid, blk, 0, st>>>(ta);
+  }
   rb_adjoint_reduce_kernel<<<ta.nL, 128, 0, st>>>(ta, galpha, gsrc);
   rb_layer_tan_kernel<<<(tn.nL * 8 + 255) / 256, 256, 0, st>>>(tn);
-  const int block = jv.nf >= 128 ? 128 : ((jv.nf + 31) / 32) * 32;
-  dim3 grid(jv.nL, (jv.nf + block - 1) / block);
-  rb_alpha_jvp_kernel<<<grid, block, 0, st>>>(jv);
+  dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
+  rb_alpha_jvp_kernel<<<grid, 256, 0, st>>>(jv);
   rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(jv.nL, grid.y, jv.part, gsrc, dT, dP, dlnX);
   return cudaGetLastError();
 }
 
-int adjoint_tiles(int nf) {
-  const int block = nf >= 128 ? 128 : ((nf + 31) / 32) * 32;
-  return (nf + block - 1) / block;
-}
+// Frequencies per CTA of rb_alpha_jvp_kernel (the rest of its 256 threads
+// split the lines).
+int adjoint_ft(int nf) { return nf >= 64 ? 64 : 32; }
+int adjoint_tiles(int nf) { return (nf + adjoint_ft(nf) - 1) / adjoint_ft(nf); }
 
 }  // namespace rb

@@ -121,7 +121,7 @@ struct rb_handle {
   DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base, d_done;
   // adjoint workspaces
-  DBuf d_ga, d_gs, d_galpha, d_gsrc, d_lt, d_jpart, d_grad, d_dth;
+  DBuf d_ga, d_gs, d_galpha, d_gsrc, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_inv;
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
@@ -147,6 +147,7 @@ int alpha_lines_occupancy(int M, int W);
 cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st);
 int adjoint_tiles(int nf);
+int adjoint_ft(int nf);
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
                              float* R32, float* T32, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
@@ -613,7 +614,7 @@ int rb_destroy(rb_handle* h) {
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
                   &h->d_done, &h->d_ga, &h->d_gs, &h->d_galpha, &h->d_gsrc, &h->d_lt, &h->d_jpart,
-                  &h->d_grad, &h->d_dth})
+                  &h->d_grad, &h->d_dth, &h->d_adjS, &h->d_inv})
     b->release();
   for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
@@ -1102,8 +1103,9 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
     return rc;
   const int launches = h->launches;
   const int max_seg = 2 * nL + 4;
-  const size_t nbuf = (size_t)nb * nf * nL;
+  const size_t nbuf = (size_t)nb * max_seg * nf;
   const int ntile = rb::adjoint_tiles(nf);
+  RB_CUDA(h->d_inv.ensure(sizeof(int) * 2 * (size_t)nb * nL));
   RB_CUDA(h->d_ga.ensure(sizeof(double) * nbuf));
   RB_CUDA(h->d_gs.ensure(sizeof(double) * nbuf));
   RB_CUDA(h->d_galpha.ensure(sizeof(double) * (size_t)nL * nf));
@@ -1124,6 +1126,11 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   ta.grad = grad;
   ta.ga = h->d_ga.as<double>();
   ta.gs = h->d_gs.as<double>();
+  ta.inv = h->d_inv.as<int>();
+  ta.nchunk = rb::tb_nchunk(max_seg);
+  ta.part = h->d_part.as<float4>();
+  RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nb * ta.nchunk * nf));
+  ta.S = h->d_adjS.as<float>();
   rb::TanArgs tn{};
   tn.nL = nL;
   tn.P = P;
@@ -1135,6 +1142,7 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   rb::JvpArgs jv{};
   jv.nL = nL;
   jv.nf = nf;
+  jv.ft = rb::adjoint_ft(nf);
   jv.freqs = h->d_f.as<double>();
   jv.freqs_hs = h->d_fhs.as<double>();
   jv.lp = h->d_lp.as<rb::LayerParams>();
@@ -1146,7 +1154,7 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   jv.part = h->d_jpart.as<double>();
   RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_galpha.as<double>(), h->d_gsrc.as<double>(), dT, dP,
                              dlnX, st));
-  h->launches = launches + 5;
+  h->launches = launches + 8;
   return RB_OK;
 }
 

@@ -154,12 +154,17 @@ struct TbAdjArgs {
   const int* layer;       // [nb][max_seg]
   const double* weights;  // [nb] or null
   const double* grad;     // [nf] (with weights: d loss / d Tb_avg) or [nb][nf]
-  double* ga;             // [nb][nf][nL] g dTb/dalpha
-  double* gs;             // [nb][nf][nL] g dTb/dT through the source term
+  double* ga;             // [nb][max_seg][nf] g dTb/dalpha per path node
+  double* gs;             // [nb][max_seg][nf] g dTb/dT through the source term per node
+  int* inv;               // [nb][nL][2] first and last node of each ray at each layer
+  const float4* part;     // forward scan partials [nb][nchunk][nf]
+  int nchunk;
+  float* S;               // [nb][nchunk][nf] per-chunk sums of dTb/dtau
 };
 
 struct JvpArgs {
   int nL, nf;
+  int ft;                 // frequencies per CTA
   const double* freqs;
   const double* freqs_hs;
   const LayerParams* lp;
