@@ -192,6 +192,30 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
                       const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
                       double* dT, double* dP, double* dlnX);
 
+/* Batches of atmospheres (no reference counterpart: the reference runs one
+ * atmosphere per Planet): nvar variants, variant v with nL_host[v] layers
+ * (HOST array).  P, T, R, N are the variants' [nL_v] arrays concatenated
+ * (device, sum nL_v values), X is [RB_NX][sum nL_v] (device).  Every
+ * variant uses the same nb impact parameters b[nb][2] and weights[nb]
+ * (device); Tb_avg[nvar][nf] (device) receives the weighted averages.  All
+ * variants run in the same launches (one persistent absorption launch over
+ * every variant's layers, one ray-walk launch over all nvar nb rays, ...).
+ * Frequencies are planned from the host array freqs_host. */
+int rb_forward_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
+                            const double* P, const double* T, const double* X, const double* R,
+                            const double* N, int nf, const double* freqs_host, double Req,
+                            double Rpol, double orient0, double orient1, int gtype, int limb,
+                            int nb, const double* b, const double* weights, double* Tb_avg);
+
+/* Forward and adjoint of a batch: grad[nvar][nf] = d loss / d Tb_avg;
+ * dT, dP [sum nL_v], dlnX [3][sum nL_v] (device). */
+int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
+                            const double* P, const double* T, const double* X, const double* R,
+                            const double* N, int nf, const double* freqs_host, double Req,
+                            double Rpol, double orient0, double orient1, int gtype, int limb,
+                            int nb, const double* b, const double* weights, const double* grad,
+                            double* Tb_avg, double* dT, double* dP, double* dlnX);
+
 /* Number of this library's kernel launches made by the last rb_forward /
  * rb_forward_device call (for launch accounting). */
 int rb_last_launch_count(rb_handle* h);

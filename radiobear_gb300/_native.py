@@ -39,7 +39,7 @@ EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set
            'rb_set_formalisms', 'rb_alpha', 'rb_raypath', 'rb_brightness', 'rb_forward',
            'rb_forward_device', 'rb_last_launch_count', 'rb_set_profiling', 'rb_phase_times',
            'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
-           'rb_adjoint_device')
+           'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device')
 
 _lib = None
 _lock = threading.Lock()
@@ -91,6 +91,13 @@ def load_library(path=None):
         lib.rb_adjoint.argtypes = [_vp, c_int, _d, _d, _d, _d, _d, c_int, _d, _d, c_double, c_double,
                                    c_double, c_double, c_int, c_int, c_int, _d, _d, _d, _d, _d, _d,
                                    _d, _d]
+        _ip = ctypes.POINTER(ctypes.c_int32)
+        lib.rb_forward_batch_device.argtypes = [_vp, _vp, c_int, _ip, _vp, _vp, _vp, _vp, _vp, c_int, _d,
+                                                c_double, c_double, c_double, c_double, c_int, c_int,
+                                                c_int, _vp, _vp, _vp]
+        lib.rb_adjoint_batch_device.argtypes = [_vp, _vp, c_int, _ip, _vp, _vp, _vp, _vp, _vp, c_int, _d,
+                                                c_double, c_double, c_double, c_double, c_int, c_int,
+                                                c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
         lib.rb_adjoint_device.argtypes = [_vp, _vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _d, _vp,
                                           c_double, c_double, c_double, c_double, c_int, c_int,
                                           c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
@@ -293,6 +300,39 @@ class Engine:
             GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), vp(grad), vp(Tb_out),
             vp(Tb_avg), vp(dT), vp(dP), vp(dlnX))
         _check(self.lib, rc, 'rb_adjoint_device')
+
+    def forward_batch_device(self, stream, nL_list, P, T, X, R, N, freqs_host, b, weights, Tb_avg,
+                             Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse', limb='shape'):
+        """Batch of atmospheres (see rb_forward_batch_device): nL_list host
+        layer counts; P, T, R, N, X, b, weights, Tb_avg integer device
+        addresses."""
+        nl = np.ascontiguousarray(nL_list, dtype=np.int32)
+        f = _f64(freqs_host)
+        rc = self.lib.rb_forward_batch_device(
+            self._h, _vp(int(stream)), nl.size, nl.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+            _vp(int(P)), _vp(int(T)), _vp(int(X)), _vp(int(R)), _vp(int(N)), f.size, _ptr(f),
+            float(Req), float(Rpol), float(orientation[0]), float(orientation[1]), GTYPE[gtype],
+            LIMB[limb], int(self._nb(b)), _vp(int(b.data_ptr())), _vp(int(weights)), _vp(int(Tb_avg)))
+        _check(self.lib, rc, 'rb_forward_batch_device')
+
+    def adjoint_batch_device(self, stream, nL_list, P, T, X, R, N, freqs_host, b, weights, grad,
+                             Tb_avg, dT, dP, dlnX, Req, Rpol, orientation=(0.0, 0.0),
+                             gtype='ellipse', limb='shape'):
+        """Forward + adjoint of a batch (see rb_adjoint_batch_device)."""
+        nl = np.ascontiguousarray(nL_list, dtype=np.int32)
+        f = _f64(freqs_host)
+        rc = self.lib.rb_adjoint_batch_device(
+            self._h, _vp(int(stream)), nl.size, nl.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+            _vp(int(P)), _vp(int(T)), _vp(int(X)), _vp(int(R)), _vp(int(N)), f.size, _ptr(f),
+            float(Req), float(Rpol), float(orientation[0]), float(orientation[1]), GTYPE[gtype],
+            LIMB[limb], int(self._nb(b)), _vp(int(b.data_ptr())), _vp(int(weights)), _vp(int(grad)),
+            _vp(int(Tb_avg)), _vp(int(dT)), _vp(int(dP)), _vp(int(dlnX)))
+        _check(self.lib, rc, 'rb_adjoint_batch_device')
+
+    @staticmethod
+    def _nb(b):
+        """Rays of a [nb, 2] device tensor of impact parameters."""
+        return int(b.shape[0])
 
     def last_launch_count(self):
         return int(self.lib.rb_last_launch_count(self._h))

@@ -13,7 +13,6 @@
 //                           (c_i the trapezoid node weight, E = exp(-tau));
 //                           adds g dTb/dalpha and g W c / intW (the
 //                           source-temperature term) per visited layer.
-//   rb_adjoint_reduce_kernel sums those over rays (fixed order).
 //   rb_layer_tan_kernel     eight threads per layer: the layer coefficients
 //                           of the absorption (widths, couplings, strength
 //                           prefactors, continua) in dual numbers, giving
@@ -52,6 +51,14 @@ __device__ __forceinline__ int wrap_l(int l, int nL) {
 //   rb_tb_adj_grad_kernel    Lam after the chunk = sum of S over later
 //                            chunks, then the chunk's nodes in reverse.
 constexpr int ADJ_CHUNK = 128;   // = the forward scan's chunk (rb_tb.cu)
+
+// d loss / d Tb of ray b at frequency f.
+__device__ __forceinline__ double adj_gb(const TbAdjArgs& a, int b, int f) {
+  if (!a.weights) return a.grad[(size_t)b * a.nf + f];
+  const int v = a.var_off ? b / a.rays_per_var : 0;
+  const int bi = a.var_off ? b % a.rays_per_var : b;
+  return a.weights[bi] * a.grad[(size_t)v * a.nf + f];
+}
 
 struct ChunkState {
   double tau_c;    // optical depth at this chunk's first node
@@ -104,8 +111,14 @@ __device__ __forceinline__ void adj_stage(const TbAdjArgs& a, AdjStage& sg, int 
                                           int N) {
   const float* hd = a.hds + (size_t)b * a.max_seg;
   const int* lay = a.layer + (size_t)b * a.max_seg;
+  int off = 0, nLr = a.nL;
+  if (a.var_off) {
+    const int v = b / a.rays_per_var;
+    off = a.var_off[v];
+    nLr = a.var_off[v + 1] - off;
+  }
   for (int t = threadIdx.x; t <= ns; t += blockDim.x) {
-    const int L = wrap_l(lay[i0 + t], a.nL);
+    const int L = off + wrap_l(lay[i0 + t], nLr);
     sg.lay[t] = L;
     sg.off[t] = L * a.nf;
     sg.T[t] = (float)a.T[L];
@@ -166,18 +179,10 @@ __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
   __syncthreads();
   if (f >= a.nf) return;
   const int nf = a.nf;
-  // per node: g dTb/dalpha and g dTb/dT (source term), [nb][max_seg][nf]
-  double* gn = a.ga + (size_t)b * a.max_seg * nf + f;
-  double* sn = a.gs + (size_t)b * a.max_seg * nf + f;
-  const double gb = a.weights ? a.weights[b] * a.grad[f] : a.grad[(size_t)b * a.nf + f];
+  const double gb = adj_gb(a, b, f);
+  if (gb == 0.0) return;
   const ChunkState st = adj_combine(a, b, c, f, nc);
-  if (gb == 0.0 || !st.live) {
-    for (int k = (c == 0 ? 0 : i0 + 1); k <= i0 + ns; ++k) {
-      gn[(size_t)k * nf] = 0.0;
-      sn[(size_t)k * nf] = 0.0;
-    }
-    return;
-  }
+  if (!st.live) return;
   const float* S = a.S + (size_t)b * a.nchunk * a.nf + f;
   double Lnext = 0.0;    // Lam of the node after this chunk's last node
   for (int k = c + 1; k < nc; ++k) Lnext += (double)S[(size_t)k * a.nf];
@@ -194,77 +199,26 @@ __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
   }
   const double Ec = exp(-st.tau_c);
   // nodes i0+ns .. i0+1 in reverse (node i0 belongs to the previous chunk,
-  // except node 0, which chunk 0 handles last)
+  // except node 0, which chunk 0 handles last); the sums over the rays and
+  // over the (at most two) visits of a layer are atomic adds into
+  // galpha[layer][f] and gsrc[layer][f]
   float ak = al[sg.off[ns]];
   for (int t = ns; t > 0; --t) {
-    const int k = i0 + t;
     const float dprev = 2.f * sg.hd[t - 1];
     const float dcur = 2.f * sg.hd[t];
     const float ck = 0.5f * (dprev + dcur);
     const double Ek = Ec * (double)__expf(-(float)tl);
     const double wk = (double)(ck * (sg.T[t] - st.Tb) * st.rIW);
     const double Lk_ = Lnext - wk * (double)ak * Ek;
-    gn[(size_t)k * nf] = gb * (wk * Ek + 0.5 * (double)dprev * Lk_ + 0.5 * (double)dcur * Lnext);
-    sn[(size_t)k * nf] = gb * (double)ak * Ek * (double)ck * (double)st.rIW;
+    atomicAdd(a.ga + sg.off[t] + f, gb * (wk * Ek + 0.5 * (double)dprev * Lk_ + 0.5 * (double)dcur * Lnext));
+    atomicAdd(a.gs + sg.off[t] + f, gb * (double)ak * Ek * (double)ck * (double)st.rIW);
     const float am = al[sg.off[t - 1]];
     tl -= (double)((am + ak) * dprev * 0.5f);
     ak = am;
     Lnext = Lk_;
   }
-  if (c == 0) {   // node 0: W_0 = 0, only the segment term
-    gn[0] = gb * 0.5 * (double)(2.f * sg.hd[0]) * Lnext;
-    sn[0] = 0.0;
-  }
-}
-
-// Inverse of the paths: first and last node of each ray at each layer (a
-// path visits a layer at most twice: down to the tangent point and back).
-__global__ void rb_ray_inverse_kernel(TbAdjArgs a) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-  const int n = min(max(a.nseg[b], 0), a.max_seg);
-  if (k >= n || n < 2) return;
-  const int L = wrap_l(a.layer[(size_t)b * a.max_seg + k], a.nL);
-  atomicMin(&a.inv[((size_t)b * a.nL + L) * 2 + 0], k);
-  atomicMax(&a.inv[((size_t)b * a.nL + L) * 2 + 1], k);
-}
-
-__global__ void rb_ray_inverse_init_kernel(int n, int2* inv) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) inv[i] = make_int2(0x7fffffff, -1);
-}
-
-// galpha[L][f] = sum over rays and the (at most two) nodes at layer L of
-// the node values; gsrc[L] likewise summed over frequencies.  Fixed order.
-__global__ void __launch_bounds__(128) rb_adjoint_reduce_kernel(TbAdjArgs a, double* galpha,
-                                                                double* gsrc) {
-  const int L = blockIdx.x;
-  const int nL = a.nL, nf = a.nf;
-  double src = 0.0;
-  for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-    double g = 0.0;
-    for (int b = 0; b < a.nb; ++b) {
-      const int k1 = a.inv[((size_t)b * nL + L) * 2 + 0], k2 = a.inv[((size_t)b * nL + L) * 2 + 1];
-      if (k2 < 0) continue;
-      const double* gn = a.ga + (size_t)b * a.max_seg * nf + f;
-      const double* sn = a.gs + (size_t)b * a.max_seg * nf + f;
-      g += gn[(size_t)k1 * nf];
-      src += sn[(size_t)k1 * nf];
-      if (k2 != k1) {
-        g += gn[(size_t)k2 * nf];
-        src += sn[(size_t)k2 * nf];
-      }
-    }
-    galpha[(size_t)L * nf + f] = g;
-  }
-  __shared__ double s[4];
-  for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(0xffffffffu, src, o);
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = src;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
-    gsrc[L] = t;
-  }
+  if (c == 0)   // node 0: W_0 = 0, only the segment term
+    atomicAdd(a.ga + sg.off[0] + f, gb * 0.5 * (double)(2.f * sg.hd[0]) * Lnext);
 }
 
 // ------------------------------------------------------------------ dual numbers
@@ -922,15 +876,18 @@ __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
   }
 }
 
-// dT = sum of tiles + source term; dP; dln X for NH3, H2O, H2S.
-__global__ void rb_adjoint_final_kernel(int nL, int ntile, const double* part, const double* gsrc,
-                                        double* dT, double* dP, double* dlnX) {
+// dT = sum of tiles + source term (summed over frequencies); dP; dln X
+// for NH3, H2O, H2S.
+__global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const double* part,
+                                        const double* gsrc, double* dT, double* dP, double* dlnX) {
   const int L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nL) return;
   double s[NTH] = {0, 0, 0, 0, 0};
   for (int t = 0; t < ntile; ++t)
     for (int q = 0; q < NTH; ++q) s[q] += part[((size_t)L * ntile + t) * NTH + q];
-  dT[L] = s[TH_T] + gsrc[L];
+  double src = 0.0;
+  for (int f = 0; f < nf; ++f) src += gsrc[(size_t)L * nf + f];
+  dT[L] = s[TH_T] + src;
   dP[L] = s[TH_P];
   dlnX[L] = s[TH_XNH3];
   dlnX[nL + L] = s[TH_XH2O];
@@ -940,20 +897,21 @@ __global__ void rb_adjoint_final_kernel(int nL, int ntile, const double* part, c
 // ------------------------------------------------------------------ launch
 cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st) {
+  const size_t nbuf = (size_t)ta.nL * ta.nf;
+  cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(double) * nbuf, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * nbuf, st);
+  if (e != cudaSuccess) return e;
   if (ta.nb > 0) {
-    const int ninv = ta.nb * ta.nL;
-    rb_ray_inverse_init_kernel<<<(ninv + 255) / 256, 256, 0, st>>>(ninv, reinterpret_cast<int2*>(ta.inv));
-    rb_ray_inverse_kernel<<<dim3((ta.max_seg + 127) / 128, ta.nb), 128, 0, st>>>(ta);
     const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
     dim3 grid((ta.nf + blk - 1) / blk, ta.nchunk, ta.nb);
     rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);
     rb_tb_adj_grad_kernel<<<grid, blk, 0, st>>>(ta);
   }
-  rb_adjoint_reduce_kernel<<<ta.nL, 128, 0, st>>>(ta, galpha, gsrc);
   rb_layer_tan_kernel<<<(tn.nL * 8 + 255) / 256, 256, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
   rb_alpha_jvp_kernel<<<grid, 256, 0, st>>>(jv);
-  rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(jv.nL, grid.y, jv.part, gsrc, dT, dP, dlnX);
+  rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(jv.nL, jv.nf, grid.y, jv.part, gsrc, dT,
+                                                                dP, dlnX);
   return cudaGetLastError();
 }
 

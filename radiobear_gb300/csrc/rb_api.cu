@@ -58,6 +58,15 @@ struct DBuf {
   T* as() const { return reinterpret_cast<T*>(p); }
 };
 
+// A batch of atmospheres (rb_forward_batch_device): variant v owns layers
+// [off[v], off[v+1]) of the concatenated arrays and rays [v nb, (v+1) nb)
+// with the shared impact parameters.
+struct Batch {
+  int nvar = 0;
+  const int* d_off = nullptr;   // device [nvar + 1]
+  int max_nL = 0;
+};
+
 int family_ncols(int fam) {
   switch (fam) {
     case rb::FAM_NH3_INV: return 4;
@@ -121,7 +130,8 @@ struct rb_handle {
   DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base, d_done;
   // adjoint workspaces
-  DBuf d_ga, d_gs, d_galpha, d_gsrc, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_inv;
+  DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff;
+  std::vector<int> batch_off;   // layer offsets of the last batch (d_voff)
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
@@ -149,13 +159,13 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
 int adjoint_tiles(int nf);
 int adjoint_ft(int nf);
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
-                             float* R32, float* T32, cudaStream_t st);
+                             float* R32, float* T32, const int* var_off, int nvar, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
 cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st);
 cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st);
 int tb_nchunk(int max_seg);
 cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
-                            cudaStream_t st);
+                            cudaStream_t st, int nvar = 1);
 cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st);
 cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, int packed, cudaStream_t st);
 }  // namespace rb
@@ -525,15 +535,19 @@ void aspect_matrix(double Req, double Rpol, double o0, double o1, double* M) {
 int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, const double* dN,
                     const double* dT, double Req, double Rpol, double o0, double o1, int gtype,
                     int limb, int nb, const double* db, int max_seg, int* dnseg, double* dds,
-                    float* dhds, int* dlayer, double* dr4, double* dll, int* dend) {
+                    float* dhds, int* dlayer, double* dr4, double* dll, int* dend,
+                    const Batch* bt = nullptr, int rays_per_var = 0) {
   RB_CUDA(h->d_dR.ensure(sizeof(float) * nL));
   RB_CUDA(h->d_sR.ensure(sizeof(float2) * nL));
   RB_CUDA(h->d_R32.ensure(sizeof(float) * nL));
   RB_CUDA(h->d_T32.ensure(sizeof(float) * nL));
   RB_CUDA(rb::launch_geom_prep(nL, dR, dT, h->d_sR.as<float2>(), h->d_dR.as<float>(),
-                               h->d_R32.as<float>(), h->d_T32.as<float>(), st));
+                               h->d_R32.as<float>(), h->d_T32.as<float>(), bt ? bt->d_off : nullptr,
+                               bt ? bt->nvar : 1, st));
   rb::RayArgs ra{};
   ra.nL = nL;
+  ra.var_off = bt ? bt->d_off : nullptr;
+  ra.rays_per_var = rays_per_var;
   ra.R = dR;
   ra.N = dN;
   ra.dR2 = h->d_sR.as<float2>();
@@ -613,8 +627,8 @@ int rb_destroy(rb_handle* h) {
                   &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part})
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
-                  &h->d_done, &h->d_ga, &h->d_gs, &h->d_galpha, &h->d_gsrc, &h->d_lt, &h->d_jpart,
-                  &h->d_grad, &h->d_dth, &h->d_adjS, &h->d_inv})
+                  &h->d_done, &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,
+                  &h->d_adjS, &h->d_voff})
     b->release();
   for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
@@ -934,38 +948,47 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
   return RB_OK;
 }
 
+// One forward pass: ray paths on the side stream concurrent with the
+// absorption, then the scan and the quadrature average.  nb = rays per
+// atmosphere; with a batch (bt), nL is the total layer count and the
+// arrays are the variants' concatenation.
 static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
                         const double* dX, const double* dR, const double* dN, const double* dscale,
                         double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
                         const double* db, const double* dw, int disc, double* dTb, double* davg,
-                        double* dl64) {
+                        double* dl64, const Batch* bt = nullptr) {
   const int nf = (int)h->plan_f.size();
-  const int max_seg = 2 * nL + 4;
-  const size_t ns = (size_t)std::max(nb, 1) * max_seg;
-  RB_CUDA(h->d_nseg.ensure(sizeof(int) * std::max(nb, 1)));
+  const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
+  const int nvar = bt ? bt->nvar : 1;
+  const int nbt = nb * nvar;
+  const size_t ns = (size_t)std::max(nbt, 1) * max_seg;
+  RB_CUDA(h->d_nseg.ensure(sizeof(int) * std::max(nbt, 1)));
   RB_CUDA(h->d_hds.ensure(sizeof(float) * ns));
   RB_CUDA(h->d_layer.ensure(sizeof(int) * ns));
-  RB_CUDA(h->d_Tb32.ensure(sizeof(float) * (size_t)std::max(nb, 1) * nf));
+  RB_CUDA(h->d_Tb32.ensure(sizeof(float) * (size_t)std::max(nbt, 1) * nf));
   const int nchunk = rb::tb_nchunk(max_seg);
-  if (!disc) RB_CUDA(h->d_part.ensure(sizeof(float4) * (size_t)std::max(nb, 1) * nchunk * nf));
+  if (!disc) RB_CUDA(h->d_part.ensure(sizeof(float4) * (size_t)std::max(nbt, 1) * nchunk * nf));
   h->launches = 0;
   // geometry + ray paths on the side stream, concurrent with the absorption
   RB_CUDA(cudaEventRecord(h->ev_fork, st));
   RB_CUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
   int rc;
   if ((rc = enqueue_raypath(h, h->side, nL, dR, dN, dT, Req, Rpol, o0, o1, gtype, limb,
-                            std::max(nb, 0), db, max_seg, h->d_nseg.as<int>(), nullptr,
-                            h->d_hds.as<float>(), h->d_layer.as<int>(), nullptr, nullptr, nullptr)))
+                            std::max(nbt, 0), db, max_seg, h->d_nseg.as<int>(), nullptr,
+                            h->d_hds.as<float>(), h->d_layer.as<int>(), nullptr, nullptr, nullptr,
+                            bt, nb)))
     return rc;
   RB_CUDA(cudaEventRecord(h->ev_join, h->side));
   if ((rc = enqueue_alpha(h, st, nL, dP, dT, dX, dscale, 0, dl64, nullptr))) return rc;
   RB_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
-  if (nb > 0) {
+  if (nbt > 0) {
     rb::TbArgs ta{};
     ta.nL = nL;
     ta.nf = nf;
-    ta.nb = nb;
+    ta.nb = nbt;
     ta.max_seg = max_seg;
+    ta.var_off = bt ? bt->d_off : nullptr;
+    ta.rays_per_var = nb;
     ta.alpha32 = h->d_a32.as<float>();
     ta.T32 = h->d_T32.as<float>();
     ta.nseg = h->d_nseg.as<int>();
@@ -986,7 +1009,7 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
     }
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[6], st));
     if (davg && dw) {
-      RB_CUDA(rb::launch_disc_avg(nb, nf, h->d_Tb32.as<float>(), dw, davg, st));
+      RB_CUDA(rb::launch_disc_avg(nb, nf, h->d_Tb32.as<float>(), dw, davg, st, nvar));
       h->launches += 1;
     }
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[7], st));
@@ -1074,49 +1097,39 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
                       nb, b, weights, disc, Tb_out, Tb_avg, nullptr);
 }
 
-// Forward (recomputed) then the adjoint sweep: galpha from the scan adjoint,
-// alpha recomputed with its layer derivatives and contracted.
-int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
-                      const double* X, const double* R, const double* N, int nf,
-                      const double* freqs_host, const double* scale, double Req, double Rpol,
-                      double orient0, double orient1, int gtype, int limb, int nb, const double* b,
-                      const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
-                      double* dT, double* dP, double* dlnX) {
-  if (!h) return fail(RB_EINVAL, "null handle");
-  if (!P || !T || !X || !R || !N || !freqs_host || !grad || !dT || !dP || !dlnX ||
-      (nb > 0 && !b))
-    return fail(RB_EINVAL, "null array");
-  if (nL < 2 || nb < 1) return fail(RB_EINVAL, "bad sizes");
-  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
-  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
-  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
-  RB_CUDA(cudaSetDevice(h->device));
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  int rc;
-  if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
-  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
-  RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
+// Forward (recomputed) then the adjoint sweep: d loss / d alpha from the
+// scan adjoint, alpha recomputed with its layer derivatives and contracted.
+static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, const double* T,
+                        const double* X, const double* R, const double* N, const double* scale,
+                        double Req, double Rpol, double orient0, double orient1, int gtype,
+                        int limb, int nb, const double* b, const double* weights,
+                        const double* grad, double* Tb_out, double* Tb_avg, double* dT, double* dP,
+                        double* dlnX, const Batch* bt = nullptr) {
+  const int nf = (int)h->plan_f.size();
+  const int nvar = bt ? bt->nvar : 1;
+  const int nbt = nb * nvar;
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nbt * nf));
+  RB_CUDA(h->d_avg.ensure(sizeof(double) * (size_t)nvar * nf));
   double* dTb = Tb_out ? Tb_out : h->d_Tb.as<double>();
   double* davg = Tb_avg ? Tb_avg : (weights ? h->d_avg.as<double>() : nullptr);
+  int rc;
   if ((rc = forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
-                         nb, b, weights, 0, dTb, davg, nullptr)))
+                         nb, b, weights, 0, dTb, davg, nullptr, bt)))
     return rc;
   const int launches = h->launches;
-  const int max_seg = 2 * nL + 4;
-  const size_t nbuf = (size_t)nb * max_seg * nf;
+  const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
   const int ntile = rb::adjoint_tiles(nf);
-  RB_CUDA(h->d_inv.ensure(sizeof(int) * 2 * (size_t)nb * nL));
-  RB_CUDA(h->d_ga.ensure(sizeof(double) * nbuf));
-  RB_CUDA(h->d_gs.ensure(sizeof(double) * nbuf));
-  RB_CUDA(h->d_galpha.ensure(sizeof(double) * (size_t)nL * nf));
-  RB_CUDA(h->d_gsrc.ensure(sizeof(double) * nL));
+  RB_CUDA(h->d_ga.ensure(sizeof(double) * (size_t)nL * nf));
+  RB_CUDA(h->d_gs.ensure(sizeof(double) * (size_t)nL * nf));
   RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
   RB_CUDA(h->d_jpart.ensure(sizeof(double) * (size_t)nL * ntile * rb::NTH));
   rb::TbAdjArgs ta{};
   ta.nL = nL;
   ta.nf = nf;
-  ta.nb = nb;
+  ta.nb = nbt;
   ta.max_seg = max_seg;
+  ta.var_off = bt ? bt->d_off : nullptr;
+  ta.rays_per_var = nb;
   ta.alpha32 = h->d_a32.as<float>();
   ta.T = T;
   ta.nseg = h->d_nseg.as<int>();
@@ -1126,10 +1139,9 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   ta.grad = grad;
   ta.ga = h->d_ga.as<double>();
   ta.gs = h->d_gs.as<double>();
-  ta.inv = h->d_inv.as<int>();
   ta.nchunk = rb::tb_nchunk(max_seg);
   ta.part = h->d_part.as<float4>();
-  RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nb * ta.nchunk * nf));
+  RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nbt * ta.nchunk * nf));
   ta.S = h->d_adjS.as<float>();
   rb::TanArgs tn{};
   tn.nL = nL;
@@ -1150,12 +1162,101 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   for (int f = 0; f < rb::NFAM; ++f) jv.tab[f] = h->fam[f].table();
   jv.cfg = h->cfg;
   jv.cfg.units_db = 0;
-  jv.galpha = h->d_galpha.as<double>();
+  jv.galpha = h->d_ga.as<double>();
   jv.part = h->d_jpart.as<double>();
-  RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_galpha.as<double>(), h->d_gsrc.as<double>(), dT, dP,
-                             dlnX, st));
-  h->launches = launches + 8;
+  RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_ga.as<double>(), h->d_gs.as<double>(), dT, dP, dlnX,
+                             st));
+  h->launches = launches + 6;
   return RB_OK;
+}
+
+int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
+                      const double* X, const double* R, const double* N, int nf,
+                      const double* freqs_host, const double* scale, double Req, double Rpol,
+                      double orient0, double orient1, int gtype, int limb, int nb, const double* b,
+                      const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
+                      double* dT, double* dP, double* dlnX) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs_host || !grad || !dT || !dP || !dlnX ||
+      (nb > 0 && !b))
+    return fail(RB_EINVAL, "null array");
+  if (nL < 2 || nb < 1) return fail(RB_EINVAL, "bad sizes");
+  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
+  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
+  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
+  RB_CUDA(cudaSetDevice(h->device));
+  int rc;
+  if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
+  return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), nL, P, T, X, R, N, scale, Req,
+                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, grad, Tb_out, Tb_avg,
+                      dT, dP, dlnX);
+}
+
+// Batch descriptor from the host layer counts (offsets uploaded once per
+// distinct batch shape).
+static int make_batch(rb_handle* h, int nvar, const int32_t* nL_host, Batch& bt, int& NLT) {
+  if (nvar < 1 || !nL_host) return fail(RB_EINVAL, "batch needs nvar >= 1 and layer counts");
+  std::vector<int> off(nvar + 1, 0);
+  int mx = 0;
+  for (int v = 0; v < nvar; ++v) {
+    if (nL_host[v] < 2) return fail(RB_EINVAL, "variant %d has %d layers (need >= 2)", v, nL_host[v]);
+    off[v + 1] = off[v] + nL_host[v];
+    mx = std::max(mx, (int)nL_host[v]);
+  }
+  if (h->batch_off != off) {
+    RB_CUDA(upload(h->d_voff, off.data(), off.size(), h->st));
+    RB_CUDA(cudaStreamSynchronize(h->st));
+    h->batch_off = off;
+  }
+  bt.nvar = nvar;
+  bt.d_off = h->d_voff.as<int>();
+  bt.max_nL = mx;
+  NLT = off[nvar];
+  return RB_OK;
+}
+
+int rb_forward_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
+                            const double* P, const double* T, const double* X, const double* R,
+                            const double* N, int nf, const double* freqs_host, double Req,
+                            double Rpol, double orient0, double orient1, int gtype, int limb,
+                            int nb, const double* b, const double* weights, double* Tb_avg) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs_host || !b || !weights || !Tb_avg)
+    return fail(RB_EINVAL, "null array");
+  if (nb < 1) return fail(RB_EINVAL, "nb must be >= 1");
+  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
+  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
+  RB_CUDA(cudaSetDevice(h->device));
+  int rc, NLT = 0;
+  Batch bt;
+  if ((rc = make_batch(h, nvar, nL_host, bt, NLT))) return rc;
+  if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nvar * nb * nf));
+  return forward_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, nullptr, Req,
+                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, 0,
+                      h->d_Tb.as<double>(), Tb_avg, nullptr, &bt);
+}
+
+int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
+                            const double* P, const double* T, const double* X, const double* R,
+                            const double* N, int nf, const double* freqs_host, double Req,
+                            double Rpol, double orient0, double orient1, int gtype, int limb,
+                            int nb, const double* b, const double* weights, const double* grad,
+                            double* Tb_avg, double* dT, double* dP, double* dlnX) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!P || !T || !X || !R || !N || !freqs_host || !b || !weights || !grad || !dT || !dP || !dlnX)
+    return fail(RB_EINVAL, "null array");
+  if (nb < 1) return fail(RB_EINVAL, "nb must be >= 1");
+  if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
+  if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
+  RB_CUDA(cudaSetDevice(h->device));
+  int rc, NLT = 0;
+  Batch bt;
+  if ((rc = make_batch(h, nvar, nL_host, bt, NLT))) return rc;
+  if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
+  return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, nullptr, Req,
+                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, grad, nullptr, Tb_avg,
+                      dT, dP, dlnX, &bt);
 }
 
 int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const double* X,

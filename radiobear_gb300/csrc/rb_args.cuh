@@ -73,8 +73,14 @@ struct AlphaArgs {
   double* gas64;            // [nL][nf][NGAS] per gas, units of cfg (or null)
 };
 
+// Batches of atmospheres: variant v owns global layers [var_off[v],
+// var_off[v+1]) and rays [v * rays_per_var, (v+1) * rays_per_var); all
+// variants share the impact parameters b[rays_per_var][2].  var_off == null
+// is a single atmosphere (one variant, every ray its own b).
 struct RayArgs {
   int nL;
+  const int* var_off;   // [nvar + 1] or null
+  int rays_per_var;
   const double* R;      // equatorial radius of each layer [km], layer 0 on top
   const double* N;      // refractive index of each layer
   const float2* dR2;    // [nL] R[(c+1)%nL]^2 - R[c]^2 as (hi, lo)   (rb_geom_prep_kernel)
@@ -97,6 +103,8 @@ struct RayArgs {
 
 struct TbArgs {
   int nL, nf, nb, max_seg;
+  const int* var_off;     // [nvar + 1] or null (see RayArgs)
+  int rays_per_var;
   const float* alpha32;   // [nL][nf] cm^-1
   const float* T32;       // [nL] K
   const int* nseg;        // [nb]
@@ -147,6 +155,8 @@ struct TanArgs {
 
 struct TbAdjArgs {
   int nL, nf, nb, max_seg;
+  const int* var_off;     // [nvar + 1] or null (see RayArgs)
+  int rays_per_var;
   const float* alpha32;   // [nL][nf] cm^-1 (forward absorption)
   const double* T;        // [nL]
   const int* nseg;        // [nb]
@@ -154,9 +164,8 @@ struct TbAdjArgs {
   const int* layer;       // [nb][max_seg]
   const double* weights;  // [nb] or null
   const double* grad;     // [nf] (with weights: d loss / d Tb_avg) or [nb][nf]
-  double* ga;             // [nb][max_seg][nf] g dTb/dalpha per path node
-  double* gs;             // [nb][max_seg][nf] g dTb/dT through the source term per node
-  int* inv;               // [nb][nL][2] first and last node of each ray at each layer
+  double* ga;             // [nL][nf] d loss / d alpha (atomic sums over rays and visits)
+  double* gs;             // [nL][nf] d loss / d T through the source term
   const float4* part;     // forward scan partials [nb][nchunk][nf]
   int nchunk;
   float* S;               // [nb][nchunk][nf] per-chunk sums of dTb/dtau

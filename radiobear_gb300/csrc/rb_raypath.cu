@@ -90,11 +90,23 @@ __device__ __forceinline__ int wrap(int idx, int nL) { return idx < 0 ? idx + nL
 
 // R[(c+1)%nL]^2 - R[c]^2 as a double-float (float64 product of the float64
 // difference and sum), R[(c+1)%nL] - R[c] and float copies of R and T.
+// With var_off (batches), the wrap is within each variant's layers.
 __global__ void rb_geom_prep_kernel(int nL, const double* R, const double* T, float2* dR2,
-                                    float* dR, float* R32, float* T32) {
+                                    float* dR, float* R32, float* T32, const int* var_off,
+                                    int nvar) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nL) return;
-  const int n = (c + 1 < nL) ? c + 1 : 0;
+  int first = 0, end = nL;
+  if (var_off) {   // variant of layer c: var_off[v] <= c < var_off[v+1]
+    int lo = 0, hi = nvar;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (var_off[mid] <= c) lo = mid; else hi = mid;
+    }
+    first = var_off[lo];
+    end = var_off[lo + 1];
+  }
+  const int n = (c + 1 < end) ? c + 1 : first;
   const double d = R[n] - R[c];
   const double q = d * (R[n] + R[c]);
   float h, l;
@@ -153,9 +165,20 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
   const int ray = blockIdx.x;
   const int lane = threadIdx.x;
   if (ray >= a.nb) return;
-  const double b0 = a.b[2 * ray], b1 = a.b[2 * ray + 1];
-  const int nL = a.nL;
-  const double rNorm = a.R[0];
+  const int bi = a.var_off ? ray % a.rays_per_var : ray;
+  const double b0 = a.b[2 * bi], b1 = a.b[2 * bi + 1];
+  int off = 0, nL = a.nL;
+  if (a.var_off) {
+    const int v = ray / a.rays_per_var;
+    off = a.var_off[v];
+    nL = a.var_off[v + 1] - off;
+  }
+  const double* R_ = a.R + off;
+  const double* N_ = a.N + off;
+  const float2* dR2_ = a.dR2 + off;
+  const float* dR_ = a.dR + off;
+  const float* R32_ = a.R32 + off;
+  const double rNorm = R_[0];
   const double k = a.k;
   double* ds_out = a.ds ? a.ds + (size_t)ray * a.max_seg : nullptr;
   float* hds_out = a.hds ? a.hds + (size_t)ray * a.max_seg : nullptr;
@@ -241,7 +264,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
   {
     const double c0 = -(sx * nx + sy * ny + sz * nz);
     const double t_inc = (c0 >= -1.0 && c0 <= 1.0) ? acos(c0) : CUDART_NAN;
-    const double nratio = a.N[0] / a.N[1];
+    const double nratio = N_[0] / N_[1];
     const double t_tran = asin(nratio * sin(t_inc));
     const double cf = nratio * cos(t_inc) - cos(t_tran);
     sx = nratio * sx + cf * nx;
@@ -284,7 +307,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
       const bool inrange = c >= -nL && c < nL && c + dir >= -nL && c + dir < nL;
       df dr2 = {0.f, 0.f};
       if (inrange) {
-        const float2 q2 = a.dR2[dir > 0 ? c : wrap(c - 1, nL)];
+        const float2 q2 = dR2_[dir > 0 ? c : wrap(c - 1, nL)];
         dr2 = dir > 0 ? df{q2.x, q2.y} : df{-q2.x, -q2.y};
       }
       float g = em1;            // E^2 - 1 at this lane's start point (guess)
@@ -332,7 +355,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
             if (ds_out) ds_out[nseg + lane] = (double)step;
             if (hds_out) hds_out[nseg + lane] = step * 0.5e5f;
             lay_out[nseg + lane] = c;
-            if (r4_out) r4_out[nseg + lane] = (double)(a.R32[wrap(c, nL)] * sqrtf(1.f + g));
+            if (r4_out) r4_out[nseg + lane] = (double)(R32_[wrap(c, nL)] * sqrtf(1.f + g));
           }
           const int src = taken - 1;
           u.h = __shfl_sync(FULL, un.h, src);
@@ -355,7 +378,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
       ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
     }
     const int j = dir > 0 ? layer : wrap(layer - 1, nL);
-    const float2 q2 = a.dR2[j];
+    const float2 q2 = dR2_[j];
     df dr2 = {q2.x, q2.y};
     if (dir < 0) dr2 = df_neg(dr2);                  // R[c-1]^2 - R[c]^2
     const df D = df_add(dr2, df_mulf(dr2, em1));     // E^2 (R[next]^2 - R[cur]^2)
@@ -389,7 +412,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
     }
     if (a.limb_sec) {
       // the secant step moves the point by |rNext - rNow| / mu instead
-      step = tangent ? 0.f : sqrtf(1.f + em1) * fabsf(a.dR[j]) / mu;
+      step = tangent ? 0.f : sqrtf(1.f + em1) * fabsf(dR_[j]) / mu;
       un = df_add(u, df{step, 0.f});
       w = df_make(df_d(un) * df_d(un));
     }
@@ -401,7 +424,7 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
       if (ds_out) ds_out[nseg] = (double)step;
       if (hds_out) hds_out[nseg] = step * 0.5e5f;
       lay_out[nseg] = layer;
-      if (r4_out) r4_out[nseg] = (double)(a.R32[wrap(layer, nL)] * sqrtf(1.f + em1));
+      if (r4_out) r4_out[nseg] = (double)(R32_[wrap(layer, nL)] * sqrtf(1.f + em1));
     }
     ++nseg;
     // advance along the ray
@@ -471,8 +494,9 @@ __global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
 }
 
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
-                             float* R32, float* T32, cudaStream_t st) {
-  rb_geom_prep_kernel<<<(nL + 127) / 128, 128, 0, st>>>(nL, R, T, dR2, dR, R32, T32);
+                             float* R32, float* T32, const int* var_off, int nvar,
+                             cudaStream_t st) {
+  rb_geom_prep_kernel<<<(nL + 127) / 128, 128, 0, st>>>(nL, R, T, dR2, dR, R32, T32, var_off, nvar);
   return cudaGetLastError();
 }
 

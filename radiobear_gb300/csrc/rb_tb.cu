@@ -76,6 +76,17 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 
 __device__ __forceinline__ int wrap_layer(int l, int nL) { return l < 0 ? l + nL : l; }
 
+// Layer offset and count of a ray's atmosphere (batches: see RayArgs).
+__device__ __forceinline__ void ray_layers(const TbArgs& a, int ray, int& off, int& nL) {
+  off = 0;
+  nL = a.nL;
+  if (a.var_off) {
+    const int v = ray / a.rays_per_var;
+    off = a.var_off[v];
+    nL = a.var_off[v + 1] - off;
+  }
+}
+
 // ------------------------------------------------------------ sequential
 __global__ void __launch_bounds__(128) rb_tb_seq_kernel(TbArgs a) {
   const int ray = blockIdx.y;
@@ -95,11 +106,13 @@ __global__ void __launch_bounds__(128) rb_tb_seq_kernel(TbArgs a) {
     a.W[pbase] = 0.0;
     a.TbL[pbase] = 0.0;
   }
-  int ii = nseg > 0 ? wrap_layer(lay[0], a.nL) : 0;
+  int off, nLr;
+  ray_layers(a, ray, off, nLr);
+  int ii = nseg > 0 ? off + wrap_layer(lay[0], nLr) : 0;
   float T0 = nseg > 0 ? a.T32[ii] : 0.f;
   float a0 = nseg > 0 ? a.alpha32[(size_t)ii * a.nf + fi] : 0.f;
   for (int i = 0; i + 1 < nseg; ++i) {
-    const int ii1 = wrap_layer(lay[i + 1], a.nL);
+    const int ii1 = off + wrap_layer(lay[i + 1], nLr);
     const float hd = hds[i];
     const float a1 = a.alpha32[(size_t)ii1 * a.nf + fi];
     const float T1 = a.T32[ii1];
@@ -156,8 +169,10 @@ __global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
   __shared__ float s_hd[TB_CHUNK];
   const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
   const int* lay = a.layer + (size_t)ray * a.max_seg + i0;
+  int off, nLr;
+  ray_layers(a, ray, off, nLr);
   for (int t = threadIdx.x; t <= n; t += blockDim.x) {
-    const int l = wrap_layer(lay[t], a.nL);
+    const int l = off + wrap_layer(lay[t], nLr);
     s_off[t] = l * a.nf;
     s_T[t] = a.T32[l];
     if (t < n) s_hd[t] = hds[t];
@@ -243,9 +258,12 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
 
 // Weighted sum over rays (disc quadrature), one thread per frequency,
 // compensated float32 over the rays.
+// blockIdx.y = variant of a batch: rays [v nb, (v+1) nb), out[v][f].
 __global__ void rb_disc_avg_kernel(int nb, int nf, const float* Tb32, const double* w, double* out) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
+  Tb32 += (size_t)blockIdx.y * nb * nf;
+  out += (size_t)blockIdx.y * nf;
   float s = 0.f, c = 0.f;
   for (int r = 0; r < nb; ++r) kahan_add(s, c, (float)w[r] * Tb32[(size_t)r * nf + f]);
   out[f] = (double)s - (double)c;
@@ -277,8 +295,8 @@ cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
-                            cudaStream_t st) {
-  rb_disc_avg_kernel<<<(nf + 127) / 128, 128, 0, st>>>(nb, nf, Tb32, w, out);
+                            cudaStream_t st, int nvar) {
+  rb_disc_avg_kernel<<<dim3((nf + 127) / 128, nvar), 128, 0, st>>>(nb, nf, Tb32, w, out);
   return cudaGetLastError();
 }
 
