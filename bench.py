@@ -48,6 +48,8 @@ def parse():
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-sample-s', type=float, default=20.0)
+    p.add_argument('--batch-variants', type=int, default=4096,
+                   help='atmospheres in the batched forward+adjoint measurement (0: skip)')
     p.add_argument('--alpha-tiling', default='',
                    help='line-sum tiling M,W,item_lines (default: automatic)')
     return p.parse_args()
@@ -143,6 +145,142 @@ def measure_gradients(args, dev, stream, flush):
                 e2e=dict(value=1.0 / float(np.mean(e2e)), unit='spectra+gradients/s',
                          h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                          api='rb_adjoint (C ABI, host buffers)'))
+
+
+BATCH_WORKLOAD = ('C4 batched retrieval sweep: {n} variants of the 1e-3..100 bar recipe (deep NH3 '
+                  'log-U 1e-4..1e-3, deep T offset U(-10, 10) K, 300..1200 layers), 128 freqs '
+                  '(0.5..50 GHz log), 32-ray disc quadrature, configuration-0 line lists; forward '
+                  'Tb_avg + adjoint dTb/dT, dTb/dP, dTb/dlnX for every variant per step, replayed '
+                  'from one captured CUDA graph, line-sum tiling from the autotuner')
+
+
+def measure_batch(args, dev, n_var):
+    """Spectra + gradients per second for a batch of n_var atmospheres
+    (rb_adjoint_batch_device captured in a CUDA graph and replayed), beside
+    the same variants run one call per atmosphere (rb_adjoint_device)."""
+    import torch
+    from radiobear_gb300 import _native, catalog, synth, tune
+    from tests import goldio
+    cats = goldio.real_catalogues()
+    wl0 = synth.make_workload(0, real=cats)
+    lines = dict(wl0.lines)
+    lines['ph3wgt'] = cats['ph3wgt']
+    nLs, nh3, dT = synth.make_variants(n_var)
+    C = {k: i for i, k in enumerate(synth.GAS_COLUMNS)}
+    LP = {k: i for i, k in enumerate(synth.PROPERTY_COLUMNS)}
+    P, T, X, R, N = [], [], [], [], []
+    for i in range(n_var):
+        g = synth.make_gas_table(int(nLs[i]), 1.0e-3, 100.0, nh3_deep=nh3[i], dT_deep=dT[i])
+        pr = synth.compute_properties(g)
+        P.append(g[C['P']])
+        T.append(g[C['T']])
+        X.append(_native.x_matrix(g, C))
+        R.append(pr[LP['R']])
+        N.append(pr[LP['N']])
+    freqs = np.logspace(np.log10(0.5), np.log10(50.0), 128)
+    b, w = synth.gauss_legendre_disc(32)
+    nf, nb, NLT = freqs.size, b.shape[0], int(np.sum(nLs))
+    f64 = dict(dtype=torch.float64, device=dev)
+    t = dict(P=torch.tensor(np.concatenate(P), **f64), T=torch.tensor(np.concatenate(T), **f64),
+             X=torch.tensor(np.ascontiguousarray(np.concatenate(X, axis=1)), **f64),
+             R=torch.tensor(np.concatenate(R), **f64), N=torch.tensor(np.concatenate(N), **f64),
+             b=torch.tensor(b, **f64), w=torch.tensor(w, **f64))
+    grad = torch.tensor(np.random.default_rng(4).normal(size=(n_var, nf)), **f64)
+    avg = torch.empty((n_var, nf), **f64)
+    gT, gP = torch.empty(NLT, **f64), torch.empty(NLT, **f64)
+    gX = torch.empty((3, NLT), **f64)
+    eng = _native.Engine(dev.index or 0)
+    catalog.upload(eng, lines)
+    eng.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        eng.adjoint_batch_device(torch.cuda.current_stream(dev).cuda_stream, nLs, t['P'].data_ptr(),
+                                 t['T'].data_ptr(), t['X'].data_ptr(), t['R'].data_ptr(),
+                                 t['N'].data_ptr(), freqs, t['b'], t['w'].data_ptr(), grad.data_ptr(),
+                                 avg.data_ptr(), gT.data_ptr(), gP.data_ptr(), gX.data_ptr(),
+                                 71492.0, 66854.0)
+
+    best, tt = tune.tune_alpha(eng, step, key=('C4', n_var, nf),
+                               candidates=((2, 2, 1024), (2, 4, 1024), (4, 1, 1024), (4, 2, 1024)),
+                               reps=1, stream=stream)
+    step()                                   # plan and buffers for the chosen tiling
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
+    graph.replay()
+    torch.cuda.synchronize()
+    n = max(3, min(args.steps, 5))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    for s, e in ev:
+        s.record(stream)
+        graph.replay()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
+    ok = bool(torch.isfinite(avg).all().item() and torch.isfinite(gT).all().item())
+    # the same variants one atmosphere per call (plain path), a sample of 16
+    one = _native.Engine(dev.index or 0)
+    catalog.upload(one, lines)
+    one.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    o = np.concatenate([[0], np.cumsum(nLs)])
+    single = []
+    for i in range(min(16, n_var)):
+        sl = slice(int(o[i]), int(o[i + 1]))
+        args1 = (t['P'][sl].contiguous(), t['T'][sl].contiguous(), t['X'][:, sl].contiguous(),
+                 t['R'][sl].contiguous(), t['N'][sl].contiguous())
+        g1 = grad[i].contiguous()
+        d1 = [torch.empty(int(nLs[i]), **f64) for _ in range(2)] + [torch.empty((3, int(nLs[i])), **f64)]
+
+        def one_step():
+            one.adjoint_device(stream.cuda_stream, int(nLs[i]), nb, args1[0].data_ptr(), args1[1].data_ptr(),
+                               args1[2].data_ptr(), args1[3].data_ptr(), args1[4].data_ptr(), freqs,
+                               t['b'].data_ptr(), 71492.0, 66854.0, g1.data_ptr(), d1[0].data_ptr(),
+                               d1[1].data_ptr(), d1[2].data_ptr(), weights=t['w'].data_ptr())
+        tb1 = torch.empty((nb, nf), **f64)
+        av1 = torch.empty(nf, **f64)
+
+        def one_fwd():
+            one.forward_device(stream.cuda_stream, int(nLs[i]), nb, args1[0].data_ptr(), args1[1].data_ptr(),
+                               args1[2].data_ptr(), args1[3].data_ptr(), args1[4].data_ptr(), freqs,
+                               t['b'].data_ptr(), 71492.0, 66854.0, tb1.data_ptr(),
+                               weights=t['w'].data_ptr(), Tb_avg=av1.data_ptr())
+        row = []
+        for fn in (one_step, one_fwd):
+            fn()
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            fn()
+            s1.record(stream)
+            torch.cuda.synchronize()
+            row.append(s0.elapsed_time(s1) * 1e3 / int(nLs[i]))   # us per layer
+        single.append(row)
+    per_layer = np.mean(np.array(single), axis=0)
+    per_var_ms = float(per_layer[0]) * float(np.mean(nLs)) * 1e-3
+    fwd_ms = float(per_layer[1]) * float(np.mean(nLs)) * 1e-3
+    eng.close()
+    one.close()
+    value = n_var / (ms * 1e-3)
+    plain = 1e3 / per_var_ms
+    fd_rate = 1e3 / (fwd_ms * (1 + 2 * 5 * float(np.mean(nLs))))
+    return dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second (batched)',
+                value=value, unit='spectra+gradients/s', ms_per_step=ms, steps=n, finite=ok,
+                config=dict(workload=BATCH_WORKLOAD.format(n=n_var), variants=n_var,
+                            layers_total=NLT, freqs=nf, rays_per_variant=nb,
+                            tiling=dict(M=best[0], W=best[1], item_lines=best[2]),
+                            tuning_ms={'{},{},{}'.format(*k): v for k, v in tt.items()},
+                            l2='working set of tens of GB, larger than L2'),
+                per_atmosphere_adjoint=dict(value=plain, unit='spectra+gradients/s',
+                                            api='rb_adjoint_device, one atmosphere per call, '
+                                                '16-variant sample scaled by layer count'),
+                plain_dropin_finite_differences=dict(
+                    value=fd_rate, unit='spectra+gradients/s',
+                    how='plain drop-in forward (rb_forward_device, one atmosphere per call) '
+                        'times 1 + 2 x 5 x nL central differences per gradient set'),
+                speedup_vs_per_atmosphere_adjoint=value / plain,
+                speedup_vs_plain_dropin=value / fd_rate)
 
 
 def alpha_flops(wl):
@@ -435,6 +573,7 @@ def run_gpu(args, rank, world, local_rank):
     d2h = out['Tb_avg'].nbytes
 
     grads = measure_gradients(args, dev, stream, flush)
+    batched = measure_batch(args, dev, args.batch_variants) if args.batch_variants > 0 else None
     if rank != 0:
         return
     # roofline of the dominant kernel (absorption) and of the Tb scan
@@ -466,7 +605,7 @@ def run_gpu(args, rank, world, local_rank):
                            unit='GB/s', frac=(scan_gbs / hbm) if hbm else None,
                            algorithmic_bytes_per_launch=sbytes,
                            peak_source='MEASURED_PEAKS.json hbm_gbs (of measured)'),
-        phase_ms=ph, clocks=clocks, gradients=grads)
+        phase_ms=ph, clocks=clocks, gradients=grads, batched=batched)
     if pool is not None:
         try:
             line['cpu_baseline'] = cpu_baseline(wl, args.cpu_sample_s, pool, cores)

@@ -128,8 +128,8 @@ __device__ __forceinline__ void adj_stage(const TbAdjArgs& a, AdjStage& sg, int 
 
 __global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
   __shared__ AdjStage sg;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y, b = blockIdx.z;
+  const int f = blockIdx.z * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y, b = blockIdx.x;   // rays in x: batches have more than 65535
   const int n = min(max(a.nseg[b], 0), a.max_seg);
   const int N = n - 1;
   const int nc = N > 0 ? (N + ADJ_CHUNK - 1) / ADJ_CHUNK : 0;
@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
 
 __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
   __shared__ AdjStage sg;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y, b = blockIdx.z;
+  const int f = blockIdx.z * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y, b = blockIdx.x;   // rays in x: batches have more than 65535
   const int n = min(max(a.nseg[b], 0), a.max_seg);
   const int N = n - 1;
   const int nc = N > 0 ? (N + ADJ_CHUNK - 1) / ADJ_CHUNK : 0;
@@ -903,7 +903,7 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   if (e != cudaSuccess) return e;
   if (ta.nb > 0) {
     const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
-    dim3 grid((ta.nf + blk - 1) / blk, ta.nchunk, ta.nb);
+    dim3 grid(ta.nb, ta.nchunk, (ta.nf + blk - 1) / blk);
     rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);
     rb_tb_adj_grad_kernel<<<grid, blk, 0, st>>>(ta);
   }

@@ -89,8 +89,8 @@ __device__ __forceinline__ void ray_layers(const TbArgs& a, int ray, int& off, i
 
 // ------------------------------------------------------------ sequential
 __global__ void __launch_bounds__(128) rb_tb_seq_kernel(TbArgs a) {
-  const int ray = blockIdx.y;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ray = blockIdx.x;
+  const int f = blockIdx.y * blockDim.x + threadIdx.x;
   if (ray >= a.nb) return;
   const bool valid = f < a.nf;
   const int fi = valid ? f : 0;
@@ -152,9 +152,9 @@ __global__ void __launch_bounds__(128) rb_tb_seq_kernel(TbArgs a) {
 constexpr int TB_CHUNK = 128;
 
 __global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
-  const int ray = blockIdx.z;
+  const int ray = blockIdx.x;   // rays in x: batches have more than 65535
   const int ch = blockIdx.y;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = blockIdx.z * blockDim.x + threadIdx.x;
   const int nseg = a.nseg[ray];
   const int nsteps = nseg - 1;                 // segments used by the scan
   const int i0 = ch * TB_CHUNK;
@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
 
 // Combine chunk partials of each (ray, frequency) into Tb.
 __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
-  const int ray = blockIdx.y;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ray = blockIdx.x;
+  const int f = blockIdx.y * blockDim.x + threadIdx.x;
   if (f >= a.nf) return;
   const float4* part = a.part + (size_t)ray * a.nchunk * a.nf + f;
   const int nsteps = a.nseg[ray] - 1;
@@ -278,18 +278,18 @@ int tb_nchunk(int max_seg) { return (max_seg + TB_CHUNK - 1) / TB_CHUNK; }
 
 cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st) {
   if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
-  dim3 grid((a.nf + 127) / 128, a.nb);
+  dim3 grid(a.nb, (a.nf + 127) / 128);
   rb_tb_seq_kernel<<<grid, 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
   if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
-  dim3 grid((a.nf + 127) / 128, a.nchunk, a.nb);
+  dim3 grid(a.nb, a.nchunk, (a.nf + 127) / 128);
   rb_tb_chunk_kernel<<<grid, 128, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  dim3 g2((a.nf + 127) / 128, a.nb);
+  dim3 g2(a.nb, (a.nf + 127) / 128);
   rb_tb_combine_kernel<<<g2, 128, 0, st>>>(a);
   return cudaGetLastError();
 }
