@@ -18,7 +18,7 @@
 //                           prefactors, continua) in dual numbers, giving
 //                           their derivatives with respect to the layer's
 //                           T, P, ln X_NH3, ln X_H2O, ln X_H2S.
-//   rb_alpha_jvp_kernel     one CTA per (layer, 64 frequencies): alpha is
+//   rb_alpha_jvp_kernel     one CTA per (layer, up to 128 frequencies): alpha is
 //                           recomputed line by line together with its
 //                           derivatives with respect to the five layer
 //                           parameters (each family depends on T, P and its
@@ -52,6 +52,15 @@ __device__ __forceinline__ int wrap_l(int l, int nL) {
 //                            chunks, then the chunk's nodes in reverse.
 constexpr int ADJ_CHUNK = 128;   // = the forward scan's chunk (rb_tb.cu)
 
+// Double-float running sum (a float pair) and compensated float sum.
+__device__ __forceinline__ void dfs_add(float& h, float& l, float v) {
+  float s, e;
+  two_sum(h, v, s, e);
+  e += l;
+  h = s + e;
+  l = e - (h - s);
+}
+
 // d loss / d Tb of ray b at frequency f.
 __device__ __forceinline__ double adj_gb(const TbAdjArgs& a, int b, int f) {
   if (!a.weights) return a.grad[(size_t)b * a.nf + f];
@@ -61,7 +70,7 @@ __device__ __forceinline__ double adj_gb(const TbAdjArgs& a, int b, int f) {
 }
 
 struct ChunkState {
-  double tau_c;    // optical depth at this chunk's first node
+  float tch, tcl;  // optical depth at this chunk's first node (double-float)
   float Tb, rIW;
   bool live;       // TbL >= T_cmb (else Tb is clamped and has no gradient)
 };
@@ -72,9 +81,12 @@ __device__ __forceinline__ ChunkState adj_combine(const TbAdjArgs& a, int b, int
   float ph = 0.f, pl = 0.f;
   float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
   ChunkState st;
-  st.tau_c = 0.0;
+  st.tch = st.tcl = 0.f;
   for (int k = 0; k < nc; ++k) {
-    if (k == c) st.tau_c = (double)ph + (double)pl;
+    if (k == c) {
+      st.tch = ph;
+      st.tcl = pl;
+    }
     const float4 p = part[(size_t)k * a.nf];
     const float sc = __expf(-ph) * (1.f - pl);
     float y = sc * p.z - iwc, t = iw + y;
@@ -149,20 +161,23 @@ __global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
     return;
   }
   const float* al = a.alpha32 + f;
-  double tl = 0.0, lam = 0.0;
+  float th = 0.f, tlo = 0.f, lam = 0.f, lamc = 0.f;
   float a0 = al[sg.off[0]];
   for (int s = 0; s < ns; ++s) {
     const float ak = al[sg.off[s + 1]];
     const float d = 2.f * sg.hd[s];
-    tl += (double)((a0 + ak) * d * 0.5f);
+    dfs_add(th, tlo, (a0 + ak) * d * 0.5f);
     const float dk = 2.f * sg.hd[s + 1];
     const float ck = 0.5f * (d + dk);
-    const float Ek = __expf(-(float)tl);
+    const float Ek = __expf(-th) * (1.f - tlo);
     const float wk = ck * (sg.T[s + 1] - st.Tb) * st.rIW;
-    lam -= (double)(wk * ak * Ek);
+    const float y = -(wk * ak * Ek) - lamc;
+    const float tt = lam + y;
+    lamc = (tt - lam) - y;
+    lam = tt;
     a0 = ak;
   }
-  *S = (float)(exp(-st.tau_c) * lam);
+  *S = __expf(-st.tch) * (1.f - st.tcl) * (lam - lamc);
 }
 
 __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
@@ -177,48 +192,66 @@ __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
   const int ns = min(ADJ_CHUNK, N - i0);
   adj_stage(a, sg, b, i0, ns, N);
   __syncthreads();
-  if (f >= a.nf) return;
+  // lanes past nf or without a gradient run with gb = 0 so the warp's
+  // source-term shuffle has every lane
+  const bool inf = f < a.nf;
   const int nf = a.nf;
-  const double gb = adj_gb(a, b, f);
-  if (gb == 0.0) return;
-  const ChunkState st = adj_combine(a, b, c, f, nc);
-  if (!st.live) return;
-  const float* S = a.S + (size_t)b * a.nchunk * a.nf + f;
-  double Lnext = 0.0;    // Lam of the node after this chunk's last node
-  for (int k = c + 1; k < nc; ++k) Lnext += (double)S[(size_t)k * a.nf];
-  const float* al = a.alpha32 + f;
-  // local optical depth at the chunk's last node
-  double tl = 0.0;
+  const int fc = inf ? f : 0;
+  double gb = inf ? adj_gb(a, b, fc) : 0.0;
+  const ChunkState st = adj_combine(a, b, c, fc, nc);
+  if (!st.live) gb = 0.0;
+  if (__all_sync(0xffffffffu, gb == 0.0)) return;
+  const unsigned am_mask = 0xffffffffu;
+  const float* S = a.S + (size_t)b * a.nchunk * a.nf + fc;
+  // Lam of the node after this chunk's last node, compensated
+  float Ln = 0.f, Lc = 0.f;
+  for (int k = c + 1; k < nc; ++k) {
+    const float y = S[(size_t)k * a.nf] - Lc;
+    const float t = Ln + y;
+    Lc = (t - Ln) - y;
+    Ln = t;
+  }
+  const float* al = a.alpha32 + fc;
+  // local optical depth at the chunk's last node (double-float)
+  float th = 0.f, tlo = 0.f;
   {
     float ap = al[sg.off[0]];
     for (int s = 0; s < ns; ++s) {
       const float ak = al[sg.off[s + 1]];
-      tl += (double)((ap + ak) * (2.f * sg.hd[s]) * 0.5f);
+      dfs_add(th, tlo, (ap + ak) * (2.f * sg.hd[s]) * 0.5f);
       ap = ak;
     }
   }
-  const double Ec = exp(-st.tau_c);
+  const float Ec = __expf(-st.tch) * (1.f - st.tcl);
+  const float g = (float)gb;
   // nodes i0+ns .. i0+1 in reverse (node i0 belongs to the previous chunk,
   // except node 0, which chunk 0 handles last); the sums over the rays and
-  // over the (at most two) visits of a layer are atomic adds into
-  // galpha[layer][f] and gsrc[layer][f]
+  // the visits of a layer are atomic adds into galpha[layer][f] and gsrc[layer]
   float ak = al[sg.off[ns]];
   for (int t = ns; t > 0; --t) {
     const float dprev = 2.f * sg.hd[t - 1];
     const float dcur = 2.f * sg.hd[t];
     const float ck = 0.5f * (dprev + dcur);
-    const double Ek = Ec * (double)__expf(-(float)tl);
-    const double wk = (double)(ck * (sg.T[t] - st.Tb) * st.rIW);
-    const double Lk_ = Lnext - wk * (double)ak * Ek;
-    atomicAdd(a.ga + sg.off[t] + f, gb * (wk * Ek + 0.5 * (double)dprev * Lk_ + 0.5 * (double)dcur * Lnext));
-    atomicAdd(a.gs + sg.off[t] + f, gb * (double)ak * Ek * (double)ck * (double)st.rIW);
+    const float Ek = Ec * __expf(-th) * (1.f - tlo);
+    const float wk = ck * (sg.T[t] - st.Tb) * st.rIW;
+    const float Lnext = Ln - Lc;
+    // Lam_k = Lam_{k+1} - w_k a_k E_k
+    const float y = -(wk * ak * Ek) - Lc;
+    const float tt = Ln + y;
+    Lc = (tt - Ln) - y;
+    Ln = tt;
+    const float Lk = Ln - Lc;
+    if (g != 0.f) atomicAdd(a.ga + sg.off[t] + f, g * (wk * Ek + 0.5f * dprev * Lk + 0.5f * dcur * Lnext));
+    // source term: summed over the warp's frequencies before the atomic
+    float src = g * ak * Ek * ck * st.rIW;
+    for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(am_mask, src, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(a.gs + sg.lay[t], (double)src);
     const float am = al[sg.off[t - 1]];
-    tl -= (double)((am + ak) * dprev * 0.5f);
+    dfs_add(th, tlo, -(am + ak) * dprev * 0.5f);
     ak = am;
-    Lnext = Lk_;
   }
-  if (c == 0)   // node 0: W_0 = 0, only the segment term
-    atomicAdd(a.ga + sg.off[0] + f, gb * 0.5 * (double)(2.f * sg.hd[0]) * Lnext);
+  if (c == 0 && g != 0.f)   // node 0: W_0 = 0, only the segment term
+    atomicAdd(a.ga + sg.off[0] + f, g * 0.5f * (2.f * sg.hd[0]) * (Ln - Lc));
 }
 
 // ------------------------------------------------------------------ dual numbers
@@ -477,7 +510,7 @@ constexpr int JV_CHUNK = 64;
 constexpr int JV_NREC = 16;
 
 struct JvpShared {
-  float rec[2][JV_NREC][JV_CHUNK];   // [coefficient set][field][line]
+  float rec[2][JV_CHUNK][JV_NREC];   // [coefficient set][line][field], 64 B per line
   double red[8][NTH + 1];
 };
 
@@ -619,18 +652,21 @@ __device__ __forceinline__ void br_eval(float F, float FL, float g, float z, flo
   const float n = fmaf(gm, F, gp * K);
   const float t = S * n * r;
   val.add(t);
-  for (int q = 0; q < 3; ++q) {
-    const float dn = (dg[q] - dz[q]) * F + (dg[q] + dz[q]) * K + gp * dK[q];
-    const float dden = -2.f * e * dK[q] + 8.f * F * g * dg[q];
-    der[q].add((q == 0 ? t * dlnS : 0.f) + S * (dn - n * r * dden) * r);
-  }
+  // dt = S r [dn - n r dden] + t dlnS with dn = (F + K) dg + (K - F) dz + gp dK,
+  // dden = 8 F g dg - 2 e dK, collected per tangent of g, z, K
+  const float nr = n * r, Sr = S * r;
+  const float Ag = Sr * ((F + K) - 8.f * F * g * nr);
+  const float Az = Sr * (K - F);
+  const float AK = Sr * fmaf(2.f * e, nr, gp);
+  for (int q = 0; q < 3; ++q) der[q].s += fmaf(Ag, dg[q], fmaf(Az, dz[q], AK * dK[q]));
+  der[0].s += t * dlnS;
 }
 
 // Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
 // sweeps lines g, g + NG, ... of every chunk and the groups' sums are added
 // per family.
 __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
-  __shared__ JvpShared sh;
+  __shared__ __align__(16) JvpShared sh;
   __shared__ float s_grp[256][4];
   const int L = blockIdx.x;
   const int tid = threadIdx.x;
@@ -697,63 +733,67 @@ __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
       for (int i = tid; i < nc; i += blockDim.x) {
         const int li = c0 + i;
         if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
-          jv_br_record(t, LF, FT, 0, li, xt, &sh.rec[0][0][i], JV_CHUNK);
-          if (two) jv_br_record(t, LF, FT, 1, li, xt, &sh.rec[1][0][i], JV_CHUNK);
+          jv_br_record(t, LF, FT, 0, li, xt, sh.rec[0][i], 1);
+          if (two) jv_br_record(t, LF, FT, 1, li, xt, sh.rec[1][i], 1);
         } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
-          jv_gross_record(t, LF, FT, li, xt, &sh.rec[0][0][i], JV_CHUNK);
+          jv_gross_record(t, LF, FT, li, xt, sh.rec[0][i], 1);
         } else if (fam == FAM_H2O) {
-          jv_vvw_record(t, LF, FT, li, xt, &sh.rec[0][0][i], JV_CHUNK, &base, dbase);
+          jv_vvw_record(t, LF, FT, li, xt, sh.rec[0][i], 1, &base, dbase);
         } else {
-          jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, &sh.rec[0][0][i], JV_CHUNK);
+          jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, sh.rec[0][i], 1);
         }
       }
       __syncthreads();
       if (on) {
-        const float(*R)[JV_CHUNK] = sh.rec[two ? set : 0];
+        const float(*Rl)[JV_NREC] = sh.rec[two ? set : 0];
         for (int i = grp; i < nc; i += NG) {
+          const float4* r4 = reinterpret_cast<const float4*>(Rl[i]);
+          const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2], q3 = r4[3];
+          // fields 0..15 = q0.xyzw q1.xyzw q2.xyzw q3.xyzw
           if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
-            const float dg[3] = {R[6][i], R[7][i], R[8][i]};
-            const float dz[3] = {R[9][i], R[10][i], R[11][i]};
-            const float dK[3] = {R[12][i], R[13][i], R[14][i]};
-            br_eval(Fx, FLx, R[0][i], R[1][i], R[2][i], R[3][i], R[4][i], R[5][i], dg, dz, dK, val,
-                    der);
+            const float dg[3] = {q1.z, q1.w, q2.x};
+            const float dz[3] = {q2.y, q2.z, q2.w};
+            const float dK[3] = {q3.x, q3.y, q3.z};
+            br_eval(Fx, FLx, q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, dg, dz, dK, val, der);
           } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
-            const float g = R[0][i], S = R[4][i];
-            const float e = (Fx - R[2][i]) + (FLx - R[3][i]);
+            const float g = q0.x, S = q1.x;
+            const float e = (Fx - q0.z) + (FLx - q0.w);
             const float den = fmaf(e, e, 4.f * Fx * g * g);
             const float r = rcp_approx(den);
             const float tt = S * g * r;
             val.add(tt);
-            for (int q = 0; q < 3; ++q) {
-              const float dg = R[6 + q][i];
-              der[q].add((q == 0 ? tt * R[5][i] : 0.f) + S * (dg - g * r * 8.f * Fx * g * dg) * r);
-            }
+            const float dgv[3] = {q1.z, q1.w, q2.x};
+            const float k8 = 8.f * Fx * g * g * r;
+            for (int q = 0; q < 3; ++q)
+              der[q].s += (q == 0 ? tt * q1.y : 0.f) + S * dgv[q] * (1.f - k8) * r;
           } else if (fam == FAM_H2O) {
-            const float df = R[0][i], S = R[4][i];
-            const float dm = (fq - R[2][i]) + (fql - R[3][i]);
-            const float dp = fq + R[2][i];
+            const float df = q0.x, S = q1.x;
+            const float dm = (fq - q0.z) + (fql - q0.w);
+            const float dp = fq + q0.z;
             const float d1 = fmaf(dm, dm, df * df), d2 = fmaf(dp, dp, df * df);
             const float r1 = rcp_approx(d1), r2 = rcp_approx(d2);
             const float h = S * df, u = r1 + r2;
             val.add(h * u);
+            const float ddf[3] = {q1.z, q1.w, q2.x};
+            const float k2 = 2.f * h * df * (r1 * r1 + r2 * r2);
             for (int q = 0; q < 3; ++q) {
-              const float ddf = R[6 + q][i];
-              const float dh = (q == 0 ? h * R[5][i] : 0.f) + S * ddf;
-              der[q].add(dh * u - h * 2.f * df * ddf * (r1 * r1 + r2 * r2));
+              const float dh = (q == 0 ? h * q1.y : 0.f) + S * ddf[q];
+              der[q].s += dh * u - k2 * ddf[q];
             }
           } else {   // nh3_sjs
-            const float G0 = R[6][i], S = R[4][i];
+            const float G0 = q1.z, S = q1.x;
             const float g = fmaf(B, G0, A), z = fmaf(D, G0, C);
             const float g2z2 = (g - z) * (g + z);
+            const float dK0[3] = {q2.y, q2.z, q2.w};
             float dg[3], dz[3], dK[3];
             for (int q = 0; q < 3; ++q) {
               dg[q] = fmaf(dB[q], G0, dA[q]);
               dz[q] = fmaf(dD[q], G0, dC[q]);
-              dK[q] = R[9 + q][i] + 2.f * g * dg[q] - 2.f * z * dz[q];
+              dK[q] = dK0[q] + 2.f * g * dg[q] - 2.f * z * dz[q];
             }
             float KH, e;
-            two_sum(R[2][i], g2z2, KH, e);
-            br_eval(Fx, FLx, g, z, KH, e + R[3][i], S, R[5][i], dg, dz, dK, val, der);
+            two_sum(q0.z, g2z2, KH, e);
+            br_eval(Fx, FLx, g, z, KH, e + q0.w, S, q1.y, dg, dz, dK, val, der);
           }
         }
       }
@@ -792,7 +832,7 @@ __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
   // assemble dalpha/dtheta (cm^-1) in float64 and contract with dTb/dalpha
   double g5[NTH] = {0, 0, 0, 0, 0};
   if (on && grp == 0) {
-    const double gal = a.galpha[(size_t)L * a.nf + j];
+    const double gal = (double)a.galpha[(size_t)L * a.nf + j];
     const double Fd = f * f, Fhd = fh * fh;
     auto pref = [&](int fam) { return ldexp((double)lp.fam[fam].fm, lp.fam[fam].fe); };
     // d(pref * S) / dtheta for a family with tangent triple (T, P, X_own)
@@ -885,9 +925,7 @@ __global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const double*
   double s[NTH] = {0, 0, 0, 0, 0};
   for (int t = 0; t < ntile; ++t)
     for (int q = 0; q < NTH; ++q) s[q] += part[((size_t)L * ntile + t) * NTH + q];
-  double src = 0.0;
-  for (int f = 0; f < nf; ++f) src += gsrc[(size_t)L * nf + f];
-  dT[L] = s[TH_T] + src;
+  dT[L] = s[TH_T] + gsrc[L];
   dP[L] = s[TH_P];
   dlnX[L] = s[TH_XNH3];
   dlnX[nL + L] = s[TH_XH2O];
@@ -895,11 +933,10 @@ __global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const double*
 }
 
 // ------------------------------------------------------------------ launch
-cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, float* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st) {
-  const size_t nbuf = (size_t)ta.nL * ta.nf;
-  cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(double) * nbuf, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * nbuf, st);
+  cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(float) * (size_t)ta.nL * ta.nf, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * (size_t)ta.nL, st);
   if (e != cudaSuccess) return e;
   if (ta.nb > 0) {
     const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
@@ -917,7 +954,7 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
 
 // Frequencies per CTA of rb_alpha_jvp_kernel (the rest of its 256 threads
 // split the lines).
-int adjoint_ft(int nf) { return nf >= 64 ? 64 : 32; }
+int adjoint_ft(int nf) { return nf >= 128 ? 128 : (nf >= 64 ? 64 : 32); }
 int adjoint_tiles(int nf) { return (nf + adjoint_ft(nf) - 1) / adjoint_ft(nf); }
 
 }  // namespace rb

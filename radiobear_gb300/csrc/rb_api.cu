@@ -154,7 +154,7 @@ namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
 cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st);
 int alpha_lines_occupancy(int M, int W);
-cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, double* galpha,
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, float* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st);
 int adjoint_tiles(int nf);
 int adjoint_ft(int nf);
@@ -1119,8 +1119,8 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   const int launches = h->launches;
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
   const int ntile = rb::adjoint_tiles(nf);
-  RB_CUDA(h->d_ga.ensure(sizeof(double) * (size_t)nL * nf));
-  RB_CUDA(h->d_gs.ensure(sizeof(double) * (size_t)nL * nf));
+  RB_CUDA(h->d_ga.ensure(sizeof(float) * (size_t)nL * nf));
+  RB_CUDA(h->d_gs.ensure(sizeof(double) * (size_t)nL));
   RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
   RB_CUDA(h->d_jpart.ensure(sizeof(double) * (size_t)nL * ntile * rb::NTH));
   rb::TbAdjArgs ta{};
@@ -1137,7 +1137,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   ta.layer = h->d_layer.as<int>();
   ta.weights = weights;
   ta.grad = grad;
-  ta.ga = h->d_ga.as<double>();
+  ta.ga = h->d_ga.as<float>();
   ta.gs = h->d_gs.as<double>();
   ta.nchunk = rb::tb_nchunk(max_seg);
   ta.part = h->d_part.as<float4>();
@@ -1162,9 +1162,9 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   for (int f = 0; f < rb::NFAM; ++f) jv.tab[f] = h->fam[f].table();
   jv.cfg = h->cfg;
   jv.cfg.units_db = 0;
-  jv.galpha = h->d_ga.as<double>();
+  jv.galpha = h->d_ga.as<float>();
   jv.part = h->d_jpart.as<double>();
-  RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_ga.as<double>(), h->d_gs.as<double>(), dT, dP, dlnX,
+  RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_ga.as<float>(), h->d_gs.as<double>(), dT, dP, dlnX,
                              st));
   h->launches = launches + 6;
   return RB_OK;

