@@ -506,11 +506,11 @@ __global__ void __launch_bounds__(256) rb_layer_tan_kernel(TanArgs a) {
 // ------------------------------------------------------------------ alpha JVP
 // Records of one line, float: value fields and derivatives along the
 // family's three tangents (T, P, ln X of its own gas).
-constexpr int JV_CHUNK = 64;
+constexpr int JV_CHUNK = 128;
 constexpr int JV_NREC = 16;
 
 struct JvpShared {
-  float rec[2][JV_CHUNK][JV_NREC];   // [coefficient set][line][field], 64 B per line
+  float rec[2][2][JV_CHUNK][JV_NREC];   // [buffer][coefficient set][line][field], 64 B per line
   double red[8][NTH + 1];
 };
 
@@ -728,24 +728,32 @@ __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
     KSum val, der[3];
     val.init();
     for (int q = 0; q < 3; ++q) der[q].init();
-    for (int c0 = 0; c0 < t.n; c0 += JV_CHUNK) {
+    // records double-buffered: chunk c+1 is built while chunk c is swept
+    auto build = [&](int bi, int c0) {
       const int nc = min(JV_CHUNK, t.n - c0);
       for (int i = tid; i < nc; i += blockDim.x) {
         const int li = c0 + i;
         if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
-          jv_br_record(t, LF, FT, 0, li, xt, sh.rec[0][i], 1);
-          if (two) jv_br_record(t, LF, FT, 1, li, xt, sh.rec[1][i], 1);
+          jv_br_record(t, LF, FT, 0, li, xt, sh.rec[bi][0][i], 1);
+          if (two) jv_br_record(t, LF, FT, 1, li, xt, sh.rec[bi][1][i], 1);
         } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
-          jv_gross_record(t, LF, FT, li, xt, sh.rec[0][i], 1);
+          jv_gross_record(t, LF, FT, li, xt, sh.rec[bi][0][i], 1);
         } else if (fam == FAM_H2O) {
-          jv_vvw_record(t, LF, FT, li, xt, sh.rec[0][i], 1, &base, dbase);
+          jv_vvw_record(t, LF, FT, li, xt, sh.rec[bi][0][i], 1, &base, dbase);
         } else {
-          jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, sh.rec[0][i], 1);
+          jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, sh.rec[bi][0][i], 1);
         }
       }
-      __syncthreads();
+    };
+    const int nchunks = (t.n + JV_CHUNK - 1) / JV_CHUNK;
+    build(0, 0);
+    __syncthreads();
+    for (int ci = 0; ci < nchunks; ++ci) {
+      const int c0 = ci * JV_CHUNK;
+      const int nc = min(JV_CHUNK, t.n - c0);
+      if (ci + 1 < nchunks) build((ci + 1) & 1, c0 + JV_CHUNK);
       if (on) {
-        const float(*Rl)[JV_NREC] = sh.rec[two ? set : 0];
+        const float(*Rl)[JV_NREC] = sh.rec[ci & 1][two ? set : 0];
         for (int i = grp; i < nc; i += NG) {
           const float4* r4 = reinterpret_cast<const float4*>(Rl[i]);
           const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2], q3 = r4[3];

@@ -1,0 +1,176 @@
+"""Drop-in classes with the reference's signatures (radiobear_gb300.dropin).
+
+CPU: scale semantics and errors of Alpha.get_layer_scale /
+total_layer_alpha (alpha.py:151-259), the alpha cache format
+(alpha.py:110-149) and install().  GPU: get_layers, get_alpha_from_calc,
+compute_ds and Brightness.single against the reference fixtures, and the
+memory / file cache round trips.
+"""
+import sys
+import types
+from argparse import Namespace
+
+import numpy as np
+import pytest
+
+from radiobear_gb300 import dropin, synth
+from tests import goldio as G
+
+LP = {k: i for i, k in enumerate(synth.PROPERTY_COLUMNS)}
+
+
+class FakeEngine:
+    def set_formalisms(self, *a, **k):
+        self.formalisms = (a, k)
+
+
+def cpu_alpha(tmp_path=None):
+    cfg = Namespace(constituent_alpha=dict(dropin.DEFAULT_CONSTITUENTS), h2state='e',
+                    scratch_directory=str(tmp_path) if tmp_path else 'Scratch')
+    return dropin.Alpha(config=cfg, engine_=FakeEngine())
+
+
+def test_layer_scale_semantics():
+    a = cpu_alpha()
+    assert a.ordered_constituents == ['h2', 'h2o', 'h2s', 'nh3', 'ph3']
+    assert a.get_layer_scale(2, 3) == [2.0, 2.0, 2.0]
+    assert a.get_layer_scale(False, 2) == [1.0, 1.0]
+    assert list(a.get_layer_scale([1.0, 2.0], 2)) == [1.0, 2.0]
+    d = a.get_layer_scale({'nh3': [1.0, 0.5]}, 2)
+    assert d == [{'nh3': 1.0}, {'nh3': 0.5}]
+    with pytest.raises(ValueError, match='Incorrect number of scale layers'):
+        a.get_layer_scale([1.0], 2)
+    with pytest.raises(ValueError, match='not found as constituent'):
+        a.get_layer_scale({'co': [1.0, 1.0]}, 2)
+    with pytest.raises(ValueError, match='Incorrect scale for nh3'):
+        a.get_layer_scale({'nh3': [1.0]}, 2)
+
+
+def test_scale_matrix_and_total():
+    a = cpu_alpha()
+    m = a._scale_matrix([2.0, {'nh3': 0.5, 'h2o': 3.0}])
+    assert np.all(m[0] == 2.0)
+    assert m[1, 3] == 0.5 and m[1, 1] == 3.0 and m[1, 0] == 1.0
+    a._save_alpha_memfil = False
+    absorb = np.arange(10.0).reshape(2, 5)
+    assert np.allclose(a.total_layer_alpha(absorb, 2.0), 2.0 * absorb.sum(axis=1))
+    want = (absorb * np.array([1, 3.0, 1, 0.5, 1])).sum(axis=1)
+    assert np.allclose(a.total_layer_alpha(absorb, {'nh3': 0.5, 'h2o': 3.0}), want)
+
+
+def test_alpha_cache_format(tmp_path):
+    a = cpu_alpha(tmp_path)
+    a.freqs = np.array([1.0, 2.0])
+    a.P = np.array([0.1, 1.0, 10.0])
+    a.tosave = list(np.random.default_rng(0).random((3, 2, 5)))
+    a.save_alpha_data('file')
+    z = np.load(a.alphafile)
+    assert sorted(z.files) == ['P', 'alpha_data', 'freqs', 'ordered_constituents']
+    assert z['alpha_data'].shape == (3, 2, 5)
+    b = cpu_alpha(tmp_path)
+    b.read_alpha_data('file')
+    assert np.array_equal(b.alpha_data, z['alpha_data'])
+    a.save_alpha_data('memory')
+    assert a.memory.alpha_data.shape == (3, 2, 5)
+
+
+def test_install_patches_package():
+    pkg = types.ModuleType('fakerb')
+    pkg.__file__ = '/nonexistent/fakerb/__init__.py'
+    al = types.ModuleType('fakerb.alpha')
+    rp = types.ModuleType('fakerb.raypath')
+    br = types.ModuleType('fakerb.brightness')
+    al.Alpha = type('Alpha', (), {'get_layers': lambda self: None})
+    rp.Ray = dropin.Ray
+    rp.compute_ds = lambda *a: None
+    br.Brightness = type('Brightness', (), {'single': lambda self: None})
+    br.ray = rp
+    saved = {k: sys.modules.get(k) for k in ('fakerb', 'fakerb.alpha', 'fakerb.raypath', 'fakerb.brightness')}
+    sys.modules.update({'fakerb': pkg, 'fakerb.alpha': al, 'fakerb.raypath': rp, 'fakerb.brightness': br})
+    try:
+        out = dropin.install(pkg, lines={}, engine_=FakeEngine())
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    assert al.Alpha.get_layers.__name__ == 'get_layers' and rp.compute_ds is out['compute_ds']
+    assert br.ray.compute_ds is out['compute_ds']
+    assert br.Brightness.single.__name__ == 'single'
+
+
+# ------------------------------------------------------------------ GPU
+def bench_atm():
+    z = G.load('benchmark')
+    gas = G.gas_table(z)
+    prop = np.zeros((len(synth.PROPERTY_COLUMNS), gas.shape[1]))
+    prop[LP['R']] = z['prop_R']
+    prop[LP['N']] = z['prop_N']
+    cfg = Namespace(C=G.C, LP=LP, Req=float(z['Req']), Rpol=float(z['Rpol']), gtype='ellipse',
+                    orientation=[0.0, 0.0])
+    return z, Namespace(gas=gas, property=prop, config=cfg)
+
+
+@pytest.fixture(scope='module')
+def gpu_alpha():
+    from radiobear_gb300 import _native
+    e = _native.Engine(0)
+    cfg = Namespace(constituent_alpha=dict(dropin.DEFAULT_CONSTITUENTS), h2state='e')
+    a = dropin.Alpha(config=cfg, engine_=e, lines=G.benchmark_lines())
+    yield a, e
+    e.close()
+
+
+@pytest.mark.gpu
+def test_get_layers_benchmark(gpu_alpha):
+    a, _ = gpu_alpha
+    z, atm = bench_atm()
+    lay = a.get_layers(z['freqs'], atm)
+    assert lay.shape == z['alpha_layers'].shape
+    assert np.max(np.abs(lay - z['alpha_layers']) / np.abs(z['alpha_layers'])) < 1e-5
+
+
+@pytest.mark.gpu
+def test_get_alpha_from_calc_one_layer(gpu_alpha):
+    a, _ = gpu_alpha
+    z, atm = bench_atm()
+    L = 7
+    g = a.get_alpha_from_calc(z['freqs'], atm.gas[G.C['T'], L], atm.gas[G.C['P'], L], atm.gas[:, L],
+                              G.C, None, None)
+    ref = z['alpha_gas'][L]      # [nf, nC] in the reference's ordered constituents
+    order = [list(z['ordered_constituents']).index(c) for c in a.ordered_constituents]
+    refo = ref[:, order]
+    tot = np.abs(ref).sum(axis=1, keepdims=True)
+    assert np.max(np.abs(g - refo) / np.maximum(np.abs(refo), 1e-7 * tot)) < 1e-5
+
+
+@pytest.mark.gpu
+def test_alpha_cache_round_trips(gpu_alpha, tmp_path):
+    a, _ = gpu_alpha
+    z, atm = bench_atm()
+    nL = atm.gas.shape[1]
+    scale = {'nh3': np.linspace(0.5, 1.5, nL), 'h2o': np.full(nL, 2.0)}
+    calc = a.get_layers(z['freqs'], atm, scale=scale, save_alpha='memory')
+    again = a.get_layers(z['freqs'], atm, scale=1.0, get_alpha='memory')
+    assert np.allclose(again, calc, rtol=1e-12, atol=0)      # stored data are already scaled
+    a.alphafile = str(tmp_path / 'alpha0000.npz')
+    a.get_layers(z['freqs'], atm, save_alpha='file')
+    from_file = a.get_layers(z['freqs'], atm, get_alpha='file')
+    plain = a.get_layers(z['freqs'], atm)
+    assert np.allclose(from_file, plain, rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+def test_compute_ds_and_brightness_benchmark(gpu_alpha):
+    a, e = gpu_alpha
+    z, atm = bench_atm()
+    for i, b in enumerate(z['b']):
+        ray = dropin.compute_ds(atm, b, engine_=e)
+        assert np.array_equal(np.array(ray.layer4ds), z['ray{}_layer'.format(i)])
+        assert np.max(np.abs(np.array(ray.ds) - z['ray{}_ds'.format(i)]) / z['ray{}_ds'.format(i)]) < 5e-7
+    a.get_layers(z['freqs'], atm)
+    br = dropin.Brightness(engine_=e)
+    for i, b in enumerate(z['b']):
+        tb = br.single(b, z['freqs'], atm, a)
+        assert np.max(np.abs(np.array(tb) - z['Tb'][i])) < 1e-3
