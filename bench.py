@@ -283,6 +283,18 @@ def measure_batch(args, dev, n_var):
                 speedup_vs_plain_dropin=value / fd_rate)
 
 
+def replica_time(tot_ms, dist=None, device=None):
+    """Replicas only: each rank times its own copy of the workload; the job
+    time is the slowest rank's (MAX all-reduce), and the job's value counts
+    every rank's spectra (world x steps) over it."""
+    if dist is None:
+        return tot_ms
+    import torch
+    t = torch.tensor([tot_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def alpha_flops(wl):
     """Algorithmic FLOPs of one absorption launch: per (layer, line, freq)
     Ben-Reuven 10, Gross 8, VVW 12 (FMA = 2); blend layers add the nh3_sjs
@@ -536,11 +548,7 @@ def run_gpu(args, rank, world, local_rank):
     if dist is not None:
         dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in ev]
-    tot_ms = float(sum(step_ms))
-    if dist is not None:
-        t = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
+    tot_ms = replica_time(float(sum(step_ms)), dist, dev)
     clocks = clk.summary()
 
     # phase timing (CUDA events recorded inside the library on the streams
