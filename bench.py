@@ -48,6 +48,7 @@ def parse():
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-sample-s', type=float, default=20.0)
+    p.add_argument('--no-image', action='store_true', help='skip the C2 image measurement')
     p.add_argument('--batch-variants', type=int, default=4096,
                    help='atmospheres in the batched forward+adjoint measurement (0: skip)')
     p.add_argument('--alpha-tiling', default='',
@@ -281,6 +282,65 @@ def measure_batch(args, dev, n_var):
                         'times 1 + 2 x 5 x nL central differences per gradient set'),
                 speedup_vs_per_atmosphere_adjoint=value / plain,
                 speedup_vs_plain_dropin=value / fd_rate)
+
+
+IMAGE_WORKLOAD = ('C2 batched image rays: 256 x 256 impact parameters at 0.01 planet radius '
+                  '(31,397 on the disc incl. limb rays of up to ~2000 segments, the rest off the '
+                  'planet -> T_cmb) x 8 freqs (1.4..44 GHz), 1000 layers, C1 line lists')
+
+
+def measure_image(args, dev, stream, flush):
+    """Images per second (and rays/s) for the C2 grid: one rb_forward_device
+    call per image, every ray in the same launches."""
+    import torch
+    from radiobear_gb300 import _native, catalog, synth
+    from tests import goldio
+    cats = goldio.real_catalogues()
+    wl = synth.make_workload(2, real=cats)
+    wl['lines']['ph3wgt'] = cats['ph3wgt']
+    a = workload_arrays(wl)
+    nL, nf, nb = a['P'].size, a['freqs'].size, a['b'].shape[0]
+    eng = _native.Engine(dev.index or 0)
+    catalog.upload(eng, wl.lines)
+    eng.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+
+    def dt(x):
+        return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)
+
+    dP, dT, dX, dR, dN, db = (dt(a[k]) for k in ('P', 'T', 'X', 'R', 'N', 'b'))
+    Tb = torch.empty((nb, nf), dtype=torch.float64, device=dev)
+    sp = stream.cuda_stream
+
+    def step():
+        eng.forward_device(sp, nL, nb, dP.data_ptr(), dT.data_ptr(), dX.data_ptr(), dR.data_ptr(),
+                           dN.data_ptr(), a['freqs'], db.data_ptr(), 71492.0, 66854.0, Tb.data_ptr())
+
+    step()
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    n = max(3, min(args.steps, 20))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    torch.cuda.synchronize()
+    for s, e in ev:
+        flush.zero_()
+        s.record(stream)
+        step()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
+    t = Tb.cpu().numpy()
+    on = np.hypot(a['b'][:, 0], a['b'][:, 1]) < 1.0
+    rays = eng.raypath(a['R'], a['N'], a['b'][on][::97], 71492.0, 66854.0)
+    eng.close()
+    return dict(metric='brightness images per second', value=1e3 / ms, unit='images/s',
+                rays_per_s=nb * 1e3 / ms, ms_per_step=ms, steps=n,
+                config=dict(workload=IMAGE_WORKLOAD, layers=nL, freqs=nf, rays=nb,
+                            rays_on_disc=int(on.sum()),
+                            max_path_segments_sampled=int(rays['nseg'].max())),
+                finite=bool(np.isfinite(t).all()),
+                off_disc_is_tcmb=bool(np.all(t[~on] == 2.725)))
 
 
 def replica_time(tot_ms, dist=None, device=None):
@@ -581,6 +641,7 @@ def run_gpu(args, rank, world, local_rank):
     d2h = out['Tb_avg'].nbytes
 
     grads = measure_gradients(args, dev, stream, flush)
+    image = None if args.no_image else measure_image(args, dev, stream, flush)
     batched = measure_batch(args, dev, args.batch_variants) if args.batch_variants > 0 else None
     if rank != 0:
         return
@@ -613,7 +674,7 @@ def run_gpu(args, rank, world, local_rank):
                            unit='GB/s', frac=(scan_gbs / hbm) if hbm else None,
                            algorithmic_bytes_per_launch=sbytes,
                            peak_source='MEASURED_PEAKS.json hbm_gbs (of measured)'),
-        phase_ms=ph, clocks=clocks, gradients=grads, batched=batched)
+        phase_ms=ph, clocks=clocks, gradients=grads, batched=batched, image=image)
     if pool is not None:
         try:
             line['cpu_baseline'] = cpu_baseline(wl, args.cpu_sample_s, pool, cores)

@@ -250,8 +250,9 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
     pl = e - (ph - s);
   }
   const float TbL = tb - tbc, IW = iw - iwc;
-  const float out = (TbL < (float)T_CMB) ? (float)T_CMB : TbL / IW;
-  a.Tb[(size_t)ray * a.nf + f] = (double)out;
+  const bool clamped = TbL < (float)T_CMB;   // off the planet or no emission: T_cmb exactly
+  const float out = clamped ? (float)T_CMB : TbL / IW;
+  a.Tb[(size_t)ray * a.nf + f] = clamped ? T_CMB : (double)out;
   if (a.Tb32) a.Tb32[(size_t)ray * a.nf + f] = out;
   if (a.intW) a.intW[(size_t)ray * a.nf + f] = (double)IW;
 }
