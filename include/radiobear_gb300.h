@@ -15,8 +15,11 @@
  *   rb_set_lines      the catalogue loaders readInputFiles of
  *                     radiobear/constituents/nh3/nh3_hs.py:62-67,
  *                     nh3/nh3_sjs.py:17-23, h2o/h2o_bk.py:17-62,
- *                     h2s/h2s_ddb.py:14-39, ph3/ph3_jh.py:18-61
+ *                     h2s/h2s_ddb.py:14-39, ph3/ph3_jh.py:18-61,
+ *                     co/co_ddb.py:14-19
  *   rb_set_formalisms Alpha.setup_formalisms, radiobear/alpha.py:49-102
+ *   rb_set_co_clouds  the other_dict entries Alpha.setup_formalisms copies
+ *                     for co and clouds, radiobear/alpha.py:90-102
  *   rb_alpha          Alpha.get_layers / get_alpha_from_calc /
  *                     total_layer_alpha, radiobear/alpha.py:151-305, and the
  *                     per-gas plugins alpha(freq, T, P, X, P_dict, other_dict)
@@ -34,7 +37,7 @@
 extern "C" {
 #endif
 
-#define RB_ABI_VERSION 1
+#define RB_ABI_VERSION 2
 
 typedef struct rb_handle rb_handle;
 
@@ -53,22 +56,43 @@ typedef struct rb_handle rb_handle;
 #define RB_FAM_H2O 4     /* f_o, I_o, E_o, w_s, x_s, w_h2, w_he, x_h2, x_he, SR */
 #define RB_FAM_H2S 5     /* f0, I0, E, GH2S                       (h2s.npz) */
 #define RB_FAM_PH3 6     /* f0, I0, E, WgtI0, WgtFGB, WgtSB       (ph3jh + PH3WGT) */
+#define RB_FAM_CO 7      /* f0, I0, E                             (co.npz, co_ddb) */
 
 /* NH3 formalism (rb_set_formalisms) */
 #define RB_NH3_OFF 0
 #define RB_NH3_HS 1     /* nh3_hs */
 #define RB_NH3_SJS 2    /* nh3_sjs */
 #define RB_NH3_HS_SJS 3 /* nh3_hs_sjs pressure blend */
+#define RB_NH3_DBS 4    /* nh3_dbs */
+#define RB_NH3_DBS_SJS 5 /* nh3_dbs_sjs pressure blend */
 
-/* gas slots of per-gas outputs: the reference's sorted constituent order */
+/* co_ddb line shape (other_dict['coshape']); any other string is STD */
+#define RB_COSHAPE_VOIGT 0 /* 'voigt': sum of Voigt shapes */
+#define RB_COSHAPE_VVW 1   /* 'vvw': sum of Van Vleck-Weisskopf shapes */
+#define RB_COSHAPE_DIFF 2  /* 'diff': Voigt minus VVW */
+#define RB_COSHAPE_STD 3   /* pressure-blended shape times line strength */
+
+/* clouds_idp particle switches (other_dict '<kind>' > 0), OR-ed */
+#define RB_CLOUD_ICE 1     /* 'ice_p':    cloud H2O / 0.9, water dielectric */
+#define RB_CLOUD_WATER 2   /* 'water_p':  cloud SOLN / 1.0, water dielectric */
+#define RB_CLOUD_NH4SH 4   /* 'nh4sh_p':  cloud NH4SH / 1.2, n = 1.7 - 0.005i */
+#define RB_CLOUD_NH3ICE 8  /* 'nh3ice_p': cloud NH3 / 1.6, n = 1.3 - 0.0001i */
+#define RB_CLOUD_H2SICE 16 /* 'h2sice_p': cloud H2S / 1.5, n = 1.15 - 0.0001i */
+#define RB_CLOUD_CH4 32    /* 'ch4':      cloud CH4 / 1.0, n = 1.3 - 0.00001i */
+
+/* gas slots of per-gas outputs: the reference's sorted constituent order
+ * of the line gases, then co and clouds */
 #define RB_GAS_H2 0
 #define RB_GAS_H2O 1
 #define RB_GAS_H2S 2
 #define RB_GAS_NH3 3
 #define RB_GAS_PH3 4
-#define RB_NGAS 5
+#define RB_GAS_CO 5
+#define RB_GAS_CLOUDS 6
+#define RB_NGAS 7
 
-/* rows of the abundance array X[RB_NX][nL] (mole fractions) */
+/* rows of the layer composition array X[RB_NX][nL]: gas mole fractions,
+ * then cloud densities (g/cm^3, the reference's cloud table columns) */
 #define RB_X_H2 0
 #define RB_X_HE 1
 #define RB_X_CH4 2
@@ -76,7 +100,14 @@ typedef struct rb_handle rb_handle;
 #define RB_X_H2O 4
 #define RB_X_H2S 5
 #define RB_X_PH3 6
-#define RB_NX 7
+#define RB_X_CO 7
+#define RB_X_CL_H2O 8    /* cloud H2O (ice) */
+#define RB_X_CL_SOLN 9   /* cloud SOLN (liquid water) */
+#define RB_X_CL_NH4SH 10
+#define RB_X_CL_NH3 11
+#define RB_X_CL_H2S 12
+#define RB_X_CL_CH4 13
+#define RB_NX 14
 
 /* geometry switches */
 #define RB_GTYPE_ELLIPSE 0
@@ -103,6 +134,11 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
 int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2s, int use_ph3,
                       int h2state);
 
+/* co_ddb (co 0/1, coshape RB_COSHAPE_*) and clouds_idp (clouds 0/1,
+ * cloud_mask of RB_CLOUD_*).  co_ddb needs RB_FAM_CO lines.  Both are off
+ * after rb_create. */
+int rb_set_co_clouds(rb_handle* h, int co, int coshape, int clouds, int cloud_mask);
+
 /* Tiling of the absorption line sums (no reference counterpart: the
  * reference has no device decomposition).  M frequency slots per thread
  * (2 or 4), W warps per CTA (1..4), item_lines lines per work item
@@ -112,7 +148,7 @@ int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2
 int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines);
 
 /* Absorption of nL layers at nf frequencies.
- *   P[nL] bar, T[nL] K, X[RB_NX][nL] mole fractions, freqs[nf] GHz.
+ *   P[nL] bar, T[nL] K, X[RB_NX][nL] composition (rows above), freqs[nf] GHz.
  *   scale:      nullable, [nL][RB_NGAS] multipliers (number, per-layer list
  *               and per-constituent dict scales of Alpha.get_layers all map
  *               onto this form).

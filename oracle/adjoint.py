@@ -61,10 +61,11 @@ def brightness_vjp(ds, layer4ds, alpha_layers, T_layers, gTb):
     return galpha, gT
 
 
-def loss_forward(gas, C, R, N, freqs, rays, lines, Req, Rpol, weights, grad, h2state='e'):
+def loss_forward(gas, C, R, N, freqs, rays, lines, Req, Rpol, weights, grad, h2state='e',
+                 **alpha_kw):
     """sum_f grad[f] Tb_avg[f] of the oracle forward model."""
     _, _, avg = O.forward(gas, C, R, N, freqs, rays, lines, Req, Rpol, weights=weights,
-                          h2state=h2state)
+                          h2state=h2state, **alpha_kw)
     return float(np.dot(grad, avg))
 
 
@@ -85,10 +86,10 @@ def perturb(gas, C, direction, h):
 
 
 def directional_fd(gas, C, R, N, freqs, rays, lines, Req, Rpol, weights, grad, direction,
-                   h=1e-4, h2state='e'):
+                   h=1e-4, h2state='e', **alpha_kw):
     """Central difference of the loss along `direction` (step h)."""
     lp = loss_forward(perturb(gas, C, direction, h), C, R, N, freqs, rays, lines, Req, Rpol,
-                      weights, grad, h2state)
+                      weights, grad, h2state, **alpha_kw)
     lm = loss_forward(perturb(gas, C, direction, -h), C, R, N, freqs, rays, lines, Req, Rpol,
-                      weights, grad, h2state)
+                      weights, grad, h2state, **alpha_kw)
     return (lp - lm) / (2.0 * h)

@@ -43,6 +43,11 @@ HS_INV_LO = (1.640, 0.75, 0.852, 0.7756, 0.666, 1.0, 1.262, 0.3, 0.5296, 0.7964,
              0.667, 1.554, -0.0498, 0.9301)
 HS_INV_HI = (1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152,
              0.8873, 0.8994, 2.0 / 3.0, -0.0627, 0.9862)
+# nh3_dbs inversion coefficients (constituents/nh3/nh3_dbs.py:133-162): its
+# own f <= 30 GHz set, the f > 30 GHz set equal to nh3_hs's
+DBS_INV_LO = (1.6937, 0.6997, 0.7523, 0.8085, 1.0, 1.0, 1.3263, 0.1607, 0.6162, 0.8199,
+              0.0, 1.3832, -0.0139, 0.9619)
+DBS_INV_HI = HS_INV_HI
 # Rotational / nu2 (Gross) constants, constituents/nh3/nh3_hs.py:234-243,272-280
 HS_ROT = dict(eta=(0.8730, 2.0 / 3.0, 1.0), gnu=(0.2984, 0.75, 3.1789), con=2.4268)
 HS_V2 = dict(eta=(0.73, 0.5716, 1.0), width=(1.4, 0.68, 9.5), con=1.1206)
@@ -138,10 +143,12 @@ def _nh3_hs_block(freq, T, P, Ph2, Phe, Pnh3, cat, coefs):
     return np.where(a < 0.0, 1.0e-8, a)       # nh3_hs.py:311-312
 
 
-def alpha_nh3_hs(freq, T, P, Xh2, Xhe, Xnh3, cat):
+def alpha_nh3_hs(freq, T, P, Xh2, Xhe, Xnh3, cat, tables=(HS_INV_LO, HS_INV_HI)):
     """nh3_hs.alpha (nh3_hs.py:70-88): the <=30 GHz block then the >30 GHz
     block, concatenated in that order (output slot k holds the k-th value of
-    that concatenation, whatever the input order).  Returns [nL, nf]."""
+    that concatenation, whatever the input order).  Returns [nL, nf].
+    nh3_dbs (nh3_dbs.py:26-313) is the same computation with the
+    DBS_INV_* tables (its H2HeBroad column is not read by either)."""
     freq = np.asarray(freq, dtype=np.float64)
     T = np.atleast_1d(np.asarray(T, dtype=np.float64))
     P = np.atleast_1d(np.asarray(P, dtype=np.float64))
@@ -150,10 +157,15 @@ def alpha_nh3_hs(freq, T, P, Xh2, Xhe, Xnh3, cat):
     lo = freq[freq <= F_SPLIT]
     hi = freq[freq > F_SPLIT]
     if lo.size:
-        parts.append(_nh3_hs_block(lo, T, P, Ph2, Phe, Pnh3, cat, HS_INV_LO))
+        parts.append(_nh3_hs_block(lo, T, P, Ph2, Phe, Pnh3, cat, tables[0]))
     if hi.size:
-        parts.append(_nh3_hs_block(hi, T, P, Ph2, Phe, Pnh3, cat, HS_INV_HI))
+        parts.append(_nh3_hs_block(hi, T, P, Ph2, Phe, Pnh3, cat, tables[1]))
     return np.concatenate(parts, axis=1)
+
+
+def alpha_nh3_dbs(freq, T, P, Xh2, Xhe, Xnh3, cat):
+    """nh3_dbs.alpha (nh3_dbs.py:26-44, __alpha__ 47-313)."""
+    return alpha_nh3_hs(freq, T, P, Xh2, Xhe, Xnh3, cat, tables=(DBS_INV_LO, DBS_INV_HI))
 
 
 # ---------------------------------------------------------------- nh3_sjs
@@ -213,9 +225,11 @@ def alpha_nh3_sjs(freq, T, P, Xh2, Xhe, Xnh3, cat):
     return GEISA_COEF * (Pnh3 / T0)[:, None] * np.power(T0 / T, 1.5 + 2)[:, None] * out * Pscale[:, None]
 
 
-def alpha_nh3_hs_sjs(freq, T, P, Xh2, Xhe, Xnh3, cat_hs, cat_sjs):
+def alpha_nh3_hs_sjs(freq, T, P, Xh2, Xhe, Xnh3, cat_hs, cat_sjs, hs=None):
     """nh3_hs_sjs.alpha (nh3_hs_sjs.py:6-26): hs below 400 bar, sjs above
-    2000 bar, linear blend W=(P-400)/1600 in between."""
+    2000 bar, linear blend W=(P-400)/1600 in between.  nh3_dbs_sjs
+    (nh3_dbs_sjs.py:6-26) is the same blend of nh3_dbs (``hs``)."""
+    hs = hs or alpha_nh3_hs
     T = np.atleast_1d(np.asarray(T, dtype=np.float64))
     P = np.atleast_1d(np.asarray(P, dtype=np.float64))
     Xh2, Xhe, Xnh3 = (np.broadcast_to(np.asarray(x, dtype=np.float64), P.shape) for x in (Xh2, Xhe, Xnh3))
@@ -224,14 +238,134 @@ def alpha_nh3_hs_sjs(freq, T, P, Xh2, Xhe, Xnh3, cat_hs, cat_sjs):
     hi = P > 2000.0
     mid = ~(lo | hi)
     if lo.any():
-        out[lo] = alpha_nh3_hs(freq, T[lo], P[lo], Xh2[lo], Xhe[lo], Xnh3[lo], cat_hs)
+        out[lo] = hs(freq, T[lo], P[lo], Xh2[lo], Xhe[lo], Xnh3[lo], cat_hs)
     if hi.any():
         out[hi] = alpha_nh3_sjs(freq, T[hi], P[hi], Xh2[hi], Xhe[hi], Xnh3[hi], cat_sjs)
     if mid.any():
         a2 = alpha_nh3_sjs(freq, T[mid], P[mid], Xh2[mid], Xhe[mid], Xnh3[mid], cat_sjs)
-        a1 = alpha_nh3_hs(freq, T[mid], P[mid], Xh2[mid], Xhe[mid], Xnh3[mid], cat_hs)
+        a1 = hs(freq, T[mid], P[mid], Xh2[mid], Xhe[mid], Xnh3[mid], cat_hs)
         W = ((P[mid] - 400.0) / (2000.0 - 400.0))[:, None]
         out[mid] = W * a2 + (1.0 - W) * a1
+    return out
+
+
+def alpha_nh3_dbs_sjs(freq, T, P, Xh2, Xhe, Xnh3, cat_hs, cat_sjs):
+    """nh3_dbs_sjs.alpha (nh3_dbs_sjs.py:6-26)."""
+    return alpha_nh3_hs_sjs(freq, T, P, Xh2, Xhe, Xnh3, cat_hs, cat_sjs, hs=alpha_nh3_dbs)
+
+
+# ---------------------------------------------------------------- co_ddb
+# Hui, Armstrong & Wray (1978) rational approximation of the complex
+# probability function, coefficients of co_ddb.py:25-28
+VOIGT_A = (122.60793178, 214.38238869, 181.92853309, 93.15558046, 30.18014220,
+           5.91262621, 0.56418958, 0.0)
+VOIGT_B = (122.60793178, 352.73062511, 457.33447878, 348.70391772, 170.35400182,
+           53.99290691, 10.47985711, 1.0)
+
+
+def alpha_co_ddb(freq, T, P, Xh2, Xhe, Xco, cat, coshape='voigt'):
+    """co_ddb.alpha (co_ddb.py:22-99) for each layer.  ``coshape`` is
+    other_dict['coshape'] ('voigt' when absent); 'voigt', 'vvw' and 'diff'
+    sum unweighted shapes, anything else the pressure blend times the line
+    strengths.  Returns [nL, nf] cm^-1."""
+    freq = np.asarray(freq, dtype=np.float64)
+    T = np.atleast_1d(np.asarray(T, dtype=np.float64))
+    P = np.atleast_1d(np.asarray(P, dtype=np.float64))
+    Xh2, Xhe, Xco = (np.broadcast_to(np.asarray(x, dtype=np.float64), P.shape) for x in (Xh2, Xhe, Xco))
+    f0, I0, E = (np.asarray(cat[k], dtype=np.float64) for k in ('f0', 'I0', 'E'))
+    T0, hck = 296.0, HCK
+    out = np.empty((P.size, freq.size))
+    for i in range(P.size):
+        Ph2, Phe, Pco = P[i] * Xh2[i], P[i] * Xhe[i], P[i] * Xco[i]
+        gamma = pow(T0 / T[i], 0.7) * (1.960 * Ph2 + 1.200 * Phe + 6.000 * Pco)
+        g2 = gamma ** 2
+        ITG = I0 * np.exp(-((1.0 / T[i]) - (1.0 / T0)) * E * hck)
+        w = min(max((P[i] - 0.001) / (0.1 - 0.001), 0.0), 1.0)
+        for j, f in enumerate(freq):
+            f2 = f ** 2
+            sV = np.zeros(f0.size)
+            if P[i] <= 0.1 or coshape in ('voigt', 'diff'):
+                betaD = 4.3e-7 * np.sqrt(T[i] / 28.0) * f
+                xi = gamma / betaD + 1j * (f - f0) / betaD
+                num = np.zeros(f0.size, dtype=np.complex128)
+                den = np.zeros(f0.size, dtype=np.complex128)
+                for k in range(8):
+                    num += VOIGT_A[k] * xi ** k
+                    den += VOIGT_B[k] * xi ** k
+                sV = GHZ * (1.0 / (np.sqrt(np.pi) * betaD)) * (num / den).real
+            sW = np.zeros(f0.size)
+            if P[i] >= 0.001 or coshape in ('vvw', 'diff'):
+                num = gamma * f2 + gamma * (f0 ** 2 + g2)
+                den = (f2 - f0 ** 2 - g2) ** 2 + 4.0 * f2 * g2
+                sW = GHZ * 2.0 * (f / f0) ** 2 * num / (np.pi * den)
+            if coshape == 'voigt':
+                out[i, j] = np.sum(sV)
+            elif coshape == 'vvw':
+                out[i, j] = np.sum(sW)
+            elif coshape == 'diff':
+                out[i, j] = np.sum(sV - sW)
+            else:
+                out[i, j] = np.sum((w * sW + (1.0 - w) * sV) * ITG)
+        out[i] *= GEISA_COEF * (Pco / T0) * pow(T0 / T[i], 3.5)
+    return out
+
+
+# ---------------------------------------------------------------- clouds_idp
+_ICE_FR = (1.0E8, 3.0E8, 1.0E9, 2.0E9, 3.0E9, 5.0E9, 1.0E10, 3.0E10, 1.0E11)
+_ICE_EIMAG = (8.0E-3, 1.5E-3, 8.0E-4, 1.0E-3, 1.2E-3, 1.5E-3, 3.0E-3, 8.0E-3, 2.0E-2)
+
+
+def water_dielectric(f, T):
+    """clouds_idp.water (clouds_idp.py:75-101): complex e of water above
+    0 C (Debye), ice below (log-log table of Im e)."""
+    Tc = T - 273.0
+    fHz = f * 1.0E9
+    if Tc >= 0.0:
+        RelT = 1.1109E-10 - Tc * 3.824E-12 + Tc ** 2 * 6.938E-14 - Tc ** 3 * 5.096E-16
+        E0 = max(88.045 - 0.4147 * Tc + Tc ** 2 * 6.295E-4 + Tc ** 3 * 1.075E-5, 0.0)
+        EINF = 4.9
+        E1 = EINF + (E0 - EINF) / (1.0 + (fHz * RelT) ** 2)
+        E2 = max(fHz * RelT * (E0 - EINF) / (1.0 + (fHz * RelT) ** 2), 0.0)
+    else:
+        E1 = 3.17
+        LF = math.log10(fHz)
+        for j in range(len(_ICE_FR) - 1):
+            if _ICE_FR[j + 1] >= fHz:
+                break
+        LF0, LF1 = math.log10(_ICE_FR[j]), math.log10(_ICE_FR[j + 1])
+        DLF = (LF - LF0) / (LF1 - LF0)
+        X0, X1 = math.log10(_ICE_EIMAG[j]), math.log10(_ICE_EIMAG[j + 1])
+        E2 = 10.0 ** (X0 + DLF * (X1 - X0))
+    return E1 - E2 * 1j
+
+
+def _acloud(k, fraction, e):
+    K = (e - 1.0) / (e + 2.0)                  # clouds_idp.py:64-68
+    return 3.0 * k * fraction * (-K.imag)
+
+
+# (other_dict key, cloud column, density divisor, refractive index or None
+# for the water dielectric), in the order of clouds_idp.py:16-49
+CLOUD_KINDS = (('ice_p', 'H2O', 0.9, None), ('water_p', 'SOLN', 1.0, None),
+               ('nh4sh_p', 'NH4SH', 1.2, 1.7 - 0.005j), ('nh3ice_p', 'NH3', 1.6, 1.3 - 0.0001j),
+               ('h2sice_p', 'H2S', 1.5, 1.15 - 0.0001j), ('ch4', 'CH4', 1.0, 1.3 - 0.00001j))
+
+
+def alpha_clouds_idp(freq, T, cloud, Cl, other_dict):
+    """clouds_idp.alpha (clouds_idp.py:6-61) for each layer: T [nL], cloud
+    table [ncol, nL] indexed by Cl.  Returns [nL, nf] cm^-1."""
+    freq = np.asarray(freq, dtype=np.float64)
+    T = np.atleast_1d(np.asarray(T, dtype=np.float64))
+    out = np.zeros((T.size, freq.size))
+    for i in range(T.size):
+        for j, f in enumerate(freq):
+            a = 0.0
+            k = 2.0 * np.pi * f / GHZ
+            for key, col, div, n in CLOUD_KINDS:
+                if key in other_dict and other_dict[key] > 0.0:
+                    e = water_dielectric(f, T[i]) if n is None else n ** 2
+                    a += _acloud(k, cloud[Cl[col]][i] / div, e)
+            out[i, j] = max(a, 0.0)
     return out
 
 
@@ -340,15 +474,19 @@ GAS_FORMALISMS = ('h2', 'h2o', 'h2s', 'nh3', 'ph3')   # sorted, alpha.py:80
 
 
 def alpha_per_gas(freq, gas, C, lines, constituents=GAS_FORMALISMS, h2state='e',
-                  nh3='nh3_hs_sjs', chunk=16):
-    """Per-gas absorption [nL, nf, nC] in cm^-1 for the Jupiter formalisms
-    (alpha.py:194-216 get_alpha_from_calc, per layer; gases in sorted order).
+                  nh3='nh3_hs_sjs', chunk=16, cloud=None, Cl=None, other=None):
+    """Per-gas absorption [nL, nf, nC] in cm^-1 (alpha.py:194-216
+    get_alpha_from_calc, per layer; ``constituents`` in sorted order).
 
-    ``gas`` is the reference gas table [ncol, nL] indexed by the dict ``C``.
+    ``gas`` is the reference gas table [ncol, nL] indexed by the dict ``C``;
+    ``cloud`` / ``Cl`` the cloud table and its dict (clouds); ``other`` the
+    other_dict per constituent (co: 'coshape', clouds: particle switches).
     """
+    other = other or {}
     P = gas[C['P']]
     T = gas[C['T']]
-    X = {k: gas[C[k]] for k in ('H2', 'HE', 'CH4', 'NH3', 'H2O', 'H2S', 'PH3')}
+    X = {k: (gas[C[k]] if k in C else np.zeros_like(P))
+         for k in ('H2', 'HE', 'CH4', 'NH3', 'H2O', 'H2S', 'PH3', 'CO')}
     nL = P.size
     out = np.zeros((nL, len(freq), len(constituents)))
     for s in range(0, nL, chunk):
@@ -370,8 +508,17 @@ def alpha_per_gas(freq, gas, C, lines, constituents=GAS_FORMALISMS, h2state='e',
                     a = alpha_nh3_hs(freq, *args, X['NH3'][sl], lines['ammonia'])
                 elif nh3 == 'nh3_sjs':
                     a = alpha_nh3_sjs(freq, *args, X['NH3'][sl], lines['nh3'])
+                elif nh3 == 'nh3_dbs':
+                    a = alpha_nh3_dbs(freq, *args, X['NH3'][sl], lines['ammonia'])
+                elif nh3 == 'nh3_dbs_sjs':
+                    a = alpha_nh3_dbs_sjs(freq, *args, X['NH3'][sl], lines['ammonia'], lines['nh3'])
                 else:
                     raise ValueError(nh3)
+            elif c == 'co':
+                a = alpha_co_ddb(freq, *args, X['CO'][sl], lines['co'],
+                                 coshape=other.get('co', {}).get('coshape', 'voigt'))
+            elif c == 'clouds':
+                a = alpha_clouds_idp(freq, T[sl], cloud[:, sl], Cl, other.get('clouds', {}))
             else:
                 raise ValueError(c)
             out[sl, :, ci] = a
@@ -622,11 +769,13 @@ def brightness(ds, layer4ds, alpha_layers, T_layers, disc=False):
 
 
 def forward(gas, C, R, N, freqs, rays, lines, Req, Rpol, orientation=(0.0, 0.0),
-            disc=False, h2state='e', scale=False, weights=None):
+            disc=False, h2state='e', scale=False, weights=None, **alpha_kw):
     """alpha for every layer, then one Brightness.single per ray.
-    Returns (Tb [nb, nf], layers [nf, nL], disc average or None)."""
-    per = alpha_per_gas(freqs, gas, C, lines, h2state=h2state)
-    layers, _ = total_alpha(per, layer_scale(scale, gas.shape[1]))
+    Returns (Tb [nb, nf], layers [nf, nL], disc average or None).
+    ``alpha_kw`` goes to alpha_per_gas (constituents, nh3, cloud, Cl, other)."""
+    per = alpha_per_gas(freqs, gas, C, lines, h2state=h2state, **alpha_kw)
+    cons = alpha_kw.get('constituents', GAS_FORMALISMS)
+    layers, _ = total_alpha(per, layer_scale(scale, gas.shape[1], cons))
     T = gas[C['T']]
     tbs = []
     for b in rays:

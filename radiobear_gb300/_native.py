@@ -17,10 +17,17 @@ from . import build as _build
 LIB_PATH = _build.LIB
 
 RB_OK = 0
-FAM = dict(NH3_INV=0, NH3_ROT=1, NH3_V2=2, NH3_SJS=3, H2O=4, H2S=5, PH3=6)
-NH3_MODE = dict(off=0, nh3_hs=1, nh3_sjs=2, nh3_hs_sjs=3)
-GASES = ('h2', 'h2o', 'h2s', 'nh3', 'ph3')        # RB_GAS_* order
-X_ROWS = ('H2', 'HE', 'CH4', 'NH3', 'H2O', 'H2S', 'PH3')   # RB_X_* order
+FAM = dict(NH3_INV=0, NH3_ROT=1, NH3_V2=2, NH3_SJS=3, H2O=4, H2S=5, PH3=6, CO=7)
+NH3_MODE = dict(off=0, nh3_hs=1, nh3_sjs=2, nh3_hs_sjs=3, nh3_dbs=4, nh3_dbs_sjs=5)
+GASES = ('h2', 'h2o', 'h2s', 'nh3', 'ph3', 'co', 'clouds')        # RB_GAS_* order
+# RB_X_* order: gas mole fractions (gas table columns), then cloud densities
+# (cloud table columns, prefixed 'cl:')
+X_ROWS = ('H2', 'HE', 'CH4', 'NH3', 'H2O', 'H2S', 'PH3', 'CO',
+          'cl:H2O', 'cl:SOLN', 'cl:NH4SH', 'cl:NH3', 'cl:H2S', 'cl:CH4')
+COSHAPE = dict(voigt=0, vvw=1, diff=2)              # anything else: 3 (blended, 'std')
+# clouds_idp other_dict keys -> RB_CLOUD_* bits (clouds_idp.py:16-49 tests
+# 'ice_p', 'water_p', 'nh4sh_p', 'nh3ice_p', 'h2sice_p' and 'ch4')
+CLOUD_BITS = dict(ice_p=1, water_p=2, nh4sh_p=4, nh3ice_p=8, h2sice_p=16, ch4=32)
 GTYPE = dict(ellipse=0, sphere=1, circle=1)
 LIMB = dict(shape=0, sec=1)
 
@@ -33,13 +40,15 @@ FAMILY_COLUMNS = {
     'H2O': ('f_o', 'I_o', 'E_o', 'w_s', 'x_s', 'w_h2', 'w_he', 'x_h2', 'x_he', 'SR'),
     'H2S': ('f0', 'I0', 'E', 'GH2S'),
     'PH3': ('f0', 'I0', 'E', 'WgtI0', 'WgtFGB', 'WgtSB'),
+    'CO': ('f0', 'I0', 'E'),
 }
 
 EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set_lines',
            'rb_set_formalisms', 'rb_alpha', 'rb_raypath', 'rb_brightness', 'rb_forward',
            'rb_forward_device', 'rb_last_launch_count', 'rb_set_profiling', 'rb_phase_times',
            'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
-           'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device')
+           'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device',
+           'rb_set_co_clouds')
 
 _lib = None
 _lock = threading.Lock()
@@ -71,6 +80,7 @@ def load_library(path=None):
         lib.rb_destroy.argtypes = [_vp]
         lib.rb_set_lines.argtypes = [_vp, c_int, c_int, c_int, _d]
         lib.rb_set_formalisms.argtypes = [_vp, c_int, c_int, c_int, c_int, c_int, c_int]
+        lib.rb_set_co_clouds.argtypes = [_vp, c_int, c_int, c_int, c_int]
         lib.rb_alpha.argtypes = [_vp, c_int, _d, _d, _d, c_int, _d, _d, c_int, _d, _d]
         lib.rb_raypath.argtypes = [_vp, c_int, _d, _d, c_double, c_double, c_double, c_double,
                                    c_int, c_int, c_int, _d, c_int, _i, _d, _i, _d, _d, _i]
@@ -167,9 +177,21 @@ class Engine:
                                                     int(h2s), int(ph3), ord(h2state)),
                'rb_set_formalisms')
 
+    def set_co_clouds(self, co=False, coshape='voigt', clouds=None):
+        """co_ddb on/off with its line shape (other_dict['coshape']), and
+        clouds_idp: None (off) or its other_dict (particle switches)."""
+        mask = 0
+        if clouds is not None:
+            for k, bit in CLOUD_BITS.items():
+                if k in clouds and clouds[k] > 0.0:
+                    mask |= bit
+        _check(self.lib, self.lib.rb_set_co_clouds(self._h, int(bool(co)), COSHAPE.get(coshape, 3),
+                                                   int(clouds is not None), mask),
+               'rb_set_co_clouds')
+
     # ------------------------------------------------------------ compute
     def alpha(self, P, T, X, freqs, scale=None, units_db=False, per_gas=False, layers=True):
-        """Absorption: returns (layers [nf, nL] or None, gas [nL, nf, 5] or None)."""
+        """Absorption: returns (layers [nf, nL] or None, gas [nL, nf, RB_NGAS] or None)."""
         P, T, X, f = _f64(P), _f64(T), _f64(X), _f64(freqs)
         nL, nf = P.size, f.size
         sc = None if scale is None else _f64(scale)
@@ -366,12 +388,16 @@ class Engine:
         return out
 
 
-def x_matrix(gas, C):
-    """[RB_NX, nL] abundance rows from a reference gas table and index dict
-    (missing constituents are zero)."""
+def x_matrix(gas, C, cloud=None, Cl=None):
+    """[RB_NX, nL] composition rows from a reference gas table and index
+    dict, plus the cloud table and its dict when given (missing columns are
+    zero)."""
     nL = gas.shape[1]
     X = np.zeros((len(X_ROWS), nL))
     for i, k in enumerate(X_ROWS):
-        if k in C:
+        if k.startswith('cl:'):
+            if cloud is not None and Cl is not None and k[3:] in Cl:
+                X[i] = cloud[Cl[k[3:]]]
+        elif k in C:
             X[i] = gas[C[k]]
     return X

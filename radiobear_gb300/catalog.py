@@ -9,6 +9,7 @@ A catalogue set is a dict with any of the keys
 ``h2s``      ``constituents/h2s/h2s.npz`` (f0 I0 E GH2S)
 ``ph3``      ``constituents/ph3/ph3jh.npz`` (f0 I0 E)
 ``ph3wgt``   ``constituents/ph3/PH3WGT.npz`` (WgtI0 WgtFGB WgtSB)
+``co``       ``constituents/co/co.npz`` (f0 I0 E)
 
 Truncation follows the reference loaders: strength truncation keeps lines
 with intensity > threshold, frequency truncation keeps f0 < threshold
@@ -21,7 +22,7 @@ import os
 import numpy as np
 
 _NPZ = dict(ammonia=('nh3', 'ammonia.npz'), nh3=('nh3', 'nh3.npz'), h2s=('h2s', 'h2s.npz'),
-            ph3=('ph3', 'ph3jh.npz'), ph3wgt=('ph3', 'PH3WGT.npz'))
+            ph3=('ph3', 'ph3jh.npz'), ph3wgt=('ph3', 'PH3WGT.npz'), co=('co', 'co.npz'))
 
 
 def load_reference_catalogues(constituents_dir, truncate_strength=None, truncate_freq=None):
@@ -83,11 +84,13 @@ def family_tables(lines):
             w = dict(WgtI0=np.ones(n), WgtFGB=np.ones(n), WgtSB=np.ones(n))
         p.update(w)
         fam['PH3'] = p
+    if lines.get('co') is not None:
+        fam['CO'] = {k: lines['co'][k] for k in ('f0', 'I0', 'E')}
     return fam
 
 
 def upload(engine, lines):
     """Upload every family present in ``lines``; absent families are cleared."""
     fam = family_tables(lines)
-    for name in ('NH3_INV', 'NH3_ROT', 'NH3_V2', 'NH3_SJS', 'H2O', 'H2S', 'PH3'):
+    for name in ('NH3_INV', 'NH3_ROT', 'NH3_V2', 'NH3_SJS', 'H2O', 'H2S', 'PH3', 'CO'):
         engine.set_lines(name, fam.get(name))

@@ -336,11 +336,15 @@ __device__ __forceinline__ void zero_tan(FamTan& o) {
   o.dcE = 0.f;
 }
 
-// Inversion coefficient sets (nh3_hs.py:139-168), as in the prep kernel.
-__device__ constexpr float INV_SET_D[2][13] = {
-    {1.640, 0.75, 0.852, 0.7756, 0.666, 1.0, 1.262, 0.3, 0.5296, 0.7964, 0.667, 1.554, -0.0498},
-    {1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152, 0.8873, 0.8994, 0.66666667,
-     -0.0627}};
+// Inversion coefficient tables [inv_table][set] (nh3_hs.py:139-168,
+// nh3_dbs.py:133-162), as in the prep kernel.
+__device__ constexpr float INV_SET_D[2][2][13] = {
+    {{1.640, 0.75, 0.852, 0.7756, 0.666, 1.0, 1.262, 0.3, 0.5296, 0.7964, 0.667, 1.554, -0.0498},
+     {1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152, 0.8873, 0.8994, 0.66666667,
+      -0.0627}},
+    {{1.6937, 0.6997, 0.7523, 0.8085, 1.0, 1.0, 1.3263, 0.1607, 0.6162, 0.8199, 0.0, 1.3832, -0.0139},
+     {1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152, 0.8873, 0.8994, 0.66666667,
+      -0.0627}}};
 
 // Derivatives of the layer coefficients, eight threads per layer (the parts
 // of rb_layer_prep_kernel: 0 shared, 1 inversion, 2 rotational, 3 nu2,
@@ -395,7 +399,7 @@ __global__ void __launch_bounds__(256) rb_layer_tan_kernel(TanArgs a) {
     }
     case 1: {
       for (int s = 0; s < 2; ++s) {
-        const float* c = INV_SET_D[s];
+        const float* c = INV_SET_D[a.inv_table][s];
         store_tan(F, s, 0, c[0] * (Ph2 * dpw(lTdiv, c[3])) + c[1] * (Phe * dpw(lTdiv, c[4])));
         store_tan(F, s, 1, c[2] * (Pnh3 * dpw(l295, c[5])));
         store_tan(F, s, 3, c[6] * (Ph2 * dpw(lTdiv, c[9])) + c[7] * (Phe * dpw(lTdiv, c[10])));
@@ -878,11 +882,11 @@ __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
     }
     if (nh3) {
       double hs = 0.0, dhs[NTH] = {0, 0, 0, 0, 0}, sj = 0.0, dsj[NTH] = {0, 0, 0, 0, 0};
-      const double INVC[2] = {0.9301, 0.9862};
+      const double INVC[2][2] = {{0.9301, 0.9862}, {0.9619, 0.9862}};   // Con, per table and set
       if (lp.use_hs) {
-        hs = Fhd * (pref(FAM_NH3_INV) * INVC[set] * fv[FAM_NH3_INV] +
+        hs = Fhd * (pref(FAM_NH3_INV) * INVC[a.cfg.inv_table][set] * fv[FAM_NH3_INV] +
                     pref(FAM_NH3_ROT) * fv[FAM_NH3_ROT] + pref(FAM_NH3_V2) * fv[FAM_NH3_V2]);
-        add_fam(FAM_NH3_INV, INVC[set], fv[FAM_NH3_INV], fd[FAM_NH3_INV], dhs);
+        add_fam(FAM_NH3_INV, INVC[a.cfg.inv_table][set], fv[FAM_NH3_INV], fd[FAM_NH3_INV], dhs);
         add_fam(FAM_NH3_ROT, 1.0, fv[FAM_NH3_ROT], fd[FAM_NH3_ROT], dhs);
         add_fam(FAM_NH3_V2, 1.0, fv[FAM_NH3_V2], fd[FAM_NH3_V2], dhs);
         for (int q = 0; q < NTH; ++q) dhs[q] *= Fhd;
@@ -927,12 +931,17 @@ __global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
 // dT = sum of tiles + source term (summed over frequencies); dP; dln X
 // for NH3, H2O, H2S.
 __global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const double* part,
-                                        const double* gsrc, double* dT, double* dP, double* dlnX) {
+                                        const double* gsrc, const double* gextra, double* dT,
+                                        double* dP, double* dlnX) {
   const int L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nL) return;
   double s[NTH] = {0, 0, 0, 0, 0};
   for (int t = 0; t < ntile; ++t)
     for (int q = 0; q < NTH; ++q) s[q] += part[((size_t)L * ntile + t) * NTH + q];
+  if (gextra) {
+    s[TH_T] += gextra[2 * L];
+    s[TH_P] += gextra[2 * L + 1];
+  }
   dT[L] = s[TH_T] + gsrc[L];
   dP[L] = s[TH_P];
   dlnX[L] = s[TH_XNH3];
@@ -941,8 +950,11 @@ __global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const double*
 }
 
 // ------------------------------------------------------------------ launch
-cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, float* galpha,
-                           double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st) {
+cudaError_t launch_extra_vjp(const ExtraArgs& ea, cudaStream_t st);
+
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
+                           const ExtraArgs* ea, float* galpha, double* gsrc, double* dT, double* dP,
+                           double* dlnX, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(float) * (size_t)ta.nL * ta.nf, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * (size_t)ta.nL, st);
   if (e != cudaSuccess) return e;
@@ -955,8 +967,12 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   rb_layer_tan_kernel<<<(tn.nL * 8 + 255) / 256, 256, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
   rb_alpha_jvp_kernel<<<grid, 256, 0, st>>>(jv);
-  rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(jv.nL, jv.nf, grid.y, jv.part, gsrc, dT,
-                                                                dP, dlnX);
+  if (ea) {
+    cudaError_t x = launch_extra_vjp(*ea, st);
+    if (x != cudaSuccess) return x;
+  }
+  rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(
+      jv.nL, jv.nf, grid.y, jv.part, gsrc, ea ? ea->grad : nullptr, dT, dP, dlnX);
   return cudaGetLastError();
 }
 

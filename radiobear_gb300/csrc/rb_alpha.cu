@@ -111,18 +111,24 @@ constexpr float GHZ_INVCM = 29.9792458f;
 constexpr float TWO_OVER_PI = 0.63661977236758134f;
 constexpr float FOUR_OVER_PI = 1.2732395447351627f;
 constexpr float DB_PER_INVCM = 434294.5f;
-__device__ constexpr float INV_CON[2] = {0.9301f, 0.9862f};
 constexpr double LOG2E = 1.4426950408889634;
 constexpr float HS_COEF = (float)(1.0E6 * 6.02297E23 / 8.31432E7);   // nh3_hs.py:49-55
 
-// Inversion coefficient sets (nh3_hs.py:139-168): gnu_H2, gnu_He, gnu_NH3,
+// Inversion coefficient tables [inv_table][set]: gnu_H2, gnu_He, gnu_NH3,
 // GAMMA_H2, GAMMA_He, GAMMA_NH3, zeta_H2, zeta_He, zeta_NH3, Z_H2, Z_He,
-// Z_NH3, d
-__device__ constexpr float INV_SET[2][13] = {
-    {1.640f, 0.75f, 0.852f, 0.7756f, 0.666f, 1.0f, 1.262f, 0.3f, 0.5296f, 0.7964f, 0.667f, 1.554f,
-     -0.0498f},
-    {1.7465f, 0.9779f, 0.7298f, 0.8202f, 1.0f, 1.0f, 1.2163f, 0.0291f, 0.5152f, 0.8873f, 0.8994f,
-     0.66666667f, -0.0627f}};
+// Z_NH3, d; set 0 for f <= 30 GHz, set 1 above.  Table 0 nh3_hs
+// (nh3_hs.py:139-168), table 1 nh3_dbs (nh3_dbs.py:133-162: its own set 0,
+// set 1 equal to nh3_hs's).  INV_CON holds each set's Con.
+__device__ constexpr float INV_SET[2][2][13] = {
+    {{1.640f, 0.75f, 0.852f, 0.7756f, 0.666f, 1.0f, 1.262f, 0.3f, 0.5296f, 0.7964f, 0.667f, 1.554f,
+      -0.0498f},
+     {1.7465f, 0.9779f, 0.7298f, 0.8202f, 1.0f, 1.0f, 1.2163f, 0.0291f, 0.5152f, 0.8873f, 0.8994f,
+      0.66666667f, -0.0627f}},
+    {{1.6937f, 0.6997f, 0.7523f, 0.8085f, 1.0f, 1.0f, 1.3263f, 0.1607f, 0.6162f, 0.8199f, 0.0f,
+      1.3832f, -0.0139f},
+     {1.7465f, 0.9779f, 0.7298f, 0.8202f, 1.0f, 1.0f, 1.2163f, 0.0291f, 0.5152f, 0.8873f, 0.8994f,
+      0.66666667f, -0.0627f}}};
+__device__ constexpr float INV_CON[2][2] = {{0.9301f, 0.9862f}, {0.9619f, 0.9862f}};
 
 __device__ __forceinline__ float pw(float lg2x, float e) { return exp2f(e * lg2x); }
 
@@ -229,9 +235,9 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
                  (Ph2 * pw(lth, 3.12f) + 1.382f * Phe * pw(lth, 2.24f) + 9.322f * Pch4 * pw(lth, 3.34f));
       return;
     }
-    case 1: {  // NH3 inversion (nh3_hs.py:137-229)
+    case 1: {  // NH3 inversion (nh3_hs.py:137-229, nh3_dbs.py:131-213)
       for (int s = 0; s < 2; ++s) {
-        const float* c = INV_SET[s];
+        const float* c = INV_SET[a.cfg.inv_table][s];
         F.c[s][0] = c[0] * Ph2 * pw(lTdiv, c[3]) + c[1] * Phe * pw(lTdiv, c[4]);
         F.c[s][1] = c[2] * Pnh3 * pw(l295, c[5]);
         F.c[s][3] = c[6] * Ph2 * pw(lTdiv, c[9]) + c[7] * Phe * pw(lTdiv, c[10]);
@@ -349,10 +355,12 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
 }
 
 // Assemble one slot: per-gas absorption (T = float or double), scaled.
+// co / cl are the co_ddb and clouds_idp absorption in cm^-1 (0 when off).
 template <typename T>
 __device__ __forceinline__ void assemble(const LayerParams& lp, const AlphaConfig& cfg, T F, T Fhs,
                                          int set, float inv, float rot, float v2, float sjs,
-                                         float h2o, float base_h2o, float h2s, float ph3, T* g) {
+                                         float h2o, float base_h2o, float h2s, float ph3, double co,
+                                         double cl, T* g) {
   const T U = cfg.units_db ? (T)434294.5 : (T)1;
   for (int k = 0; k < NGAS; ++k) g[k] = (T)0;
   auto sc = [](float m, int e, float v) -> T {
@@ -369,7 +377,7 @@ __device__ __forceinline__ void assemble(const LayerParams& lp, const AlphaConfi
   if (cfg.nh3_mode != NH3_OFF) {
     T hs = (T)0, sj = (T)0;
     if (lp.use_hs) {
-      hs = Fhs * (sc(lp.fam[FAM_NH3_INV].fm * INV_CON[set], lp.fam[FAM_NH3_INV].fe, inv) +
+      hs = Fhs * (sc(lp.fam[FAM_NH3_INV].fm * INV_CON[cfg.inv_table][set], lp.fam[FAM_NH3_INV].fe, inv) +
                   sc(lp.fam[FAM_NH3_ROT].fm, lp.fam[FAM_NH3_ROT].fe, rot) +
                   sc(lp.fam[FAM_NH3_V2].fm, lp.fam[FAM_NH3_V2].fe, v2));
       hs *= U;
@@ -382,6 +390,8 @@ __device__ __forceinline__ void assemble(const LayerParams& lp, const AlphaConfi
     else
       g[GAS_NH3] = lp.use_hs ? hs : sj;
   }
+  if (cfg.use_co) g[GAS_CO] = (T)co * U;
+  if (cfg.use_clouds) g[GAS_CLOUDS] = (T)cl * U;
   for (int k = 0; k < NGAS; ++k) g[k] *= (T)lp.scale[k];
 }
 
@@ -929,17 +939,23 @@ __device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int til
   }
   if (a.cfg.use_h2s) h2s = fam_sum(a, r, FAM_H2S);
   if (a.cfg.use_ph3) ph3 = fam_sum(a, r, FAM_PH3);
+  double co = 0.0, cl = 0.0;
+  if (a.extra) {
+    co = a.extra[(size_t)L * a.nf + j];
+    cl = a.extra[((size_t)a.nL + L) * a.nf + j];
+  }
   const float2 Fs = a.sp.F[s], Hs = a.sp.Fhs[s];
   float g32[NGAS];
   assemble<float>(lp, a.cfg, Fs.x + Fs.y, Hs.x + Hs.y, set, inv, rot, v2, sjs, h2o, base, h2s, ph3,
-                  g32);
+                  co, cl, g32);
   float tot = 0.f;
   for (int k = 0; k < NGAS; ++k) tot += g32[k];
   a.alpha32[(size_t)L * a.nf + j] = a.cfg.units_db ? tot / DB_PER_INVCM : tot;
   if (a.layers64 || a.gas64) {
     const double f = a.freqs[j], fh = a.freqs_hs[j];
     double g64[NGAS];
-    assemble<double>(lp, a.cfg, f * f, fh * fh, set, inv, rot, v2, sjs, h2o, base, h2s, ph3, g64);
+    assemble<double>(lp, a.cfg, f * f, fh * fh, set, inv, rot, v2, sjs, h2o, base, h2s, ph3, co, cl,
+                     g64);
     double t64 = 0.0;
     for (int k = 0; k < NGAS; ++k) {
       if (a.gas64) a.gas64[((size_t)L * a.nf + j) * NGAS + k] = g64[k];

@@ -120,7 +120,11 @@ struct rb_handle {
   cudaStream_t st = nullptr, side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   FamilyStore fam[rb::NFAM];
-  rb::AlphaConfig cfg{rb::NH3_HS_SJS, 1, 1, 1, 1, 'e', 0};
+  rb::AlphaConfig cfg{rb::NH3_HS_SJS, 1, 1, 1, 1, 'e', 0, 0, 0, rb::CO_VOIGT, 0, 0};
+  // co_ddb lines (co.npz: f0 GHz, I0, E cm^-1), float64
+  int nco = 0;
+  DBuf d_co_f0, d_co_I0, d_co_E;
+  DBuf d_extra, d_xgrad;   // [2][nL][nf] co / cloud absorption; [nL][2] their adjoint
   // frequency plan
   std::vector<double> plan_f;
   int plan_M = 0, plan_W = 0, plan_spt = 0, plan_ntile = 0, plan_nslot = 0, plan_ntmpl = 0;
@@ -153,8 +157,10 @@ void set_last_error(const char* msg) { g_err = msg; }
 namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
 cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st);
+cudaError_t launch_extra(const ExtraArgs& a, cudaStream_t st);
 int alpha_lines_occupancy(int M, int W);
-cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv, float* galpha,
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
+                           const ExtraArgs* ea, float* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st);
 int adjoint_tiles(int nf);
 int adjoint_ft(int nf);
@@ -441,6 +447,24 @@ int validate_atm(int nL, const double* P, const double* T, const double* X) {
   return RB_OK;
 }
 
+// Arguments of the co_ddb / clouds_idp kernels (device inputs, d_extra
+// already sized for nL layers).
+void extra_args(rb_handle* h, rb::ExtraArgs& ea, int nL, const double* dP, const double* dT,
+                const double* dX) {
+  ea.nL = nL;
+  ea.nf = (int)h->plan_f.size();
+  ea.P = dP;
+  ea.T = dT;
+  ea.X = dX;
+  ea.freqs = h->d_f.as<double>();
+  ea.nco = h->nco;
+  ea.co_f0 = h->d_co_f0.as<double>();
+  ea.co_I0 = h->d_co_I0.as<double>();
+  ea.co_E = h->d_co_E.as<double>();
+  ea.cfg = h->cfg;
+  ea.out = h->d_extra.as<double>();
+}
+
 int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
                   const double* dX, const double* dscale, int units_db, double* d_layers64,
                   double* d_gas64) {
@@ -504,12 +528,22 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   aa.alpha32 = h->d_a32.as<float>();
   aa.layers64 = d_layers64;
   aa.gas64 = d_gas64;
+  aa.extra = nullptr;
+  rb::ExtraArgs ea{};
+  const bool extra = h->cfg.use_co || h->cfg.use_clouds;
+  if (extra) {
+    if (h->cfg.use_co && h->nco == 0) return fail(RB_ESTATE, "co_ddb selected but no CO lines uploaded");
+    RB_CUDA(h->d_extra.ensure(sizeof(double) * 2 * (size_t)nL * nf));
+    extra_args(h, ea, nL, dP, dT, dX);
+    aa.extra = ea.out;
+  }
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[0], st));
   RB_CUDA(rb::launch_prep(pa, st));
+  if (extra) RB_CUDA(rb::launch_extra(ea, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[1], st));
   RB_CUDA(rb::launch_alpha_lines(aa, h->plan_grid, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[2], st));
-  h->launches += 2;
+  h->launches += extra ? 3 : 2;
   return RB_OK;
 }
 
@@ -628,7 +662,8 @@ int rb_destroy(rb_handle* h) {
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
                   &h->d_done, &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,
-                  &h->d_adjS, &h->d_voff})
+                  &h->d_adjS, &h->d_voff, &h->d_co_f0, &h->d_co_I0, &h->d_co_E, &h->d_extra,
+                  &h->d_xgrad})
     b->release();
   for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
@@ -646,8 +681,27 @@ int rb_destroy(rb_handle* h) {
   return RB_OK;
 }
 
+// co_ddb lines: f0, I0, E kept in float64 (no line-sum kernel involved).
+static int set_co_lines(rb_handle* h, int n, int ncols, const double* cols) {
+  if (ncols != 3) return fail(RB_EINVAL, "family %d takes 3 columns, got %d", RB_FAM_CO, ncols);
+  if (n < 0 || (n > 0 && !cols)) return fail(RB_EINVAL, "bad line count / pointer");
+  if (!finite_all(cols, (size_t)n * 3)) return fail(RB_EINVAL, "line columns not finite");
+  for (int i = 0; i < n; ++i)
+    if (!(cols[i] > 0.0)) return fail(RB_EINVAL, "line %d: centre must be > 0", i);
+  RB_CUDA(cudaSetDevice(h->device));
+  h->nco = 0;
+  cudaStream_t st = h->st;
+  RB_CUDA(upload(h->d_co_f0, cols, n, st));
+  RB_CUDA(upload(h->d_co_I0, cols + n, n, st));
+  RB_CUDA(upload(h->d_co_E, cols + 2 * (size_t)n, n, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  h->nco = n;
+  return RB_OK;
+}
+
 int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols) {
   if (!h) return fail(RB_EINVAL, "null handle");
+  if (family == RB_FAM_CO) return set_co_lines(h, n, ncols, cols);
   if (family < 0 || family >= rb::NFAM) return fail(RB_EINVAL, "unknown family %d", family);
   if (ncols != family_ncols(family))
     return fail(RB_EINVAL, "family %d takes %d columns, got %d", family, family_ncols(family), ncols);
@@ -764,14 +818,29 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
 int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2s, int use_ph3,
                       int h2state) {
   if (!h) return fail(RB_EINVAL, "null handle");
-  if (nh3 < RB_NH3_OFF || nh3 > RB_NH3_HS_SJS) return fail(RB_EINVAL, "bad nh3 formalism %d", nh3);
+  if (nh3 < RB_NH3_OFF || nh3 > RB_NH3_DBS_SJS) return fail(RB_EINVAL, "bad nh3 formalism %d", nh3);
   if (h2state != 'e' && h2state != 'n') return fail(RB_EINVAL, "h2state must be 'e' or 'n'");
-  h->cfg.nh3_mode = nh3;
+  // nh3_dbs / nh3_dbs_sjs: the nh3_hs / nh3_hs_sjs structure with the
+  // nh3_dbs inversion coefficients (nh3_dbs_sjs.py:6-26 blends nh3_dbs
+  // with nh3_sjs exactly as nh3_hs_sjs blends nh3_hs)
+  h->cfg.inv_table = (nh3 == RB_NH3_DBS || nh3 == RB_NH3_DBS_SJS) ? 1 : 0;
+  h->cfg.nh3_mode = nh3 == RB_NH3_DBS ? rb::NH3_HS : (nh3 == RB_NH3_DBS_SJS ? rb::NH3_HS_SJS : nh3);
   h->cfg.use_h2 = use_h2 != 0;
   h->cfg.use_h2o = use_h2o != 0;
   h->cfg.use_h2s = use_h2s != 0;
   h->cfg.use_ph3 = use_ph3 != 0;
   h->cfg.h2state = h2state;
+  return RB_OK;
+}
+
+int rb_set_co_clouds(rb_handle* h, int co, int coshape, int clouds, int cloud_mask) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (coshape < RB_COSHAPE_VOIGT || coshape > RB_COSHAPE_STD) return fail(RB_EINVAL, "bad coshape %d", coshape);
+  if (cloud_mask & ~63) return fail(RB_EINVAL, "bad cloud mask %d", cloud_mask);
+  h->cfg.use_co = co != 0;
+  h->cfg.coshape = coshape;
+  h->cfg.use_clouds = clouds != 0;
+  h->cfg.cloud_mask = cloud_mask;
   return RB_OK;
 }
 
@@ -1150,6 +1219,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   tn.X = X;
   tn.nh3_mode = h->cfg.nh3_mode;
   tn.h2state = h->cfg.h2state;
+  tn.inv_table = h->cfg.inv_table;
   tn.out = h->d_lt.as<rb::LayerTan>();
   rb::JvpArgs jv{};
   jv.nL = nL;
@@ -1164,9 +1234,18 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   jv.cfg.units_db = 0;
   jv.galpha = h->d_ga.as<float>();
   jv.part = h->d_jpart.as<double>();
-  RB_CUDA(rb::launch_adjoint(ta, tn, jv, h->d_ga.as<float>(), h->d_gs.as<double>(), dT, dP, dlnX,
-                             st));
-  h->launches = launches + 6;
+  rb::ExtraArgs ea{};
+  const bool extra = h->cfg.use_co || h->cfg.use_clouds;
+  if (extra) {
+    RB_CUDA(h->d_xgrad.ensure(sizeof(double) * 2 * (size_t)nL));
+    extra_args(h, ea, nL, P, T, X);
+    ea.galpha = h->d_ga.as<float>();
+    ea.scale = scale;
+    ea.grad = h->d_xgrad.as<double>();
+  }
+  RB_CUDA(rb::launch_adjoint(ta, tn, jv, extra ? &ea : nullptr, h->d_ga.as<float>(),
+                             h->d_gs.as<double>(), dT, dP, dlnX, st));
+  h->launches = launches + (extra ? 7 : 6);
   return RB_OK;
 }
 

@@ -71,6 +71,28 @@ struct AlphaArgs {
   float* alpha32;           // [nL][nf] total, cm^-1 (brightness input)
   double* layers64;         // [nf][nL] total, units of cfg (or null)
   double* gas64;            // [nL][nf][NGAS] per gas, units of cfg (or null)
+  const double* extra;      // [2][nL][nf] co_ddb, clouds_idp in cm^-1 (or null)
+};
+
+// Closed-form absorbers co_ddb (constituents/co/co_ddb.py) and clouds_idp
+// (constituents/clouds/clouds_idp.py), float64, one thread per (layer,
+// frequency).  The forward writes out; the adjoint contracts d loss / d
+// alpha with their temperature and pressure derivatives.
+struct ExtraArgs {
+  int nL, nf;
+  const double* P;          // [nL] bar
+  const double* T;          // [nL] K
+  const double* X;          // [NX][nL]
+  const double* freqs;      // [nf] GHz
+  int nco;                  // co.npz lines: f0 (GHz), I0, E (cm^-1)
+  const double* co_f0;
+  const double* co_I0;
+  const double* co_E;
+  AlphaConfig cfg;
+  double* out;              // [2][nL][nf] cm^-1
+  const float* galpha;      // [nL][nf] d loss / d alpha (cm^-1)
+  const double* scale;      // [nL][NGAS] or null
+  double* grad;             // [nL][2] d loss / dT, d loss / dP
 };
 
 // Batches of atmospheres: variant v owns global layers [var_off[v],
@@ -150,6 +172,7 @@ struct TanArgs {
   const double* T;
   const double* X;
   int nh3_mode, h2state;
+  int inv_table;          // AlphaConfig::inv_table
   LayerTan* out;
 };
 

@@ -30,15 +30,34 @@ enum Family : int {
   NFAM = 7
 };
 
-// Gas slots of the per-gas output, the reference's sorted constituent order
-// (alpha.py:80): h2, h2o, h2s, nh3, ph3.
-enum Gas : int { GAS_H2 = 0, GAS_H2O = 1, GAS_H2S = 2, GAS_NH3 = 3, GAS_PH3 = 4, NGAS = 5 };
+// Gas slots of the per-gas output: the reference's sorted constituent order
+// (alpha.py:80) for the line gases h2, h2o, h2s, nh3, ph3, then the
+// closed-form absorbers co (co_ddb) and clouds (clouds_idp).
+enum Gas : int {
+  GAS_H2 = 0, GAS_H2O = 1, GAS_H2S = 2, GAS_NH3 = 3, GAS_PH3 = 4, GAS_CO = 5, GAS_CLOUDS = 6,
+  NGAS = 7
+};
 
-// Abundance rows of the X input [NX][nL].
-enum XRow : int { X_H2 = 0, X_HE = 1, X_CH4 = 2, X_NH3 = 3, X_H2O = 4, X_H2S = 5, X_PH3 = 6, NX = 7 };
+// Rows of the X input [NX][nL]: gas mole fractions, then the cloud
+// densities (g/cm^3) of the reference's cloud table columns H2O (ice),
+// SOLN (liquid), NH4SH, NH3, H2S and CH4.
+enum XRow : int {
+  X_H2 = 0, X_HE = 1, X_CH4 = 2, X_NH3 = 3, X_H2O = 4, X_H2S = 5, X_PH3 = 6, X_CO = 7,
+  X_CL_H2O = 8, X_CL_SOLN = 9, X_CL_NH4SH = 10, X_CL_NH3 = 11, X_CL_H2S = 12, X_CL_CH4 = 13,
+  NX = 14
+};
 
-// NH3 formalism selector.
+// NH3 formalism selector (structure of the blend; the inversion
+// coefficient table is AlphaConfig::inv_table).
 enum Nh3Mode : int { NH3_OFF = 0, NH3_HS = 1, NH3_SJS = 2, NH3_HS_SJS = 3 };
+
+// co_ddb line shape (other_dict['coshape'], co_ddb.py:36-39,86-93).
+enum CoShape : int { CO_VOIGT = 0, CO_VVW = 1, CO_DIFF = 2, CO_STD = 3 };
+
+// clouds_idp particle switches (other_dict '<kind>_p' > 0, clouds_idp.py:16-49).
+enum CloudBit : int {
+  CL_ICE = 1, CL_WATER = 2, CL_NH4SH = 4, CL_NH3ICE = 8, CL_H2SICE = 16, CL_CH4 = 32
+};
 
 // One line family on the device (SoA, sorted by centre).
 struct LineTable {
@@ -97,6 +116,11 @@ struct AlphaConfig {
   int use_h2, use_h2o, use_h2s, use_ph3;
   int h2state;         // 'e' or 'n'
   int units_db;        // 0: cm^-1, 1: dB/km (the nh3 clamp applies after units)
+  int inv_table;       // NH3 inversion coefficients: 0 nh3_hs, 1 nh3_dbs
+  int use_co;          // co_ddb
+  int coshape;         // CoShape
+  int use_clouds;      // clouds_idp
+  int cloud_mask;      // CloudBit set
 };
 
 // Frequency slot plan (see AlphaArgs for the slot -> thread mapping).

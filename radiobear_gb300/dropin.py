@@ -33,8 +33,13 @@ T_CMB = 2.725   # radiobear/utils.py:77
 # Jupiter's default absorbers (radiobear default_config.json)
 DEFAULT_CONSTITUENTS = {'nh3': 'nh3_hs_sjs', 'h2o': 'h2o_bk', 'h2s': 'h2s_ddb',
                         'ph3': 'ph3_jh', 'h2': 'h2_jj_ddb'}
-_NH3_FORMALISMS = {'nh3_hs': 'nh3_hs', 'nh3_sjs': 'nh3_sjs', 'nh3_hs_sjs': 'nh3_hs_sjs'}
-_SUPPORTED = {'h2o': 'h2o_bk', 'h2s': 'h2s_ddb', 'ph3': 'ph3_jh', 'h2': 'h2_jj_ddb'}
+_NH3_FORMALISMS = ('nh3_hs', 'nh3_sjs', 'nh3_hs_sjs', 'nh3_dbs', 'nh3_dbs_sjs')
+_SUPPORTED = {'h2o': 'h2o_bk', 'h2s': 'h2s_ddb', 'ph3': 'ph3_jh', 'h2': 'h2_jj_ddb', 'co': 'co_ddb',
+              'clouds': 'clouds_idp'}
+# config attributes Alpha.setup_formalisms copies into other_dict (alpha.py:90-102)
+_OTHER_TO_COPY = {'h2': ['h2state', 'h2newset'],
+                  'clouds': ['water_p', 'ice_p', 'nh4sh_p', 'nh3ice_p', 'h2sice_p', 'ch4_p'],
+                  'co': ['coshape']}
 _GAS_SLOT = {g: i for i, g in enumerate(_native.GASES)}
 
 _ENGINES = {}
@@ -100,10 +105,19 @@ class Alpha:
             else:
                 raise ValueError('absorber {} for {} is not on the GPU path'.format(absorber, c))
         self.ordered_constituents = sorted(self.constituent.keys())
+        self.other_dict = {}
+        for absorber in self.ordered_constituents:
+            self.other_dict[absorber] = {}
+            for oc in _OTHER_TO_COPY.get(absorber, []):
+                if self.config is not None and hasattr(self.config, oc):
+                    self.other_dict[absorber][oc] = getattr(self.config, oc)
         self.engine.set_formalisms(self.constituent.get('nh3') or 'off',
                                    h2='h2' in self.constituent, h2o='h2o' in self.constituent,
                                    h2s='h2s' in self.constituent, ph3='ph3' in self.constituent,
                                    h2state=_cfg(self.config, 'h2state', 'e'))
+        co = self.other_dict.get('co', {})
+        self.engine.set_co_clouds(co='co' in self.constituent, coshape=co.get('coshape', 'voigt'),
+                                  clouds=self.other_dict.get('clouds'))
         if self.lines is not None:
             catalog.upload(self.engine, self.lines)
 
@@ -170,7 +184,7 @@ class Alpha:
         return layer_scale
 
     def _scale_matrix(self, lscale):
-        """Per-layer scale entries -> the C ABI's [nL][5] gas multipliers."""
+        """Per-layer scale entries -> the C ABI's [nL][RB_NGAS] gas multipliers."""
         nL = len(lscale)
         m = np.ones((nL, len(_native.GASES)))
         for lyr, s in enumerate(lscale):
@@ -182,9 +196,10 @@ class Alpha:
         return m
 
     # -------------------------------------------------------------- absorption
-    def _per_gas(self, freqs, gas, C, scale_matrix=None):
-        """[nL, nf, nC] per-constituent absorption (cm^-1) of gas [nC_gas, nL]."""
-        X = _native.x_matrix(gas, C)
+    def _per_gas(self, freqs, gas, C, cloud=None, Cl=None, scale_matrix=None):
+        """[nL, nf, nC] per-constituent absorption (cm^-1) of gas [nC_gas, nL]
+        and cloud [nC_cloud, nL]."""
+        X = _native.x_matrix(gas, C, cloud, Cl)
         _, g = self.engine.alpha(gas[C['P']], gas[C['T']], X, freqs, scale=scale_matrix,
                                  per_gas=True, layers=False)
         cols = [_GAS_SLOT[c] for c in self.ordered_constituents]
@@ -197,7 +212,9 @@ class Alpha:
         g = np.asarray(gas, dtype=np.float64).reshape(-1, 1).copy()
         g[gas_dict['T'], 0] = T
         g[gas_dict['P'], 0] = P
-        return self._per_gas(np.atleast_1d(np.asarray(freqs, dtype=np.float64)), g, gas_dict)[0]
+        cl = None if cloud is None else np.asarray(cloud, dtype=np.float64).reshape(-1, 1)
+        return self._per_gas(np.atleast_1d(np.asarray(freqs, dtype=np.float64)), g, gas_dict,
+                             cl, cloud_dict)[0]
 
     def get_single_layer(self, freqs, layer, atm, lscale, units='invcm'):
         """alpha.py:218-233."""
@@ -205,8 +222,10 @@ class Alpha:
             absorb = self.alpha_data[layer]
         else:
             C = atm.config.C
+            cloud, Cl = _clouds(atm)
             absorb = self.get_alpha_from_calc(freqs, atm.gas[C['T']][layer], atm.gas[C['P']][layer],
-                                              atm.gas[:, layer], C, None, None, units)
+                                              atm.gas[:, layer], C,
+                                              None if cloud is None else cloud[:, layer], Cl, units)
         return self.total_layer_alpha(absorb=absorb, lscale=lscale)
 
     def get_layers(self, freqs, atm, scale=False, get_alpha='calc', save_alpha='none'):
@@ -229,7 +248,7 @@ class Alpha:
         else:
             f = np.atleast_1d(np.asarray(freqs, dtype=np.float64))
             sm = self._scale_matrix(lscale)
-            X = _native.x_matrix(atm.gas, C)
+            X = _native.x_matrix(atm.gas, C, *_clouds(atm))
             lay, g = self.engine.alpha(atm.gas[C['P']], atm.gas[C['T']], X, f, scale=sm,
                                        per_gas=self._save_alpha_memfil)
             self.layers = lay
@@ -240,6 +259,15 @@ class Alpha:
             self.save_alpha_data(save_alpha)
         del lscale, self.alpha_data, self.tosave
         return self.layers
+
+
+def _clouds(atm):
+    """(atm.cloud, atm.config.Cl) when the atmosphere carries clouds."""
+    cloud = getattr(atm, 'cloud', None)
+    Cl = getattr(atm.config, 'Cl', None)
+    if cloud is None or Cl is None:
+        return None, None
+    return np.asarray(cloud, dtype=np.float64), Cl
 
 
 # ------------------------------------------------------------------ ray paths

@@ -34,6 +34,13 @@ Fixtures (all float64, ``numpy.savez_compressed``):
 ``scale_cases.npz``
     ``Alpha.get_layers`` with number, list and dict scales on the C0
     atmosphere, plus the ``save_alpha='memory'`` cube.
+``f2.npz``
+    The formalisms beside the Jupiter set: nh3_dbs, nh3_dbs_sjs, co_ddb
+    (every coshape) and clouds_idp (every particle kind), through the
+    reference's ``Alpha.get_alpha_from_calc`` per layer (its own
+    other_dict / cloud dispatch) and direct module calls, on a 48-layer
+    synthetic atmosphere from 1e-4 to 2500 bar with CO and a cloud table,
+    the C0 NH3 line lists and the real CO lines.
 """
 import os
 import sys
@@ -356,8 +363,97 @@ def golden_scale_cases():
     print('wrote', path)
 
 
+F2_FREQS = [0.05, 0.6, 1.4, 5.0, 12.0, 22.2, 24.0, 29.9, 30.1, 33.0, 44.0, 60.0, 115.0,
+            115.271, 150.0, 230.0]
+
+
+def f2_atmosphere(nL=48):
+    """Gas and cloud tables of the f2 fixture (CO 1e-6; cloud decks of every
+    kind, ice / liquid water on either side of 273 K)."""
+    gas = synth.make_gas_table(nL, 1.0e-4, 2500.0)
+    C = {k: i for i, k in enumerate(synth.GAS_COLUMNS)}
+    gas[C['CO']] = 1.0e-6
+    Cl = {k: i for i, k in enumerate(synth.CLOUD_COLUMNS)}
+    cloud = np.zeros((len(synth.CLOUD_COLUMNS), nL))
+    for k in ('Z', 'T', 'P'):
+        cloud[Cl[k]] = gas[C[k]]
+    T, P = gas[C['T']], gas[C['P']]
+    rng = np.random.default_rng(21)
+    dens = 10.0 ** rng.uniform(-6.0, -3.0, nL)
+    cloud[Cl['H2O']] = np.where((T < 273.0) & (P > 1.0), dens, 0.0)
+    cloud[Cl['SOLN']] = np.where(T >= 250.0, dens[::-1], 0.0)
+    cloud[Cl['NH4SH']] = np.where((P > 1.0) & (P < 30.0), 0.3 * dens, 0.0)
+    cloud[Cl['NH3']] = np.where((P > 0.3) & (P < 3.0), 2.0 * dens, 0.0)
+    cloud[Cl['H2S']] = np.where((P > 0.1) & (P < 10.0), 0.5 * dens, 0.0)
+    cloud[Cl['CH4']] = np.where(P < 1.0, 0.1 * dens, 0.0)
+    return gas, C, cloud, Cl
+
+
+def golden_f2():
+    cats = real_catalogues()
+    rh.import_reference()
+    rh.reset_lines()
+    import importlib
+    from argparse import Namespace
+    import radiobear.alpha as ralpha
+    z = np.load(os.path.join(HERE, 'c0.npz'))
+    amm = {k[len('ammonia__'):]: z[k] for k in z.files if k.startswith('ammonia__')}
+    nh3 = {k[len('nh3__'):]: z[k] for k in z.files if k.startswith('nh3__')}
+    lines = dict(ammonia=amm, nh3=nh3, h2o=cats['h2o'], h2s=cats['h2s'], ph3=cats['ph3'],
+                 ph3wgt=cats['ph3wgt'])
+    rh.inject_lines(lines)
+    dbs = importlib.import_module('radiobear.constituents.nh3.nh3_dbs')
+    dbs.data = {k: np.asarray(v, dtype=np.float64) for k, v in amm.items()}
+    gas, C, cloud, Cl = f2_atmosphere()
+    nL = gas.shape[1]
+    freqs = list(F2_FREQS)
+    work = tempfile.mkdtemp(prefix='rbgold_f2_')
+    out = dict(freqs=np.array(freqs), gas=gas, cloud=cloud)
+    full = {'nh3': 'nh3_dbs_sjs', 'co': 'co_ddb', 'clouds': 'clouds_idp', 'h2': 'h2_jj_ddb',
+            'h2o': 'h2o_bk', 'h2s': 'h2s_ddb', 'ph3': 'ph3_jh'}
+    runs = dict(
+        A=(full, dict(coshape='voigt', water_p=1.0e-4, ice_p=1.0e-4, nh4sh_p=1.0e-4,
+                      nh3ice_p=1.0e-4, h2sice_p=1.0e-4, ch4_p=1.0e-4)),
+        B=({'nh3': 'nh3_dbs', 'co': 'co_ddb', 'clouds': 'clouds_idp'},
+           dict(coshape='std', water_p=1.0e-4, ice_p=1.0e-4, nh4sh_p=0.0, nh3ice_p=0.0,
+                h2sice_p=0.0, ch4_p=0.0)))
+    for name, (ca, other) in runs.items():
+        cfg = Namespace(constituent_alpha=ca, truncate_method={}, scratch_directory=work,
+                        h2state='e', h2newset=False, **other)
+        al = ralpha.Alpha(config=cfg, verbose=False)
+        if 'nh3_dbs' in sys.modules:      # the bare module the dispatcher imported for 'nh3_dbs'
+            sys.modules['nh3_dbs'].data = dbs.data
+        per = np.zeros((nL, len(freqs), len(al.ordered_constituents)))
+        for L in range(nL):
+            per[L] = al.get_alpha_from_calc(freqs, gas[C['T']][L], gas[C['P']][L], gas[:, L], C,
+                                            cloud[:, L], Cl, units='invcm')
+        out['run{}_alpha'.format(name)] = per
+        out['run{}_ordered'.format(name)] = np.array(al.ordered_constituents)
+        for k, v in other.items():
+            out['run{}_{}'.format(name, k)] = np.array(v)
+    co = sys.modules['co_ddb']
+    for shape in ('vvw', 'diff'):
+        a = np.zeros((nL, len(freqs)))
+        for L in range(nL):
+            a[L] = co.alpha(freqs, gas[C['T']][L], gas[C['P']][L], gas[:, L], C,
+                            {'coshape': shape}, units='invcm', path=rh.constituents_dir('co'),
+                            verbose=False)
+        out['co_' + shape] = a
+    cl = sys.modules['clouds_idp']
+    a = np.zeros((nL, len(freqs)))
+    for L in range(nL):
+        a[L] = cl.alpha(freqs, gas[C['T']][L], gas[C['P']][L], cloud[:, L], Cl, {'ch4': 1.0},
+                        units='invcm', verbose=False)
+    out['clouds_ch4key'] = a
+    for k, v in co.data.items():
+        out['co__' + k] = np.asarray(v, dtype=np.float64)
+    path = os.path.join(HERE, 'f2.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
 JOBS = dict(cats=real_catalogues, bench=golden_benchmark, c0=golden_c0,
-            c1a=golden_c1_alpha, c1tb=golden_c1_tb, scale=golden_scale_cases)
+            c1a=golden_c1_alpha, c1tb=golden_c1_tb, scale=golden_scale_cases, f2=golden_f2)
 
 if __name__ == '__main__':
     which = sys.argv[1:] or list(JOBS)

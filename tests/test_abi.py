@@ -32,7 +32,7 @@ def test_library_builds_and_exports_every_declared_symbol():
 
 def test_abi_version_and_error_path_without_gpu():
     lib = _native.load_library()
-    assert lib.rb_abi_version() == 1
+    assert lib.rb_abi_version() == 2
     try:
         import torch
         has_gpu = torch.cuda.is_available()

@@ -23,6 +23,9 @@ class FakeEngine:
     def set_formalisms(self, *a, **k):
         self.formalisms = (a, k)
 
+    def set_co_clouds(self, *a, **k):
+        self.co_clouds = (a, k)
+
 
 def cpu_alpha(tmp_path=None):
     cfg = Namespace(constituent_alpha=dict(dropin.DEFAULT_CONSTITUENTS), h2state='e',
@@ -44,6 +47,31 @@ def test_layer_scale_semantics():
         a.get_layer_scale({'co': [1.0, 1.0]}, 2)
     with pytest.raises(ValueError, match='Incorrect scale for nh3'):
         a.get_layer_scale({'nh3': [1.0]}, 2)
+
+
+def test_neptune_formalisms_and_other_dict():
+    """nh3_dbs_sjs, co_ddb and clouds_idp: sorted constituents and the
+    other_dict entries copied from the configuration (alpha.py:80-102);
+    CH4 clouds stay off ('ch4_p' is copied, clouds_idp tests 'ch4')."""
+    ca = dict(dropin.DEFAULT_CONSTITUENTS, nh3='nh3_dbs_sjs', co='co_ddb', clouds='clouds_idp')
+    cfg = Namespace(constituent_alpha=ca, h2state='e', scratch_directory='Scratch', coshape='voigt',
+                    water_p=1e-4, ice_p=1e-4, nh4sh_p=0.0, nh3ice_p=1e-4, h2sice_p=1e-4, ch4_p=1e-4)
+    eng = FakeEngine()
+    a = dropin.Alpha(config=cfg, engine_=eng)
+    assert a.ordered_constituents == ['clouds', 'co', 'h2', 'h2o', 'h2s', 'nh3', 'ph3']
+    assert a.other_dict['co'] == {'coshape': 'voigt'}
+    assert a.other_dict['clouds']['ch4_p'] == 1e-4
+    assert eng.formalisms[0][0] == 'nh3_dbs_sjs'
+    k = eng.co_clouds[1]
+    assert k['co'] is True and k['coshape'] == 'voigt' and k['clouds'] is a.other_dict['clouds']
+    from radiobear_gb300 import _native
+    mask = sum(b for key, b in _native.CLOUD_BITS.items() if k['clouds'].get(key, 0) > 0)
+    assert mask == _native.CLOUD_BITS['water_p'] | _native.CLOUD_BITS['ice_p'] | \
+        _native.CLOUD_BITS['nh3ice_p'] | _native.CLOUD_BITS['h2sice_p']
+    m = a._scale_matrix([{'co': 2.0, 'clouds': 0.5}])
+    assert m[0, _native.GASES.index('co')] == 2.0 and m[0, _native.GASES.index('clouds')] == 0.5
+    with pytest.raises(ValueError, match='not on the GPU path'):
+        dropin.Alpha(config=Namespace(constituent_alpha={'hcn': 'hcn_x'}), engine_=FakeEngine())
 
 
 def test_scale_matrix_and_total():
