@@ -9,8 +9,8 @@ the GPU tests hold the CUDA path to it.
 
 Tolerances: the line gases (float32 line sums) within 1e-5 relative, as
 for the Jupiter set; co_ddb and clouds_idp are evaluated in float64 on the
-device and agree to 1e-10 relative (co 'diff' crosses zero: measured
-against 1e-12 of its largest magnitude).
+device and agree to 1e-10 relative (co 'diff', a difference of two sums
+that cancel, is measured against the size of the VVW sum).
 """
 import numpy as np
 import pytest
@@ -152,7 +152,10 @@ def test_gpu_co_shapes(engine, shape):
     ordered, _, per = _gpu_per_gas(engine, 'B', 'nh3_dbs', coshape=shape)
     r = z['co_' + shape]
     a = per[:, :, ordered.index('co')]
-    assert rel_err(a, r, 1e-12 * np.max(np.abs(r))) < EXTRA_RTOL
+    # 'diff' = Voigt - VVW cancels where the shapes agree: its rounding is
+    # relative to the size of the terms (the VVW sum), not to the difference
+    floor = np.abs(z['co_vvw']) if shape == 'diff' else 1e-12 * np.max(np.abs(r))
+    assert rel_err(a, r, floor) < EXTRA_RTOL
 
 
 @pytest.mark.gpu
