@@ -159,6 +159,15 @@ __device__ __forceinline__ void zero_fam(LayerFam& F) {
   F.M2 = 0.f;
   for (int s = 0; s < 2; ++s)
     for (int k = 0; k < 8; ++k) F.c[s][k] = 0.f;
+  F.wide = 0;
+}
+
+// Ben-Reuven width floor (gamma >= c[s][0], the line-independent part) at
+// least 0.32 of the largest shifted centre in every coefficient set.
+__device__ __forceinline__ int wide_br(const LayerFam& F, int nsets, float cmax) {
+  int w = cmax > 0.f;
+  for (int s = 0; s < nsets; ++s) w &= F.c[s][0] >= 0.32f * (cmax + fabsf(F.c[s][7]));
+  return w;
 }
 
 // Eight threads per layer, one per part of the layer's parameters:
@@ -246,6 +255,7 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
       }
       set_cE(F, cE300);
       set_fac(F, hs_base * TWO_OVER_PI, scale_bound(a, FAM_NH3_INV, (float)cE300));
+      F.wide = wide_br(F, 2, a.cmax[FAM_NH3_INV]);
       o.fam[FAM_NH3_INV] = F;
       return;
     }
@@ -318,6 +328,7 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
       set_cE(F, cE296g);
       set_fac(F, 7.244E+21f * (Ph2s / 296.f) * pw(l296, 3.5f) * GHZ_INVCM * TWO_OVER_PI,
               scale_bound(a, FAM_H2S, (float)cE296g));
+      F.wide = wide_br(F, 1, a.cmax[FAM_H2S]);
       o.fam[FAM_H2S] = F;
       return;
     }
@@ -435,7 +446,7 @@ __device__ __forceinline__ float line_strength(const LineTable& t, const LayerFa
 // denominator >= 3/4 for every F >= 0 (K = 1, G4 = 1), so they add exactly 0.
 template <int KIND>
 __device__ __forceinline__ void line_fields(const LineTable& t, const LayerFam& LF, int set, int li,
-                                            bool valid, float sjs_shift, float* v,
+                                            bool valid, float S, float sjs_shift, float* v,
                                             float& base_part) {
   if (!valid) {
     if (KIND == K_SJS) {
@@ -447,7 +458,6 @@ __device__ __forceinline__ void line_fields(const LineTable& t, const LayerFam& 
     }
     return;
   }
-  const float S = line_strength(t, LF, li);
   if (KIND == K_BR) {
     const float* c = LF.c[set];
     const float w1 = t.w1[li], w2 = t.w2[li];
@@ -510,22 +520,35 @@ __device__ __forceinline__ void line_fields(const LineTable& t, const LayerFam& 
   }
 }
 
-// Build the records of lines [c0, c1) into `ck` (np = 2 * quads pairs).
+// Build the records of lines [c0, c1), padded to whole quads, into ck0
+// (coefficient set 0) and ck1 (set 1), either may be null.  One line per
+// thread: the strength is formed once for both sets, and every thread of
+// the CTA takes an equal share.  In a chunk, field f of line l is float
+// f * CH_LINES + l (quad q packs lines 4q .. 4q+3).
 template <int KIND>
-__device__ __forceinline__ void build_chunk(Chunk& ck, const LineTable& t, const LayerFam& LF,
-                                            int set, int c0, int c1, float sjs_shift,
+__device__ __forceinline__ void build_chunk(Chunk* ck0, Chunk* ck1, const LineTable& t,
+                                            const LayerFam& LF, int c0, int c1, float sjs_shift,
                                             float& base_part) {
   constexpr int NF = KIND == K_SJS ? 4 : NFIELD;
-  const int np = 2 * ((c1 - c0 + 3) >> 2);
-  f2* out = reinterpret_cast<f2*>(&ck);
-  for (int p = threadIdx.x; p < np; p += blockDim.x) {
-    const int la = c0 + 2 * p;
-    float va[NFIELD], vb[NFIELD];
-    line_fields<KIND>(t, LF, set, la, la < c1, sjs_shift, va, base_part);
-    line_fields<KIND>(t, LF, set, la + 1, la + 1 < c1, sjs_shift, vb, base_part);
-    const int q = p >> 1, h = p & 1;
+  const int nl = 4 * ((c1 - c0 + 3) >> 2);
+  float* o0 = reinterpret_cast<float*>(ck0);
+  float* o1 = reinterpret_cast<float*>(ck1);
+  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+    const int li = c0 + l;
+    const bool valid = li < c1;
+    const float S = valid ? line_strength(t, LF, li) : 0.f;
+    float v[NFIELD];
+    if (o0) {
+      line_fields<KIND>(t, LF, 0, li, valid, S, sjs_shift, v, base_part);
 #pragma unroll
-    for (int f = 0; f < NF; ++f) out[(f * CH_QUADS + q) * 2 + h] = pk(va[f], vb[f]);
+      for (int f = 0; f < NF; ++f) o0[f * CH_LINES + l] = v[f];
+    }
+    if (KIND == K_BR && o1) {
+      float u = 0.f;   // the VVW base term is counted once (set 0 only)
+      line_fields<KIND>(t, LF, 1, li, valid, S, sjs_shift, v, u);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) o1[f * CH_LINES + l] = v[f];
+    }
   }
 }
 
@@ -604,13 +627,15 @@ struct QuadRec {
   ulonglong2 mKH, mKL, G4, h;       // precise fields 4..7
 };
 
-template <int KIND, bool PREC>
+// Fields for the chains of one record set: FAST if some chain takes the
+// expanded form, PREC if some chain takes the double-float form.
+template <int KIND, bool FAST, bool PREC>
 __device__ __forceinline__ void load_quad(const Chunk& ck, int q, QuadRec& r) {
-  if (!PREC || KIND != K_VVW) {   // the precise VVW path needs no fast fields
-    if (!PREC) {
-      r.c1 = ck.f[0][q];
-      r.c2 = ck.f[1][q];
-    }
+  if (FAST) {
+    r.c1 = ck.f[0][q];
+    r.c2 = ck.f[1][q];
+  }
+  if (FAST || KIND != K_VVW) {   // the precise VVW path needs no a, b
     r.a = ck.f[2][q];
     r.b = KIND == K_GROSS ? r.a : ck.f[3][q];
   }
@@ -633,34 +658,44 @@ __device__ __forceinline__ void eval_tier(const QuadRec& r, const ChainF& c, Acc
   }
 }
 
-// Quads [q0, q1) for all M chains at one precision tier.  Chains [0, KS)
-// read set-0 records (ck0), chains past the split read set-1 records (ck1);
-// with MIX, chain KS reads per lane from the set of its own slot.  Every
-// record load is shared by the chains of its set; Kahan flush every 32 lines
-// (all terms are positive, so a 16-term float32 block sum per lane is good
-// to ~1e-6 before compensation).
-template <int M, int KIND, bool PREC, int KS, bool MIX>
+// Chains [lo, hi) at precision mask PM: any of them fast / precise.
+template <int PM>
+__host__ __device__ constexpr bool any_fast(int lo, int hi) {
+  return lo >= hi ? false : (((PM >> lo) & 1) == 0 || any_fast<PM>(lo + 1, hi));
+}
+template <int PM>
+__host__ __device__ constexpr bool any_prec(int lo, int hi) {
+  return lo >= hi ? false : (((PM >> lo) & 1) != 0 || any_prec<PM>(lo + 1, hi));
+}
+
+// Quads [q0, q1) for all M chains, chain k at the double-float tier when
+// bit k of PM is set.  Chains [0, KS) read set-0 records (ck0), chains past
+// the split read set-1 records (ck1); with MIX, chain KS reads per lane
+// from the set of its own slot.  Every record load is shared by the chains
+// of its set; Kahan flush every 32 lines (all terms are positive, so a
+// 16-term float32 block sum per lane is good to ~1e-6 before compensation).
+template <int M, int KIND, int PM, int KS, bool MIX>
 __device__ __forceinline__ void run_tier(const Chunk& ck0, const Chunk& ck1, const Chunk& ckl,
                                          int q0, int q1, const ChainF (&cf)[M], Acc2 (&acc)[M]) {
   constexpr bool USE0 = KS > 0;
   constexpr bool USE1 = KS + (MIX ? 1 : 0) < M;
+  constexpr int K1 = KS + (MIX ? 1 : 0);
   int q = q0;
   for (; q < q1;) {
     const int qe = min(q1, q + 8);
 #pragma unroll 2
     for (; q < qe; ++q) {
       QuadRec r0, r1, rl;
-      if (USE0) load_quad<KIND, PREC>(ck0, q, r0);
-      if (USE1) load_quad<KIND, PREC>(ck1, q, r1);
-      if (MIX) load_quad<KIND, PREC>(ckl, q, rl);
+      if (USE0) load_quad<KIND, any_fast<PM>(0, KS), any_prec<PM>(0, KS)>(ck0, q, r0);
+      if (USE1) load_quad<KIND, any_fast<PM>(K1, M), any_prec<PM>(K1, M)>(ck1, q, r1);
+      if (MIX) load_quad<KIND, any_fast<PM>(KS, KS + 1), any_prec<PM>(KS, KS + 1)>(ckl, q, rl);
 #pragma unroll
       for (int k = 0; k < M; ++k) {
-        if (k < KS)
-          eval_tier<KIND, PREC>(r0, cf[k], acc[k]);
-        else if (MIX && k == KS)
-          eval_tier<KIND, PREC>(rl, cf[k], acc[k]);
+        const QuadRec& r = k < KS ? r0 : ((MIX && k == KS) ? rl : r1);
+        if ((PM >> k) & 1)
+          eval_tier<KIND, true>(r, cf[k], acc[k]);
         else
-          eval_tier<KIND, PREC>(r1, cf[k], acc[k]);
+          eval_tier<KIND, false>(r, cf[k], acc[k]);
       }
     }
 #pragma unroll
@@ -669,56 +704,89 @@ __device__ __forceinline__ void run_tier(const Chunk& ck0, const Chunk& ck1, con
 }
 
 // Set split of one warp -> one compiled variant (M = 2 or 4).
-template <int M, int KIND, bool PREC>
+template <int M, int KIND, int PM>
 __device__ __forceinline__ void run_split(int ks, bool mix, const Chunk& ck0, const Chunk& ck1,
                                           const Chunk& ckl, int q0, int q1,
                                           const ChainF (&cf)[M], Acc2 (&acc)[M]) {
   if (KIND != K_BR || ks >= M) {
-    run_tier<M, KIND, PREC, M, false>(ck0, ck1, ckl, q0, q1, cf, acc);
+    run_tier<M, KIND, PM, M, false>(ck0, ck1, ckl, q0, q1, cf, acc);
     return;
   }
   // inversion lines with set-1 chains in this warp
   if (!mix) {
     switch (ks) {
-      case 0: run_tier<M, KIND, PREC, 0, false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
-      case 1: run_tier<M, KIND, PREC, 1, false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
-      case 2: run_tier<M, KIND, PREC, (M > 2 ? 2 : 0), false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
-      default: run_tier<M, KIND, PREC, (M > 3 ? 3 : 0), false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 0: run_tier<M, KIND, PM, 0, false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 1: run_tier<M, KIND, PM, 1, false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 2: run_tier<M, KIND, PM, (M > 2 ? 2 : 0), false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      default: run_tier<M, KIND, PM, (M > 3 ? 3 : 0), false>(ck0, ck1, ckl, q0, q1, cf, acc); break;
     }
   } else {
     switch (ks) {
-      case 0: run_tier<M, KIND, PREC, 0, true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
-      case 1: run_tier<M, KIND, PREC, 1, true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
-      case 2: run_tier<M, KIND, PREC, (M > 2 ? 2 : 0), true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
-      default: run_tier<M, KIND, PREC, (M > 3 ? 3 : 0), true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 0: run_tier<M, KIND, PM, 0, true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 1: run_tier<M, KIND, PM, 1, true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      case 2: run_tier<M, KIND, PM, (M > 2 ? 2 : 0), true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
+      default: run_tier<M, KIND, PM, (M > 3 ? 3 : 0), true>(ck0, ck1, ckl, q0, q1, cf, acc); break;
     }
   }
 }
 
-// One chunk: the quads where some chain of the warp sees a line within its
-// double-float window run at the precise tier for every chain, the rest at
-// the fast tier.
+// One chunk.  M = 2: the quads are cut where a chain's double-float window
+// starts or ends, and each chain takes the double-float form only inside
+// its own window (the other chain of the warp stays on the expanded form).
+// M = 4: the hull of the chains' windows runs at the double-float tier for
+// every chain.
 template <int M, int KIND>
 __device__ __forceinline__ void sweep_chunk(const Chunk& ck0, const Chunk& ck1, const Chunk& ckl,
                                             int c0, int c1, int ks, bool mix, const int (&na)[M],
                                             const int (&nb)[M], const ChainF (&cf)[M],
                                             Acc2 (&acc)[M]) {
   const int nq = (c1 - c0 + 3) >> 2;
-  int qa = nq, qb = 0;   // hull of the chains' windows, in quads
+  int qa[M], qb[M];   // each chain's window, in quads of this chunk
 #pragma unroll
   for (int k = 0; k < M; ++k) {
+    qa[k] = nq;
+    qb[k] = 0;
     if (na[k] < nb[k]) {
-      qa = min(qa, max((na[k] - c0) >> 2, 0));
-      qb = max(qb, min((nb[k] - c0 + 3) >> 2, nq));
+      qa[k] = max((na[k] - c0) >> 2, 0);
+      qb[k] = min((nb[k] - c0 + 3) >> 2, nq);
     }
   }
-  if (qa >= qb) {
-    run_split<M, KIND, false>(ks, mix, ck0, ck1, ckl, 0, nq, cf, acc);
+  if (M == 2) {
+    int q = 0;
+    while (q < nq) {
+      int e = nq, pm = 0;
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        const bool in = qa[k] < qb[k] && q >= qa[k] && q < qb[k];
+        pm |= in ? (1 << k) : 0;
+        e = min(e, in ? qb[k] : (qa[k] > q && qa[k] < qb[k] ? qa[k] : nq));
+      }
+      switch (pm) {
+        case 0: run_split<M, KIND, 0>(ks, mix, ck0, ck1, ckl, q, e, cf, acc); break;
+        case 1: run_split<M, KIND, 1>(ks, mix, ck0, ck1, ckl, q, e, cf, acc); break;
+        case 2: run_split<M, KIND, 2>(ks, mix, ck0, ck1, ckl, q, e, cf, acc); break;
+        default: run_split<M, KIND, 3>(ks, mix, ck0, ck1, ckl, q, e, cf, acc); break;
+      }
+      q = e;
+    }
     return;
   }
-  if (qa > 0) run_split<M, KIND, false>(ks, mix, ck0, ck1, ckl, 0, qa, cf, acc);
-  run_split<M, KIND, true>(ks, mix, ck0, ck1, ckl, qa, qb, cf, acc);
-  if (qb < nq) run_split<M, KIND, false>(ks, mix, ck0, ck1, ckl, qb, nq, cf, acc);
+  int ha = nq, hb = 0;   // hull
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    if (qa[k] < qb[k]) {
+      ha = min(ha, qa[k]);
+      hb = max(hb, qb[k]);
+    }
+  }
+  constexpr int ALL = (1 << M) - 1;
+  if (ha >= hb) {
+    run_split<M, KIND, 0>(ks, mix, ck0, ck1, ckl, 0, nq, cf, acc);
+    return;
+  }
+  if (ha > 0) run_split<M, KIND, 0>(ks, mix, ck0, ck1, ckl, 0, ha, cf, acc);
+  run_split<M, KIND, ALL>(ks, mix, ck0, ck1, ckl, ha, hb, cf, acc);
+  if (hb < nq) run_split<M, KIND, 0>(ks, mix, ck0, ck1, ckl, hb, nq, cf, acc);
 }
 
 __device__ __forceinline__ bool fam_is_hs(int fam) {
@@ -781,28 +849,23 @@ __device__ __forceinline__ void lines_item(const AlphaArgs& a, Chunk (&buf)[2][2
     }
     if (mix && k == ks) lane_set = a.sp.set[s];
     const int2 nr = cp[k].near[fam];
-    na[k] = nr.x;
-    nb[k] = nr.y;
+    na[k] = LF.wide ? 0 : nr.x;
+    nb[k] = LF.wide ? 0 : nr.y;
   }
   Acc2 acc[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) acc[k].init();
   float base_part = 0.f;
   const int nch = (l1 - l0 + CH_LINES - 1) / CH_LINES;
-  {
-    const int c1 = min(l1, l0 + CH_LINES);
-    if (b0) build_chunk<KIND>(buf[0][0], tab, LF, 0, l0, c1, 0.f, base_part);
-    if (b1) build_chunk<KIND>(buf[0][1], tab, LF, 1, l0, c1, 0.f, base_part);
-  }
+  build_chunk<KIND>(b0 ? &buf[0][0] : nullptr, b1 ? &buf[0][1] : nullptr, tab, LF, l0,
+                    min(l1, l0 + CH_LINES), 0.f, base_part);
   __syncthreads();
   for (int c = 0; c < nch; ++c) {
     const int c0 = l0 + c * CH_LINES, c1 = min(l1, c0 + CH_LINES);
     const int nbuf = (c + 1) & 1;
-    if (c + 1 < nch) {
-      const int n1 = min(l1, c1 + CH_LINES);
-      if (b0) build_chunk<KIND>(buf[nbuf][0], tab, LF, 0, c1, n1, 0.f, base_part);
-      if (b1) build_chunk<KIND>(buf[nbuf][1], tab, LF, 1, c1, n1, 0.f, base_part);
-    }
+    if (c + 1 < nch)
+      build_chunk<KIND>(b0 ? &buf[nbuf][0] : nullptr, b1 ? &buf[nbuf][1] : nullptr, tab, LF, c1,
+                        min(l1, c1 + CH_LINES), 0.f, base_part);
     const Chunk& ck0 = buf[c & 1][0];
     const Chunk& ck1 = buf[c & 1][1];
     sweep_chunk<M, KIND>(ck0, ck1, lane_set ? ck1 : ck0, c0, c1, ks, mix, na, nb, cf, acc);
@@ -856,12 +919,13 @@ __device__ __forceinline__ void sjs_item(const AlphaArgs& a, Chunk (&buf)[2][2],
   float unused = 0.f;
   const f2 mone = dup(-1.f);
   const int nch = (l1 - l0 + CH_LINES - 1) / CH_LINES;
-  build_chunk<K_SJS>(buf[0][0], tab, LF, 0, l0, min(l1, l0 + CH_LINES), shift, unused);
+  build_chunk<K_SJS>(&buf[0][0], nullptr, tab, LF, l0, min(l1, l0 + CH_LINES), shift, unused);
   __syncthreads();
   for (int c = 0; c < nch; ++c) {
     const int c0 = l0 + c * CH_LINES, c1 = min(l1, c0 + CH_LINES);
     if (c + 1 < nch)
-      build_chunk<K_SJS>(buf[(c + 1) & 1][0], tab, LF, 0, c1, min(l1, c1 + CH_LINES), shift, unused);
+      build_chunk<K_SJS>(&buf[(c + 1) & 1][0], nullptr, tab, LF, c1, min(l1, c1 + CH_LINES), shift,
+                         unused);
     const Chunk& ck = buf[c & 1][0];
     const int nq = (c1 - c0 + 3) >> 2;
 #pragma unroll
@@ -974,19 +1038,44 @@ __device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int til
 template <int M>
 __global__ void __launch_bounds__(128, M >= 4 ? 4 : 6) rb_alpha_lines_kernel(AlphaArgs a) {
   __shared__ __align__(16) Chunk buf[2][2];   // [double buffer][coefficient set]
-  __shared__ int s_item[2];
+  __shared__ int s_item[2], s_asm[2];
   __shared__ int s_last;
   __shared__ float s_red[4];
   const int per = a.nL * a.ntile;
   for (int it = 0;; ++it) {
-    if (threadIdx.x == 0) s_item[it & 1] = atomicAdd(a.counter, 1);
+    // Thread 0 takes items until one has work: an item whose family is off
+    // in its layer (nh3_sjs outside the blend layers, say) only counts as
+    // done, and if it was the last of its (layer, tile) the CTA assembles.
+    if (threadIdx.x == 0) {
+      int item, lt = -1;
+      for (;;) {
+        item = atomicAdd(a.counter, 1);
+        if (item >= a.nitems) break;
+        const int t = item / per, rem = item - t * per;
+        const int L = a.nL - 1 - rem / a.ntile, tile = rem % a.ntile;
+        if (fam_enabled(a, a.lp[L], a.tmpl[t].fam)) break;
+        if (atomicAdd(a.done + (size_t)L * a.ntile + tile, 1) == a.ntmpl - 1) {
+          __threadfence();
+          lt = L * a.ntile + tile;
+          break;
+        }
+      }
+      s_item[it & 1] = item;
+      s_asm[it & 1] = lt;
+    }
     __syncthreads();
     const int item = s_item[it & 1];
+    if (s_asm[it & 1] >= 0) {
+      const int lt = s_asm[it & 1];
+      for (int ls = threadIdx.x; ls < a.spt; ls += blockDim.x)
+        assemble_slot(a, lt / a.ntile, lt % a.ntile, ls);
+      continue;
+    }
     if (item >= a.nitems) break;
     const int t = item / per, rem = item - t * per;
     const int L = a.nL - 1 - rem / a.ntile, tile = rem % a.ntile;
     const TmplEntry e = a.tmpl[t];
-    if (fam_enabled(a, a.lp[L], e.fam)) {
+    {
       switch (e.fam) {
         case FAM_NH3_INV:
         case FAM_H2S:

@@ -281,9 +281,10 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
         c.near[fam] = make_int2(a, std::max(a, b));
       }
     }
-  // Partition of each tile's blocks into W warps of M chains.  A warp runs
-  // the double-float tier over the hull of its chains' windows, so blocks
-  // whose windows overlap are grouped; the cost is the modelled packed-op
+  // Partition of each tile's blocks into W warps of M chains.  With M = 2 a
+  // chain runs the double-float tier over its own window; with M = 4 a warp
+  // runs it over the hull of its chains' windows, so blocks whose windows
+  // overlap are grouped.  The cost is the modelled packed-op
   // count (fast / double-float per line quad and chain: Ben-Reuven 10 / 16,
   // Gross 8 / 12, VVW 10 / 22), the objective half the sum and half W times
   // the largest warp (warps of a CTA meet at a barrier every chunk).
@@ -291,6 +292,8 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
     static const int fams[6] = {rb::FAM_NH3_INV, rb::FAM_NH3_ROT, rb::FAM_NH3_V2,
                                 rb::FAM_H2O, rb::FAM_H2S, rb::FAM_PH3};
     static const double cf[6] = {10, 8, 8, 10, 10, 10}, cp[6] = {16, 12, 12, 22, 16, 16};
+    // M = 2: each chain takes the double-float form inside its own window;
+    // M = 4: every chain of the warp inside the hull of the windows
     double cost = 0.0;
     for (int q = 0; q < 6; ++q) {
       const int n = h->fam[fams[q]].n;
@@ -301,9 +304,10 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
         if (r.x < r.y) {
           lo = std::min(lo, r.x);
           hi = std::max(hi, r.y);
+          if (M == 2) cost += (r.y - r.x) * (cp[q] - cf[q]);
         }
       }
-      const int hull = std::max(0, hi - lo);
+      const int hull = M == 2 ? 0 : std::max(0, hi - lo);
       cost += (double)g.size() * ((n - hull) * cf[q] + hull * cp[q]);
     }
     return cost;
@@ -483,6 +487,7 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
     pa.l2Imax[f] = h->fam[f].l2Imax;
     pa.Emin[f] = h->fam[f].Emin;
     pa.Emax[f] = h->fam[f].Emax;
+    pa.cmax[f] = h->fam[f].n > 0 ? (float)h->fam[f].centre.back() : 0.f;
     pa.nlines[f] = h->fam[f].n;
   }
   pa.out = h->d_lp.as<rb::LayerParams>();

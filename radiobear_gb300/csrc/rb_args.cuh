@@ -13,6 +13,7 @@ struct PrepArgs {
   const double* scale;   // [nL][NGAS] or null
   AlphaConfig cfg;
   float l2Imax[NFAM], Emin[NFAM], Emax[NFAM];
+  float cmax[NFAM];      // largest line centre of each family (GHz)
   int nlines[NFAM];
   LayerParams* out;
   int* counter;          // line-sum work counter to reset (or null)

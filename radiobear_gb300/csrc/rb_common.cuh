@@ -95,6 +95,11 @@ struct LayerFam {
   // Gross: gamma = c1*w1 + c2*w2 + c3*w3 (set 0).
   // VVW:  df = c1*w1*Th^x1 + c2*w2*Th^x2 + c3*w3*Th^x3, c0 = log2(Theta).
   float c[2][8];
+  // 1 when the lines are wide enough at this layer for the expanded
+  // denominator everywhere: 4 gamma^2 >= 0.27 K for every line (gamma at
+  // least 0.32 of the largest centre), which bounds its rounding error by
+  // ~18 ulp as outside the near-line windows.  Ben-Reuven families only.
+  int wide;
 };
 
 // Per-layer parameters.
