@@ -50,7 +50,7 @@ __device__ __forceinline__ int wrap_l(int l, int nL) {
 //                            dTb/dtau_k = -w_k a_k E_k
 //   rb_tb_adj_grad_kernel    Lam after the chunk = sum of S over later
 //                            chunks, then the chunk's nodes in reverse.
-constexpr int ADJ_CHUNK = 128;   // = the forward scan's chunk (rb_tb.cu)
+constexpr int ADJ_CHUNK = SCAN_CHUNK;   // the forward scan's chunk
 
 // Double-float running sum (a float pair) and compensated float sum.
 __device__ __forceinline__ void dfs_add(float& h, float& l, float v) {

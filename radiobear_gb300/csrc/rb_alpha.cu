@@ -39,46 +39,12 @@
 // Strengths: S'_l = 2^(l2I_l + cE E_l - M2) with the exponent formed as a
 // double-float and split into integer and fractional parts before exp2.
 #include "rb_args.cuh"
+#include "rb_f32x2.cuh"
 #include <math_constants.h>
 
 #include <algorithm>
 
 namespace rb {
-
-// ------------------------------------------------------------------ f32x2
-typedef unsigned long long f2;
-
-__device__ __forceinline__ f2 pk(float a, float b) {
-  f2 r;
-  asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ float lo2(f2 v) {
-  float a, b;
-  asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  return a;
-}
-__device__ __forceinline__ float hi2(f2 v) {
-  float a, b;
-  asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  return b;
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-  f2 d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-  f2 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-  f2 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ f2 dup(float a) { return pk(a, a); }
 
 // Kahan-compensated pair of sums; `part` collects a block of terms.
 // The running block sum is kept as two scalars (p0, p1) so the reciprocal
@@ -672,7 +638,7 @@ __host__ __device__ constexpr bool any_prec(int lo, int hi) {
 // bit k of PM is set.  Chains [0, KS) read set-0 records (ck0), chains past
 // the split read set-1 records (ck1); with MIX, chain KS reads per lane
 // from the set of its own slot.  Every record load is shared by the chains
-// of its set; Kahan flush every 32 lines (all terms are positive, so a
+// of its set; Kahan flush every 64 lines (all terms are positive, so a
 // 16-term float32 block sum per lane is good to ~1e-6 before compensation).
 template <int M, int KIND, int PM, int KS, bool MIX>
 __device__ __forceinline__ void run_tier(const Chunk& ck0, const Chunk& ck1, const Chunk& ckl,
@@ -682,8 +648,8 @@ __device__ __forceinline__ void run_tier(const Chunk& ck0, const Chunk& ck1, con
   constexpr int K1 = KS + (MIX ? 1 : 0);
   int q = q0;
   for (; q < q1;) {
-    const int qe = min(q1, q + 8);
-#pragma unroll 2
+    const int qe = min(q1, q + 16);
+#pragma unroll 1
     for (; q < qe; ++q) {
       QuadRec r0, r1, rl;
       if (USE0) load_quad<KIND, any_fast<PM>(0, KS), any_prec<PM>(0, KS)>(ck0, q, r0);

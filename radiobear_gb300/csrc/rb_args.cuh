@@ -5,6 +5,10 @@
 
 namespace rb {
 
+// Segments per chunk of the parallel brightness scan; the adjoint's reverse
+// sweep runs over the same chunks (it reuses the forward's chunk partials).
+constexpr int SCAN_CHUNK = 64;
+
 struct PrepArgs {
   int nL;
   const double* P;

@@ -17,11 +17,13 @@
 // tau_c being the optical depth at the chunk's first point.  One CTA covers
 // (128 frequencies, one chunk, one ray); the chunk's ds / layer / T are
 // staged in shared memory so the loop's only global loads are the
-// alpha[layer][f0..f127] rows (coalesced, L2 resident).
+// alpha[layer][f0..f127] rows (coalesced, L2 resident).  With an even
+// number of frequencies the packed variant takes two per thread.
 // Sequential path: one thread per (ray, frequency) over the whole path; used
 // for the E2 weighting of b = 'disc' and when per-segment profiles
 // (tau, W, TbL) are requested.
 #include "rb_args.cuh"
+#include "rb_f32x2.cuh"
 #include <math_constants.h>
 
 namespace rb {
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(128) rb_tb_seq_kernel(TbArgs a) {
 }
 
 // ------------------------------------------------------------ chunked
-constexpr int TB_CHUNK = 128;
+constexpr int TB_CHUNK = SCAN_CHUNK;
 
 __global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
   const int ray = blockIdx.x;   // rays in x: batches have more than 65535
@@ -228,6 +230,110 @@ __global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
   part[f] = make_float4(th, tl, iw - iwc, tb - tbc);
 }
 
+// Packed scan: the same arithmetic for two adjacent frequencies per thread
+// in f32x2 (double-float optical depth and the two compensated sums lane by
+// lane, one exp per lane); alpha rows are read as float2.  Needs an even
+// frequency count (8-byte aligned pairs).  One CTA covers (256 frequencies,
+// one chunk, one ray); the partials are the scalar kernel's.
+__device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
+  s = add2(a, b);
+  const f2 bb = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+__device__ __forceinline__ void kahan_add2(f2& s, f2& c, f2 v) {
+  const f2 y = sub2(v, c);
+  const f2 t = add2(s, y);
+  c = sub2(sub2(t, s), y);
+  s = t;
+}
+
+__global__ void __launch_bounds__(128) rb_tb_chunk2_kernel(TbArgs a) {
+  const int ray = blockIdx.x;
+  const int ch = blockIdx.y;
+  const int f = 2 * (blockIdx.z * blockDim.x + threadIdx.x);   // first of the pair
+  const int nseg = a.nseg[ray];
+  const int nsteps = nseg - 1;
+  const int i0 = ch * TB_CHUNK;
+  float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
+  if (i0 >= nsteps) {
+    if (f < a.nf) {
+      part[f] = make_float4(0.f, 0.f, 0.f, 0.f);
+      part[f + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return;
+  }
+  const int n = min(TB_CHUNK, nsteps - i0);
+  __shared__ int s_off[TB_CHUNK + 1];
+  __shared__ float s_T[TB_CHUNK + 1];
+  __shared__ float s_hd[TB_CHUNK];
+  const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
+  const int* lay = a.layer + (size_t)ray * a.max_seg + i0;
+  int off, nLr;
+  ray_layers(a, ray, off, nLr);
+  for (int t = threadIdx.x; t <= n; t += blockDim.x) {
+    const int l = off + wrap_layer(lay[t], nLr);
+    s_off[t] = l * a.nf;
+    s_T[t] = a.T32[l];
+    if (t < n) s_hd[t] = hds[t];
+  }
+  __syncthreads();
+  if (f >= a.nf) return;
+  const float* al = a.alpha32 + f;
+  auto ld = [&](int o) -> f2 { return *reinterpret_cast<const f2*>(al + o); };
+  f2 th = 0ull, tl = 0ull;
+  f2 a0 = ld(s_off[0]);
+  f2 W0 = (i0 == 0) ? 0ull : a0;
+  f2 T0 = dup(s_T[0]);
+  f2 iw = 0ull, iwc = 0ull, tb = 0ull, tbc = 0ull;
+  const f2 one = dup(1.f);
+  int i = 0;
+  constexpr int BLK = 16;   // steps whose alpha loads are in flight together
+  for (; i + BLK <= n; i += BLK) {
+    f2 an[BLK];
+#pragma unroll
+    for (int k = 0; k < BLK; ++k) an[k] = ld(s_off[i + 1 + k]);
+#pragma unroll
+    for (int k = 0; k < BLK; ++k) {
+      const f2 hd = dup(s_hd[i + k]);
+      const f2 a1 = an[k];
+      const f2 T1 = dup(s_T[i + 1 + k]);
+      f2 ss, e;
+      two_sum2(th, mul2(add2(a0, a1), hd), ss, e);
+      e = add2(e, tl);
+      th = add2(ss, e);
+      tl = sub2(e, sub2(th, ss));
+      const f2 ex = pk(__expf(-lo2(th)), __expf(-hi2(th)));
+      const f2 W1 = mul2(mul2(a1, ex), sub2(one, tl));
+      kahan_add2(iw, iwc, mul2(add2(W1, W0), hd));
+      kahan_add2(tb, tbc, mul2(fma2(T1, W1, mul2(T0, W0)), hd));
+      W0 = W1;
+      T0 = T1;
+      a0 = a1;
+    }
+  }
+  for (; i < n; ++i) {
+    const f2 hd = dup(s_hd[i]);
+    const f2 a1 = ld(s_off[i + 1]);
+    const f2 T1 = dup(s_T[i + 1]);
+    f2 ss, e;
+    two_sum2(th, mul2(add2(a0, a1), hd), ss, e);
+    e = add2(e, tl);
+    th = add2(ss, e);
+    tl = sub2(e, sub2(th, ss));
+    const f2 ex = pk(__expf(-lo2(th)), __expf(-hi2(th)));
+    const f2 W1 = mul2(mul2(a1, ex), sub2(one, tl));
+    kahan_add2(iw, iwc, mul2(add2(W1, W0), hd));
+    kahan_add2(tb, tbc, mul2(fma2(T1, W1, mul2(T0, W0)), hd));
+    W0 = W1;
+    T0 = T1;
+    a0 = a1;
+  }
+  const f2 IW = sub2(iw, iwc), TB = sub2(tb, tbc);
+  part[f] = make_float4(lo2(th), lo2(tl), lo2(IW), lo2(TB));
+  part[f + 1] = make_float4(hi2(th), hi2(tl), hi2(IW), hi2(TB));
+}
+
 // Combine chunk partials of each (ray, frequency) into Tb.
 __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
   const int ray = blockIdx.x;
@@ -238,16 +344,25 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
   const int nc = nsteps > 0 ? (nsteps + TB_CHUNK - 1) / TB_CHUNK : 0;
   float ph = 0.f, pl = 0.f;          // optical depth at the chunk start
   float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
-  for (int c = 0; c < nc; ++c) {
-    const float4 p = part[(size_t)c * a.nf];
-    const float sc = __expf(-ph) * (1.f - pl);
-    kahan_add(iw, iwc, sc * p.z);
-    kahan_add(tb, tbc, sc * p.w);
-    float s, e;
-    two_sum(ph, p.x, s, e);
-    e += pl + p.y;
-    ph = s + e;
-    pl = e - (ph - s);
+  constexpr int CB = 8;              // partials loaded together
+  for (int c0 = 0; c0 < nc; c0 += CB) {
+    float4 pb[CB];
+#pragma unroll
+    for (int k = 0; k < CB; ++k)
+      pb[k] = c0 + k < nc ? part[(size_t)(c0 + k) * a.nf] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < CB; ++k) {
+      if (c0 + k >= nc) break;
+      const float4 p = pb[k];
+      const float sc = __expf(-ph) * (1.f - pl);
+      kahan_add(iw, iwc, sc * p.z);
+      kahan_add(tb, tbc, sc * p.w);
+      float s, e;
+      two_sum(ph, p.x, s, e);
+      e += pl + p.y;
+      ph = s + e;
+      pl = e - (ph - s);
+    }
   }
   const float TbL = tb - tbc, IW = iw - iwc;
   const bool clamped = TbL < (float)T_CMB;   // off the planet or no emission: T_cmb exactly
@@ -257,17 +372,20 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
   if (a.intW) a.intW[(size_t)ray * a.nf + f] = (double)IW;
 }
 
-// Weighted sum over rays (disc quadrature), one thread per frequency,
-// compensated float32 over the rays.
+// Weighted sum over rays (disc quadrature): one warp per frequency, lane i
+// takes rays i, i + 32, ... in float64 and the warp adds the lanes' sums.
 // blockIdx.y = variant of a batch: rays [v nb, (v+1) nb), out[v][f].
-__global__ void rb_disc_avg_kernel(int nb, int nf, const float* Tb32, const double* w, double* out) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128) rb_disc_avg_kernel(int nb, int nf, const float* Tb32,
+                                                          const double* w, double* out) {
+  const int f = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (f >= nf) return;
   Tb32 += (size_t)blockIdx.y * nb * nf;
   out += (size_t)blockIdx.y * nf;
-  float s = 0.f, c = 0.f;
-  for (int r = 0; r < nb; ++r) kahan_add(s, c, (float)w[r] * Tb32[(size_t)r * nf + f]);
-  out[f] = (double)s - (double)c;
+  double s = 0.0;
+  for (int r = lane; r < nb; r += 32) s += w[r] * (double)Tb32[(size_t)r * nf + f];
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[f] = s;
 }
 
 __global__ void rb_e2_kernel(int n, const double* x, double* out) {
@@ -286,8 +404,13 @@ cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st) {
 
 cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
   if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
-  dim3 grid(a.nb, a.nchunk, (a.nf + 127) / 128);
-  rb_tb_chunk_kernel<<<grid, 128, 0, st>>>(a);
+  if (a.nf % 2 == 0) {
+    dim3 grid(a.nb, a.nchunk, (a.nf / 2 + 127) / 128);
+    rb_tb_chunk2_kernel<<<grid, 128, 0, st>>>(a);
+  } else {
+    dim3 grid(a.nb, a.nchunk, (a.nf + 127) / 128);
+    rb_tb_chunk_kernel<<<grid, 128, 0, st>>>(a);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   dim3 g2(a.nb, (a.nf + 127) / 128);
@@ -297,7 +420,7 @@ cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
 
 cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
                             cudaStream_t st, int nvar) {
-  rb_disc_avg_kernel<<<dim3((nf + 127) / 128, nvar), 128, 0, st>>>(nb, nf, Tb32, w, out);
+  rb_disc_avg_kernel<<<dim3((nf + 3) / 4, nvar), 128, 0, st>>>(nb, nf, Tb32, w, out);
   return cudaGetLastError();
 }
 
