@@ -41,6 +41,11 @@ Fixtures (all float64, ``numpy.savez_compressed``):
     other_dict / cloud dispatch) and direct module calls, on a 48-layer
     synthetic atmosphere from 1e-4 to 2500 bar with CO and a cloud table,
     the C0 NH3 line lists and the real CO lines.
+``f4.npz``
+    ``set_utils.set_b`` b lists (float grids with image blocks, a stamp,
+    line requests with and without an angle) and the text files
+    ``fileIO.FileIO.write`` produces for image, spectrum, profile and disc
+    data (frequency and wavelength axes).
 """
 import os
 import sys
@@ -452,8 +457,72 @@ def golden_f2():
     print('wrote', path)
 
 
+class _GridSpacing(float):
+    """A float grid request whose len() is 1: lets the reference's set_b
+    return its b list (its own imSize line takes len() of the float and
+    raises TypeError, set_utils.py:78)."""
+
+    def __len__(self):
+        return 1
+
+
+F4_SETB = dict(grid_a=(0.1, [1, 1]), grid_b=(0.1, [2, 4]), grid_c=(0.05, [3, 3]),
+               grid_d=(0.25, [1, 1]))
+F4_STRINGS = dict(stamp='stamp:0.1:-0.2,0.2,-0.3,0.3', line_angle='0:1.2:0.1<30',
+                  line_csv='0.1,0.5,0.9,0.999', line_flat='0:1:0.25', disc='disc')
+
+
+def golden_f4():
+    """set_b requests and the FileIO text formats from the reference."""
+    rh.import_reference()
+    from argparse import Namespace
+    from radiobear import set_utils, fileIO
+    out = {}
+    for name, (spacing, block) in F4_SETB.items():
+        rv = set_utils.set_b(_GridSpacing(spacing), block)
+        out['setb_' + name] = np.asarray(rv.b, dtype=np.float64)
+    for name, req in F4_STRINGS.items():
+        rv = set_utils.set_b(req, [1, 1], Rpol=66854.0, Req=71492.0)
+        out['setb_' + name] = np.asarray(rv.b if name != 'disc' else [[0.0, 0.0]], dtype=np.float64)
+        out['setb_' + name + '_type'] = np.array(rv.data_type)
+    rng = np.random.default_rng(44)
+    work = tempfile.mkdtemp(prefix='rbgold_f4_')
+    cwd = os.getcwd()
+    os.chdir(work)
+    os.makedirs('Scratch', exist_ok=True)
+    try:
+        hdr = {'b': '# b request:  0.25  [1, 1]', 'freqs': '# freqs request: 22.0 GHz'}
+        cases = dict(
+            image=Namespace(type='image', header=hdr, f=[22.0], freqUnit='GHz',
+                            b=[[0.0, 0.0]] * 25, Tb=(100.0 + 200.0 * rng.random((5, 5))).tolist()),
+            spectrum=Namespace(type='spectrum', header=hdr, f=[1.4, 5.0, 22.0], freqUnit='GHz',
+                               b=[[0.0, 0.0], [0.25, 0.1]],
+                               Tb=(100.0 + 300.0 * rng.random((2, 3))).tolist()),
+            profile=Namespace(type='profile', header=hdr, f=[1.4, 22.0], freqUnit='GHz',
+                              b=[[0.1 * i, 0.0] for i in range(12)],
+                              Tb=(100.0 + 300.0 * rng.random((12, 2))).tolist()),
+            disc=Namespace(type='spectrum', header=hdr, f=[1.4, 5.0], freqUnit='GHz', b=['disc'],
+                           Tb=(100.0 + 300.0 * rng.random((1, 2))).tolist()))
+        for name, data in cases.items():
+            for xaxis in ('frequency', 'wavelength'):
+                if name == 'image' and xaxis == 'wavelength':
+                    continue
+                path = os.path.join(work, '{}_{}.dat'.format(name, xaxis))
+                fileIO.FileIO().write(path, data, xaxis=xaxis)
+                with open(path) as fp:
+                    out['file_{}_{}'.format(name, xaxis)] = np.array(fp.read())
+            out['data_{}_Tb'.format(name)] = np.asarray(data.Tb, dtype=np.float64)
+            out['data_{}_f'.format(name)] = np.asarray(data.f, dtype=np.float64)
+    finally:
+        os.chdir(cwd)
+    path = os.path.join(HERE, 'f4.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
 JOBS = dict(cats=real_catalogues, bench=golden_benchmark, c0=golden_c0,
-            c1a=golden_c1_alpha, c1tb=golden_c1_tb, scale=golden_scale_cases, f2=golden_f2)
+            c1a=golden_c1_alpha, c1tb=golden_c1_tb, scale=golden_scale_cases, f2=golden_f2,
+            f4=golden_f4)
 
 if __name__ == '__main__':
     which = sys.argv[1:] or list(JOBS)
