@@ -27,6 +27,9 @@
  *   rb_brightness     Brightness.single, radiobear/brightness.py:30-126
  *   rb_forward        Planet.run's alpha_layers + b loop + bright_run,
  *                     radiobear/planet.py:59-160 (one call per spectrum set)
+ *   rb_atm_props      AtmosphereBase.computeProp, radiobear/atm_base.py:120-194
+ *   rb_regrid         regrid.regrid (regridType = number of log-P steps or a
+ *                     pressure grid), radiobear/regrid.py:11-176
  */
 #ifndef RADIOBEAR_GB300_H
 #define RADIOBEAR_GB300_H
@@ -255,6 +258,57 @@ int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t*
 /* Number of this library's kernel launches made by the last rb_forward /
  * rb_forward_device call (for launch accounting). */
 int rb_last_launch_count(rb_handle* h);
+
+/* ---- atmosphere producer (gas / cloud column tables, float64) ----------
+ * Tables are the reference's [ncol][n] column tables (n layers, pressure
+ * increasing).  roles[4] = column indices of Z (km), T (K), P (bar), DZ
+ * (cm); chem[3][ncol] = per column the molar mass (g/mol), c_p / R and the
+ * microwave refractivity constant of chemistry.ConstituentProperties (a
+ * negative refractivity selects the H2O law 245 + 1.28e6 / T); the role
+ * columns are not constituents.  Property rows (RB_PROP_*) follow the
+ * reference's LP order. */
+#define RB_PROP_Z 0
+#define RB_PROP_R 1      /* radius, km (Req at the layer nearest p_ref) */
+#define RB_PROP_P 2
+#define RB_PROP_GM 3
+#define RB_PROP_AMU 4
+#define RB_PROP_REFR 5
+#define RB_PROP_N 6      /* refractive index */
+#define RB_PROP_H 7
+#define RB_PROP_LAPSE 8
+#define RB_PROP_LAPSEP 9
+#define RB_PROP_g 10
+#define RB_NPROP 11
+#define RB_ATM_MAXCOL 32
+
+/* computeProp of one table: prop[RB_NPROP][nL] (host buffers). */
+int rb_atm_props(rb_handle* h, int nL, int ncol, const int32_t* roles, const double* chem,
+                 const double* gas, double Req, double p_ref, double GM_ref, double* prop);
+/* computeProp of nvar tables concatenated along layers (device gas
+ * [ncol][sum nL_v], prop [RB_NPROP][sum nL_v]), enqueued on `stream`. */
+int rb_atm_props_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host, int ncol,
+                        const int32_t* roles, const double* chem, const double* gas, double Req,
+                        double p_ref, double GM_ref, double* prop);
+/* regrid onto the increasing pressure grid Pgrid[nout]: linear in P inside
+ * the table; deeper, constituents at their deepest value and T, Z along a
+ * dry adiabat in hydrostatic equilibrium; above, T and Z along the last
+ * slope; Z renormalised to 0 at the deepest point and DZ reset.  The cloud
+ * table (nullable, same layers as the gas table, no chemistry) is
+ * interpolated with 0 outside.  Host buffers; gas_out [ncol][nout],
+ * cloud_out [ncl][nout]. */
+int rb_regrid(rb_handle* h, int nin, int ncol, const int32_t* roles, const double* chem,
+              const double* gas_in, int ncl, const int32_t* roles_cl, const double* cloud_in,
+              int nout, const double* Pgrid, double Req, double p_ref, double GM_ref,
+              double* gas_out, double* cloud_out);
+/* Device form for nvar tables (layer counts nin_host, concatenated along
+ * layers): every table onto nout points of its own grid pgrid + v *
+ * pgrid_stride (stride 0: one shared grid); outputs [ncol][nvar * nout]
+ * with table v at columns v * nout.  Enqueued on `stream`. */
+int rb_regrid_device(rb_handle* h, void* stream, int nvar, const int32_t* nin_host, int ncol,
+                     const int32_t* roles, const double* chem, const double* gas_in, int ncl,
+                     const int32_t* roles_cl, const double* cloud_in, int nout, const double* pgrid,
+                     int pgrid_stride, double Req, double p_ref, double GM_ref, double* gas_out,
+                     double* cloud_out);
 
 /* Phase timing.  With profiling on, rb_forward / rb_forward_device record
  * CUDA events around each kernel on the stream it is launched on;

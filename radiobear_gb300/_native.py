@@ -48,7 +48,8 @@ EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set
            'rb_forward_device', 'rb_last_launch_count', 'rb_set_profiling', 'rb_phase_times',
            'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
            'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device',
-           'rb_set_co_clouds')
+           'rb_set_co_clouds', 'rb_atm_props', 'rb_atm_props_device', 'rb_regrid',
+           'rb_regrid_device')
 
 _lib = None
 _lock = threading.Lock()
@@ -81,6 +82,15 @@ def load_library(path=None):
         lib.rb_set_lines.argtypes = [_vp, c_int, c_int, c_int, _d]
         lib.rb_set_formalisms.argtypes = [_vp, c_int, c_int, c_int, c_int, c_int, c_int]
         lib.rb_set_co_clouds.argtypes = [_vp, c_int, c_int, c_int, c_int]
+        _ip32 = ctypes.POINTER(ctypes.c_int32)
+        lib.rb_atm_props.argtypes = [_vp, c_int, c_int, _ip32, _d, _d, c_double, c_double, c_double, _d]
+        lib.rb_atm_props_device.argtypes = [_vp, _vp, c_int, _ip32, c_int, _ip32, _d, _vp, c_double,
+                                            c_double, c_double, _vp]
+        lib.rb_regrid.argtypes = [_vp, c_int, c_int, _ip32, _d, _d, c_int, _ip32, _d, c_int, _d,
+                                  c_double, c_double, c_double, _d, _d]
+        lib.rb_regrid_device.argtypes = [_vp, _vp, c_int, _ip32, c_int, _ip32, _d, _vp, c_int, _ip32,
+                                         _vp, c_int, _vp, c_int, c_double, c_double, c_double, _vp,
+                                         _vp]
         lib.rb_alpha.argtypes = [_vp, c_int, _d, _d, _d, c_int, _d, _d, c_int, _d, _d]
         lib.rb_raypath.argtypes = [_vp, c_int, _d, _d, c_double, c_double, c_double, c_double,
                                    c_int, c_int, c_int, _d, c_int, _i, _d, _i, _d, _d, _i]

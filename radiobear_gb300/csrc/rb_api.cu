@@ -125,6 +125,7 @@ struct rb_handle {
   int nco = 0;
   DBuf d_co_f0, d_co_I0, d_co_E;
   DBuf d_extra, d_xgrad;   // [2][nL][nf] co / cloud absorption; [nL][2] their adjoint
+  DBuf d_agas, d_acl, d_aout, d_aclout, d_aprop, d_agrid, d_aoff;   // atmosphere producer
   // frequency plan
   std::vector<double> plan_f;
   int plan_M = 0, plan_W = 0, plan_spt = 0, plan_ntile = 0, plan_nslot = 0, plan_ntmpl = 0;
@@ -158,6 +159,8 @@ namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
 cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st);
 cudaError_t launch_extra(const ExtraArgs& a, cudaStream_t st);
+cudaError_t launch_atm_props(const AtmPropArgs& a, int nvar, cudaStream_t st);
+cudaError_t launch_atm_regrid(const AtmRegridArgs& a, int nvar, cudaStream_t st);
 int alpha_lines_occupancy(int M, int W);
 cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
                            const ExtraArgs* ea, float* galpha,
@@ -668,7 +671,8 @@ int rb_destroy(rb_handle* h) {
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
                   &h->d_done, &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,
                   &h->d_adjS, &h->d_voff, &h->d_co_f0, &h->d_co_I0, &h->d_co_E, &h->d_extra,
-                  &h->d_xgrad})
+                  &h->d_xgrad, &h->d_agas, &h->d_acl, &h->d_aout, &h->d_aclout, &h->d_aprop,
+                  &h->d_agrid, &h->d_aoff})
     b->release();
   for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
@@ -1400,6 +1404,176 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
 }
 
 int rb_last_launch_count(rb_handle* h) { return h ? h->launches : 0; }
+
+// ------------------------------------------------------------ atmosphere producer
+// Column roles [Z, T, P, DZ] and chemistry [3][ncol] (amu, c_p / R, refr)
+// -> the kernel's column description.
+static int atm_cols(int ncol, const int32_t* roles, const double* chem, rb::AtmCols& c) {
+  if (ncol < 4 || ncol > rb::ATM_MAXCOL) return fail(RB_EINVAL, "ncol must be in 4..%d", rb::ATM_MAXCOL);
+  if (!roles) return fail(RB_EINVAL, "null column roles");
+  for (int r = 0; r < 4; ++r)
+    if (roles[r] < 0 || roles[r] >= ncol) return fail(RB_EINVAL, "column role %d out of range", r);
+  c.ncol = ncol;
+  c.iz = roles[0];
+  c.it = roles[1];
+  c.ip = roles[2];
+  c.idz = roles[3];
+  for (int k = 0; k < ncol; ++k) {
+    c.amu[k] = chem ? chem[k] : 0.0;
+    c.cp[k] = chem ? chem[ncol + k] : 0.0;
+    c.refr[k] = chem ? chem[2 * ncol + k] : 0.0;
+  }
+  if (chem && !finite_all(chem, 3 * (size_t)ncol)) return fail(RB_EINVAL, "chemistry not finite");
+  return RB_OK;
+}
+
+static int atm_check_table(int n, int ncol, int ip, int it, const double* tab, bool need_T) {
+  if (!finite_all(tab, (size_t)ncol * n)) return fail(RB_EINVAL, "table has non-finite entries");
+  const double* P = tab + (size_t)ip * n;
+  for (int i = 0; i < n; ++i) {
+    if (!(P[i] > 0.0)) return fail(RB_EINVAL, "P[%d] must be > 0", i);
+    if (i && !(P[i] > P[i - 1])) return fail(RB_EINVAL, "P must increase (layer %d)", i);
+    if (need_T && !(tab[(size_t)it * n + i] > 0.0)) return fail(RB_EINVAL, "T[%d] must be > 0", i);
+  }
+  return RB_OK;
+}
+
+static int atm_offsets(rb_handle* h, int nvar, const int32_t* n_host, int minn, int& tot) {
+  if (nvar < 1 || !n_host) return fail(RB_EINVAL, "need nvar >= 1 and layer counts");
+  std::vector<int> off(nvar + 1, 0);
+  for (int v = 0; v < nvar; ++v) {
+    if (n_host[v] < minn) return fail(RB_EINVAL, "atmosphere %d has %d layers (need >= %d)", v, n_host[v], minn);
+    off[v + 1] = off[v] + n_host[v];
+  }
+  RB_CUDA(upload(h->d_aoff, off.data(), off.size(), h->st));
+  RB_CUDA(cudaStreamSynchronize(h->st));
+  tot = off[nvar];
+  return RB_OK;
+}
+
+int rb_atm_props_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host, int ncol,
+                        const int32_t* roles, const double* chem, const double* gas, double Req,
+                        double p_ref, double GM_ref, double* prop) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!gas || !prop) return fail(RB_EINVAL, "null array");
+  rb::AtmPropArgs a{};
+  int rc;
+  if ((rc = atm_cols(ncol, roles, chem, a.cols))) return rc;
+  RB_CUDA(cudaSetDevice(h->device));
+  int tot = 0;
+  if ((rc = atm_offsets(h, nvar, nL_host, 1, tot))) return rc;
+  a.gas = gas;
+  a.ld = tot;
+  a.off = h->d_aoff.as<int>();
+  a.Req = Req;
+  a.p_ref = p_ref;
+  a.GM_ref = GM_ref;
+  a.prop = prop;
+  RB_CUDA(rb::launch_atm_props(a, nvar, reinterpret_cast<cudaStream_t>(stream)));
+  h->launches = 1;
+  return RB_OK;
+}
+
+int rb_atm_props(rb_handle* h, int nL, int ncol, const int32_t* roles, const double* chem,
+                 const double* gas, double Req, double p_ref, double GM_ref, double* prop) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!gas || !prop) return fail(RB_EINVAL, "null array");
+  if (nL < 1) return fail(RB_EINVAL, "nL must be >= 1");
+  rb::AtmCols c{};
+  int rc;
+  if ((rc = atm_cols(ncol, roles, chem, c))) return rc;
+  if ((rc = atm_check_table(nL, ncol, c.ip, c.it, gas, true))) return rc;
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  RB_CUDA(upload(h->d_agas, gas, (size_t)ncol * nL, st));
+  RB_CUDA(h->d_aprop.ensure(sizeof(double) * rb::NPROP * (size_t)nL));
+  const int32_t n1 = nL;
+  if ((rc = rb_atm_props_device(h, st, 1, &n1, ncol, roles, chem, h->d_agas.as<double>(), Req, p_ref,
+                                GM_ref, h->d_aprop.as<double>())))
+    return rc;
+  RB_CUDA(cudaMemcpyAsync(prop, h->d_aprop.p, sizeof(double) * rb::NPROP * (size_t)nL,
+                          cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
+
+int rb_regrid_device(rb_handle* h, void* stream, int nvar, const int32_t* nin_host, int ncol,
+                     const int32_t* roles, const double* chem, const double* gas_in, int ncl,
+                     const int32_t* roles_cl, const double* cloud_in, int nout, const double* pgrid,
+                     int pgrid_stride, double Req, double p_ref, double GM_ref, double* gas_out,
+                     double* cloud_out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!gas_in || !gas_out || !pgrid) return fail(RB_EINVAL, "null array");
+  if (nout < 2) return fail(RB_EINVAL, "nout must be >= 2");
+  if (pgrid_stride != 0 && pgrid_stride < nout) return fail(RB_EINVAL, "pgrid_stride must be 0 or >= nout");
+  if ((cloud_in == nullptr) != (cloud_out == nullptr)) return fail(RB_EINVAL, "cloud_in and cloud_out go together");
+  rb::AtmRegridArgs a{};
+  int rc;
+  if ((rc = atm_cols(ncol, roles, chem, a.cols))) return rc;
+  if (cloud_in && (rc = atm_cols(ncl, roles_cl, nullptr, a.cloud_cols))) return rc;
+  RB_CUDA(cudaSetDevice(h->device));
+  int tot = 0;
+  if ((rc = atm_offsets(h, nvar, nin_host, 2, tot))) return rc;
+  a.gas_in = gas_in;
+  a.cloud_in = cloud_in;
+  a.ld_in = tot;
+  a.in_off = h->d_aoff.as<int>();
+  a.nout = nout;
+  a.pgrid = pgrid;
+  a.pgrid_stride = pgrid_stride;
+  a.ld_out = nvar * nout;
+  a.Req = Req;
+  a.p_ref = p_ref;
+  a.GM_ref = GM_ref;
+  a.gas_out = gas_out;
+  a.cloud_out = cloud_out;
+  RB_CUDA(rb::launch_atm_regrid(a, nvar, reinterpret_cast<cudaStream_t>(stream)));
+  h->launches = 1;
+  return RB_OK;
+}
+
+int rb_regrid(rb_handle* h, int nin, int ncol, const int32_t* roles, const double* chem,
+              const double* gas_in, int ncl, const int32_t* roles_cl, const double* cloud_in,
+              int nout, const double* Pgrid, double Req, double p_ref, double GM_ref,
+              double* gas_out, double* cloud_out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (!gas_in || !gas_out || !Pgrid) return fail(RB_EINVAL, "null array");
+  if (nin < 2 || nout < 2) return fail(RB_EINVAL, "need >= 2 input layers and grid points");
+  rb::AtmCols c{}, cl{};
+  int rc;
+  if ((rc = atm_cols(ncol, roles, chem, c))) return rc;
+  if ((rc = atm_check_table(nin, ncol, c.ip, c.it, gas_in, true))) return rc;
+  if (cloud_in) {
+    if ((rc = atm_cols(ncl, roles_cl, nullptr, cl))) return rc;
+    if ((rc = atm_check_table(nin, ncl, cl.ip, cl.it, cloud_in, false))) return rc;
+  }
+  for (int i = 0; i < nout; ++i) {
+    if (!(Pgrid[i] > 0.0) || !std::isfinite(Pgrid[i])) return fail(RB_EINVAL, "Pgrid[%d] must be > 0", i);
+    if (i && !(Pgrid[i] > Pgrid[i - 1])) return fail(RB_EINVAL, "Pgrid must increase");
+  }
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  RB_CUDA(upload(h->d_agas, gas_in, (size_t)ncol * nin, st));
+  RB_CUDA(upload(h->d_agrid, Pgrid, (size_t)nout, st));
+  RB_CUDA(h->d_aout.ensure(sizeof(double) * (size_t)ncol * nout));
+  if (cloud_in) {
+    RB_CUDA(upload(h->d_acl, cloud_in, (size_t)ncl * nin, st));
+    RB_CUDA(h->d_aclout.ensure(sizeof(double) * (size_t)ncl * nout));
+  }
+  const int32_t n1 = nin;
+  if ((rc = rb_regrid_device(h, st, 1, &n1, ncol, roles, chem, h->d_agas.as<double>(), ncl, roles_cl,
+                             cloud_in ? h->d_acl.as<double>() : nullptr, nout,
+                             h->d_agrid.as<double>(), 0, Req, p_ref, GM_ref, h->d_aout.as<double>(),
+                             cloud_in ? h->d_aclout.as<double>() : nullptr)))
+    return rc;
+  RB_CUDA(cudaMemcpyAsync(gas_out, h->d_aout.p, sizeof(double) * (size_t)ncol * nout,
+                          cudaMemcpyDeviceToHost, st));
+  if (cloud_in)
+    RB_CUDA(cudaMemcpyAsync(cloud_out, h->d_aclout.p, sizeof(double) * (size_t)ncl * nout,
+                            cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
 
 int rb_set_profiling(rb_handle* h, int on) {
   if (!h) return fail(RB_EINVAL, "null handle");

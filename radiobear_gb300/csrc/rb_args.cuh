@@ -79,6 +79,46 @@ struct AlphaArgs {
   const double* extra;      // [2][nL][nf] co_ddb, clouds_idp in cm^-1 (or null)
 };
 
+// Atmosphere tables (rb_atm.cu): the reference's column tables [ncol][n]
+// with the roles of the Z, T, P and DZ columns and per-column chemistry of
+// chemistry.ConstituentProperties (amu g/mol, c_p / R, refractivity
+// constant; refr < 0 selects the H2O law 245 + 1.28e6 / T).
+constexpr int ATM_MAXCOL = 32;
+struct AtmCols {
+  int ncol, iz, it, ip, idz;
+  double amu[ATM_MAXCOL], cp[ATM_MAXCOL], refr[ATM_MAXCOL];
+};
+
+// Property rows of AtmosphereBase.computeProp (config LP order).
+enum PropRow : int {
+  PROP_Z = 0, PROP_R = 1, PROP_P = 2, PROP_GM = 3, PROP_AMU = 4, PROP_REFR = 5, PROP_N = 6,
+  PROP_H = 7, PROP_LAPSE = 8, PROP_LAPSEP = 9, PROP_g = 10, NPROP = 11
+};
+
+struct AtmPropArgs {
+  AtmCols cols;
+  const double* gas;     // [ncol][ld]
+  int ld;                // layers of all atmospheres (column stride)
+  const int* off;        // [nvar + 1] layer offsets, or null for one table of ld layers
+  double Req, p_ref, GM_ref;
+  double* prop;          // [NPROP][ld]
+};
+
+struct AtmRegridArgs {
+  AtmCols cols, cloud_cols;
+  const double* gas_in;    // [ncol][ld_in]
+  const double* cloud_in;  // [ncol_cloud][ld_in] (same layers as gas) or null
+  int ld_in;
+  const int* in_off;       // [nvar + 1]
+  int nout;                // grid points per atmosphere
+  const double* pgrid;     // [nvar][pgrid_stride] increasing pressures (stride 0: shared)
+  int pgrid_stride;
+  int ld_out;              // nvar * nout
+  double Req, p_ref, GM_ref;
+  double* gas_out;         // [ncol][ld_out], atmosphere v at v * nout
+  double* cloud_out;       // [ncol_cloud][ld_out] or null
+};
+
 // Closed-form absorbers co_ddb (constituents/co/co_ddb.py) and clouds_idp
 // (constituents/clouds/clouds_idp.py), float64, one thread per (layer,
 // frequency).  The forward writes out; the adjoint contracts d loss / d

@@ -248,37 +248,58 @@ __device__ __forceinline__ void kahan_add2(f2& s, f2& c, f2 v) {
   s = t;
 }
 
+// Lanes per item of the packed scan: frequency pairs (a power of two in
+// [4, 128]); a CTA of 128 threads takes 128 / lanes (ray, chunk) items so
+// that few frequencies still fill it.
+__host__ __device__ __forceinline__ int scan_lanes(int npair) {
+  int l = 4;
+  while (l < npair && l < 128) l <<= 1;
+  return l;
+}
+constexpr int SCAN_ITEM_WORDS = 3 * TB_CHUNK + 2;   // staged words per item
+
 __global__ void __launch_bounds__(128) rb_tb_chunk2_kernel(TbArgs a) {
-  const int ray = blockIdx.x;
-  const int ch = blockIdx.y;
-  const int f = 2 * (blockIdx.z * blockDim.x + threadIdx.x);   // first of the pair
-  const int nseg = a.nseg[ray];
-  const int nsteps = nseg - 1;
-  const int i0 = ch * TB_CHUNK;
-  float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
-  if (i0 >= nsteps) {
-    if (f < a.nf) {
-      part[f] = make_float4(0.f, 0.f, 0.f, 0.f);
-      part[f + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    return;
+  const int npair = a.nf / 2;
+  const int FP = scan_lanes(npair);
+  const int IPB = 128 / FP;
+  const int sub = threadIdx.x / FP, fl = threadIdx.x % FP;
+  const long long item = (long long)blockIdx.x * IPB + sub;
+  const long long nitem = (long long)a.nb * a.nchunk;
+  // per item: offsets, T (TB_CHUNK + 1 each) and ds / 2 (TB_CHUNK)
+  extern __shared__ __align__(16) int s_scan[];
+  int ray = 0, ch = 0, n = 0, i0 = 0;
+  bool live = false;
+  if (item < nitem) {
+    ray = (int)(item / a.nchunk);
+    ch = (int)(item % a.nchunk);
+    const int nsteps = a.nseg[ray] - 1;
+    i0 = ch * TB_CHUNK;
+    live = i0 < nsteps;
+    n = live ? min(TB_CHUNK, nsteps - i0) : 0;
   }
-  const int n = min(TB_CHUNK, nsteps - i0);
-  __shared__ int s_off[TB_CHUNK + 1];
-  __shared__ float s_T[TB_CHUNK + 1];
-  __shared__ float s_hd[TB_CHUNK];
-  const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
-  const int* lay = a.layer + (size_t)ray * a.max_seg + i0;
-  int off, nLr;
-  ray_layers(a, ray, off, nLr);
-  for (int t = threadIdx.x; t <= n; t += blockDim.x) {
-    const int l = off + wrap_layer(lay[t], nLr);
-    s_off[t] = l * a.nf;
-    s_T[t] = a.T32[l];
-    if (t < n) s_hd[t] = hds[t];
+  const int f = 2 * (blockIdx.z * FP + fl);   // first of the pair
+  float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
+  if (item < nitem && !live && f < a.nf) {     // chunk past the end of this ray
+    part[f] = make_float4(0.f, 0.f, 0.f, 0.f);
+    part[f + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  int* s_off = s_scan + sub * SCAN_ITEM_WORDS;
+  float* s_T = reinterpret_cast<float*>(s_off + TB_CHUNK + 1);
+  float* s_hd = s_T + TB_CHUNK + 1;
+  if (live) {
+    const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
+    const int* lay = a.layer + (size_t)ray * a.max_seg + i0;
+    int off, nLr;
+    ray_layers(a, ray, off, nLr);
+    for (int t = fl; t <= n; t += FP) {
+      const int l = off + wrap_layer(lay[t], nLr);
+      s_off[t] = l * a.nf;
+      s_T[t] = a.T32[l];
+      if (t < n) s_hd[t] = hds[t];
+    }
   }
   __syncthreads();
-  if (f >= a.nf) return;
+  if (!live || f >= a.nf) return;
   const float* al = a.alpha32 + f;
   auto ld = [&](int o) -> f2 { return *reinterpret_cast<const f2*>(al + o); };
   f2 th = 0ull, tl = 0ull;
@@ -335,10 +356,17 @@ __global__ void __launch_bounds__(128) rb_tb_chunk2_kernel(TbArgs a) {
 }
 
 // Combine chunk partials of each (ray, frequency) into Tb.
+__host__ __device__ __forceinline__ int combine_lanes(int nf) {
+  int l = 8;
+  while (l < nf && l < 128) l <<= 1;
+  return l;
+}
+
 __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
-  const int ray = blockIdx.x;
-  const int f = blockIdx.y * blockDim.x + threadIdx.x;
-  if (f >= a.nf) return;
+  const int FT = combine_lanes(a.nf);
+  const int ray = blockIdx.x * (128 / FT) + threadIdx.x / FT;
+  const int f = blockIdx.y * FT + threadIdx.x % FT;
+  if (ray >= a.nb || f >= a.nf) return;
   const float4* part = a.part + (size_t)ray * a.nchunk * a.nf + f;
   const int nsteps = a.nseg[ray] - 1;
   const int nc = nsteps > 0 ? (nsteps + TB_CHUNK - 1) / TB_CHUNK : 0;
@@ -405,15 +433,20 @@ cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st) {
 cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
   if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
   if (a.nf % 2 == 0) {
-    dim3 grid(a.nb, a.nchunk, (a.nf / 2 + 127) / 128);
-    rb_tb_chunk2_kernel<<<grid, 128, 0, st>>>(a);
+    const int FP = scan_lanes(a.nf / 2);
+    const long long nitem = (long long)a.nb * a.nchunk;
+    const long long nblk = (nitem + 128 / FP - 1) / (128 / FP);
+    dim3 grid((unsigned)nblk, 1, (a.nf / 2 + FP - 1) / FP);
+    const size_t smem = sizeof(int) * SCAN_ITEM_WORDS * (128 / FP);
+    rb_tb_chunk2_kernel<<<grid, 128, smem, st>>>(a);
   } else {
     dim3 grid(a.nb, a.nchunk, (a.nf + 127) / 128);
     rb_tb_chunk_kernel<<<grid, 128, 0, st>>>(a);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  dim3 g2(a.nb, (a.nf + 127) / 128);
+  const int FT = combine_lanes(a.nf);
+  dim3 g2((a.nb + 128 / FT - 1) / (128 / FT), (a.nf + FT - 1) / FT);
   rb_tb_combine_kernel<<<g2, 128, 0, st>>>(a);
   return cudaGetLastError();
 }

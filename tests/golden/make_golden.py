@@ -41,6 +41,10 @@ Fixtures (all float64, ``numpy.savez_compressed``):
     other_dict / cloud dispatch) and direct module calls, on a 48-layer
     synthetic atmosphere from 1e-4 to 2500 bar with CO and a cloud table,
     the C0 NH3 line lists and the real CO lines.
+``f3.npz``
+    ``AtmosphereBase.computeProp`` and ``regrid.regrid`` (interpolation
+    inside the table, inward dry-adiabat and outward slope extrapolation)
+    on an 80-layer synthetic gas + cloud table.
 ``f4.npz``
     ``set_utils.set_b`` b lists (float grids with image blocks, a stamp,
     line requests with and without an angle) and the text files
@@ -520,9 +524,66 @@ def golden_f4():
     print('wrote', path)
 
 
+def f3_tables(nL=80, Pmin=1.0e-2, Pmax=300.0):
+    """Gas and cloud tables of the f3 fixture (the C1 recipe, cloud decks)."""
+    gas = synth.make_gas_table(nL, Pmin, Pmax)
+    C = {k: i for i, k in enumerate(synth.GAS_COLUMNS)}
+    gas[C['CO']] = 1.0e-7
+    Cl = {k: i for i, k in enumerate(synth.CLOUD_COLUMNS)}
+    cloud = np.zeros((len(synth.CLOUD_COLUMNS), nL))
+    for k in ('Z', 'T', 'P'):
+        cloud[Cl[k]] = gas[C[k]]
+    P = gas[C['P']]
+    cloud[Cl['NH3']] = np.where((P > 0.4) & (P < 1.0), 2.0e-4, 0.0)
+    cloud[Cl['H2O']] = np.where((P > 4.0) & (P < 8.0), 5.0e-4, 0.0)
+    cloud[Cl['DZ']] = np.append(0.0, np.abs(np.diff(cloud[Cl['Z']])) * 1e5)
+    return gas, C, cloud, Cl
+
+
+def golden_f3():
+    """AtmosphereBase.computeProp and regrid.regrid on synthetic tables,
+    run through the reference's own functions bound to a minimal atmosphere
+    object (gas, cloud, config)."""
+    rh.import_reference()
+    import types
+    from argparse import Namespace
+    import radiobear.regrid as rregrid
+    from radiobear.atm_base import AtmosphereBase
+    LP = {k: i for i, k in enumerate(synth.PROPERTY_COLUMNS)}
+    J = synth.JUPITER
+    out = {}
+
+    def make_atm(gas, C, cloud, Cl):
+        atm = Namespace(gas=np.array(gas), cloud=np.array(cloud),
+                        config=Namespace(C=C, Cl=Cl, LP=LP, p_ref=J['p_ref'], Req=J['Req'],
+                                         GM_ref=J['GM_ref'], regridType='none', path='.'))
+        atm.computeProp = types.MethodType(AtmosphereBase.computeProp, atm)
+        atm._renorm_z = types.MethodType(AtmosphereBase._renorm_z, atm)
+        return atm
+
+    gas, C, cloud, Cl = f3_tables()
+    out['gas_in'] = gas
+    out['cloud_in'] = cloud
+    atm = make_atm(gas, C, cloud, Cl)
+    atm.computeProp()
+    out['prop_in'] = np.asarray(atm.property, dtype=np.float64)
+    cases = dict(inside=(200, 0, 0), extend=(250, 3.0e-3, 1000.0), deeper=(120, 1.0e-2, 2000.0))
+    for name, (n, pmin, pmax) in cases.items():
+        atm = make_atm(gas, C, cloud, Cl)
+        rregrid.regrid(atm, regridType=n, Pmin=pmin or None, Pmax=pmax or None)
+        out['gas_' + name] = np.asarray(atm.gas, dtype=np.float64)
+        out['cloud_' + name] = np.asarray(atm.cloud, dtype=np.float64)
+        atm.computeProp()
+        out['prop_' + name] = np.asarray(atm.property, dtype=np.float64)
+        out['case_' + name] = np.array([n, pmin, pmax], dtype=np.float64)
+    path = os.path.join(HERE, 'f3.npz')
+    np.savez_compressed(path, **out)
+    print('wrote', path)
+
+
 JOBS = dict(cats=real_catalogues, bench=golden_benchmark, c0=golden_c0,
             c1a=golden_c1_alpha, c1tb=golden_c1_tb, scale=golden_scale_cases, f2=golden_f2,
-            f4=golden_f4)
+            f3=golden_f3, f4=golden_f4)
 
 if __name__ == '__main__':
     which = sys.argv[1:] or list(JOBS)
