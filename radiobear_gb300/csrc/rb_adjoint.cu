@@ -669,7 +669,7 @@ __device__ __forceinline__ void br_eval(float F, float FL, float g, float z, flo
 // Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
 // sweeps lines g, g + NG, ... of every chunk and the groups' sums are added
 // per family.
-__global__ void __launch_bounds__(256, 2) rb_alpha_jvp_kernel(JvpArgs a) {
+__global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
   __shared__ __align__(16) JvpShared sh;
   __shared__ float s_grp[256][4];
   const int L = blockIdx.x;

@@ -161,7 +161,7 @@ __device__ __forceinline__ df df_sqrt(df a) {
 __device__ __forceinline__ float df_val(df a) { return a.h + a.l; }
 __device__ __forceinline__ double df_d(df a) { return (double)a.h + (double)a.l; }
 
-__global__ void __launch_bounds__(32) rb_raypath_kernel(RayArgs a) {
+__global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
   const int ray = blockIdx.x;
   const int lane = threadIdx.x;
   if (ray >= a.nb) return;
