@@ -96,9 +96,10 @@ def load_library(path=None):
                                    c_int, c_int, c_int, _d, c_int, _i, _d, _i, _d, _d, _i]
         lib.rb_brightness.argtypes = [_vp, c_int, _d, c_int, _d, c_int, _i, _d, _i, c_int, c_int,
                                       _d, _d, _d, _d, _d]
-        lib.rb_forward.argtypes = [_vp, c_int, _d, _d, _d, _d, _d, c_int, _d, _d, c_double,
-                                   c_double, c_double, c_double, c_int, c_int, c_int, _d, _d,
-                                   c_int, _d, _d, _d]
+        # host arrays as addresses (numpy .ctypes.data): cheaper per call than pointer objects
+        lib.rb_forward.argtypes = [_vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _vp, _vp, c_double,
+                                   c_double, c_double, c_double, c_int, c_int, c_int, _vp, _vp,
+                                   c_int, _vp, _vp, _vp]
         lib.rb_forward_device.argtypes = [_vp, _vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _d, _vp,
                                           c_double, c_double, c_double, c_double, c_int, c_int,
                                           c_int, _vp, _vp, c_int, _vp, _vp]
@@ -108,9 +109,9 @@ def load_library(path=None):
         lib.rb_phase_times.argtypes = [_vp, _d, c_int]
         lib.rb_probe_fp32_peak.argtypes = [_vp, _d]
         lib.rb_set_alpha_tiling.argtypes = [_vp, c_int, c_int, c_int]
-        lib.rb_adjoint.argtypes = [_vp, c_int, _d, _d, _d, _d, _d, c_int, _d, _d, c_double, c_double,
-                                   c_double, c_double, c_int, c_int, c_int, _d, _d, _d, _d, _d, _d,
-                                   _d, _d]
+        lib.rb_adjoint.argtypes = [_vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _vp, _vp, c_double,
+                                   c_double, c_double, c_double, c_int, c_int, c_int, _vp, _vp, _vp,
+                                   _vp, _vp, _vp, _vp, _vp]
         _ip = ctypes.POINTER(ctypes.c_int32)
         lib.rb_forward_batch_device.argtypes = [_vp, _vp, c_int, _ip, _vp, _vp, _vp, _vp, _vp, c_int, _d,
                                                 c_double, c_double, c_double, c_double, c_int, c_int,
@@ -136,6 +137,11 @@ def _ptr(a, ctype=ctypes.c_double):
 
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _addr(a):
+    """Address of a contiguous numpy array (None stays None)."""
+    return None if a is None else a.ctypes.data
 
 
 def _check(lib, rc, what):
@@ -265,10 +271,10 @@ class Engine:
         Tb = np.empty((nb, nf)) if want_rays else None
         avg = np.empty(nf) if w is not None else None
         lay = np.empty((nf, nL)) if want_layers else None
-        rc = self.lib.rb_forward(self._h, nL, _ptr(P), _ptr(T), _ptr(X), _ptr(R), _ptr(N), nf,
-                                 _ptr(f), _ptr(sc), float(Req), float(Rpol), float(orientation[0]),
-                                 float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _ptr(b),
-                                 _ptr(w), int(disc), _ptr(Tb), _ptr(avg), _ptr(lay))
+        rc = self.lib.rb_forward(self._h, nL, _addr(P), _addr(T), _addr(X), _addr(R), _addr(N), nf,
+                                 _addr(f), _addr(sc), float(Req), float(Rpol), float(orientation[0]),
+                                 float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _addr(b),
+                                 _addr(w), int(disc), _addr(Tb), _addr(avg), _addr(lay))
         _check(self.lib, rc, 'rb_forward')
         return dict(Tb=Tb, Tb_avg=avg, layers=lay)
 
@@ -308,11 +314,11 @@ class Engine:
         Tb = np.empty((nb, nf))
         avg = np.empty(nf) if w is not None else None
         dT, dP, dlnX = np.empty(nL), np.empty(nL), np.empty((3, nL))
-        rc = self.lib.rb_adjoint(self._h, nL, _ptr(P), _ptr(T), _ptr(X), _ptr(R), _ptr(N), nf,
-                                 _ptr(f), _ptr(sc), float(Req), float(Rpol), float(orientation[0]),
-                                 float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _ptr(b),
-                                 _ptr(w), _ptr(g), _ptr(Tb), _ptr(avg), _ptr(dT), _ptr(dP),
-                                 _ptr(dlnX))
+        rc = self.lib.rb_adjoint(self._h, nL, _addr(P), _addr(T), _addr(X), _addr(R), _addr(N), nf,
+                                 _addr(f), _addr(sc), float(Req), float(Rpol), float(orientation[0]),
+                                 float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _addr(b),
+                                 _addr(w), _addr(g), _addr(Tb), _addr(avg), _addr(dT), _addr(dP),
+                                 _addr(dlnX))
         _check(self.lib, rc, 'rb_adjoint')
         return dict(Tb=Tb, Tb_avg=avg, dT=dT, dP=dP, dlnX=dlnX)
 

@@ -1102,20 +1102,18 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
                double* Tb_avg, double* layers_out) {
   if (!h) return fail(RB_EINVAL, "null handle");
   if (!P || !T || !X || !R || !N || !freqs || (nb > 0 && !b)) return fail(RB_EINVAL, "null input array");
-  int rc = validate_atm(nL, P, T, X);
-  if (rc) return rc;
+  if (nL < 1) return fail(RB_EINVAL, "nL must be >= 1");
+  if (nb < 0) return fail(RB_EINVAL, "nb must be >= 0");
+  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
   std::vector<double> bb;
   if (disc) {  // 'disc' evaluates the nadir ray (brightness.py:32-34)
     bb.assign(2 * (size_t)nb, 0.0);
     b = bb.data();
   }
-  if ((rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b))) return rc;
-  if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
-  if (weights && !finite_all(weights, nb)) return fail(RB_EINVAL, "weights not finite");
-  if (scale && !finite_all(scale, (size_t)nL * rb::NGAS)) return fail(RB_EINVAL, "scale not finite");
   RB_CUDA(cudaSetDevice(h->device));
   cudaStream_t st = h->st;
-  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  // the copies run while the inputs are validated; nothing is launched on
+  // them before validation passes, and an error waits for the copies
   RB_CUDA(upload(h->d_P, P, nL, st));
   RB_CUDA(upload(h->d_T, T, nL, st));
   RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
@@ -1132,6 +1130,15 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
     RB_CUDA(upload(h->d_w, weights, nb, st));
     dw = h->d_w.as<double>();
   }
+  int rc = validate_atm(nL, P, T, X);
+  if (!rc) rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
+  if (!rc && weights && !finite_all(weights, nb)) rc = fail(RB_EINVAL, "weights not finite");
+  if (!rc && scale && !finite_all(scale, (size_t)nL * rb::NGAS)) rc = fail(RB_EINVAL, "scale not finite");
+  if (rc) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * std::max((size_t)nb * nf, (size_t)1)));
   RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
   double* dl = nullptr;
@@ -1355,16 +1362,12 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
   if (!h) return fail(RB_EINVAL, "null handle");
   if (!P || !T || !X || !R || !N || !freqs || !grad || !dT || !dP || !dlnX || (nb > 0 && !b))
     return fail(RB_EINVAL, "null array");
-  int rc = validate_atm(nL, P, T, X);
-  if (rc) return rc;
-  if ((rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b))) return rc;
+  if (nL < 1) return fail(RB_EINVAL, "nL must be >= 1");
   if (nb < 1) return fail(RB_EINVAL, "nb must be >= 1");
-  if (weights && !finite_all(weights, nb)) return fail(RB_EINVAL, "weights not finite");
-  if (!finite_all(grad, weights ? (size_t)nf : (size_t)nb * nf)) return fail(RB_EINVAL, "grad not finite");
-  if (scale && !finite_all(scale, (size_t)nL * rb::NGAS)) return fail(RB_EINVAL, "scale not finite");
+  if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
   RB_CUDA(cudaSetDevice(h->device));
   cudaStream_t st = h->st;
-  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  // the copies run while the inputs are validated (see rb_forward)
   RB_CUDA(upload(h->d_P, P, nL, st));
   RB_CUDA(upload(h->d_T, T, nL, st));
   RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
@@ -1382,6 +1385,16 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
     RB_CUDA(upload(h->d_w, weights, nb, st));
     dw = h->d_w.as<double>();
   }
+  int rc = validate_atm(nL, P, T, X);
+  if (!rc) rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
+  if (!rc && weights && !finite_all(weights, nb)) rc = fail(RB_EINVAL, "weights not finite");
+  if (!rc && !finite_all(grad, weights ? (size_t)nf : (size_t)nb * nf)) rc = fail(RB_EINVAL, "grad not finite");
+  if (!rc && scale && !finite_all(scale, (size_t)nL * rb::NGAS)) rc = fail(RB_EINVAL, "scale not finite");
+  if (rc) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
   RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
   RB_CUDA(h->d_dth.ensure(sizeof(double) * 5 * (size_t)nL));
