@@ -15,10 +15,10 @@
 //                            packed in pairs as f32x2; each thread sweeps
 //                            them for M frequency slots ("chains") with
 //                            packed f32x2 arithmetic, two line pairs sharing
-//                            one reciprocal, Kahan-compensated every 16
+//                            one reciprocal, Kahan-compensated every 64
 //                            lines.  One float per (item, slot) goes to a
-//                            scratch table; the CTA finishing the last item
-//                            of a (layer, tile) assembles it: family sums,
+//                            scratch table.
+//   rb_alpha_assemble_kernel one thread per (layer, slot): family sums,
 //                            prefactors (mantissa x 2^exponent), units,
 //                            clamp, blend and scaling; float32 total for the
 //                            brightness scan, optional float64 outputs.
@@ -194,8 +194,6 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
       o.use_sjs = use_sjs;
       o.blendW = blendW;
       for (int g = 0; g < NGAS; ++g) o.scale[g] = a.scale ? (float)a.scale[(size_t)L * NGAS + g] : 1.f;
-      if (a.done)
-        for (int t = 0; t < a.ntile; ++t) a.done[(size_t)L * a.ntile + t] = 0;
       // H2 CIA (h2_jj_ddb.py:7-38)
       const float th = 273.f / T;
       const float lth = log2f(th);
@@ -936,8 +934,8 @@ __device__ __forceinline__ void sjs_item(const AlphaArgs& a, Chunk (&buf)[2][2],
 }
 
 // ------------------------------------------------------------------ assembly
-// Sum of the items of one family for one slot (read through L2: the items
-// were written by other CTAs).
+// Sum of the items of one family for one slot, in template order (the
+// items were written by the line-sum kernel launched before).
 __device__ __forceinline__ float fam_sum(const AlphaArgs& a, const float* r, int fam) {
   float v = 0.f;
 #pragma unroll 4
@@ -998,79 +996,57 @@ __device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int til
 // ------------------------------------------------------------------ kernels
 // Persistent line-sum kernel: every CTA takes items from a.counter until
 // none are left.  Item i -> template entry i / (nL ntile), then layers deep
-// to shallow, then tiles; template entries come heaviest family first.  The
-// CTA that finishes the last item of a (layer, tile) assembles it (counter
-// a.done after a memory fence; nothing waits on another CTA).
+// to shallow, then tiles; template entries come heaviest family first, so
+// the queue ends with the smallest items.  Each item writes its per-slot
+// sums; rb_alpha_assemble_kernel, launched next, assembles them.
 template <int M>
 __global__ void __launch_bounds__(128, M >= 4 ? 4 : 6) rb_alpha_lines_kernel(AlphaArgs a) {
   __shared__ __align__(16) Chunk buf[2][2];   // [double buffer][coefficient set]
-  __shared__ int s_item[2], s_asm[2];
-  __shared__ int s_last;
+  __shared__ int s_item[2];
   __shared__ float s_red[4];
   const int per = a.nL * a.ntile;
   for (int it = 0;; ++it) {
-    // Thread 0 takes items until one has work: an item whose family is off
-    // in its layer (nh3_sjs outside the blend layers, say) only counts as
-    // done, and if it was the last of its (layer, tile) the CTA assembles.
+    // Thread 0 takes items until one has work (an item whose family is off
+    // in its layer, nh3_sjs outside the blend layers say, is skipped).  The
+    // previous item's last barrier orders its record reads before the next
+    // item's record stores; s_item is double-buffered across iterations.
     if (threadIdx.x == 0) {
-      int item, lt = -1;
+      int item;
       for (;;) {
         item = atomicAdd(a.counter, 1);
         if (item >= a.nitems) break;
         const int t = item / per, rem = item - t * per;
-        const int L = a.nL - 1 - rem / a.ntile, tile = rem % a.ntile;
+        const int L = a.nL - 1 - rem / a.ntile;
         if (fam_enabled(a, a.lp[L], a.tmpl[t].fam)) break;
-        if (atomicAdd(a.done + (size_t)L * a.ntile + tile, 1) == a.ntmpl - 1) {
-          __threadfence();
-          lt = L * a.ntile + tile;
-          break;
-        }
       }
       s_item[it & 1] = item;
-      s_asm[it & 1] = lt;
     }
     __syncthreads();
     const int item = s_item[it & 1];
-    if (s_asm[it & 1] >= 0) {
-      const int lt = s_asm[it & 1];
-      for (int ls = threadIdx.x; ls < a.spt; ls += blockDim.x)
-        assemble_slot(a, lt / a.ntile, lt % a.ntile, ls);
-      continue;
-    }
     if (item >= a.nitems) break;
     const int t = item / per, rem = item - t * per;
     const int L = a.nL - 1 - rem / a.ntile, tile = rem % a.ntile;
     const TmplEntry e = a.tmpl[t];
-    {
-      switch (e.fam) {
-        case FAM_NH3_INV:
-        case FAM_H2S:
-        case FAM_PH3: lines_item<M, K_BR>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
-        case FAM_NH3_ROT:
-        case FAM_NH3_V2: lines_item<M, K_GROSS>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
-        case FAM_H2O: lines_item<M, K_VVW>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
-        default: sjs_item<M>(a, buf, L, tile, t, e.l0, e.l1); break;
-      }
+    switch (e.fam) {
+      case FAM_NH3_INV:
+      case FAM_H2S:
+      case FAM_PH3: lines_item<M, K_BR>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
+      case FAM_NH3_ROT:
+      case FAM_NH3_V2: lines_item<M, K_GROSS>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
+      case FAM_H2O: lines_item<M, K_VVW>(a, buf, s_red, L, tile, t, e.fam, e.l0, e.l1); break;
+      default: sjs_item<M>(a, buf, L, tile, t, e.l0, e.l1); break;
     }
-    // the barrier orders every thread's result stores before thread 0's
-    // fence, which releases them at device scope with the counter update
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      s_last = atomicAdd(a.done + (size_t)L * a.ntile + tile, 1) == a.ntmpl - 1;
-      if (s_last) __threadfence();
-    }
-    __syncthreads();
-    if (s_last)
-      for (int ls = threadIdx.x; ls < a.spt; ls += blockDim.x) assemble_slot(a, L, tile, ls);
   }
 }
 
-// Assembly alone, for a plan without line items (continua only).
+// Assembly: one thread per (layer, slot), layers x nslot threads in a 1-D
+// grid (the batched sweeps have millions of layers).
 __global__ void __launch_bounds__(128) rb_alpha_assemble_kernel(AlphaArgs a) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.nslot) return;
-  assemble_slot(a, blockIdx.y, s / a.spt, s % a.spt);
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (size_t)a.nL * a.nslot) return;
+  const int L = (int)(g / a.nslot);
+  const int s = (int)(g - (size_t)L * a.nslot);
+  assemble_slot(a, L, s / a.spt, s % a.spt);
 }
 
 // ------------------------------------------------------------------ launch
@@ -1095,10 +1071,9 @@ cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st
     const int nthr = 32 * aa.W;
     if (aa.M == 4) rb_alpha_lines_kernel<4><<<nb, nthr, 0, st>>>(aa);
     else rb_alpha_lines_kernel<2><<<nb, nthr, 0, st>>>(aa);
-  } else {
-    dim3 grid((aa.nslot + 127) / 128, aa.nL);
-    rb_alpha_assemble_kernel<<<grid, 128, 0, st>>>(aa);
   }
+  const size_t n = (size_t)aa.nL * aa.nslot;
+  rb_alpha_assemble_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(aa);
   return cudaGetLastError();
 }
 

@@ -133,7 +133,7 @@ struct rb_handle {
   int plan_vbeg[rb::NFAM] = {}, plan_vend[rb::NFAM] = {};
   int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
   DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
-      d_res, d_base, d_done;
+      d_res, d_base;
   // adjoint workspaces
   DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff;
   std::vector<int> batch_off;   // layer offsets of the last batch (d_voff)
@@ -522,10 +522,6 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   aa.counter = h->d_counter.as<int>();
   RB_CUDA(h->d_res.ensure(sizeof(float) * std::max<size_t>(1, (size_t)nL * aa.ntile * aa.ntmpl * aa.spt)));
   RB_CUDA(h->d_base.ensure(sizeof(float) * std::max<size_t>(1, (size_t)nL * aa.ntile * aa.ntmpl)));
-  RB_CUDA(h->d_done.ensure(sizeof(int) * (size_t)nL * aa.ntile));
-  aa.done = h->d_done.as<int>();
-  pa.done = aa.done;
-  pa.ntile = aa.ntile;
   aa.res = h->d_res.as<float>();
   aa.base = h->d_base.as<float>();
   aa.freqs = h->d_f.as<double>();
@@ -551,7 +547,8 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[1], st));
   RB_CUDA(rb::launch_alpha_lines(aa, h->plan_grid, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[2], st));
-  h->launches += extra ? 3 : 2;
+  // prep, [extra,] [line sums,] assembly
+  h->launches += (extra ? 1 : 0) + 1 + (aa.nitems > 0 ? 2 : 1);
   return RB_OK;
 }
 
@@ -669,7 +666,7 @@ int rb_destroy(rb_handle* h) {
                   &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part})
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
-                  &h->d_done, &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,
+                  &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,
                   &h->d_adjS, &h->d_voff, &h->d_co_f0, &h->d_co_I0, &h->d_co_E, &h->d_extra,
                   &h->d_xgrad, &h->d_agas, &h->d_acl, &h->d_aout, &h->d_aclout, &h->d_aprop,
                   &h->d_agrid, &h->d_aoff})

@@ -21,8 +21,6 @@ struct PrepArgs {
   int nlines[NFAM];
   LayerParams* out;
   int* counter;          // line-sum work counter to reset (or null)
-  int* done;             // [nL][ntile] finished-item counters to reset (or null)
-  int ntile;
 };
 
 // Line-sum work decomposition.
@@ -67,7 +65,6 @@ struct AlphaArgs {
   int* counter;             // work counter, zeroed by rb_layer_prep_kernel
   float* res;               // [nL][ntile][ntmpl][spt] per-item line sums
   float* base;              // [nL][ntile][ntmpl] h2o frequency-independent term per item
-  int* done;                // [nL][ntile] finished items, zeroed by rb_layer_prep_kernel
   const double* freqs;      // [nf] (float64 outputs only)
   const double* freqs_hs;   // [nf] frequency evaluated by nh3_hs in slot j
   const LayerParams* lp;
