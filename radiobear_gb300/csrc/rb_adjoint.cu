@@ -513,9 +513,24 @@ __global__ void __launch_bounds__(256) rb_layer_tan_kernel(TanArgs a) {
 constexpr int JV_CHUNK = 128;
 constexpr int JV_NREC = 16;
 
+constexpr int JV_FTMAX = 128;   // frequencies per CTA at most
+
 struct JvpShared {
   float rec[2][2][JV_CHUNK][JV_NREC];   // [buffer][coefficient set][line][field], 64 B per line
+  float fam[NFAM][JV_FTMAX][4];         // per family and frequency: value, three derivatives
   double red[8][NTH + 1];
+};
+
+// Line kinds of the JVP sweep.
+enum JvKind : int { JK_BR = 0, JK_GROSS = 1, JK_VVW = 2, JK_SJS = 3 };
+
+// Frequency of one thread of rb_alpha_jvp_kernel.
+struct JvFreq {
+  float F, FL;     // f^2 (hi, lo)
+  float Fh, FhL;   // f^2 of the frequency nh3_hs evaluates in this slot
+  float fq, fql;   // f (hi, lo)
+  float wJ;        // nh3_sjs Spilker / Joiner weight
+  int set;         // inversion coefficient set
 };
 
 // Compensated float sum.
@@ -560,7 +575,7 @@ __device__ __forceinline__ float strength(const LineTable& t, const LayerFam& F,
 
 // Ben-Reuven record, fields: 0 g, 1 z, 2 KH, 3 KL, 4 S, 5 dlnS/dT,
 // 6..8 dg, 9..11 dz, 12..14 dK.
-__device__ void jv_br_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int set,
+__device__ __forceinline__ void jv_br_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int set,
                              int li, int xt, float* r, int stride) {
   const float* c = LF.c[set];
   const float w1 = t.w1[li], w2 = t.w2[li];
@@ -589,7 +604,7 @@ __device__ void jv_br_record(const LineTable& t, const LayerFam& LF, const FamTa
 }
 
 // Gross record: 0 g, 2 KH, 3 KL, 4 S, 5 dlnS/dT, 6..8 dg.
-__device__ void jv_gross_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int li,
+__device__ __forceinline__ void jv_gross_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int li,
                                 int xt, float* r, int stride) {
   const float g = LF.c[0][1] * t.w1[li] + LF.c[0][2] * t.w2[li] + LF.c[0][3] * t.w3[li];
   r[0 * stride] = g;
@@ -603,7 +618,7 @@ __device__ void jv_gross_record(const LineTable& t, const LayerFam& LF, const Fa
 }
 
 // VVW record: 0 df, 2 fo_hi, 3 fo_lo, 4 S, 5 dlnS/dT, 6..8 d(df).
-__device__ void jv_vvw_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int li,
+__device__ __forceinline__ void jv_vvw_record(const LineTable& t, const LayerFam& LF, const FamTan& FT, int li,
                               int xt, float* r, int stride, float* base, float* dbase) {
   const float l2T = LF.c[0][0];
   const float e1 = exp2f(t.x1[li] * l2T), e2 = exp2f(t.x2[li] * l2T), e3 = exp2f(t.x3[li] * l2T);
@@ -631,7 +646,7 @@ __device__ void jv_vvw_record(const LineTable& t, const LayerFam& LF, const FamT
 }
 
 // nh3_sjs record: 2 KH0, 3 KL0 ((fo + shift)^2), 4 S, 5 dlnS/dT, 6 G0, 9..11 dK0.
-__device__ void jv_sjs_record(const LineTable& t, const LayerFam& LF, const FamTan& FT,
+__device__ __forceinline__ void jv_sjs_record(const LineTable& t, const LayerFam& LF, const FamTan& FT,
                               const LayerTan& LT, float shift, int li, float* r, int stride) {
   const float fo = t.ch[li];
   float KH, e;
@@ -644,10 +659,10 @@ __device__ void jv_sjs_record(const LineTable& t, const LayerFam& LF, const FamT
   for (int q = 0; q < 3; ++q) r[(9 + q) * stride] = 2.f * (fo + shift) * tan3(LT.dsjs[0][4], q, TH_XNH3);
 }
 
-// Ben-Reuven term and its three derivatives.
-__device__ __forceinline__ void br_eval(float F, float FL, float g, float z, float KH, float KL,
-                                        float S, float dlnS, const float* dg, const float* dz,
-                                        const float* dK, KSum& val, KSum* der) {
+// Ben-Reuven term t = S n / den; its three derivatives are added to d.
+__device__ __forceinline__ float br_eval(float F, float FL, float g, float z, float KH, float KL,
+                                         float S, float dlnS, const float* dg, const float* dz,
+                                         const float* dK, float* d) {
   const float e = (F - KH) + (FL - KL);
   const float K = KH + KL;
   const float den = fmaf(e, e, 4.f * F * g * g);
@@ -655,15 +670,176 @@ __device__ __forceinline__ void br_eval(float F, float FL, float g, float z, flo
   const float gp = g + z, gm = g - z;
   const float n = fmaf(gm, F, gp * K);
   const float t = S * n * r;
-  val.add(t);
   // dt = S r [dn - n r dden] + t dlnS with dn = (F + K) dg + (K - F) dz + gp dK,
   // dden = 8 F g dg - 2 e dK, collected per tangent of g, z, K
   const float nr = n * r, Sr = S * r;
   const float Ag = Sr * ((F + K) - 8.f * F * g * nr);
   const float Az = Sr * (K - F);
   const float AK = Sr * fmaf(2.f * e, nr, gp);
-  for (int q = 0; q < 3; ++q) der[q].s += fmaf(Ag, dg[q], fmaf(Az, dz[q], AK * dK[q]));
-  der[0].s += t * dlnS;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) d[q] += fmaf(Ag, dg[q], fmaf(Az, dz[q], AK * dK[q]));
+  d[0] += t * dlnS;
+  return t;
+}
+
+// A record of JV_NREC fields as four 16-byte stores.
+__device__ __forceinline__ void store_rec(float* dst, const float* r) {
+  float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int k = 0; k < JV_NREC / 4; ++k) d4[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+}
+
+// One family of one layer for the CTA's frequencies.  Records of JV_CHUNK
+// lines at a time, double-buffered (chunk c+1 is built, one line per
+// thread, while chunk c is swept); the NG line groups of a frequency sweep
+// lines grp, grp + NG, ...; value terms are added in blocks of 16 into a
+// compensated sum.  The groups' sums (value and three derivatives) go to
+// sh.fam[fam][fi], added in group order.  Called by every thread.
+template <int KIND>
+__device__ __forceinline__ void jv_family(const JvpArgs& a, JvpShared& sh, int L, int fam,
+                                          const JvFreq& fr, bool on, float& base, float* dbase) {
+  const int tid = threadIdx.x;
+  const int FTL = a.ft, NG = blockDim.x / a.ft;
+  const int fi = tid % FTL, grp = tid / FTL;
+  const LayerParams& lp = a.lp[L];
+  const LayerTan& LT = a.lt[L];
+  const LineTable& t = a.tab[fam];
+  const LayerFam& LF = lp.fam[fam];
+  const FamTan& FT = LT.fam[fam];
+  const int xt = fam_xtan(fam);
+  const bool two = fam == FAM_NH3_INV;
+  const bool hsf = fam == FAM_NH3_INV || fam == FAM_NH3_ROT || fam == FAM_NH3_V2;
+  const float Fx = hsf ? fr.Fh : fr.F, FLx = hsf ? fr.FhL : fr.FL;
+  auto build = [&](int bi, int c0) {
+    const int nc = min(JV_CHUNK, t.n - c0);
+    for (int i = tid; i < nc; i += blockDim.x) {
+      const int li = c0 + i;
+      float r[JV_NREC];
+#pragma unroll
+      for (int k = 0; k < JV_NREC; ++k) r[k] = 0.f;
+      if (KIND == JK_BR) {
+        jv_br_record(t, LF, FT, 0, li, xt, r, 1);
+        store_rec(sh.rec[bi][0][i], r);
+        if (two) {
+          jv_br_record(t, LF, FT, 1, li, xt, r, 1);
+          store_rec(sh.rec[bi][1][i], r);
+        }
+      } else if (KIND == JK_GROSS) {
+        jv_gross_record(t, LF, FT, li, xt, r, 1);
+        store_rec(sh.rec[bi][0][i], r);
+      } else if (KIND == JK_VVW) {
+        jv_vvw_record(t, LF, FT, li, xt, r, 1, &base, dbase);
+        store_rec(sh.rec[bi][0][i], r);
+      } else {
+        jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, r, 1);
+        store_rec(sh.rec[bi][0][i], r);
+      }
+    }
+  };
+  // nh3_sjs per-frequency coefficients and their derivatives
+  float A = 0.f, B = 0.f, C = 0.f, D = 0.f, dA[3] = {0, 0, 0}, dB[3] = {0, 0, 0}, dC[3] = {0, 0, 0},
+        dD[3] = {0, 0, 0};
+  if (KIND == JK_SJS) {
+    auto lerp = [&](float j0, float s0) { return fmaf(j0 - s0, fr.wJ, s0); };
+    A = lerp(lp.sjs[0][0], lp.sjs[1][0]);
+    B = lerp(lp.sjs[0][1], lp.sjs[1][1]);
+    C = lerp(lp.sjs[0][2], lp.sjs[1][2]);
+    D = lerp(lp.sjs[0][3], lp.sjs[1][3]);
+    for (int q = 0; q < 3; ++q) {
+      dA[q] = lerp(tan3(LT.dsjs[0][0], q, xt), tan3(LT.dsjs[1][0], q, xt));
+      dB[q] = lerp(tan3(LT.dsjs[0][1], q, xt), tan3(LT.dsjs[1][1], q, xt));
+      dC[q] = lerp(tan3(LT.dsjs[0][2], q, xt), tan3(LT.dsjs[1][2], q, xt));
+      dD[q] = lerp(tan3(LT.dsjs[0][3], q, xt), tan3(LT.dsjs[1][3], q, xt));
+    }
+  }
+  KSum val;
+  val.init();
+  float vp = 0.f, der[3] = {0.f, 0.f, 0.f};
+  int nv = 0;
+  const int nchunks = (t.n + JV_CHUNK - 1) / JV_CHUNK;
+  build(0, 0);
+  __syncthreads();
+  for (int ci = 0; ci < nchunks; ++ci) {
+    const int c0 = ci * JV_CHUNK;
+    const int nc = min(JV_CHUNK, t.n - c0);
+    if (ci + 1 < nchunks) build((ci + 1) & 1, c0 + JV_CHUNK);
+    if (on) {
+      const float(*Rl)[JV_NREC] = sh.rec[ci & 1][two ? fr.set : 0];
+      for (int i = grp; i < nc; i += NG) {
+        const float4* r4 = reinterpret_cast<const float4*>(Rl[i]);
+        // fields 0..15 = q0.xyzw q1.xyzw q2.xyzw q3.xyzw
+        const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2];
+        float tv;
+        if (KIND == JK_BR) {
+          const float4 q3 = r4[3];
+          const float dg[3] = {q1.z, q1.w, q2.x};
+          const float dz[3] = {q2.y, q2.z, q2.w};
+          const float dK[3] = {q3.x, q3.y, q3.z};
+          tv = br_eval(Fx, FLx, q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, dg, dz, dK, der);
+        } else if (KIND == JK_GROSS) {
+          const float g = q0.x, S = q1.x;
+          const float e = (Fx - q0.z) + (FLx - q0.w);
+          const float den = fmaf(e, e, 4.f * Fx * g * g);
+          const float r = rcp_approx(den);
+          tv = S * g * r;
+          const float dgv[3] = {q1.z, q1.w, q2.x};
+          const float k8 = 8.f * Fx * g * g * r;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) der[q] += (q == 0 ? tv * q1.y : 0.f) + S * dgv[q] * (1.f - k8) * r;
+        } else if (KIND == JK_VVW) {
+          const float df = q0.x, S = q1.x;
+          const float dm = (fr.fq - q0.z) + (fr.fql - q0.w);
+          const float dp = fr.fq + q0.z;
+          const float d1 = fmaf(dm, dm, df * df), d2 = fmaf(dp, dp, df * df);
+          const float r1 = rcp_approx(d1), r2 = rcp_approx(d2);
+          const float h = S * df, u = r1 + r2;
+          tv = h * u;
+          const float ddf[3] = {q1.z, q1.w, q2.x};
+          const float k2 = 2.f * h * df * (r1 * r1 + r2 * r2);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const float dh = (q == 0 ? h * q1.y : 0.f) + S * ddf[q];
+            der[q] += dh * u - k2 * ddf[q];
+          }
+        } else {
+          const float G0 = q1.z, S = q1.x;
+          const float g = fmaf(B, G0, A), z = fmaf(D, G0, C);
+          const float g2z2 = (g - z) * (g + z);
+          const float dK0[3] = {q2.y, q2.z, q2.w};
+          float dg[3], dz[3], dK[3];
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            dg[q] = fmaf(dB[q], G0, dA[q]);
+            dz[q] = fmaf(dD[q], G0, dC[q]);
+            dK[q] = dK0[q] + 2.f * g * dg[q] - 2.f * z * dz[q];
+          }
+          float KH, e;
+          two_sum(q0.z, g2z2, KH, e);
+          tv = br_eval(Fx, FLx, g, z, KH, e + q0.w, S, q1.y, dg, dz, dK, der);
+        }
+        vp += tv;
+        if (++nv == 16) {
+          val.add(vp);
+          vp = 0.f;
+          nv = 0;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  val.add(vp);
+  // the line groups' sums, staged in the (now free) record buffer
+  float(*s_grp)[4] = reinterpret_cast<float(*)[4]>(&sh.rec[0][0][0][0]);
+  s_grp[tid][0] = val.val();
+  for (int q = 0; q < 3; ++q) s_grp[tid][1 + q] = der[q];
+  __syncthreads();
+  if (grp == 0) {
+    float v4[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int gg = 0; gg < NG; ++gg)
+      for (int q = 0; q < 4; ++q) v4[q] += s_grp[gg * FTL + fi][q];
+    for (int q = 0; q < 4; ++q) sh.fam[fam][fi][q] = v4[q];
+  }
+  __syncthreads();
 }
 
 // Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
@@ -671,10 +847,9 @@ __device__ __forceinline__ void br_eval(float F, float FL, float g, float z, flo
 // per family.
 __global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
   __shared__ __align__(16) JvpShared sh;
-  __shared__ float s_grp[256][4];
   const int L = blockIdx.x;
   const int tid = threadIdx.x;
-  const int FTL = a.ft, NG = blockDim.x / a.ft;
+  const int FTL = a.ft;
   const int fi = tid % FTL, grp = tid / FTL;
   const int j = blockIdx.y * FTL + fi;
   const bool on = j < a.nf;
@@ -682,19 +857,20 @@ __global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
   const LayerTan& LT = a.lt[L];
   // this thread's frequency
   const double f = on ? a.freqs[j] : 1.0, fh = on ? a.freqs_hs[j] : 1.0;
-  float F, FL, Fh, FhL, fq, fql;
-  split_double(f * f, F, FL);
-  split_double(fh * fh, Fh, FhL);
-  split_double(f, fq, fql);
+  JvFreq fr;
+  split_double(f * f, fr.F, fr.FL);
+  split_double(fh * fh, fr.Fh, fr.FhL);
+  split_double(f, fr.fq, fr.fql);
   const int set = fh > 30.0 ? 1 : 0;
-  const float wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)((f - 26.0) / 8.0));
+  fr.set = set;
+  fr.wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)((f - 26.0) / 8.0));
   const bool nh3 = a.cfg.nh3_mode != NH3_OFF;
-  // per family: value sum and three derivative sums
-  float fv[NFAM], fd[NFAM][3];
+  // families that are off keep zero sums (read back by the same thread)
+  if (grp == 0)
+    for (int fam = 0; fam < NFAM; ++fam)
+      for (int q = 0; q < 4; ++q) sh.fam[fam][fi][q] = 0.f;
   float base = 0.f, dbase[3] = {0.f, 0.f, 0.f};
   for (int fam = 0; fam < NFAM; ++fam) {
-    fv[fam] = 0.f;
-    fd[fam][0] = fd[fam][1] = fd[fam][2] = 0.f;
     bool en;
     switch (fam) {
       case FAM_NH3_INV:
@@ -705,124 +881,16 @@ __global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
       case FAM_H2S: en = a.cfg.use_h2s; break;
       default: en = a.cfg.use_ph3; break;
     }
-    const LineTable& t = a.tab[fam];
-    if (!en || t.n == 0) continue;
-    const LayerFam& LF = lp.fam[fam];
-    const FamTan& FT = LT.fam[fam];
-    const int xt = fam_xtan(fam);
-    const bool two = fam == FAM_NH3_INV;
-    const bool hsf = fam == FAM_NH3_INV || fam == FAM_NH3_ROT || fam == FAM_NH3_V2;
-    const float Fx = hsf ? Fh : F, FLx = hsf ? FhL : FL;
-    // nh3_sjs per-frequency coefficients and their derivatives
-    float A = 0.f, B = 0.f, C = 0.f, D = 0.f, dA[3] = {0, 0, 0}, dB[3] = {0, 0, 0}, dC[3] = {0, 0, 0},
-          dD[3] = {0, 0, 0};
-    if (fam == FAM_NH3_SJS) {
-      auto lerp = [&](float j0, float s0) { return fmaf(j0 - s0, wJ, s0); };
-      A = lerp(lp.sjs[0][0], lp.sjs[1][0]);
-      B = lerp(lp.sjs[0][1], lp.sjs[1][1]);
-      C = lerp(lp.sjs[0][2], lp.sjs[1][2]);
-      D = lerp(lp.sjs[0][3], lp.sjs[1][3]);
-      for (int q = 0; q < 3; ++q) {
-        dA[q] = lerp(tan3(LT.dsjs[0][0], q, xt), tan3(LT.dsjs[1][0], q, xt));
-        dB[q] = lerp(tan3(LT.dsjs[0][1], q, xt), tan3(LT.dsjs[1][1], q, xt));
-        dC[q] = lerp(tan3(LT.dsjs[0][2], q, xt), tan3(LT.dsjs[1][2], q, xt));
-        dD[q] = lerp(tan3(LT.dsjs[0][3], q, xt), tan3(LT.dsjs[1][3], q, xt));
-      }
+    if (!en || a.tab[fam].n == 0) continue;
+    switch (fam) {
+      case FAM_NH3_INV:
+      case FAM_H2S:
+      case FAM_PH3: jv_family<JK_BR>(a, sh, L, fam, fr, on, base, dbase); break;
+      case FAM_NH3_ROT:
+      case FAM_NH3_V2: jv_family<JK_GROSS>(a, sh, L, fam, fr, on, base, dbase); break;
+      case FAM_H2O: jv_family<JK_VVW>(a, sh, L, fam, fr, on, base, dbase); break;
+      default: jv_family<JK_SJS>(a, sh, L, fam, fr, on, base, dbase); break;
     }
-    KSum val, der[3];
-    val.init();
-    for (int q = 0; q < 3; ++q) der[q].init();
-    // records double-buffered: chunk c+1 is built while chunk c is swept
-    auto build = [&](int bi, int c0) {
-      const int nc = min(JV_CHUNK, t.n - c0);
-      for (int i = tid; i < nc; i += blockDim.x) {
-        const int li = c0 + i;
-        if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
-          jv_br_record(t, LF, FT, 0, li, xt, sh.rec[bi][0][i], 1);
-          if (two) jv_br_record(t, LF, FT, 1, li, xt, sh.rec[bi][1][i], 1);
-        } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
-          jv_gross_record(t, LF, FT, li, xt, sh.rec[bi][0][i], 1);
-        } else if (fam == FAM_H2O) {
-          jv_vvw_record(t, LF, FT, li, xt, sh.rec[bi][0][i], 1, &base, dbase);
-        } else {
-          jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, sh.rec[bi][0][i], 1);
-        }
-      }
-    };
-    const int nchunks = (t.n + JV_CHUNK - 1) / JV_CHUNK;
-    build(0, 0);
-    __syncthreads();
-    for (int ci = 0; ci < nchunks; ++ci) {
-      const int c0 = ci * JV_CHUNK;
-      const int nc = min(JV_CHUNK, t.n - c0);
-      if (ci + 1 < nchunks) build((ci + 1) & 1, c0 + JV_CHUNK);
-      if (on) {
-        const float(*Rl)[JV_NREC] = sh.rec[ci & 1][two ? set : 0];
-        for (int i = grp; i < nc; i += NG) {
-          const float4* r4 = reinterpret_cast<const float4*>(Rl[i]);
-          const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2], q3 = r4[3];
-          // fields 0..15 = q0.xyzw q1.xyzw q2.xyzw q3.xyzw
-          if (fam == FAM_NH3_INV || fam == FAM_H2S || fam == FAM_PH3) {
-            const float dg[3] = {q1.z, q1.w, q2.x};
-            const float dz[3] = {q2.y, q2.z, q2.w};
-            const float dK[3] = {q3.x, q3.y, q3.z};
-            br_eval(Fx, FLx, q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, dg, dz, dK, val, der);
-          } else if (fam == FAM_NH3_ROT || fam == FAM_NH3_V2) {
-            const float g = q0.x, S = q1.x;
-            const float e = (Fx - q0.z) + (FLx - q0.w);
-            const float den = fmaf(e, e, 4.f * Fx * g * g);
-            const float r = rcp_approx(den);
-            const float tt = S * g * r;
-            val.add(tt);
-            const float dgv[3] = {q1.z, q1.w, q2.x};
-            const float k8 = 8.f * Fx * g * g * r;
-            for (int q = 0; q < 3; ++q)
-              der[q].s += (q == 0 ? tt * q1.y : 0.f) + S * dgv[q] * (1.f - k8) * r;
-          } else if (fam == FAM_H2O) {
-            const float df = q0.x, S = q1.x;
-            const float dm = (fq - q0.z) + (fql - q0.w);
-            const float dp = fq + q0.z;
-            const float d1 = fmaf(dm, dm, df * df), d2 = fmaf(dp, dp, df * df);
-            const float r1 = rcp_approx(d1), r2 = rcp_approx(d2);
-            const float h = S * df, u = r1 + r2;
-            val.add(h * u);
-            const float ddf[3] = {q1.z, q1.w, q2.x};
-            const float k2 = 2.f * h * df * (r1 * r1 + r2 * r2);
-            for (int q = 0; q < 3; ++q) {
-              const float dh = (q == 0 ? h * q1.y : 0.f) + S * ddf[q];
-              der[q].s += dh * u - k2 * ddf[q];
-            }
-          } else {   // nh3_sjs
-            const float G0 = q1.z, S = q1.x;
-            const float g = fmaf(B, G0, A), z = fmaf(D, G0, C);
-            const float g2z2 = (g - z) * (g + z);
-            const float dK0[3] = {q2.y, q2.z, q2.w};
-            float dg[3], dz[3], dK[3];
-            for (int q = 0; q < 3; ++q) {
-              dg[q] = fmaf(dB[q], G0, dA[q]);
-              dz[q] = fmaf(dD[q], G0, dC[q]);
-              dK[q] = dK0[q] + 2.f * g * dg[q] - 2.f * z * dz[q];
-            }
-            float KH, e;
-            two_sum(q0.z, g2z2, KH, e);
-            br_eval(Fx, FLx, g, z, KH, e + q0.w, S, q1.y, dg, dz, dK, val, der);
-          }
-        }
-      }
-      __syncthreads();
-    }
-    // add the line groups' sums
-    s_grp[tid][0] = val.val();
-    for (int q = 0; q < 3; ++q) s_grp[tid][1 + q] = der[q].val();
-    __syncthreads();
-    if (grp == 0) {
-      float v4[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int gg = 0; gg < NG; ++gg)
-        for (int q = 0; q < 4; ++q) v4[q] += s_grp[gg * FTL + fi][q];
-      fv[fam] = v4[0];
-      for (int q = 0; q < 3; ++q) fd[fam][q] = v4[1 + q];
-    }
-    __syncthreads();
   }
   // h2o base term summed over the CTA (every thread built some lines)
   {
@@ -844,6 +912,8 @@ __global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
   // assemble dalpha/dtheta (cm^-1) in float64 and contract with dTb/dalpha
   double g5[NTH] = {0, 0, 0, 0, 0};
   if (on && grp == 0) {
+    auto fv = [&](int fam) { return sh.fam[fam][fi][0]; };
+    auto fd = [&](int fam) { return &sh.fam[fam][fi][1]; };
     const double gal = (double)a.galpha[(size_t)L * a.nf + j];
     const double Fd = f * f, Fhd = fh * fh;
     auto pref = [&](int fam) { return ldexp((double)lp.fam[fam].fm, lp.fam[fam].fe); };
@@ -866,29 +936,29 @@ __global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
     // H2O lines and continuum
     if (a.cfg.use_h2o) {
       double d[NTH] = {0, 0, 0, 0, 0};
-      const float ds[3] = {fd[FAM_H2O][0] - dbase[0], fd[FAM_H2O][1] - dbase[1], fd[FAM_H2O][2] - dbase[2]};
-      add_fam(FAM_H2O, 1.0, (double)fv[FAM_H2O] - base, ds, d);
+      const float ds[3] = {fd(FAM_H2O)[0] - dbase[0], fd(FAM_H2O)[1] - dbase[1], fd(FAM_H2O)[2] - dbase[2]};
+      add_fam(FAM_H2O, 1.0, (double)fv(FAM_H2O) - base, ds, d);
       for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2O] * (d[q] + (double)LT.dh2o_cont[q]) * Fd;
     }
     if (a.cfg.use_h2s) {
       double d[NTH] = {0, 0, 0, 0, 0};
-      add_fam(FAM_H2S, 1.0, fv[FAM_H2S], fd[FAM_H2S], d);
+      add_fam(FAM_H2S, 1.0, fv(FAM_H2S), fd(FAM_H2S), d);
       for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2S] * d[q] * Fd;
     }
     if (a.cfg.use_ph3) {
       double d[NTH] = {0, 0, 0, 0, 0};
-      add_fam(FAM_PH3, 1.0, fv[FAM_PH3], fd[FAM_PH3], d);
+      add_fam(FAM_PH3, 1.0, fv(FAM_PH3), fd(FAM_PH3), d);
       for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_PH3] * d[q] * Fd;
     }
     if (nh3) {
       double hs = 0.0, dhs[NTH] = {0, 0, 0, 0, 0}, sj = 0.0, dsj[NTH] = {0, 0, 0, 0, 0};
       const double INVC[2][2] = {{0.9301, 0.9862}, {0.9619, 0.9862}};   // Con, per table and set
       if (lp.use_hs) {
-        hs = Fhd * (pref(FAM_NH3_INV) * INVC[a.cfg.inv_table][set] * fv[FAM_NH3_INV] +
-                    pref(FAM_NH3_ROT) * fv[FAM_NH3_ROT] + pref(FAM_NH3_V2) * fv[FAM_NH3_V2]);
-        add_fam(FAM_NH3_INV, INVC[a.cfg.inv_table][set], fv[FAM_NH3_INV], fd[FAM_NH3_INV], dhs);
-        add_fam(FAM_NH3_ROT, 1.0, fv[FAM_NH3_ROT], fd[FAM_NH3_ROT], dhs);
-        add_fam(FAM_NH3_V2, 1.0, fv[FAM_NH3_V2], fd[FAM_NH3_V2], dhs);
+        hs = Fhd * (pref(FAM_NH3_INV) * INVC[a.cfg.inv_table][set] * fv(FAM_NH3_INV) +
+                    pref(FAM_NH3_ROT) * fv(FAM_NH3_ROT) + pref(FAM_NH3_V2) * fv(FAM_NH3_V2));
+        add_fam(FAM_NH3_INV, INVC[a.cfg.inv_table][set], fv(FAM_NH3_INV), fd(FAM_NH3_INV), dhs);
+        add_fam(FAM_NH3_ROT, 1.0, fv(FAM_NH3_ROT), fd(FAM_NH3_ROT), dhs);
+        add_fam(FAM_NH3_V2, 1.0, fv(FAM_NH3_V2), fd(FAM_NH3_V2), dhs);
         for (int q = 0; q < NTH; ++q) dhs[q] *= Fhd;
         if (hs < 0.0) {   // clamped to 1e-8 (nh3_hs.py:311-312): no derivative
           hs = 1.0e-8;
@@ -896,8 +966,8 @@ __global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
         }
       }
       if (lp.use_sjs) {
-        sj = Fd * pref(FAM_NH3_SJS) * fv[FAM_NH3_SJS];
-        add_fam(FAM_NH3_SJS, 1.0, fv[FAM_NH3_SJS], fd[FAM_NH3_SJS], dsj);
+        sj = Fd * pref(FAM_NH3_SJS) * fv(FAM_NH3_SJS);
+        add_fam(FAM_NH3_SJS, 1.0, fv(FAM_NH3_SJS), fd(FAM_NH3_SJS), dsj);
         for (int q = 0; q < NTH; ++q) dsj[q] *= Fd;
       }
       double dn[NTH];
