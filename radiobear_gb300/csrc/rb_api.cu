@@ -2,6 +2,7 @@
 // handle, device-memory management, catalogue preprocessing, frequency
 // plans and the launch sequences.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -36,6 +37,11 @@ int fail(int code, const char* fmt, ...) {
                   #call, cudaGetErrorString(e_), __FILE__, __LINE__);                  \
   } while (0)
 
+// Counts (re)allocations of device and pinned host buffers: a captured
+// CUDA graph holds buffer addresses and is replayed only while this count
+// is unchanged.
+std::atomic<unsigned long long> g_alloc_epoch{0};
+
 struct DBuf {
   void* p = nullptr;
   size_t cap = 0;
@@ -44,6 +50,7 @@ struct DBuf {
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;
+    ++g_alloc_epoch;
     size_t want = std::max(bytes, (size_t)256);
     cudaError_t e = cudaMalloc(&p, want);
     if (e == cudaSuccess) cap = want;
@@ -51,11 +58,50 @@ struct DBuf {
   }
   void release() {
     if (p) cudaFree(p);
+    if (p) ++g_alloc_epoch;
     p = nullptr;
     cap = 0;
   }
   template <class T>
   T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Pinned host staging buffer.
+struct HBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    ++g_alloc_epoch;
+    size_t want = std::max(bytes, (size_t)4096);
+    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    if (p) ++g_alloc_epoch;
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Shape of an rb_forward call from host buffers: everything a captured
+// graph of it bakes in (sizes, kernel scalars, configuration, addresses).
+struct FwdKey {
+  int nL = -1, nf = 0, nb = 0, disc = 0, gtype = 0, limb = 0, flags = 0;
+  double Req = 0, Rpol = 0, o0 = 0, o1 = 0;
+  unsigned long long cfg = 0, epoch = 0;
+  bool operator==(const FwdKey& o) const {
+    return nL == o.nL && nf == o.nf && nb == o.nb && disc == o.disc && gtype == o.gtype &&
+           limb == o.limb && flags == o.flags && Req == o.Req && Rpol == o.Rpol && o0 == o.o0 &&
+           o1 == o.o1 && cfg == o.cfg && epoch == o.epoch;
+  }
 };
 
 // A batch of atmospheres (rb_forward_batch_device): variant v owns layers
@@ -142,6 +188,15 @@ struct rb_handle {
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
       d_T32, d_hds, d_Tb32, d_part;
   int launches = 0;
+  // rb_forward from host buffers: the inputs are staged in one pinned block
+  // and uploaded with one copy, the outputs come back the same way, and a
+  // call whose shape has run before is replayed from a captured graph
+  unsigned long long cfg_gen = 0;   // bumped by every setter and re-plan
+  HBuf h_in, h_out;
+  DBuf d_in;
+  FwdKey fwd_seen, fwd_key;
+  cudaGraphExec_t fwd_exec = nullptr;
+  int fwd_launches = 0;
   // phase timing (rb_set_profiling)
   int profiling = 0;
   cudaEvent_t pev[10] = {};
@@ -434,6 +489,7 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
   RB_CUDA(h->d_counter.ensure(sizeof(int)));
   RB_CUDA(cudaStreamSynchronize(st));
   h->plan_f.assign(freqs, freqs + nf);
+  ++h->cfg_gen;
   h->plan_M = M;
   h->plan_W = W;
   h->plan_spt = spt;
@@ -679,6 +735,10 @@ int rb_destroy(rb_handle* h) {
   for (auto& e : h->pev)
     if (e) cudaEventDestroy(e);
   h->d_probe.release();
+  h->d_in.release();
+  h->h_in.release();
+  h->h_out.release();
+  if (h->fwd_exec) cudaGraphExecDestroy(h->fwd_exec);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->st) cudaStreamDestroy(h->st);
@@ -707,6 +767,7 @@ static int set_co_lines(rb_handle* h, int n, int ncols, const double* cols) {
 
 int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols) {
   if (!h) return fail(RB_EINVAL, "null handle");
+  ++h->cfg_gen;
   if (family == RB_FAM_CO) return set_co_lines(h, n, ncols, cols);
   if (family < 0 || family >= rb::NFAM) return fail(RB_EINVAL, "unknown family %d", family);
   if (ncols != family_ncols(family))
@@ -824,6 +885,7 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
 int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2s, int use_ph3,
                       int h2state) {
   if (!h) return fail(RB_EINVAL, "null handle");
+  ++h->cfg_gen;
   if (nh3 < RB_NH3_OFF || nh3 > RB_NH3_DBS_SJS) return fail(RB_EINVAL, "bad nh3 formalism %d", nh3);
   if (h2state != 'e' && h2state != 'n') return fail(RB_EINVAL, "h2state must be 'e' or 'n'");
   // nh3_dbs / nh3_dbs_sjs: the nh3_hs / nh3_hs_sjs structure with the
@@ -841,6 +903,7 @@ int rb_set_formalisms(rb_handle* h, int nh3, int use_h2, int use_h2o, int use_h2
 
 int rb_set_co_clouds(rb_handle* h, int co, int coshape, int clouds, int cloud_mask) {
   if (!h) return fail(RB_EINVAL, "null handle");
+  ++h->cfg_gen;
   if (coshape < RB_COSHAPE_VOIGT || coshape > RB_COSHAPE_STD) return fail(RB_EINVAL, "bad coshape %d", coshape);
   if (cloud_mask & ~63) return fail(RB_EINVAL, "bad cloud mask %d", cloud_mask);
   h->cfg.use_co = co != 0;
@@ -852,6 +915,7 @@ int rb_set_co_clouds(rb_handle* h, int co, int coshape, int clouds, int cloud_ma
 
 int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines) {
   if (!h) return fail(RB_EINVAL, "null handle");
+  ++h->cfg_gen;
   if (!(M == 0 || M == 2 || M == 4)) return fail(RB_EINVAL, "M must be 0, 2 or 4");
   if (W < 0 || W > 4) return fail(RB_EINVAL, "W must be in 0..4");
   if ((M == 0) != (W == 0)) return fail(RB_EINVAL, "M and W are set together");
@@ -1107,53 +1171,101 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
     bb.assign(2 * (size_t)nb, 0.0);
     b = bb.data();
   }
-  RB_CUDA(cudaSetDevice(h->device));
-  cudaStream_t st = h->st;
-  // the copies run while the inputs are validated; nothing is launched on
-  // them before validation passes, and an error waits for the copies
-  RB_CUDA(upload(h->d_P, P, nL, st));
-  RB_CUDA(upload(h->d_T, T, nL, st));
-  RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
-  RB_CUDA(upload(h->d_R, R, nL, st));
-  RB_CUDA(upload(h->d_N, N, nL, st));
-  if (nb > 0) RB_CUDA(upload(h->d_b, b, 2 * (size_t)nb, st));
-  const double* dscale = nullptr;
-  if (scale) {
-    RB_CUDA(upload(h->d_scale, scale, (size_t)nL * rb::NGAS, st));
-    dscale = h->d_scale.as<double>();
-  }
-  const double* dw = nullptr;
-  if (weights && nb > 0) {
-    RB_CUDA(upload(h->d_w, weights, nb, st));
-    dw = h->d_w.as<double>();
-  }
   int rc = validate_atm(nL, P, T, X);
   if (!rc) rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
   if (!rc && weights && !finite_all(weights, nb)) rc = fail(RB_EINVAL, "weights not finite");
   if (!rc && scale && !finite_all(scale, (size_t)nL * rb::NGAS)) rc = fail(RB_EINVAL, "scale not finite");
-  if (rc) {
-    cudaStreamSynchronize(st);
-    return rc;
-  }
+  if (rc) return rc;
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
   if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  // one staged input block (each array at a 256-byte boundary) and one output block
+  auto al = [](size_t n) { return (n + 31) / 32 * 32; };
+  const bool has_w = weights && nb > 0;
+  const size_t oP = 0, oT = oP + al(nL), oX = oT + al(nL), oR = oX + al((size_t)rb::NX * nL),
+               oN = oR + al(nL), ob = oN + al(nL), osc = ob + al(2 * (size_t)nb),
+               ow = osc + (scale ? al((size_t)rb::NGAS * nL) : 0), nin = ow + (has_w ? al(nb) : 0);
+  const size_t nTb = Tb_out && nb > 0 ? (size_t)nb * nf : 0, navg = Tb_avg && nb > 0 ? (size_t)nf : 0,
+               nlay = layers_out ? (size_t)nf * nL : 0;
+  const size_t oTb = 0, oavg = al(nTb), olay = oavg + al(navg), nout = olay + nlay;
+  RB_CUDA(h->h_in.ensure(sizeof(double) * nin));
+  RB_CUDA(h->h_out.ensure(sizeof(double) * std::max<size_t>(nout, 1)));
+  RB_CUDA(h->d_in.ensure(sizeof(double) * nin));
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * std::max((size_t)nb * nf, (size_t)1)));
   RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
-  double* dl = nullptr;
-  if (layers_out) {
-    RB_CUDA(h->d_l64.ensure(sizeof(double) * (size_t)nf * nL));
-    dl = h->d_l64.as<double>();
+  if (layers_out) RB_CUDA(h->d_l64.ensure(sizeof(double) * (size_t)nf * nL));
+  double* hin = h->h_in.as<double>();
+  std::memcpy(hin + oP, P, sizeof(double) * nL);
+  std::memcpy(hin + oT, T, sizeof(double) * nL);
+  std::memcpy(hin + oX, X, sizeof(double) * rb::NX * (size_t)nL);
+  std::memcpy(hin + oR, R, sizeof(double) * nL);
+  std::memcpy(hin + oN, N, sizeof(double) * nL);
+  if (nb > 0) std::memcpy(hin + ob, b, sizeof(double) * 2 * (size_t)nb);
+  if (scale) std::memcpy(hin + osc, scale, sizeof(double) * rb::NGAS * (size_t)nL);
+  if (has_w) std::memcpy(hin + ow, weights, sizeof(double) * nb);
+  const double* din = h->d_in.as<double>();
+  double* dl = layers_out ? h->d_l64.as<double>() : nullptr;
+  double* hout = h->h_out.as<double>();
+  auto enqueue = [&]() -> int {
+    RB_CUDA(cudaMemcpyAsync(h->d_in.p, hin, sizeof(double) * nin, cudaMemcpyHostToDevice, st));
+    int r = forward_core(h, st, nL, din + oP, din + oT, din + oX, din + oR, din + oN,
+                         scale ? din + osc : nullptr, Req, Rpol, orient0, orient1, gtype, limb, nb,
+                         din + ob, has_w ? din + ow : nullptr, disc, h->d_Tb.as<double>(),
+                         Tb_avg ? h->d_avg.as<double>() : nullptr, dl);
+    if (r) return r;
+    if (nTb) RB_CUDA(cudaMemcpyAsync(hout + oTb, h->d_Tb.p, sizeof(double) * nTb, cudaMemcpyDeviceToHost, st));
+    if (navg) RB_CUDA(cudaMemcpyAsync(hout + oavg, h->d_avg.p, sizeof(double) * navg, cudaMemcpyDeviceToHost, st));
+    if (nlay) RB_CUDA(cudaMemcpyAsync(hout + olay, dl, sizeof(double) * nlay, cudaMemcpyDeviceToHost, st));
+    return RB_OK;
+  };
+  // Replay: the same call shape, configuration and buffer addresses as the
+  // captured graph.  Capture: the shape ran once already (every buffer is
+  // sized, so nothing is allocated while capturing).  Else run directly.
+  FwdKey key;
+  key.nL = nL;
+  key.nf = nf;
+  key.nb = nb;
+  key.disc = disc;
+  key.gtype = gtype;
+  key.limb = limb;
+  key.flags = (scale ? 1 : 0) | (has_w ? 2 : 0) | (nTb ? 4 : 0) | (navg ? 8 : 0) | (nlay ? 16 : 0);
+  key.Req = Req;
+  key.Rpol = Rpol;
+  key.o0 = orient0;
+  key.o1 = orient1;
+  key.cfg = h->cfg_gen;
+  key.epoch = g_alloc_epoch.load();
+  const bool graphs = !h->profiling;
+  if (graphs && h->fwd_exec && key == h->fwd_key) {
+    RB_CUDA(cudaGraphLaunch(h->fwd_exec, st));
+    h->launches = h->fwd_launches;
+  } else if (graphs && key == h->fwd_seen) {
+    RB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rc || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return rc ? rc : fail(RB_ECUDA, "graph capture of rb_forward: %s", cudaGetErrorString(ec));
+    }
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(RB_ECUDA, "graph instantiation: %s", cudaGetErrorString(ei));
+    if (h->fwd_exec) cudaGraphExecDestroy(h->fwd_exec);
+    h->fwd_exec = ex;
+    h->fwd_key = key;
+    h->fwd_launches = h->launches;
+    RB_CUDA(cudaGraphLaunch(ex, st));
+  } else {
+    if ((rc = enqueue())) return rc;
+    key.epoch = g_alloc_epoch.load();   // after the buffers this shape needs exist
+    h->fwd_seen = graphs ? key : FwdKey{};
   }
-  if ((rc = forward_core(h, st, nL, h->d_P.as<double>(), h->d_T.as<double>(), h->d_X.as<double>(),
-                         h->d_R.as<double>(), h->d_N.as<double>(), dscale, Req, Rpol, orient0,
-                         orient1, gtype, limb, nb, h->d_b.as<double>(), dw, disc,
-                         h->d_Tb.as<double>(), Tb_avg ? h->d_avg.as<double>() : nullptr, dl)))
-    return rc;
-  if (Tb_out && nb > 0)
-    RB_CUDA(cudaMemcpyAsync(Tb_out, h->d_Tb.p, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
-  if (Tb_avg && nb > 0)
-    RB_CUDA(cudaMemcpyAsync(Tb_avg, h->d_avg.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
-  if (dl) RB_CUDA(cudaMemcpyAsync(layers_out, dl, sizeof(double) * (size_t)nf * nL, cudaMemcpyDeviceToHost, st));
   RB_CUDA(cudaStreamSynchronize(st));
+  if (nTb) std::memcpy(Tb_out, hout + oTb, sizeof(double) * nTb);
+  if (navg) std::memcpy(Tb_avg, hout + oavg, sizeof(double) * navg);
+  if (nlay) std::memcpy(layers_out, hout + olay, sizeof(double) * nlay);
   return RB_OK;
 }
 
