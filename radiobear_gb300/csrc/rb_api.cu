@@ -91,8 +91,9 @@ struct HBuf {
   T* as() const { return reinterpret_cast<T*>(p); }
 };
 
-// Shape of an rb_forward call from host buffers: everything a captured
-// graph of it bakes in (sizes, kernel scalars, configuration, addresses).
+// Shape of an rb_forward / rb_adjoint call from host buffers: everything a
+// captured graph of it bakes in (sizes, kernel scalars, configuration,
+// addresses).
 struct FwdKey {
   int nL = -1, nf = 0, nb = 0, disc = 0, gtype = 0, limb = 0, flags = 0;
   double Req = 0, Rpol = 0, o0 = 0, o1 = 0;
@@ -101,6 +102,18 @@ struct FwdKey {
     return nL == o.nL && nf == o.nf && nb == o.nb && disc == o.disc && gtype == o.gtype &&
            limb == o.limb && flags == o.flags && Req == o.Req && Rpol == o.Rpol && o0 == o.o0 &&
            o1 == o.o1 && cfg == o.cfg && epoch == o.epoch;
+  }
+};
+
+// The graph of the last call shape that ran twice, and the shape of the
+// last call that ran directly.
+struct GraphCache {
+  FwdKey seen, key;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
   }
 };
 
@@ -194,9 +207,7 @@ struct rb_handle {
   unsigned long long cfg_gen = 0;   // bumped by every setter and re-plan
   HBuf h_in, h_out;
   DBuf d_in;
-  FwdKey fwd_seen, fwd_key;
-  cudaGraphExec_t fwd_exec = nullptr;
-  int fwd_launches = 0;
+  GraphCache g_fwd, g_adj;
   // phase timing (rb_set_profiling)
   int profiling = 0;
   cudaEvent_t pev[10] = {};
@@ -738,7 +749,8 @@ int rb_destroy(rb_handle* h) {
   h->d_in.release();
   h->h_in.release();
   h->h_out.release();
-  if (h->fwd_exec) cudaGraphExecDestroy(h->fwd_exec);
+  h->g_fwd.release();
+  h->g_adj.release();
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->st) cudaStreamDestroy(h->st);
@@ -1091,6 +1103,47 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
 // absorption, then the scan and the quadrature average.  nb = rays per
 // atmosphere; with a batch (bt), nL is the total layer count and the
 // arrays are the variants' concatenation.
+// Runs a host-buffer call's work on st: replayed from the cached graph when
+// the call shape, configuration and buffer addresses match it; captured
+// and replayed when the same shape ran directly last time (every buffer is
+// sized then, so nothing is allocated while capturing); else run directly.
+static int run_cached(rb_handle* h, GraphCache& gc, FwdKey key, cudaStream_t st,
+                      const std::function<int()>& enqueue) {
+  key.cfg = h->cfg_gen;
+  key.epoch = g_alloc_epoch.load();
+  const bool graphs = !h->profiling;
+  if (graphs && gc.exec && key == gc.key) {
+    RB_CUDA(cudaGraphLaunch(gc.exec, st));
+    h->launches = gc.launches;
+    return RB_OK;
+  }
+  if (graphs && key == gc.seen) {
+    RB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rc || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return rc ? rc : fail(RB_ECUDA, "graph capture: %s", cudaGetErrorString(ec));
+    }
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(RB_ECUDA, "graph instantiation: %s", cudaGetErrorString(ei));
+    gc.release();
+    gc.exec = ex;
+    gc.key = key;
+    gc.launches = h->launches;
+    RB_CUDA(cudaGraphLaunch(ex, st));
+    return RB_OK;
+  }
+  const int rc = enqueue();
+  if (rc) return rc;
+  key.epoch = g_alloc_epoch.load();   // after the buffers this shape needs exist
+  gc.seen = graphs ? key : FwdKey{};
+  return RB_OK;
+}
+
 static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
                         const double* dX, const double* dR, const double* dN, const double* dscale,
                         double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
@@ -1218,9 +1271,6 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
     if (nlay) RB_CUDA(cudaMemcpyAsync(hout + olay, dl, sizeof(double) * nlay, cudaMemcpyDeviceToHost, st));
     return RB_OK;
   };
-  // Replay: the same call shape, configuration and buffer addresses as the
-  // captured graph.  Capture: the shape ran once already (every buffer is
-  // sized, so nothing is allocated while capturing).  Else run directly.
   FwdKey key;
   key.nL = nL;
   key.nf = nf;
@@ -1233,35 +1283,7 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
   key.Rpol = Rpol;
   key.o0 = orient0;
   key.o1 = orient1;
-  key.cfg = h->cfg_gen;
-  key.epoch = g_alloc_epoch.load();
-  const bool graphs = !h->profiling;
-  if (graphs && h->fwd_exec && key == h->fwd_key) {
-    RB_CUDA(cudaGraphLaunch(h->fwd_exec, st));
-    h->launches = h->fwd_launches;
-  } else if (graphs && key == h->fwd_seen) {
-    RB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    rc = enqueue();
-    cudaGraph_t g = nullptr;
-    const cudaError_t ec = cudaStreamEndCapture(st, &g);
-    if (rc || ec != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return rc ? rc : fail(RB_ECUDA, "graph capture of rb_forward: %s", cudaGetErrorString(ec));
-    }
-    cudaGraphExec_t ex = nullptr;
-    const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
-    cudaGraphDestroy(g);
-    if (ei != cudaSuccess) return fail(RB_ECUDA, "graph instantiation: %s", cudaGetErrorString(ei));
-    if (h->fwd_exec) cudaGraphExecDestroy(h->fwd_exec);
-    h->fwd_exec = ex;
-    h->fwd_key = key;
-    h->fwd_launches = h->launches;
-    RB_CUDA(cudaGraphLaunch(ex, st));
-  } else {
-    if ((rc = enqueue())) return rc;
-    key.epoch = g_alloc_epoch.load();   // after the buffers this shape needs exist
-    h->fwd_seen = graphs ? key : FwdKey{};
-  }
+  if ((rc = run_cached(h, h->g_fwd, key, st, enqueue))) return rc;
   RB_CUDA(cudaStreamSynchronize(st));
   if (nTb) std::memcpy(Tb_out, hout + oTb, sizeof(double) * nTb);
   if (navg) std::memcpy(Tb_avg, hout + oavg, sizeof(double) * navg);
@@ -1474,54 +1496,72 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
   if (nL < 1) return fail(RB_EINVAL, "nL must be >= 1");
   if (nb < 1) return fail(RB_EINVAL, "nb must be >= 1");
   if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
-  RB_CUDA(cudaSetDevice(h->device));
-  cudaStream_t st = h->st;
-  // the copies run while the inputs are validated (see rb_forward)
-  RB_CUDA(upload(h->d_P, P, nL, st));
-  RB_CUDA(upload(h->d_T, T, nL, st));
-  RB_CUDA(upload(h->d_X, X, (size_t)rb::NX * nL, st));
-  RB_CUDA(upload(h->d_R, R, nL, st));
-  RB_CUDA(upload(h->d_N, N, nL, st));
-  RB_CUDA(upload(h->d_b, b, 2 * (size_t)nb, st));
-  RB_CUDA(upload(h->d_grad, grad, weights ? (size_t)nf : (size_t)nb * nf, st));
-  const double* dscale = nullptr;
-  if (scale) {
-    RB_CUDA(upload(h->d_scale, scale, (size_t)nL * rb::NGAS, st));
-    dscale = h->d_scale.as<double>();
-  }
-  const double* dw = nullptr;
-  if (weights) {
-    RB_CUDA(upload(h->d_w, weights, nb, st));
-    dw = h->d_w.as<double>();
-  }
   int rc = validate_atm(nL, P, T, X);
   if (!rc) rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
   if (!rc && weights && !finite_all(weights, nb)) rc = fail(RB_EINVAL, "weights not finite");
-  if (!rc && !finite_all(grad, weights ? (size_t)nf : (size_t)nb * nf)) rc = fail(RB_EINVAL, "grad not finite");
+  const size_t ng = weights ? (size_t)nf : (size_t)nb * nf;
+  if (!rc && !finite_all(grad, ng)) rc = fail(RB_EINVAL, "grad not finite");
   if (!rc && scale && !finite_all(scale, (size_t)nL * rb::NGAS)) rc = fail(RB_EINVAL, "scale not finite");
-  if (rc) {
-    cudaStreamSynchronize(st);
-    return rc;
-  }
+  if (rc) return rc;
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
   if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
+  // one staged input block (each array at a 256-byte boundary) and one output block
+  auto al = [](size_t n) { return (n + 31) / 32 * 32; };
+  const size_t oP = 0, oT = oP + al(nL), oX = oT + al(nL), oR = oX + al((size_t)rb::NX * nL),
+               oN = oR + al(nL), ob = oN + al(nL), og = ob + al(2 * (size_t)nb), osc = og + al(ng),
+               ow = osc + (scale ? al((size_t)rb::NGAS * nL) : 0), nin = ow + (weights ? al(nb) : 0);
+  const size_t nTb = Tb_out ? (size_t)nb * nf : 0, navg = Tb_avg && weights ? (size_t)nf : 0;
+  const size_t oTb = 0, oavg = al(nTb), oth = oavg + al(navg), nout = oth + 5 * (size_t)nL;
+  RB_CUDA(h->h_in.ensure(sizeof(double) * nin));
+  RB_CUDA(h->h_out.ensure(sizeof(double) * nout));
+  RB_CUDA(h->d_in.ensure(sizeof(double) * nin));
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
   RB_CUDA(h->d_avg.ensure(sizeof(double) * nf));
   RB_CUDA(h->d_dth.ensure(sizeof(double) * 5 * (size_t)nL));
+  double* hin = h->h_in.as<double>();
+  std::memcpy(hin + oP, P, sizeof(double) * nL);
+  std::memcpy(hin + oT, T, sizeof(double) * nL);
+  std::memcpy(hin + oX, X, sizeof(double) * rb::NX * (size_t)nL);
+  std::memcpy(hin + oR, R, sizeof(double) * nL);
+  std::memcpy(hin + oN, N, sizeof(double) * nL);
+  std::memcpy(hin + ob, b, sizeof(double) * 2 * (size_t)nb);
+  std::memcpy(hin + og, grad, sizeof(double) * ng);
+  if (scale) std::memcpy(hin + osc, scale, sizeof(double) * rb::NGAS * (size_t)nL);
+  if (weights) std::memcpy(hin + ow, weights, sizeof(double) * nb);
+  const double* din = h->d_in.as<double>();
   double* dd = h->d_dth.as<double>();
-  if ((rc = rb_adjoint_device(h, st, nL, h->d_P.as<double>(), h->d_T.as<double>(),
-                              h->d_X.as<double>(), h->d_R.as<double>(), h->d_N.as<double>(), nf,
-                              freqs, dscale, Req, Rpol, orient0, orient1, gtype, limb, nb,
-                              h->d_b.as<double>(), dw, h->d_grad.as<double>(), h->d_Tb.as<double>(),
-                              dw ? h->d_avg.as<double>() : nullptr, dd, dd + nL, dd + 2 * (size_t)nL)))
-    return rc;
-  if (Tb_out)
-    RB_CUDA(cudaMemcpyAsync(Tb_out, h->d_Tb.p, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
-  if (Tb_avg && dw)
-    RB_CUDA(cudaMemcpyAsync(Tb_avg, h->d_avg.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
-  RB_CUDA(cudaMemcpyAsync(dT, dd, sizeof(double) * nL, cudaMemcpyDeviceToHost, st));
-  RB_CUDA(cudaMemcpyAsync(dP, dd + nL, sizeof(double) * nL, cudaMemcpyDeviceToHost, st));
-  RB_CUDA(cudaMemcpyAsync(dlnX, dd + 2 * (size_t)nL, sizeof(double) * 3 * nL, cudaMemcpyDeviceToHost, st));
+  double* hout = h->h_out.as<double>();
+  auto enqueue = [&]() -> int {
+    RB_CUDA(cudaMemcpyAsync(h->d_in.p, hin, sizeof(double) * nin, cudaMemcpyHostToDevice, st));
+    int r = adjoint_core(h, st, nL, din + oP, din + oT, din + oX, din + oR, din + oN,
+                         scale ? din + osc : nullptr, Req, Rpol, orient0, orient1, gtype, limb, nb,
+                         din + ob, weights ? din + ow : nullptr, din + og, h->d_Tb.as<double>(),
+                         weights ? h->d_avg.as<double>() : nullptr, dd, dd + nL, dd + 2 * (size_t)nL);
+    if (r) return r;
+    if (nTb) RB_CUDA(cudaMemcpyAsync(hout + oTb, h->d_Tb.p, sizeof(double) * nTb, cudaMemcpyDeviceToHost, st));
+    if (navg) RB_CUDA(cudaMemcpyAsync(hout + oavg, h->d_avg.p, sizeof(double) * navg, cudaMemcpyDeviceToHost, st));
+    RB_CUDA(cudaMemcpyAsync(hout + oth, dd, sizeof(double) * 5 * (size_t)nL, cudaMemcpyDeviceToHost, st));
+    return RB_OK;
+  };
+  FwdKey key;
+  key.nL = nL;
+  key.nf = nf;
+  key.nb = nb;
+  key.gtype = gtype;
+  key.limb = limb;
+  key.flags = (scale ? 1 : 0) | (weights ? 2 : 0) | (nTb ? 4 : 0) | (navg ? 8 : 0);
+  key.Req = Req;
+  key.Rpol = Rpol;
+  key.o0 = orient0;
+  key.o1 = orient1;
+  if ((rc = run_cached(h, h->g_adj, key, st, enqueue))) return rc;
   RB_CUDA(cudaStreamSynchronize(st));
+  if (nTb) std::memcpy(Tb_out, hout + oTb, sizeof(double) * nTb);
+  if (navg) std::memcpy(Tb_avg, hout + oavg, sizeof(double) * navg);
+  std::memcpy(dT, hout + oth, sizeof(double) * nL);
+  std::memcpy(dP, hout + oth + nL, sizeof(double) * nL);
+  std::memcpy(dlnX, hout + oth + 2 * (size_t)nL, sizeof(double) * 3 * nL);
   return RB_OK;
 }
 
