@@ -199,7 +199,7 @@ struct rb_handle {
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
       d_layer, d_r4, d_ll, d_end, d_Tb, d_avg, d_iw, d_tau, d_W, d_tbl, d_x, d_dR, d_sR, d_R32,
-      d_T32, d_hds, d_Tb32, d_part;
+      d_T32, d_hds, d_Tb32, d_part, d_rstart;
   int launches = 0;
   // rb_forward from host buffers: the inputs are staged in one pinned block
   // and uploaded with one copy, the outputs come back the same way, and a
@@ -638,6 +638,9 @@ void aspect_matrix(double Req, double Rpol, double o0, double o1, double* M) {
 
 // Geometry tables (float radii differences, float T) then the ray walk.
 // T may be null (no float temperature table needed).
+// Ray count from which the ray set-up runs one ray per thread in its own kernel.
+constexpr int RAY_SETUP_KERNEL_MIN = 2048;
+
 int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, const double* dN,
                     const double* dT, double Req, double Rpol, double o0, double o1, int gtype,
                     int limb, int nb, const double* db, int max_seg, int* dnseg, double* dds,
@@ -672,10 +675,20 @@ int enqueue_raypath(rb_handle* h, cudaStream_t st, int nL, const double* dR, con
   ra.r4ds = dr4;
   ra.latlng = dll;
   ra.end_code = dend;
+  // The float64 set-up of a ray (findEdge, first refraction) costs the same
+  // per warp instruction for one lane as for 32: with many rays it runs one
+  // ray per thread in its own kernel; with few, inside the walk's warp, so
+  // the walk starts (and takes its SM slots, ahead of the line sums on the
+  // other stream) without waiting for a second launch.
+  const bool setup_kernel = nb >= RAY_SETUP_KERNEL_MIN;
+  if (setup_kernel) {
+    RB_CUDA(h->d_rstart.ensure(sizeof(rb::RayStart) * nb));
+    ra.start = h->d_rstart.as<rb::RayStart>();
+  }
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[3], st));
   RB_CUDA(rb::launch_raypath(ra, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[4], st));
-  h->launches += 2;
+  h->launches += nb > 0 ? (setup_kernel ? 3 : 2) : 1;
   return RB_OK;
 }
 
@@ -730,7 +743,7 @@ int rb_destroy(rb_handle* h) {
   if (h->side) cudaStreamSynchronize(h->side);
   for (auto& f : h->fam) f.release();
   for (DBuf* b : {&h->d_sj, &h->d_sF, &h->d_sFhs, &h->d_sf, &h->d_swJ, &h->d_sset, &h->d_dR,
-                  &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part})
+                  &h->d_sR, &h->d_R32, &h->d_T32, &h->d_hds, &h->d_Tb32, &h->d_part, &h->d_rstart})
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
                   &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,

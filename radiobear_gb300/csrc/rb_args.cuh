@@ -141,6 +141,20 @@ struct ExtraArgs {
 // var_off[v+1]) and rays [v * rays_per_var, (v+1) * rays_per_var); all
 // variants share the impact parameters b[rays_per_var][2].  var_off == null
 // is a single atmosphere (one variant, every ray its own b).
+// Where a ray enters the atmosphere and its direction after the one
+// refraction at the top shell (raypath.py:60-160), written by
+// rb_ray_setup_kernel for the walk.
+struct RayStart {
+  double r0[3];     // edge point on the top shell [km]
+  double s[3];      // direction after the refraction
+  double u0;        // r0 . s
+  double ll0[2];    // latitude, longitude of the edge point [deg] (latlng output only)
+  float em1;        // E^2 - 1 at the edge point
+  float em1_eq;     // E^2 - 1 on the equator (the lat == 0 rule)
+  float mu;         // sqrt(1 - b^2)
+  int hit;          // 0: the ray misses the planet
+};
+
 struct RayArgs {
   int nL;
   const int* var_off;   // [nvar + 1] or null
@@ -163,6 +177,7 @@ struct RayArgs {
   double* r4ds;         // [nb][max_seg] or null
   double* latlng;       // [nb][max_seg+1][2] degrees or null
   int* end_code;        // [nb] or null: 1 index exit, 2 break, 3 capacity
+  RayStart* start;      // [nb] rb_ray_setup_kernel -> rb_raypath_kernel
 };
 
 struct TbArgs {

@@ -2,13 +2,20 @@
 // raypath.compute_ds / findEdge (raypath.py:60-273) and Shape._calcEllipse
 // (shape.py:223-274) for sm_103a.
 //
-// One warp per ray.
-//  * findEdge's trial points (a 0.005 rNorm march along the line of sight,
-//    raypath.py:62-87) are evaluated in float64, 32 at a time, one per lane;
-//    the first point inside the top shell is found with a ballot.
+// rb_ray_setup_kernel, one thread per ray (GB300 float64 costs the same
+// per warp instruction whatever the number of active lanes, so the float64
+// set-up is spread over the lanes, one ray each):
+//  * findEdge's march (trial points 0.005 rNorm apart along the line of
+//    sight, raypath.py:62-87) starts just before the line meets the sphere
+//    r = max(1, k) rNorm that encloses the top shell (no trial before it can
+//    be inside); each trial is tested with r1 < r2 rewritten without square
+//    roots (|v|^2 - |v|^4 > (1 - k^2) v_y^2, v the trial point / rNorm); the
+//    reference's own float64 formula then confirms the first inside trial
+//    and gives the two distances that findEdge interpolates.
 //  * The edge point, the first normal and the one refraction at the top
-//    (nratio = nr[0]/nr[1]) are float64 on lane 0.
-//  * The shell walk is a dependent chain on lane 0 in float32 / double-float.
+//    (nratio = nr[0]/nr[1]) follow in float64; the result is a RayStart.
+// rb_raypath_kernel, one warp per ray:
+//  * The shell walk is a dependent chain in float32 / double-float.
 //    After the first step the reference sets nratio = 1, so the direction s
 //    stays fixed (except the rare fold of arcsin(sin t) when the ray meets
 //    the local normal beyond 90 degrees, handled in float64).  The ray is
@@ -161,102 +168,99 @@ __device__ __forceinline__ df df_sqrt(df a) {
 __device__ __forceinline__ float df_val(df a) { return a.h + a.l; }
 __device__ __forceinline__ double df_d(df a) { return (double)a.h + (double)a.l; }
 
-__global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
-  const int ray = blockIdx.x;
-  const int lane = threadIdx.x;
-  if (ray >= a.nb) return;
-  const int bi = a.var_off ? ray % a.rays_per_var : ray;
-  const double b0 = a.b[2 * bi], b1 = a.b[2 * bi + 1];
-  int off = 0, nL = a.nL;
-  if (a.var_off) {
-    const int v = ray / a.rays_per_var;
-    off = a.var_off[v];
-    nL = a.var_off[v + 1] - off;
-  }
-  const double* R_ = a.R + off;
-  const double* N_ = a.N + off;
-  const float2* dR2_ = a.dR2 + off;
-  const float* dR_ = a.dR + off;
-  const float* R32_ = a.R32 + off;
-  const double rNorm = R_[0];
-  const double k = a.k;
-  double* ds_out = a.ds ? a.ds + (size_t)ray * a.max_seg : nullptr;
-  float* hds_out = a.hds ? a.hds + (size_t)ray * a.max_seg : nullptr;
-  int* lay_out = a.layer + (size_t)ray * a.max_seg;
-  double* r4_out = a.r4ds ? a.r4ds + (size_t)ray * a.max_seg : nullptr;
-  double* ll_out = a.latlng ? a.latlng + (size_t)ray * (a.max_seg + 1) * 2 : nullptr;
+// findEdge's distance r1 - r2 of trial point z (raypath.py:66-80), float64
+// exactly as the reference forms it.
+__device__ __forceinline__ double edge_dist(const double* rot, double b0, double b1, double z,
+                                            double rNorm, double k) {
+  double vx, vy, vz;
+  rot_apply(rot, b0, b1, z, vx, vy, vz);
+  const double r1 = sqrt(vx * vx + vy * vy + vz * vz) * rNorm;
+  const LatLng g = latlng_of(vx, vy, vz);
+  const double r2 = rNorm * sqrt(ellipse_factor2(g, k));
+  return r1 - r2;
+}
 
+// Trial points of findEdge (raypath.py:62-87, numpy arange semantics) and
+// the first one that can be inside: the line v(z) = p + z q (rNorm units)
+// meets the sphere of radius max(1, k) that encloses the top shell at
+// z = -B +/- sqrt(B^2 - A + K^2); every trial above the upper crossing is
+// outside.  i0 = -1: the line misses that sphere (no trial is inside).
+struct EdgeMarch {
+  double b0, b1, start, delta, c, ef2_eq;
+  long ntrial, i0;
+  __device__ __forceinline__ double z(long i) const { return i == 0 ? start : start + (double)i * delta; }
+  // r1 < r2 of raypath.py:66-80 without square roots:
+  // |v|^2 < (k^2 v_y^2 + v_x^2 + v_z^2) / |v|^2  <=>  |v|^2 - |v|^4 > (1 - k^2) v_y^2
+  // (v_y == 0 takes the reference's lat = 1e-6 rad rule).
+  __device__ __forceinline__ bool inside(const double* rot, long i) const {
+    double vx, vy, vz;
+    rot_apply(rot, b0, b1, z(i), vx, vy, vz);
+    const double rho = vx * vx + vy * vy + vz * vz;
+    return vy == 0.0 ? rho < ef2_eq : rho - rho * rho > c * (vy * vy);
+  }
+};
+
+__device__ __forceinline__ EdgeMarch edge_march(const double* rot, double b0, double b1, double k) {
+  EdgeMarch m;
+  m.b0 = b0;
+  m.b1 = b1;
   const double tmp = b0 * b0 + b1 * b1;
-  if (tmp >= 1.0) {   // raypath.py:126-127
-    if (lane == 0) {
-      a.nseg[ray] = 0;
-      if (a.end_code) a.end_code[ray] = 0;
-    }
-    return;
+  m.start = sqrt(1.0 - tmp) * 1.01;
+  m.ntrial = (long)ceil((0.0 - m.start) / -0.005);
+  m.delta = (m.start + -0.005) - m.start;
+  m.c = 1.0 - k * k;
+  m.ef2_eq = ellipse_factor2(latlng_of(1.0, 0.0, 1.0), k);
+  double px, py, pz, qx, qy, qz;
+  rot_apply(rot, b0, b1, 0.0, px, py, pz);
+  rot_apply(rot, 0.0, 0.0, 1.0, qx, qy, qz);
+  const double K2 = k > 1.0 ? k * k : 1.0;
+  const double A = px * px + py * py + pz * pz, B = px * qx + py * qy + pz * qz;
+  const double disc = B * B - A + K2;
+  m.i0 = disc > 0.0 ? (long)fmax(0.0, floor((m.start - (-B + sqrt(disc))) / 0.005) - 2.0) : -1;
+  return m;
+}
+
+// From a candidate first-inside trial to findEdge's edge point: the
+// reference's own float64 distance confirms the first inside trial (moving
+// the candidate if the two tests disagree at the surface) and gives the two
+// distances it interpolates.  Returns false if no trial is inside.
+__device__ __forceinline__ bool edge_point(const RayArgs& a, const EdgeMarch& m, long hit,
+                                           double rNorm, double k, double& zQ) {
+  if (hit < 0) return false;
+  double d_hit = edge_dist(a.rot, m.b0, m.b1, m.z(hit), rNorm, k), d_prev = 0.0;
+  while (!(d_hit < 0.0) && hit + 1 < m.ntrial) {
+    ++hit;
+    d_hit = edge_dist(a.rot, m.b0, m.b1, m.z(hit), rNorm, k);
   }
-  // ---------------- findEdge (raypath.py:60-105), numpy arange semantics
-  const double start = sqrt(1.0 - tmp) * 1.01;
-  const long ntrial = (long)ceil((0.0 - start) / -0.005);
-  const double delta = (start + -0.005) - start;
-  long hit = -1;
-  double d_hit = 0.0, z_hit = 0.0, d_prev = 0.0, z_prev = 0.0;
-  double d_last_lane31 = 0.0, z_last_lane31 = 0.0;
-  for (long base = 0; base < ntrial && hit < 0; base += 32) {
-    const long i = base + lane;
-    double d = 0.0, z = 0.0;
-    bool h = false;
-    if (i < ntrial) {
-      z = (i == 0) ? start : start + (double)i * delta;
-      double vx, vy, vz;
-      rot_apply(a.rot, b0, b1, z, vx, vy, vz);
-      const double r1 = sqrt(vx * vx + vy * vy + vz * vz) * rNorm;
-      const LatLng g = latlng_of(vx, vy, vz);
-      const double r2 = rNorm * sqrt(ellipse_factor2(g, k));
-      d = r1 - r2;
-      h = r1 < r2;
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, h);
-    const double dprev_in = __shfl_up_sync(0xffffffffu, d, 1);
-    const double zprev_in = __shfl_up_sync(0xffffffffu, z, 1);
-    if (m) {
-      const int first = __ffs(m) - 1;
-      const double dp = (first == 0) ? d_last_lane31 : dprev_in;
-      const double zp = (first == 0) ? z_last_lane31 : zprev_in;
-      d_hit = __shfl_sync(0xffffffffu, d, first);
-      z_hit = __shfl_sync(0xffffffffu, z, first);
-      d_prev = __shfl_sync(0xffffffffu, dp, first);
-      z_prev = __shfl_sync(0xffffffffu, zp, first);
-      hit = base + first;
-    }
-    d_last_lane31 = __shfl_sync(0xffffffffu, d, 31);
-    z_last_lane31 = __shfl_sync(0xffffffffu, z, 31);
+  if (!(d_hit < 0.0)) return false;
+  while (hit > 0) {
+    d_prev = edge_dist(a.rot, m.b0, m.b1, m.z(hit - 1), rNorm, k);
+    if (!(d_prev < 0.0)) break;
+    --hit;
+    d_hit = d_prev;
   }
-  if (hit < 0) {
-    if (lane == 0) {
-      a.nseg[ray] = 0;
-      if (a.end_code) a.end_code[ray] = 0;
-    }
-    return;
-  }
-  // From here every lane holds the same state (the float64 set-up is
-  // evaluated redundantly, which costs nothing extra per warp); lane 0
-  // writes the outputs of sequential steps, lane i those of the i-th step of
-  // a parallel block.
-  double zQ;
   if (hit == 0) {
-    zQ = z_hit;    // np.interp on a single point
+    zQ = m.z(0);   // np.interp on a single point
   } else {         // np.interp(0, [d_hit, d_prev], [z_hit, z_prev])
+    const double z_hit = m.z(hit), z_prev = m.z(hit - 1);
     const double slope = (z_prev - z_hit) / (d_prev - d_hit);
     zQ = slope * (0.0 - d_hit) + z_hit;
   }
+  return true;
+}
+
+// Edge point, first normal and the one refraction (raypath.py:106-160).
+__device__ __forceinline__ void ray_start(const RayArgs& a, double b0, double b1, double zQ,
+                                          double rNorm, double k, const double* N_, RayStart& o) {
   double ex, ey, ez;
   rot_apply(a.rot, b0, b1, zQ, ex, ey, ez);
   ex *= rNorm;
   ey *= rNorm;
   ez *= rNorm;
-  // ---------------- initial point, normal and refraction (raypath.py:130-160)
   const LatLng g0 = latlng_of(ex, ey, ez);
-  double r0x = g0.sg * (rNorm * g0.cl), r0y = k * rNorm * g0.sl, r0z = g0.cg * (rNorm * g0.cl);
+  o.r0[0] = g0.sg * (rNorm * g0.cl);
+  o.r0[1] = k * rNorm * g0.sl;
+  o.r0[2] = g0.cg * (rNorm * g0.cl);
   double nx, ny, nz;
   ellipse_normal(g0, k, nx, ny, nz);
   double sx, sy, sz;
@@ -271,10 +275,122 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
     sy = nratio * sy + cf * ny;
     sz = nratio * sz + cf * nz;
   }
-  const float mu = (float)sqrt(1.0 - b0 * b0 - b1 * b1);
+  o.s[0] = sx;
+  o.s[1] = sy;
+  o.s[2] = sz;
+  o.u0 = o.r0[0] * sx + o.r0[1] * sy + o.r0[2] * sz;
+  o.ll0[0] = o.ll0[1] = 0.0;
+  if (a.latlng) {
+    o.ll0[0] = (g0.sl == SIN_1EM6) ? 0.0 : asin(g0.sl) * 180.0 / CUDART_PI;
+    o.ll0[1] = atan2(g0.sg, g0.cg) * 180.0 / CUDART_PI;
+  }
+  o.em1 = (float)(ellipse_factor2(g0, k) - 1.0);   // step 0 uses the edge's latitude
+  o.em1_eq = (float)(ellipse_factor2(latlng_of(1.0, 0.0, 1.0), k) - 1.0);
+  o.mu = (float)sqrt(1.0 - b0 * b0 - b1 * b1);
+  o.hit = 1;
+}
+
+// Impact parameter and layer block of ray `ray`.
+__device__ __forceinline__ void ray_geometry(const RayArgs& a, int ray, double& b0, double& b1,
+                                             int& off, int& nL) {
+  const int bi = a.var_off ? ray % a.rays_per_var : ray;
+  b0 = a.b[2 * bi];
+  b1 = a.b[2 * bi + 1];
+  off = 0;
+  nL = a.nL;
+  if (a.var_off) {
+    const int v = ray / a.rays_per_var;
+    off = a.var_off[v];
+    nL = a.var_off[v + 1] - off;
+  }
+}
+
+// One thread per ray (many rays): findEdge trial by trial from the first
+// trial that can be inside, then the start of the walk.
+__global__ void __launch_bounds__(128) rb_ray_setup_kernel(RayArgs a) {
+  const int ray = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ray >= a.nb) return;
+  RayStart o{};
+  double b0, b1;
+  int off, nL;
+  ray_geometry(a, ray, b0, b1, off, nL);
+  const double rNorm = a.R[off];
+  if (b0 * b0 + b1 * b1 < 1.0) {   // raypath.py:126-127
+    const EdgeMarch m = edge_march(a.rot, b0, b1, a.k);
+    long hit = -1;
+    if (m.i0 >= 0)
+      for (long i = m.i0; i < m.ntrial; ++i)
+        if (m.inside(a.rot, i)) {
+          hit = i;
+          break;
+        }
+    double zQ;
+    if (edge_point(a, m, hit, rNorm, a.k, zQ)) ray_start(a, b0, b1, zQ, rNorm, a.k, a.N + off, o);
+  }
+  a.start[ray] = o;
+}
+
+// One warp per ray (few rays): findEdge 32 trials a pass, the rest of the
+// set-up evaluated alike on every lane (the walk then starts at once).
+__device__ __forceinline__ void ray_setup_warp(const RayArgs& a, int ray, int lane, RayStart& o) {
+  o = RayStart{};
+  double b0, b1;
+  int off, nL;
+  ray_geometry(a, ray, b0, b1, off, nL);
+  const double rNorm = a.R[off];
+  if (b0 * b0 + b1 * b1 >= 1.0) return;   // raypath.py:126-127
+  const EdgeMarch m = edge_march(a.rot, b0, b1, a.k);
+  long hit = -1;
+  if (m.i0 >= 0)
+    for (long base = m.i0; base < m.ntrial && hit < 0; base += 32) {
+      const long i = base + lane;
+      const unsigned in = __ballot_sync(0xffffffffu, i < m.ntrial && m.inside(a.rot, i));
+      if (in) hit = base + __ffs(in) - 1;
+    }
+  double zQ;
+  if (edge_point(a, m, hit, rNorm, a.k, zQ)) ray_start(a, b0, b1, zQ, rNorm, a.k, a.N + off, o);
+}
+
+__global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
+  const int ray = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (ray >= a.nb) return;
+  int off = 0, nL = a.nL;
+  if (a.var_off) {
+    const int v = ray / a.rays_per_var;
+    off = a.var_off[v];
+    nL = a.var_off[v + 1] - off;
+  }
+  const double* R_ = a.R + off;
+  const float2* dR2_ = a.dR2 + off;
+  const float* dR_ = a.dR + off;
+  const float* R32_ = a.R32 + off;
+  const double rNorm = R_[0];
+  const double k = a.k;
+  double* ds_out = a.ds ? a.ds + (size_t)ray * a.max_seg : nullptr;
+  float* hds_out = a.hds ? a.hds + (size_t)ray * a.max_seg : nullptr;
+  int* lay_out = a.layer + (size_t)ray * a.max_seg;
+  double* r4_out = a.r4ds ? a.r4ds + (size_t)ray * a.max_seg : nullptr;
+  double* ll_out = a.latlng ? a.latlng + (size_t)ray * (a.max_seg + 1) * 2 : nullptr;
+  RayStart rs;
+  if (a.start) rs = a.start[ray];
+  else ray_setup_warp(a, ray, lane, rs);
+  if (!rs.hit) {
+    if (lane == 0) {
+      a.nseg[ray] = 0;
+      if (a.end_code) a.end_code[ray] = 0;
+    }
+    return;
+  }
+  // every lane holds the same state; lane 0 writes the outputs of
+  // sequential steps, lane i those of the i-th step of a parallel block
+  double r0x = rs.r0[0], r0y = rs.r0[1], r0z = rs.r0[2];
+  double sx = rs.s[0], sy = rs.s[1], sz = rs.s[2];
+  double nx, ny, nz;
+  const float mu = rs.mu;
   const float omk2 = (float)(1.0 - k * k);
   // parametrisation r(S) = r0 + S s; S = u - u0
-  double u0 = r0x * sx + r0y * sy + r0z * sz;
+  double u0 = rs.u0;
   df u = df_make(u0);
   df mu0 = df_neg(u);
   df w = df_make(u0 * u0);
@@ -282,9 +398,9 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
   float twou0 = (float)(2.0 * u0);
   float y0 = (float)r0y, syf = (float)sy;
   // E^2 - 1 at the current point (step 0 uses the edge's latitude)
-  float em1 = (float)(ellipse_factor2(g0, k) - 1.0);
+  float em1 = rs.em1;
   const float kf = (float)k;
-  const float em1_eq = (float)(ellipse_factor2(latlng_of(1.0, 0.0, 1.0), k) - 1.0);
+  const float em1_eq = rs.em1_eq;
   const unsigned FULL = 0xffffffffu;
 
   int layer = 0;
@@ -372,10 +488,15 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
     // ======== one sequential step (tangent, exit, fold, end of path, or
     //          a block that did not converge); identical on every lane
     if (ll_out && lane == 0) {   // float64 reconstruction of the current point
-      const double S64 = df_d(u) - u0;
-      const LatLng g = nseg == 0 ? g0 : latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
-      ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
-      ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
+      if (nseg == 0) {
+        ll_out[0] = rs.ll0[0];
+        ll_out[1] = rs.ll0[1];
+      } else {
+        const double S64 = df_d(u) - u0;
+        const LatLng g = latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
+        ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
+        ll_out[2 * nseg + 1] = atan2(g.sg, g.cg) * 180.0 / CUDART_PI;
+      }
     }
     const int j = dir > 0 ? layer : wrap(layer - 1, nL);
     const float2 q2 = dR2_[j];
@@ -482,7 +603,10 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
     }
   }
   if (lane == 0) {
-    if (ll_out && code != 3) {
+    if (ll_out && code != 3 && nseg == 0) {
+      ll_out[0] = rs.ll0[0];
+      ll_out[1] = rs.ll0[1];
+    } else if (ll_out && code != 3) {
       const double S64 = df_d(u) - u0;
       const LatLng g = latlng_of(r0x + S64 * sx, r0y + S64 * sy, r0z + S64 * sz);
       ll_out[2 * nseg] = (g.sl == SIN_1EM6) ? 0.0 : asin(g.sl) * 180.0 / CUDART_PI;
@@ -502,6 +626,7 @@ cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* d
 
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st) {
   if (a.nb <= 0) return cudaSuccess;
+  if (a.start) rb_ray_setup_kernel<<<(a.nb + 127) / 128, 128, 0, st>>>(a);
   rb_raypath_kernel<<<a.nb, 32, 0, st>>>(a);
   return cudaGetLastError();
 }
