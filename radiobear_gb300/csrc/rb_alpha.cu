@@ -934,6 +934,8 @@ __device__ __forceinline__ void sjs_item(const AlphaArgs& a, Chunk (&buf)[2][2],
 }
 
 // ------------------------------------------------------------------ assembly
+constexpr int ASM_TMAX = 16;   // templates summed from registers by the assembly
+
 // Sum of the items of one family for one slot, in template order (the
 // items were written by the line-sum kernel launched before).
 __device__ __forceinline__ float fam_sum(const AlphaArgs& a, const float* r, int fam) {
@@ -953,20 +955,36 @@ __device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int til
   const LayerParams& lp = a.lp[L];
   const float* r = a.res + res_index(a, L, tile, 0) + ls;
   const int set = a.sp.set[s];
-  float inv = 0.f, rot = 0.f, v2 = 0.f, sjs = 0.f, h2o = 0.f, base = 0.f, h2s = 0.f, ph3 = 0.f;
-  if (fam_enabled(a, lp, FAM_NH3_INV)) {
-    inv = fam_sum(a, r, FAM_NH3_INV);
-    rot = fam_sum(a, r, FAM_NH3_ROT);
-    v2 = fam_sum(a, r, FAM_NH3_V2);
+  // Family sums in template order.  Up to ASM_TMAX templates every item's
+  // value is loaded first (independent loads, one round trip to L2) and
+  // added under the family's template range; items of a family that is off
+  // in this layer were not written and are never selected.
+  float fs[NFAM];
+#pragma unroll
+  for (int f = 0; f < NFAM; ++f) fs[f] = 0.f;
+  if (a.ntmpl <= ASM_TMAX) {
+    float v[ASM_TMAX];
+#pragma unroll
+    for (int t = 0; t < ASM_TMAX; ++t) v[t] = t < a.ntmpl ? __ldcg(r + (size_t)t * a.spt) : 0.f;
+#pragma unroll
+    for (int f = 0; f < NFAM; ++f)
+#pragma unroll
+      for (int t = 0; t < ASM_TMAX; ++t)
+        if (t >= a.vbeg[f] && t < a.vend[f]) fs[f] += v[t];
+  } else {
+    for (int f = 0; f < NFAM; ++f) fs[f] = fam_sum(a, r, f);
   }
-  if (fam_enabled(a, lp, FAM_NH3_SJS)) sjs = fam_sum(a, r, FAM_NH3_SJS);
+  const bool hs_on = fam_enabled(a, lp, FAM_NH3_INV);
+  const float inv = hs_on ? fs[FAM_NH3_INV] : 0.f, rot = hs_on ? fs[FAM_NH3_ROT] : 0.f,
+              v2 = hs_on ? fs[FAM_NH3_V2] : 0.f;
+  const float sjs = fam_enabled(a, lp, FAM_NH3_SJS) ? fs[FAM_NH3_SJS] : 0.f;
+  const float h2o = a.cfg.use_h2o ? fs[FAM_H2O] : 0.f;
+  const float h2s = a.cfg.use_h2s ? fs[FAM_H2S] : 0.f, ph3 = a.cfg.use_ph3 ? fs[FAM_PH3] : 0.f;
+  float base = 0.f;
   if (a.cfg.use_h2o) {
-    h2o = fam_sum(a, r, FAM_H2O);
     const float* bs = a.base + ((size_t)L * a.ntile + tile) * a.ntmpl;
     for (int t = a.vbeg[FAM_H2O]; t < a.vend[FAM_H2O]; ++t) base += __ldcg(bs + t);
   }
-  if (a.cfg.use_h2s) h2s = fam_sum(a, r, FAM_H2S);
-  if (a.cfg.use_ph3) ph3 = fam_sum(a, r, FAM_PH3);
   double co = 0.0, cl = 0.0;
   if (a.extra) {
     co = a.extra[(size_t)L * a.nf + j];
