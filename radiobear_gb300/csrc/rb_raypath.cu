@@ -152,14 +152,28 @@ __device__ __forceinline__ df df_mulf(df a, float b) {
   r.l = e - (r.h - p);
   return r;
 }
-// sqrt of a positive double-float: one Newton correction of sqrtf(hi)
+// a + b without the final renormalisation (prefix scans: the low words
+// stay a few ulp of the high word and are renormalised once at the end)
+__device__ __forceinline__ df df_add_lazy(df a, df b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return {s, e + (a.l + b.l)};
+}
+__device__ __forceinline__ df df_norm(df a) {
+  df r;
+  r.h = a.h + a.l;
+  r.l = a.l - (r.h - a.h);
+  return r;
+}
+// sqrt of a positive double-float: one Newton correction of sqrtf(hi); the
+// correction (~1e-7 of the result) takes an approximate reciprocal
 __device__ __forceinline__ df df_sqrt(df a) {
   const float y = sqrtf(a.h);
   if (y == 0.f) return {0.f, 0.f};
   const float r = fmaf(-y, y, a.h) + a.l;
   df o;
   o.h = y;
-  o.l = r / (2.f * y);
+  o.l = r * rcp_approx(2.f * y);
   const float t = o.h + o.l;
   o.l = o.l - (t - o.h);
   o.h = t;
@@ -437,9 +451,9 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const float h = __shfl_up_sync(FULL, v.h, o), l = __shfl_up_sync(FULL, v.l, o);
-          if (lane >= o) v = df_add(df{h, l}, v);
+          if (lane >= o) v = df_add_lazy(df{h, l}, v);
         }
-        W = df_add(w, v);
+        W = df_add(w, df_norm(v));
         const bool negl = W.h < 0.f || (W.h == 0.f && W.l < 0.f);
         const df r = df_sqrt(negl ? df{0.f, 0.f} : W);
         un = dir == 1 ? df_neg(r) : r;
