@@ -159,6 +159,17 @@ __device__ __forceinline__ df df_add_lazy(df a, df b) {
   two_sum(a.h, b.h, s, e);
   return {s, e + (a.l + b.l)};
 }
+// float value of a + b (the high word of the normalised sum)
+__device__ __forceinline__ float df_sum(df a, df b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return s + (e + (a.l + b.l));
+}
+// a * b for a double-float and a float, not renormalised
+__device__ __forceinline__ df df_mulf_lazy(df a, float b) {
+  const float p = a.h * b;
+  return {p, fmaf(a.h, b, -p) + a.l * b};
+}
 __device__ __forceinline__ df df_norm(df a) {
   df r;
   r.h = a.h + a.l;
@@ -446,7 +457,7 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
       int first = 32;
       bool conv = false;
       for (int it = 0; it < 4 && !conv; ++it) {
-        const df D = df_add(dr2, df_mulf(dr2, g));
+        const df D = df_add_lazy(dr2, df_mulf_lazy(dr2, g));   // renormalised after the scan
         df v = D;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -457,7 +468,7 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
         const bool negl = W.h < 0.f || (W.h == 0.f && W.l < 0.f);
         const df r = df_sqrt(negl ? df{0.f, 0.f} : W);
         un = dir == 1 ? df_neg(r) : r;
-        const float S = df_val(df_add(un, mu0));
+        const float S = df_sum(un, mu0);
         const float rr2 = fmaf(S, S + twou0, R0sq);
         const float y = fmaf(S, syf, y0);
         em1n = (y == 0.f) ? em1_eq : -omk2 * __fdividef(y * y, rr2);
@@ -481,7 +492,7 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
           const float uph = __shfl_up_sync(FULL, un.h, 1), upl = __shfl_up_sync(FULL, un.l, 1);
           const df uprev = lane == 0 ? u : df{uph, upl};
           if (lane < taken) {
-            const float step = df_val(df_add(un, df_neg(uprev)));
+            const float step = df_sum(un, df_neg(uprev));
             if (ds_out) ds_out[nseg + lane] = (double)step;
             if (hds_out) hds_out[nseg + lane] = step * 0.5e5f;
             lay_out[nseg + lane] = c;
@@ -538,7 +549,7 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
     } else {
       const df r = df_sqrt(wn);
       un = dir == 1 ? df_neg(r) : r;
-      step = df_val(df_add(un, df_neg(u)));
+      step = df_sum(un, df_neg(u));
       w = wn;
     }
     if (step < 0.f) {
@@ -564,7 +575,7 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
     ++nseg;
     // advance along the ray
     u = un;
-    const float S = df_val(df_add(u, mu0));
+    const float S = df_sum(u, mu0);
     const float rr2 = fmaf(S, S + twou0, R0sq);
     const float y = fmaf(S, syf, y0);
     em1 = (y == 0.f) ? em1_eq : -omk2 * __fdividef(y * y, rr2);
