@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
           const float h = __shfl_up_sync(FULL, v.h, o), l = __shfl_up_sync(FULL, v.l, o);
           if (lane >= o) v = df_add_lazy(df{h, l}, v);
         }
-        W = df_add(w, df_norm(v));
+        W = df_norm(df_add_lazy(w, v));
         const bool negl = W.h < 0.f || (W.h == 0.f && W.l < 0.f);
         const df r = df_sqrt(negl ? df{0.f, 0.f} : W);
         un = dir == 1 ? df_neg(r) : r;
@@ -472,6 +472,11 @@ __global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
         const float rr2 = fmaf(S, S + twou0, R0sq);
         const float y = fmaf(S, syf, y0);
         em1n = (y == 0.f) ? em1_eq : -omk2 * __fdividef(y * y, rr2);
+        if (it == 0) {   // predictor: one shared guess almost never is the fixed point
+          g = __shfl_up_sync(FULL, em1n, 1);
+          if (lane == 0) g = em1;
+          continue;
+        }
         // fold check at the new point (c < 0 <=> dir (k u + (1-k) s_y y) > 0)
         const float uf = df_val(un);
         const float val = (float)dir * fmaf(kf, uf, (1.f - kf) * syf * y);
