@@ -291,11 +291,15 @@ __device__ __forceinline__ void ray_start(const RayArgs& a, double b0, double b1
   double sx, sy, sz;
   rot_apply(a.rot, 0.0, 0.0, -1.0, sx, sy, sz);
   {
+    // raypath.py:150-160: t_inc = arccos(c0), t_tran = arcsin(nratio sin t_inc),
+    // cf = nratio cos t_inc - cos t_tran, with sin(arccos c0) = sqrt(1 - c0^2)
+    // and cos(arcsin x) = sqrt(1 - x^2) (no trigonometric calls; nan where
+    // numpy's arccos / arcsin give nan)
     const double c0 = -(sx * nx + sy * ny + sz * nz);
-    const double t_inc = (c0 >= -1.0 && c0 <= 1.0) ? acos(c0) : CUDART_NAN;
     const double nratio = N_[0] / N_[1];
-    const double t_tran = asin(nratio * sin(t_inc));
-    const double cf = nratio * cos(t_inc) - cos(t_tran);
+    const double s2 = fma(-c0, c0, 1.0);                      // sin^2 t_inc
+    const double ct2 = fma(-(nratio * nratio), s2, 1.0);      // cos^2 t_tran
+    const double cf = (c0 >= -1.0 && c0 <= 1.0) ? nratio * c0 - sqrt(ct2) : CUDART_NAN;
     sx = nratio * sx + cf * nx;
     sy = nratio * sy + cf * ny;
     sz = nratio * sz + cf * nz;
