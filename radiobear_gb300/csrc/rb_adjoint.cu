@@ -844,8 +844,12 @@ __device__ __forceinline__ void jv_family(const JvpArgs& a, JvpShared& sh, int L
 
 // Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
 // sweeps lines g, g + NG, ... of every chunk and the groups' sums are added
-// per family.
-__global__ void __launch_bounds__(256, 3) rb_alpha_jvp_kernel(JvpArgs a) {
+// per family.  MINB resident CTAs per SM: 4 (64 registers) for 128-frequency
+// tiles, 3 (80 registers) for smaller ones (measured: C4's 128 frequencies
+// 68.4 -> 64.2 ms per 512 variants at 4; C3's 64 frequencies 0.693 -> 0.719
+// ms per step at 4).
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
   __shared__ __align__(16) JvpShared sh;
   const int L = blockIdx.x;
   const int tid = threadIdx.x;
@@ -1036,7 +1040,8 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   }
   rb_layer_tan_kernel<<<(tn.nL * 8 + 255) / 256, 256, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
-  rb_alpha_jvp_kernel<<<grid, 256, 0, st>>>(jv);
+  if (jv.ft >= 128) rb_alpha_jvp_kernel<4><<<grid, 256, 0, st>>>(jv);
+  else rb_alpha_jvp_kernel<3><<<grid, 256, 0, st>>>(jv);
   if (ea) {
     cudaError_t x = launch_extra_vjp(*ea, st);
     if (x != cudaSuccess) return x;
