@@ -867,7 +867,7 @@ __global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
   split_double(f, fr.fq, fr.fql);
   const int set = fh > 30.0 ? 1 : 0;
   fr.set = set;
-  fr.wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)((f - 26.0) / 8.0));
+  fr.wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)(f - 26.0) * 0.125f);   // (f - 26) / 8
   const bool nh3 = a.cfg.nh3_mode != NH3_OFF;
   // families that are off keep zero sums (read back by the same thread)
   if (grp == 0)
@@ -913,72 +913,75 @@ __global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
       dbase[2] += s_b[w][3];
     }
   }
-  // assemble dalpha/dtheta (cm^-1) in float64 and contract with dTb/dalpha
-  double g5[NTH] = {0, 0, 0, 0, 0};
+  // dalpha/dtheta (cm^-1) of this (layer, frequency), contracted with
+  // dTb/dalpha.  The per-frequency combination is float32 (its inputs, the
+  // family sums, tangents and coefficients, are float32; GB300's float64
+  // rate made it ~10 % of the kernel); the sum over frequencies, where terms
+  // of both signs meet, is float64.
+  float g5[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f};
   if (on && grp == 0) {
     auto fv = [&](int fam) { return sh.fam[fam][fi][0]; };
     auto fd = [&](int fam) { return &sh.fam[fam][fi][1]; };
-    const double gal = (double)a.galpha[(size_t)L * a.nf + j];
-    const double Fd = f * f, Fhd = fh * fh;
-    auto pref = [&](int fam) { return ldexp((double)lp.fam[fam].fm, lp.fam[fam].fe); };
+    const float gal = a.galpha[(size_t)L * a.nf + j];
+    const float Fd = fr.F + fr.FL, Fhd = fr.Fh + fr.FhL;
+    auto pref = [&](int fam) { return ldexpf(lp.fam[fam].fm, lp.fam[fam].fe); };
     // d(pref * S) / dtheta for a family with tangent triple (T, P, X_own)
-    double dal[NTH] = {0, 0, 0, 0, 0};
-    auto add_fam = [&](int fam, double mult, double s, const float* ds, double* out) {
+    float dal[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    auto add_fam = [&](int fam, float mult, float sv, const float* ds, float* out) {
       const FamTan& FT = LT.fam[fam];
-      const double p = pref(fam) * mult;
+      const float pm = pref(fam) * mult;
       const int xt = fam_xtan(fam);
-      out[TH_T] += p * ((double)FT.dlnpref[TH_T] * s + ds[0]);
-      out[TH_P] += p * ((double)FT.dlnpref[TH_P] * s + ds[1]);
-      for (int q = 2; q < NTH; ++q) {
-        const double dx = (q == xt) ? ds[2] : 0.0;
-        out[q] += p * ((double)FT.dlnpref[q] * s + dx);
-      }
+      out[TH_T] += pm * fmaf(FT.dlnpref[TH_T], sv, ds[0]);
+      out[TH_P] += pm * fmaf(FT.dlnpref[TH_P], sv, ds[1]);
+#pragma unroll
+      for (int q = 2; q < NTH; ++q) out[q] += pm * fmaf(FT.dlnpref[q], sv, q == xt ? ds[2] : 0.f);
     };
     // H2 CIA
     if (a.cfg.use_h2)
-      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2] * (double)LT.dh2_cia[q] * Fd;
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2] * LT.dh2_cia[q] * Fd;
     // H2O lines and continuum
     if (a.cfg.use_h2o) {
-      double d[NTH] = {0, 0, 0, 0, 0};
+      float d[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f};
       const float ds[3] = {fd(FAM_H2O)[0] - dbase[0], fd(FAM_H2O)[1] - dbase[1], fd(FAM_H2O)[2] - dbase[2]};
-      add_fam(FAM_H2O, 1.0, (double)fv(FAM_H2O) - base, ds, d);
-      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2O] * (d[q] + (double)LT.dh2o_cont[q]) * Fd;
+      add_fam(FAM_H2O, 1.f, fv(FAM_H2O) - base, ds, d);
+      for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2O] * (d[q] + LT.dh2o_cont[q]) * Fd;
     }
     if (a.cfg.use_h2s) {
-      double d[NTH] = {0, 0, 0, 0, 0};
-      add_fam(FAM_H2S, 1.0, fv(FAM_H2S), fd(FAM_H2S), d);
+      float d[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      add_fam(FAM_H2S, 1.f, fv(FAM_H2S), fd(FAM_H2S), d);
       for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_H2S] * d[q] * Fd;
     }
     if (a.cfg.use_ph3) {
-      double d[NTH] = {0, 0, 0, 0, 0};
-      add_fam(FAM_PH3, 1.0, fv(FAM_PH3), fd(FAM_PH3), d);
+      float d[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      add_fam(FAM_PH3, 1.f, fv(FAM_PH3), fd(FAM_PH3), d);
       for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_PH3] * d[q] * Fd;
     }
     if (nh3) {
-      double hs = 0.0, dhs[NTH] = {0, 0, 0, 0, 0}, sj = 0.0, dsj[NTH] = {0, 0, 0, 0, 0};
-      const double INVC[2][2] = {{0.9301, 0.9862}, {0.9619, 0.9862}};   // Con, per table and set
+      float hs = 0.f, dhs[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f}, sj = 0.f, dsj[NTH] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      const float INVC[2][2] = {{0.9301f, 0.9862f}, {0.9619f, 0.9862f}};   // Con, per table and set
       if (lp.use_hs) {
-        hs = Fhd * (pref(FAM_NH3_INV) * INVC[a.cfg.inv_table][set] * fv(FAM_NH3_INV) +
-                    pref(FAM_NH3_ROT) * fv(FAM_NH3_ROT) + pref(FAM_NH3_V2) * fv(FAM_NH3_V2));
-        add_fam(FAM_NH3_INV, INVC[a.cfg.inv_table][set], fv(FAM_NH3_INV), fd(FAM_NH3_INV), dhs);
-        add_fam(FAM_NH3_ROT, 1.0, fv(FAM_NH3_ROT), fd(FAM_NH3_ROT), dhs);
-        add_fam(FAM_NH3_V2, 1.0, fv(FAM_NH3_V2), fd(FAM_NH3_V2), dhs);
+        const float con = INVC[a.cfg.inv_table][set];
+        hs = Fhd * (pref(FAM_NH3_INV) * con * fv(FAM_NH3_INV) + pref(FAM_NH3_ROT) * fv(FAM_NH3_ROT) +
+                    pref(FAM_NH3_V2) * fv(FAM_NH3_V2));
+        add_fam(FAM_NH3_INV, con, fv(FAM_NH3_INV), fd(FAM_NH3_INV), dhs);
+        add_fam(FAM_NH3_ROT, 1.f, fv(FAM_NH3_ROT), fd(FAM_NH3_ROT), dhs);
+        add_fam(FAM_NH3_V2, 1.f, fv(FAM_NH3_V2), fd(FAM_NH3_V2), dhs);
         for (int q = 0; q < NTH; ++q) dhs[q] *= Fhd;
-        if (hs < 0.0) {   // clamped to 1e-8 (nh3_hs.py:311-312): no derivative
-          hs = 1.0e-8;
-          for (int q = 0; q < NTH; ++q) dhs[q] = 0.0;
+        if (hs < 0.f) {   // clamped to 1e-8 (nh3_hs.py:311-312): no derivative
+          hs = 1.0e-8f;
+          for (int q = 0; q < NTH; ++q) dhs[q] = 0.f;
         }
       }
       if (lp.use_sjs) {
         sj = Fd * pref(FAM_NH3_SJS) * fv(FAM_NH3_SJS);
-        add_fam(FAM_NH3_SJS, 1.0, fv(FAM_NH3_SJS), fd(FAM_NH3_SJS), dsj);
+        add_fam(FAM_NH3_SJS, 1.f, fv(FAM_NH3_SJS), fd(FAM_NH3_SJS), dsj);
         for (int q = 0; q < NTH; ++q) dsj[q] *= Fd;
       }
-      double dn[NTH];
+      float dn[NTH];
       if (lp.use_hs && lp.use_sjs) {
-        const double W = lp.blendW;
-        for (int q = 0; q < NTH; ++q) dn[q] = W * dsj[q] + (1.0 - W) * dhs[q];
-        dn[TH_P] += (double)LT.dblendW_dP * (sj - hs);
+        const float W = lp.blendW;
+        for (int q = 0; q < NTH; ++q) dn[q] = W * dsj[q] + (1.f - W) * dhs[q];
+        dn[TH_P] += LT.dblendW_dP * (sj - hs);
       } else {
         for (int q = 0; q < NTH; ++q) dn[q] = lp.use_hs ? dhs[q] : dsj[q];
       }
@@ -986,18 +989,22 @@ __global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
     }
     for (int q = 0; q < NTH; ++q) g5[q] = gal * dal[q];
   }
-  // reduce over the CTA's frequencies
-  for (int q = 0; q < NTH; ++q)
-    for (int o = 16; o; o >>= 1) g5[q] += __shfl_xor_sync(0xffffffffu, g5[q], o);
-  if ((tid & 31) == 0)
-    for (int q = 0; q < NTH; ++q) sh.red[tid >> 5][q] = g5[q];
-  // (sh.red holds up to 8 warps)
+  // reduce over the CTA's frequencies (float64; only the warps of line
+  // group 0 hold values: FTL is a multiple of 32)
+  const int nw0 = FTL >> 5;
+  if (grp == 0) {
+    for (int q = 0; q < NTH; ++q) {
+      double g = (double)g5[q];
+      for (int o = 16; o; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+      if ((tid & 31) == 0) sh.red[tid >> 5][q] = g;
+    }
+  }
   __syncthreads();
   if (tid == 0) {
     for (int q = 0; q < NTH; ++q) {
-      double s = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh.red[w][q];
-      a.part[((size_t)L * gridDim.y + blockIdx.y) * NTH + q] = s;
+      double sq = 0.0;
+      for (int w = 0; w < nw0; ++w) sq += sh.red[w][q];
+      a.part[((size_t)L * gridDim.y + blockIdx.y) * NTH + q] = sq;
     }
   }
 }
