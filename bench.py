@@ -645,7 +645,8 @@ def run_gpu(args, rank, world, local_rank):
     batched = measure_batch(args, dev, args.batch_variants) if args.batch_variants > 0 else None
     if rank != 0:
         return
-    # roofline of the dominant kernel (absorption) and of the Tb scan
+    # roofline of the dominant kernel (the line sums, timed alone on their
+    # stream) and of the Tb scan
     flops, counts = alpha_flops(wl)
     fp32_peak = eng.probe_fp32_peak()
     ach = flops / (ph['alpha'] * 1e-3) / 1e12
@@ -666,11 +667,11 @@ def run_gpu(args, rank, world, local_rank):
         e2e=dict(value=1.0 / float(np.mean(e2e_times)), unit=UNIT, h2d_bytes_per_step=int(h2d),
                  d2h_bytes_per_step=int(d2h), api='rb_forward (C ABI, pinned host buffers)'),
         gpu_launches=int(launches_per_step * args.steps),
-        roofline=dict(bound='fp32', kernel='rb_alpha_kernel', achieved=ach, peak=fp32_peak,
+        roofline=dict(bound='fp32', kernel='rb_alpha_lines_kernel', achieved=ach, peak=fp32_peak,
                       unit='TFLOP/s', frac=ach / fp32_peak, traffic=read_profile_traffic(),
                       algorithmic_flops_per_launch=flops,
                       peak_source='in-run FFMA probe (no fp32 entry in MEASURED_PEAKS.json)'),
-        roofline_scan=dict(bound='hbm', kernel='rb_tb_kernel', achieved=scan_gbs, peak=hbm,
+        roofline_scan=dict(bound='hbm', kernel='rb_tb_chunk2_kernel+rb_tb_combine_kernel', achieved=scan_gbs, peak=hbm,
                            unit='GB/s', frac=(scan_gbs / hbm) if hbm else None,
                            algorithmic_bytes_per_launch=sbytes,
                            peak_source='MEASURED_PEAKS.json hbm_gbs (of measured)'),

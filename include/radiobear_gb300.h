@@ -312,8 +312,9 @@ int rb_regrid_device(rb_handle* h, void* stream, int nvar, const int32_t* nin_ho
 
 /* Phase timing.  With profiling on, rb_forward / rb_forward_device record
  * CUDA events around each kernel on the stream it is launched on;
- * rb_phase_times then fills ms[0..4] = layer prep, absorption, ray paths,
- * brightness, disc average of the last call (synchronises the handle). */
+ * rb_phase_times then fills ms[0..5] = layer prep, line sums, ray paths,
+ * brightness, disc average, assembly of the absorption (first n of them)
+ * of the last call (synchronises the handle). */
 int rb_set_profiling(rb_handle* h, int on);
 int rb_phase_times(rb_handle* h, double* ms, int n);
 

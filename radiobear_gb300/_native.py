@@ -384,12 +384,12 @@ class Engine:
     def set_profiling(self, on=True):
         _check(self.lib, self.lib.rb_set_profiling(self._h, int(on)), 'rb_set_profiling')
 
-    PHASES = ('prep', 'alpha', 'raypath', 'brightness', 'disc_avg')
+    PHASES = ('prep', 'alpha', 'raypath', 'brightness', 'disc_avg', 'assembly')
 
     def phase_times(self):
         """Milliseconds of each phase of the last forward call."""
-        ms = np.zeros(5)
-        _check(self.lib, self.lib.rb_phase_times(self._h, _ptr(ms), 5), 'rb_phase_times')
+        ms = np.zeros(len(self.PHASES))
+        _check(self.lib, self.lib.rb_phase_times(self._h, _ptr(ms), ms.size), 'rb_phase_times')
         return dict(zip(self.PHASES, ms.tolist()))
 
     def probe_fp32_peak(self):

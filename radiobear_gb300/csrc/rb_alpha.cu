@@ -1090,6 +1090,10 @@ cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st
     if (aa.M == 4) rb_alpha_lines_kernel<4><<<nb, nthr, 0, st>>>(aa);
     else rb_alpha_lines_kernel<2><<<nb, nthr, 0, st>>>(aa);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_alpha_assemble(const AlphaArgs& aa, cudaStream_t st) {
   const size_t n = (size_t)aa.nL * aa.nslot;
   rb_alpha_assemble_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(aa);
   return cudaGetLastError();

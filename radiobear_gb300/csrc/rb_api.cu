@@ -224,6 +224,7 @@ void set_last_error(const char* msg) { g_err = msg; }
 namespace rb {
 cudaError_t launch_prep(const PrepArgs& pa, cudaStream_t st);
 cudaError_t launch_alpha_lines(const AlphaArgs& aa, int nblocks, cudaStream_t st);
+cudaError_t launch_alpha_assemble(const AlphaArgs& aa, cudaStream_t st);
 cudaError_t launch_extra(const ExtraArgs& a, cudaStream_t st);
 cudaError_t launch_atm_props(const AtmPropArgs& a, int nvar, cudaStream_t st);
 cudaError_t launch_atm_regrid(const AtmRegridArgs& a, int nvar, cudaStream_t st);
@@ -613,6 +614,8 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   if (extra) RB_CUDA(rb::launch_extra(ea, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[1], st));
   RB_CUDA(rb::launch_alpha_lines(aa, h->plan_grid, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[8], st));
+  RB_CUDA(rb::launch_alpha_assemble(aa, st));
   if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[2], st));
   // prep, [extra,] [line sums,] assembly
   h->launches += (extra ? 1 : 0) + 1 + (aa.nitems > 0 ? 2 : 1);
@@ -1764,13 +1767,14 @@ int rb_phase_times(rb_handle* h, double* ms, int n) {
   if (!h->profiling) return fail(RB_ESTATE, "profiling is off (rb_set_profiling)");
   RB_CUDA(cudaSetDevice(h->device));
   RB_CUDA(cudaEventSynchronize(h->pev[7]));
-  float t[5] = {0, 0, 0, 0, 0};
+  float t[6] = {0, 0, 0, 0, 0, 0};
   RB_CUDA(cudaEventElapsedTime(&t[0], h->pev[0], h->pev[1]));
-  RB_CUDA(cudaEventElapsedTime(&t[1], h->pev[1], h->pev[2]));
+  RB_CUDA(cudaEventElapsedTime(&t[1], h->pev[1], h->pev[8]));
   RB_CUDA(cudaEventElapsedTime(&t[2], h->pev[3], h->pev[4]));
   RB_CUDA(cudaEventElapsedTime(&t[3], h->pev[5], h->pev[6]));
   RB_CUDA(cudaEventElapsedTime(&t[4], h->pev[6], h->pev[7]));
-  for (int i = 0; i < n && i < 5; ++i) ms[i] = t[i];
+  RB_CUDA(cudaEventElapsedTime(&t[5], h->pev[8], h->pev[2]));
+  for (int i = 0; i < n && i < 6; ++i) ms[i] = t[i];
   return RB_OK;
 }
 
