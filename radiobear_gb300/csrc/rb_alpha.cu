@@ -934,7 +934,7 @@ __device__ __forceinline__ void sjs_item(const AlphaArgs& a, Chunk (&buf)[2][2],
 }
 
 // ------------------------------------------------------------------ assembly
-constexpr int ASM_TMAX = 16;   // templates summed from registers by the assembly
+constexpr int ASM_TMAX = 16;   // templates summed from registers by the assembly (= tfam size)
 
 // Sum of the items of one family for one slot, in template order (the
 // items were written by the line-sum kernel launched before).
@@ -947,18 +947,18 @@ __device__ __forceinline__ float fam_sum(const AlphaArgs& a, const float* r, int
 
 // One slot of one layer: family sums -> per-gas absorption, scaled, float32
 // total for the brightness scan and the optional float64 outputs.
-__device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int tile, int ls) {
+__device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int tile, int ls,
+                                              const LayerParams& lp) {
   const int s = tile * a.spt + ls;
   if (s >= a.nslot) return;
-  const int j = a.sp.j[s];
+  const int j = s < a.nf ? s : -1;   // the frequency plan's slot -> frequency map (padding -1)
   if (j < 0) return;
-  const LayerParams& lp = a.lp[L];
   const float* r = a.res + res_index(a, L, tile, 0) + ls;
   const int set = a.sp.set[s];
   // Family sums in template order.  Up to ASM_TMAX templates every item's
   // value is loaded first (independent loads, one round trip to L2) and
-  // added under the family's template range; items of a family that is off
-  // in this layer were not written and are never selected.
+  // added to its template's family; items of a family that is off in this
+  // layer were not written and their sums are not used.
   float fs[NFAM];
 #pragma unroll
   for (int f = 0; f < NFAM; ++f) fs[f] = 0.f;
@@ -967,10 +967,18 @@ __device__ __forceinline__ void assemble_slot(const AlphaArgs& a, int L, int til
 #pragma unroll
     for (int t = 0; t < ASM_TMAX; ++t) v[t] = t < a.ntmpl ? __ldcg(r + (size_t)t * a.spt) : 0.f;
 #pragma unroll
-    for (int f = 0; f < NFAM; ++f)
-#pragma unroll
-      for (int t = 0; t < ASM_TMAX; ++t)
-        if (t >= a.vbeg[f] && t < a.vend[f]) fs[f] += v[t];
+    for (int t = 0; t < ASM_TMAX; ++t) {
+      if (t >= a.ntmpl) break;
+      switch (a.tfam[t]) {   // kernel argument, the same for every thread
+        case FAM_NH3_INV: fs[FAM_NH3_INV] += v[t]; break;
+        case FAM_NH3_ROT: fs[FAM_NH3_ROT] += v[t]; break;
+        case FAM_NH3_V2: fs[FAM_NH3_V2] += v[t]; break;
+        case FAM_NH3_SJS: fs[FAM_NH3_SJS] += v[t]; break;
+        case FAM_H2O: fs[FAM_H2O] += v[t]; break;
+        case FAM_H2S: fs[FAM_H2S] += v[t]; break;
+        default: fs[FAM_PH3] += v[t]; break;
+      }
+    }
   } else {
     for (int f = 0; f < NFAM; ++f) fs[f] = fam_sum(a, r, f);
   }
@@ -1058,13 +1066,30 @@ __global__ void __launch_bounds__(128, M >= 4 ? 4 : 6) rb_alpha_lines_kernel(Alp
 }
 
 // Assembly: one thread per (layer, slot), layers x nslot threads in a 1-D
-// grid (the batched sweeps have millions of layers).
+// grid (the batched sweeps have millions of layers).  The CTA first copies
+// the LayerParams of the layers it spans into shared memory with one
+// coalesced read (the slots' coefficient reads then wait on no round trips);
+// a CTA spans at most ASM_LMAX layers when a layer has 32 slots or more.
+constexpr int ASM_LMAX = 5;
 __global__ void __launch_bounds__(128) rb_alpha_assemble_kernel(AlphaArgs a) {
-  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= (size_t)a.nL * a.nslot) return;
+  __shared__ __align__(16) LayerParams s_lp[ASM_LMAX];
+  const size_t ntot = (size_t)a.nL * a.nslot;
+  const size_t g0 = (size_t)blockIdx.x * blockDim.x;
+  const int L0 = (int)(g0 / a.nslot);
+  const int nlay = (int)((min(g0 + blockDim.x, ntot) - 1) / a.nslot) - L0 + 1;
+  const bool staged = nlay <= ASM_LMAX;
+  if (staged) {
+    constexpr int WORDS = (int)(sizeof(LayerParams) / sizeof(int));
+    const int* src = reinterpret_cast<const int*>(a.lp + L0);
+    int* dst = reinterpret_cast<int*>(s_lp);
+    for (int i = threadIdx.x; i < nlay * WORDS; i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+  const size_t g = g0 + threadIdx.x;
+  if (g >= ntot) return;
   const int L = (int)(g / a.nslot);
   const int s = (int)(g - (size_t)L * a.nslot);
-  assemble_slot(a, L, s / a.spt, s % a.spt);
+  assemble_slot(a, L, s / a.spt, s % a.spt, staged ? s_lp[L - L0] : a.lp[L]);
 }
 
 // ------------------------------------------------------------------ launch

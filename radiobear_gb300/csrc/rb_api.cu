@@ -585,6 +585,7 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   for (int v = 0; v < rb::NFAM; ++v) {
     aa.vbeg[v] = h->plan_vbeg[v];
     aa.vend[v] = h->plan_vend[v];
+    for (int t = h->plan_vbeg[v]; t < h->plan_vend[v] && t < 16; ++t) aa.tfam[t] = (unsigned char)v;
   }
   aa.nitems = aa.ntmpl * nL * aa.ntile;
   aa.counter = h->d_counter.as<int>();

@@ -61,6 +61,7 @@ struct AlphaArgs {
   const TmplEntry* tmpl;    // [ntmpl], grouped by family
   int ntmpl;
   int vbeg[NFAM], vend[NFAM];  // template range of each family
+  unsigned char tfam[16];      // family of templates 0..15 (the assembly's sums)
   int nitems;               // ntmpl * nL * ntile
   int* counter;             // work counter, zeroed by rb_layer_prep_kernel
   float* res;               // [nL][ntile][ntmpl][spt] per-item line sums
