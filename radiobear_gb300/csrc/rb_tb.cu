@@ -273,8 +273,10 @@ __global__ void __launch_bounds__(128, 6) rb_tb_chunk2_kernel(TbArgs a) {
   int ray = 0, ch = 0, n = 0, i0 = 0;
   bool live = false;
   if (item < nitem) {
-    ray = (int)(item / a.nchunk);
-    ch = (int)(item % a.nchunk);
+    // chunk-major: a CTA's items are one chunk index of consecutive rays, so
+    // the chunks past the rays' ends gather in CTAs that exit at once
+    ch = (int)(item / a.nb);
+    ray = (int)(item % a.nb);
     const int nsteps = a.nseg[ray] - 1;
     i0 = ch * TB_CHUNK;
     live = i0 < nsteps;
