@@ -150,14 +150,19 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
   const double Pd = a.P[L], Td = a.T[L];
   const float P = (float)Pd, T = (float)Td;
   const double* X = a.X;
-  const float Ph2 = (float)(Pd * X[X_H2 * nL + L]), Phe = (float)(Pd * X[X_HE * nL + L]);
-  const float Pch4 = (float)(Pd * X[X_CH4 * nL + L]), Pnh3 = (float)(Pd * X[X_NH3 * nL + L]);
-  const float Ph2o = (float)(Pd * X[X_H2O * nL + L]), Ph2s = (float)(Pd * X[X_H2S * nL + L]);
-  const float Pph3 = (float)(Pd * X[X_PH3 * nL + L]);
+  // partial pressures in float32 (they are float32 from here on; float64
+  // products cost ~64 cycles of GB300's FP64 pipe per warp instruction)
+  const float Ph2 = P * (float)X[X_H2 * nL + L], Phe = P * (float)X[X_HE * nL + L];
+  const float Pch4 = P * (float)X[X_CH4 * nL + L], Pnh3 = P * (float)X[X_NH3 * nL + L];
+  const float Ph2o = P * (float)X[X_H2O * nL + L], Ph2s = P * (float)X[X_H2S * nL + L];
+  const float Pph3 = P * (float)X[X_PH3 * nL + L];
   LayerParams& o = a.out[L];
   // strength temperature coefficients, log2 units, float64 (the only
   // float64 of the absorption path: 1/T - 1/T0 cancels near T0)
-  const double invT = 1.0 / Td;
+  // (a float reciprocal refined by one float64 Newton step, ~1e-14 relative,
+  // instead of a float64 division)
+  const double r0 = (double)__frcp_rn((float)Td);
+  const double invT = fma(r0, fma(-Td, r0, 1.0), r0);
   // NH3 formalism choice (nh3_hs_sjs.py:6-26)
   int use_hs = 0, use_sjs = 0;
   float blendW = 0.f;
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
     } else {
       use_hs = 1;
       use_sjs = 1;
-      blendW = (float)((Pd - 400.0) / (2000.0 - 400.0));
+      blendW = (float)(Pd - 400.0) * (1.f / (2000.f - 400.f));
     }
   }
   const float Tdiv = 300.f / T;
