@@ -15,6 +15,7 @@ import numpy as np
 from . import build as _build
 
 LIB_PATH = _build.LIB
+ABI_VERSION = 2      # RB_ABI_VERSION of include/radiobear_gb300.h
 
 RB_OK = 0
 FAM = dict(NH3_INV=0, NH3_ROT=1, NH3_V2=2, NH3_SJS=3, H2O=4, H2S=5, PH3=6, CO=7)
@@ -125,6 +126,10 @@ def load_library(path=None):
         for name in EXPORTS:
             getattr(lib, name).restype = getattr(lib, name).restype or c_int
         lib.rb_last_error.restype = ctypes.c_char_p
+        if lib.rb_abi_version() != ABI_VERSION:
+            raise RBError('{} has ABI version {}, this binding expects {}; rebuild it with '
+                          '`python -m radiobear_gb300.build`'.format(p, lib.rb_abi_version(),
+                                                                     ABI_VERSION))
         _lib = lib
         return lib
 

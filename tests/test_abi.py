@@ -20,6 +20,9 @@ def declared_symbols():
 def test_header_declares_entry_points():
     syms = declared_symbols()
     assert 'rb_forward' in syms and 'rb_alpha' in syms and len(syms) >= 12
+    with open(os.path.join(ROOT, 'include', 'radiobear_gb300.h')) as fp:
+        ver = re.search(r'#define RB_ABI_VERSION (\d+)', fp.read())
+    assert ver and int(ver.group(1)) == _native.ABI_VERSION
 
 
 def test_library_builds_and_exports_every_declared_symbol():
@@ -32,7 +35,7 @@ def test_library_builds_and_exports_every_declared_symbol():
 
 def test_abi_version_and_error_path_without_gpu():
     lib = _native.load_library()
-    assert lib.rb_abi_version() == 2
+    assert lib.rb_abi_version() == _native.ABI_VERSION == 2
     try:
         import torch
         has_gpu = torch.cuda.is_available()
