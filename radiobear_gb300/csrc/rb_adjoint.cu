@@ -13,7 +13,7 @@
 //                           (c_i the trapezoid node weight, E = exp(-tau));
 //                           adds g dTb/dalpha and g W c / intW (the
 //                           source-temperature term) per visited layer.
-//   rb_layer_tan_kernel     eight threads per layer: the layer coefficients
+//   rb_layer_tan_kernel     eight parts per layer: the layer coefficients
 //                           of the absorption (widths, couplings, strength
 //                           prefactors, continua) in dual numbers, giving
 //                           their derivatives with respect to the layer's
@@ -346,13 +346,15 @@ __device__ constexpr float INV_SET_D[2][2][13] = {
      {1.7465, 0.9779, 0.7298, 0.8202, 1.0, 1.0, 1.2163, 0.0291, 0.5152, 0.8873, 0.8994, 0.66666667,
       -0.0627}}};
 
-// Derivatives of the layer coefficients, eight threads per layer (the parts
-// of rb_layer_prep_kernel: 0 shared, 1 inversion, 2 rotational, 3 nu2,
-// 4 nh3_sjs, 5 H2S, 6 PH3, 7 H2O).
-__global__ void __launch_bounds__(256) rb_layer_tan_kernel(TanArgs a) {
+// Derivatives of the layer coefficients, eight parts per layer (those of
+// rb_layer_prep_kernel: 0 shared, 1 inversion, 2 rotational, 3 nu2,
+// 4 nh3_sjs, 5 H2S, 6 PH3, 7 H2O), threads numbered part-major over the
+// layers padded to a multiple of 32 (one part per warp).
+__global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int L = gid / 8, part = gid % 8;
-  if (L >= a.nL) return;
+  const int nLp = (a.nL + 31) & ~31;
+  const int part = gid / nLp, L = gid - part * nLp;
+  if (part >= 8 || L >= a.nL) return;
   const int nL = a.nL;
   const double Pd = a.P[L], Td = a.T[L];
   const double* X = a.X;
@@ -1045,7 +1047,7 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
     rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);
     rb_tb_adj_grad_kernel<<<grid, blk, 0, st>>>(ta);
   }
-  rb_layer_tan_kernel<<<(tn.nL * 8 + 255) / 256, 256, 0, st>>>(tn);
+  rb_layer_tan_kernel<<<(((tn.nL + 31) & ~31) * 8 + 63) / 64, 64, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
   if (jv.ft >= 128) rb_alpha_jvp_kernel<4><<<grid, 256, 0, st>>>(jv);
   else rb_alpha_jvp_kernel<3><<<grid, 256, 0, st>>>(jv);
