@@ -25,7 +25,7 @@
 //
 // Numerics (per line l, frequency f, F = f^2):
 //   Ben-Reuven  S_l [(g-z) F + (g+z) K_l] / [(F - K_l)^2 + 4 F g^2],
-//               K_l = (fo+d)^2 + g^2 - z^2      (nh3_hs.py:216-225, h2s_ddb.py:270-272)
+//               K_l = (fo+d)^2 + g^2 - z^2      (nh3_hs.py:216-225, h2s_ddb.py:77-78)
 //   Gross       S_l g / [(F - fo^2)^2 + 4 F g^2]          (nh3_hs.py:260-263)
 //   VVW         S_l df [1/((f-fo)^2+df^2) + 1/((f+fo)^2+df^2) - 2/(750^2+df^2)]
 //                                                         (h2o_bk.py:174-187)
