@@ -382,24 +382,48 @@ def scan_bytes(nseg, nf, nb):
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
+    """nvidia-smi samples every 50 ms while the timed steps run.  Entering
+    waits (at most 3 s) for the first sample so the sampler is live before
+    the first timed step; `region(t0, t1)` gives the timed region's wall
+    clock, and the summary keeps the samples stamped inside it (all samples
+    if none is)."""
+    FIELDS = ('timestamp', 'index', 'clocks.sm', 'clocks.max.sm', 'power.draw',
+              'clocks_event_reasons.active', 'clocks_event_reasons.hw_slowdown',
+              'clocks_event_reasons.hw_thermal_slowdown',
+              'clocks_event_reasons.sw_thermal_slowdown', 'clocks_event_reasons.sw_power_cap')
+    REASONS = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.path = None
+        self.window = None
+
+    def _start(self, period_ms):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index),
+                                          '--query-gpu=' + ','.join(self.FIELDS),
+                                          '--format=csv,noheader,nounits', '-lms', str(period_ms)],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+            return
+        deadline = time.time() + 3.0
+        while time.time() < deadline and self.proc.poll() is None:
+            if self._rows():
+                return
+            time.sleep(0.01)
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix='.csv')
         os.close(fd)
-        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
-             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
-             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
-        try:
-            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + q,
-                                          '--format=csv,noheader,nounits', '-lms', '200'],
-                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
-        except OSError:
-            self.proc = None
+        self._start(50)
+        if self.proc is not None and self.proc.poll() is not None and not self._rows():
+            self._start(200)     # the 50 ms period refused: the usual 200 ms
         return self
+
+    def region(self, t0, t1):
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -409,27 +433,57 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
+    def _rows(self):
         rows = []
         try:
             with open(self.path) as fp:
                 for line in fp:
+                    if not line.endswith('\n'):
+                        break
                     parts = [p.strip() for p in line.split(',')]
-                    if len(parts) >= 9:
+                    if len(parts) >= len(self.FIELDS):
                         rows.append(parts)
         except OSError:
             pass
-        finally:
-            if self.path and os.path.exists(self.path):
-                os.unlink(self.path)
+        return rows
+
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text, '%Y/%m/%d %H:%M:%S.%f').timestamp()
+        except ValueError:
+            return None
+
+    @staticmethod
+    def _num(text):
+        try:
+            return float(text)
+        except ValueError:
+            return None
+
+    def summary(self):
+        rows = self._rows()
+        if self.path and os.path.exists(self.path):
+            os.unlink(self.path)
         if not rows:
             return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
-        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
-        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        inside = []
+        if self.window is not None:
+            t0, t1 = self.window[0] - 0.025, self.window[1] + 0.025
+            for r in rows:
+                t = self._stamp(r[0])
+                if t is not None and t0 <= t <= t1:
+                    inside.append(r)
+        in_region = bool(inside)
+        use = inside if in_region else rows
+        sm = [v for v in (self._num(r[2]) for r in use) if v is not None]
+        mx = [v for v in (self._num(r[3]) for r in use) if v is not None]
+        reasons = sorted({self.REASONS[i] for r in use for i in range(4)
+                          if r[6 + i].lower() == 'active'})
         return {'sm_mhz': statistics.median(sm) if sm else None,
-                'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons, 'samples': len(rows)}
+                'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons,
+                'samples': len(use), 'in_timed_region': in_region}
 
 
 def read_profile_traffic():
@@ -599,12 +653,14 @@ def run_gpu(args, rank, world, local_rank):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     with ClockSampler(local_rank) as clk:
+        t_wall0 = time.time()
         for i in range(args.steps):
             flush.zero_()
             ev[i][0].record(stream)
             step()
             ev[i][1].record(stream)
         torch.cuda.synchronize()
+        clk.region(t_wall0, time.time())
     if dist is not None:
         dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in ev]
