@@ -46,3 +46,12 @@ def test_abi_version_and_error_path_without_gpu():
     with pytest.raises(_native.RBError):
         _native.Engine(0)
     assert lib.rb_last_error()
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """The product path has no CPU fallback: without the built library the
+    binding raises instead of computing anything."""
+    with pytest.raises(_native.RBError, match='not built'):
+        _native.load_library(str(tmp_path / 'librbgpu.so'))
+    # the cached library of the other tests is untouched
+    assert _native.load_library() is _native.load_library()
