@@ -408,7 +408,7 @@ def alpha_h2o_bk(freq, T, P, Xh2, Xhe, Xh2o, cat):
 # ---------------------------------------------------------------- h2s / ph3
 def _br_geisa(freq, f0, gamma, zeta, delta, ITG):
     """The Ben-Reuven line sum shared by nh3_sjs / h2s_ddb / ph3_jh
-    (h2s_ddb.py:68-73, ph3_jh.py:75-81).  gamma etc. [nL, nlines]."""
+    (h2s_ddb.py:74-80, ph3_jh.py:95-101).  gamma etc. [nL, nlines]."""
     out = np.empty((gamma.shape[0], len(freq)))
     g2 = gamma ** 2
     z2 = zeta ** 2

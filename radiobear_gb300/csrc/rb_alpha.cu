@@ -477,7 +477,7 @@ __device__ __forceinline__ void line_fields(const LineTable& t, const LayerFam& 
     v[5] = -cl;
     v[6] = d2;
     v[7] = h;
-    base_part += 2.f * h / (562500.f + d2);     // the -2 df / (750^2 + df^2) term (h2o_bk.py:183-185)
+    base_part += 2.f * h / (562500.f + d2);     // the -2 df / (750^2 + df^2) term (h2o_bk.py:174-176,184)
   } else {  // K_SJS
     const float fo = t.ch[li];
     float KH, e;

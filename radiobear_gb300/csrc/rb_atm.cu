@@ -26,7 +26,7 @@ namespace rb {
 
 constexpr double ATM_GRAV = 6.6738e-20;   // km3/kg/s2, chemistry.py:7
 constexpr double ATM_RGAS = 8.314462;     // J/K/mol, chemistry.py:8
-constexpr double ATM_FILL = -999.9;       // regrid.py:66
+constexpr double ATM_FILL = -999.9;       // regrid.py:63
 constexpr int ATM_THREADS = 256;
 
 __device__ __forceinline__ double refr_col(const AtmCols& c, int k, double T) {

@@ -156,7 +156,7 @@ __device__ S co_alpha(const ExtraArgs& a, int L, S T, S P, double f) {
 
 // ------------------------------------------------------------------ clouds_idp
 // Imaginary part of the dielectric constant of ice below 0 C, log-log
-// interpolated in frequency (clouds_idp.py:71-72,88-100).
+// interpolated in frequency (clouds_idp.py:68-69,88-99).
 __device__ constexpr double ICE_FR[9] = {1.0E8, 3.0E8, 1.0E9, 2.0E9, 3.0E9, 5.0E9, 1.0E10, 3.0E10, 1.0E11};
 __device__ constexpr double ICE_EIMAG[9] = {8.0E-3, 1.5E-3, 8.0E-4, 1.0E-3, 1.2E-3, 1.5E-3, 3.0E-3, 8.0E-3, 2.0E-2};
 
