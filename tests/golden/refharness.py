@@ -11,7 +11,7 @@ What it does to run the reference (none of it edits reference files):
   ``Atmosphere.std`` path) because matplotlib is not installed;
 * runs in a scratch working directory holding a ``Jupiter/`` folder, since
   the reference resolves ``<Planet>/config.par`` relative to the cwd
-  (``radiobear/planet_base.py:52``, ``radiobear/config.py:193``);
+  (``radiobear/planet_base.py:52``, ``radiobear/config.py:76``);
 * injects line lists by setting the module-global ``data`` of the formalism
   module objects the dispatcher actually calls (bare names for
   ``h2o_bk``/``h2s_ddb``/``ph3_jh``, ``alpha.py:63-67``; package paths for
