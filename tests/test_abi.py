@@ -55,3 +55,31 @@ def test_missing_library_fails_loudly(tmp_path):
         _native.load_library(str(tmp_path / 'librbgpu.so'))
     # the cached library of the other tests is untouched
     assert _native.load_library() is _native.load_library()
+
+
+def test_header_is_plain_c99_and_links(tmp_path):
+    """A C caller (cgo, N-API, a C application) includes the header under
+    strict C99 and links every entry point against the library."""
+    import shutil
+    import subprocess
+    if shutil.which('gcc') is None:
+        pytest.skip('gcc not available')
+    lib = build.build()
+    syms = declared_symbols()
+    src = tmp_path / 'caller.c'
+    src.write_text(
+        '#include "radiobear_gb300.h"\n#include <stdio.h>\n'
+        'typedef void (*rb_fn)(void);\n'
+        'int main(void) {\n  const rb_fn entry[] = {\n' +
+        ''.join('    (rb_fn)&{},\n'.format(s) for s in syms) +
+        '  };\n  printf("%d %d\\n", (int)(sizeof entry / sizeof entry[0]), rb_abi_version());\n'
+        '  return 0;\n}\n')
+    exe = tmp_path / 'caller'
+    libdir = os.path.dirname(lib)
+    r = subprocess.run(['gcc', '-std=c99', '-Wall', '-Wextra', '-Werror', '-pedantic',
+                        '-I' + os.path.join(ROOT, 'include'), str(src), '-o', str(exe),
+                        '-L' + libdir, '-l' + os.path.basename(lib)[3:-3],
+                        '-Wl,-rpath,' + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out == [str(len(syms)), str(_native.ABI_VERSION)]
