@@ -185,6 +185,20 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
                   int disc, double* Tb_out, double* intW_out, double* tau_out, double* W_out,
                   double* TbL_out);
 
+/* The b loop of Planet.run (radiobear/planet.py:118-133 -> bright_run,
+ * planet_base.py:244-274 -> Brightness.single, brightness.py:30-126) for nb
+ * rays through one atmosphere at once, given the absorption the run already
+ * computed: layers[nf][nL] (cm^-1, Alpha.layers), T[nL] K, R/N and the
+ * geometry as in rb_raypath.  Ray paths stay on the device; the
+ * absorption is uploaded once.  Exp weighting (the reference's 'disc' is a
+ * single nadir ray: use rb_brightness with disc = 1).
+ * Tb_out[nb][nf]; nullable intW_out[nb][nf]; nullable nseg_out[nb]
+ * (0 for a ray that misses the planet, whose Tb is T_cmb). */
+int rb_bright_run(rb_handle* h, int nL, const double* T, const double* R, const double* N,
+                  double Req, double Rpol, double orient0, double orient1, int gtype, int limb,
+                  int nf, const double* layers, int nb, const double* b, double* Tb_out,
+                  double* intW_out, int32_t* nseg_out);
+
 /* Fused forward model from host buffers: absorption, ray paths and Tb for
  * nb rays with device-resident intermediates.  Optional weights[nb] give
  * Tb_avg[nf] = sum_k weights[k] Tb[k][:].  disc = 1 evaluates every ray as
@@ -343,8 +357,12 @@ int rb_probe_fp32_peak(rb_handle* h, double* tflops);
  * without synchronising.  Its scratch is one fixed file-scope device array
  * shared by every call, so calls that overlap on the GPU race: serialise
  * them.  The first call on a device looks up that array's address; make it
- * before any stream capture.  Sizes beyond RB_NOALLOC_SCRATCH_ELEMS are
- * rejected with RB_EINVAL. */
+ * before any stream capture.  That address is cached for the life of the
+ * process: do not use this entry point after cudaDeviceReset (or another
+ * reset of the device's primary context) on a device it has already run on.
+ * Sizes beyond RB_NOALLOC_SCRATCH_ELEMS, and ceil(max_seg / 128) or
+ * ceil(nf / 128) above 65535, are rejected with RB_EINVAL; nb itself is
+ * limited only by the scratch size. */
 int rb_brightness_noalloc(void* stream, int nL, int nf, const float* alpha32, const double* T,
                           int nb, const int32_t* nseg, const double* ds, const int32_t* layer,
                           int max_seg, double* Tb);

@@ -50,7 +50,7 @@ EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set
            'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
            'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device',
            'rb_set_co_clouds', 'rb_atm_props', 'rb_atm_props_device', 'rb_regrid',
-           'rb_regrid_device')
+           'rb_regrid_device', 'rb_bright_run')
 
 _lib = None
 _lock = threading.Lock()
@@ -97,6 +97,8 @@ def load_library(path=None):
                                    c_int, c_int, c_int, _d, c_int, _i, _d, _i, _d, _d, _i]
         lib.rb_brightness.argtypes = [_vp, c_int, _d, c_int, _d, c_int, _i, _d, _i, c_int, c_int,
                                       _d, _d, _d, _d, _d]
+        lib.rb_bright_run.argtypes = [_vp, c_int, _d, _d, _d, c_double, c_double, c_double, c_double,
+                                      c_int, c_int, c_int, _d, c_int, _d, _d, _d, _i]
         # host arrays as addresses (numpy .ctypes.data): cheaper per call than pointer objects
         lib.rb_forward.argtypes = [_vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _vp, _vp, c_double,
                                    c_double, c_double, c_double, c_int, c_int, c_int, _vp, _vp,
@@ -264,6 +266,25 @@ class Engine:
                                     _ptr(tau), _ptr(W), _ptr(tbl))
         _check(self.lib, rc, 'rb_brightness')
         return dict(Tb=Tb, intW=iw, tau=tau, W=W, TbL=tbl)
+
+    def bright_run(self, T, R, N, layers, b, Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse',
+                   limb='shape'):
+        """Every ray of b[nb, 2] through one atmosphere with the given
+        absorption layers [nf, nL] (rb_bright_run): returns Tb [nb, nf],
+        intW [nb, nf] and nseg [nb]."""
+        T, R, N, layers = _f64(T), _f64(R), _f64(N), _f64(layers)
+        b = _f64(np.atleast_2d(b))
+        nf, nL = layers.shape
+        nb = b.shape[0]
+        Tb = np.empty((nb, nf))
+        iw = np.empty((nb, nf))
+        nseg = np.zeros(nb, dtype=np.int32)
+        rc = self.lib.rb_bright_run(self._h, nL, _ptr(T), _ptr(R), _ptr(N), float(Req), float(Rpol),
+                                    float(orientation[0]), float(orientation[1]), GTYPE[gtype],
+                                    LIMB[limb], nf, _ptr(layers), nb, _ptr(b), _ptr(Tb), _ptr(iw),
+                                    _ptr(nseg, ctypes.c_int32))
+        _check(self.lib, rc, 'rb_bright_run')
+        return dict(Tb=Tb, intW=iw, nseg=nseg)
 
     def forward(self, P, T, X, R, N, freqs, b, Req, Rpol, orientation=(0.0, 0.0),
                 gtype='ellipse', limb='shape', weights=None, disc=False, scale=None,

@@ -1116,6 +1116,71 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
   return RB_OK;
 }
 
+// Planet.run's b loop (planet.py:118-133 -> planet_base.py:244-274 ->
+// Brightness.single) for every ray of one atmosphere at once, given the
+// absorption the run computed (Alpha.layers): ray paths into device
+// buffers, then the chunked scan, the absorption uploaded once per call.
+int rb_bright_run(rb_handle* h, int nL, const double* T, const double* R, const double* N,
+                  double Req, double Rpol, double orient0, double orient1, int gtype, int limb,
+                  int nf, const double* layers, int nb, const double* b, double* Tb_out,
+                  double* intW_out, int32_t* nseg_out) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
+  if (!T || !R || !N || !layers || (nb > 0 && (!b || !Tb_out))) return fail(RB_EINVAL, "null array");
+  int rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
+  if (rc) return rc;
+  if (!finite_all(T, nL)) return fail(RB_EINVAL, "T not finite");
+  if (!finite_all(layers, (size_t)nf * nL)) return fail(RB_EINVAL, "layers not finite");
+  if (nb == 0) return RB_OK;
+  RB_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = h->st;
+  const int max_seg = 2 * nL + 4;
+  const size_t ns = (size_t)nb * max_seg;
+  std::vector<float> a32((size_t)nL * nf);
+  for (int f = 0; f < nf; ++f)
+    for (int l = 0; l < nL; ++l) a32[(size_t)l * nf + f] = (float)layers[(size_t)f * nL + l];
+  RB_CUDA(upload(h->d_R, R, nL, st));
+  RB_CUDA(upload(h->d_N, N, nL, st));
+  RB_CUDA(upload(h->d_T, T, nL, st));
+  RB_CUDA(upload(h->d_b, b, 2 * (size_t)nb, st));
+  RB_CUDA(upload(h->d_a32, a32.data(), a32.size(), st));
+  RB_CUDA(h->d_nseg.ensure(sizeof(int) * nb));
+  RB_CUDA(h->d_hds.ensure(sizeof(float) * ns));
+  RB_CUDA(h->d_layer.ensure(sizeof(int) * ns));
+  RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nb * nf));
+  RB_CUDA(h->d_iw.ensure(sizeof(double) * (size_t)nb * nf));
+  const int nchunk = rb::tb_nchunk(max_seg);
+  RB_CUDA(h->d_part.ensure(sizeof(float4) * (size_t)nb * nchunk * nf));
+  h->launches = 0;
+  if ((rc = enqueue_raypath(h, st, nL, h->d_R.as<double>(), h->d_N.as<double>(),
+                            h->d_T.as<double>(), Req, Rpol, orient0, orient1, gtype, limb, nb,
+                            h->d_b.as<double>(), max_seg, h->d_nseg.as<int>(), nullptr,
+                            h->d_hds.as<float>(), h->d_layer.as<int>(), nullptr, nullptr, nullptr)))
+    return rc;
+  rb::TbArgs ta{};
+  ta.nL = nL;
+  ta.nf = nf;
+  ta.nb = nb;
+  ta.max_seg = max_seg;
+  ta.alpha32 = h->d_a32.as<float>();
+  ta.T32 = h->d_T32.as<float>();
+  ta.nseg = h->d_nseg.as<int>();
+  ta.hds = h->d_hds.as<float>();
+  ta.layer = h->d_layer.as<int>();
+  ta.Tb = h->d_Tb.as<double>();
+  ta.intW = h->d_iw.as<double>();
+  ta.nchunk = nchunk;
+  ta.part = h->d_part.as<float4>();
+  RB_CUDA(rb::launch_tb_chunked(ta, st));
+  h->launches += 2;
+  RB_CUDA(cudaMemcpyAsync(Tb_out, ta.Tb, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
+  if (intW_out)
+    RB_CUDA(cudaMemcpyAsync(intW_out, ta.intW, sizeof(double) * (size_t)nb * nf, cudaMemcpyDeviceToHost, st));
+  if (nseg_out) RB_CUDA(cudaMemcpyAsync(nseg_out, ta.nseg, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+  RB_CUDA(cudaStreamSynchronize(st));
+  return RB_OK;
+}
+
 // One forward pass: ray paths on the side stream concurrent with the
 // absorption, then the scan and the quadrature average.  nb = rays per
 // atmosphere; with a batch (bt), nL is the total layer count and the

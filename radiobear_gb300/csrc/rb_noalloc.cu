@@ -15,6 +15,10 @@
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress while that device is current, checks the result
 // and caches it per device; make that first call before any stream capture.
+// The cached address belongs to the device's primary context as it was when
+// the first call ran: after cudaDeviceReset (or any reset of the primary
+// context) the module is loaded again at a new address, so do not use this
+// entry point in a process that resets a device it has already used.
 // All calls share the one array, so calls that overlap on the GPU (different
 // streams, or the same array from several host threads) race; serialise
 // them. Each call writes every scratch element it later reads, so nothing
@@ -36,6 +40,7 @@ void set_last_error(const char* msg);   // rb_api.cu: the message rb_last_error 
 namespace {
 
 constexpr int NA_CHUNK = 128;
+constexpr double NA_T_CMB = 2.725;   // utils.py:77
 // Maximum scratch: nb * ceil(max_seg / 128) * nf float4 elements (8 MiB).
 constexpr size_t NA_SCRATCH_ELEMS = RB_NOALLOC_SCRATCH_ELEMS;
 
@@ -69,9 +74,10 @@ __global__ void __launch_bounds__(128)
     rb_tb_chunk_noalloc_kernel(int nL, int nf, int max_seg, int nchunk, const float* alpha32,
                                const double* T, const int* nseg_in, const double* ds,
                                const int* layer, float4* part_all) {
-  const int ray = blockIdx.z;
+  // rays in blockIdx.x (up to 2^31 - 1 of them), chunks in y, frequency blocks in z
+  const int ray = blockIdx.x;
   const int ch = blockIdx.y;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = blockIdx.z * blockDim.x + threadIdx.x;
   const int nseg = min(max(nseg_in[ray], 0), max_seg);
   const int nsteps = nseg - 1;
   const int i0 = ch * NA_CHUNK;
@@ -122,8 +128,8 @@ __global__ void __launch_bounds__(128)
 __global__ void __launch_bounds__(128)
     rb_tb_combine_noalloc_kernel(int nf, int max_seg, int nchunk, const int* nseg_in,
                                  const float4* part_all, double* Tb) {
-  const int ray = blockIdx.y;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ray = blockIdx.x;
+  const int f = blockIdx.y * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const float4* part = part_all + (size_t)ray * nchunk * nf + f;
   const int nsteps = min(max(nseg_in[ray], 0), max_seg) - 1;
@@ -142,8 +148,10 @@ __global__ void __launch_bounds__(128)
     pl = e - (ph - s);
   }
   const float TbL = tb - tbc, IW = iw - iwc;
-  const float tcmb = 2.725f;                       // utils.py:77
-  Tb[(size_t)ray * nf + f] = (double)((TbL < tcmb) ? tcmb : TbL / IW);
+  // off the planet or no emission: T_cmb (utils.py:77) stored exactly in
+  // double, as the allocating scan stores it
+  const bool clamped = TbL < (float)NA_T_CMB;
+  Tb[(size_t)ray * nf + f] = clamped ? NA_T_CMB : (double)(TbL / IW);
 }
 
 int na_fail(int code, const char* msg) {
@@ -161,6 +169,10 @@ extern "C" int rb_brightness_noalloc(void* stream, int nL, int nf, const float* 
   if (nb == 0) return RB_OK;
   if (!alpha32 || !T || !nseg || !ds || !layer || !Tb) return na_fail(RB_EINVAL, "null pointer");
   const int nchunk = (max_seg + NA_CHUNK - 1) / NA_CHUNK;
+  const int nfblk = (nf + 127) / 128;
+  if (nchunk > 65535 || nfblk > 65535)
+    return na_fail(RB_EINVAL, "rb_brightness_noalloc: max_seg or nf beyond the launch grid "
+                              "(ceil(max_seg/128) and ceil(nf/128) must be at most 65535)");
   const size_t need = (size_t)nb * nchunk * nf;
   if (need > NA_SCRATCH_ELEMS) {
     char msg[256];
@@ -185,12 +197,12 @@ extern "C" int rb_brightness_noalloc(void* stream, int nL, int nf, const float* 
     scratch = g_na_addr[dev];
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  dim3 grid((nf + 127) / 128, nchunk, nb);
+  dim3 grid(nb, nchunk, nfblk);
   rb_tb_chunk_noalloc_kernel<<<grid, 128, 0, st>>>(nL, nf, max_seg, nchunk, alpha32, T, nseg, ds,
                                                    layer, scratch);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return na_fail(RB_ECUDA, cudaGetErrorString(e));
-  dim3 g2((nf + 127) / 128, nb);
+  dim3 g2(nb, nfblk);
   rb_tb_combine_noalloc_kernel<<<g2, 128, 0, st>>>(nf, max_seg, nchunk, nseg, scratch, Tb);
   e = cudaGetLastError();
   if (e != cudaSuccess) return na_fail(RB_ECUDA, cudaGetErrorString(e));

@@ -17,7 +17,9 @@ this path: ``gas`` [nC, nL], ``config.C`` (gas row index by name),
 ``config.Rpol``, ``config.gtype``, ``config.orientation``.
 
 ``install()`` routes an importable ``radiobear`` package's own classes to
-these implementations (the reference-side binding of INTEGRATION.md).
+these implementations, and makes ``Planet.run``'s b loop one GPU call per
+atmosphere (all rays' paths and scans together, the absorption uploaded
+once).
 """
 from __future__ import annotations
 
@@ -320,9 +322,19 @@ def compute_ds(atm, b, orientation=None, gtype=None, verbose=False, engine_=None
     lay = out['layer'][0, :n]
     C = atm.config.C
     P = atm.gas[C['P']]
+    tip, rotate = _aspect(orient, Req, Rpol)
     path.update(ds=list(out['ds'][0, :n]), layer4ds=list(lay), r4ds=list(out['r4ds'][0, :n]),
-                P4ds=list(P[lay]), rNorm=R[0])
+                P4ds=list(P[lay]), tip=tip, rotate=rotate, rNorm=R[0])
     return path
+
+
+def _aspect(orientation, Req, Rpol):
+    """computeAspect (raypath.py:39-44): the 'tip' to north and the
+    sub-earth planetocentric latitude, radians."""
+    f = 1.0 - Rpol / Req
+    tip = -orientation[0] * np.pi / 180.0
+    rotate = -np.arctan(np.tan(orientation[1] * np.pi / 180.0) * (1.0 - f) ** 2)
+    return tip, rotate
 
 
 # ------------------------------------------------------------------ brightness
@@ -373,30 +385,150 @@ class Brightness:
 
 
 # ------------------------------------------------------------------ binding
+_RAY_STATE = ('travel', 'tau', 'W', 'Tb_lyr', 'P', 'z')
+
+
+class _RayState:
+    """Class attribute of the installed Brightness for the per-ray results
+    that Planet.run's batched b loop does not compute up front (the path,
+    tau, W, Tb_lyr, P, z of brightness.py:30-126).  A ray served from the
+    batch leaves a pending record; the first read of any of these names
+    evaluates that one ray on the GPU (path + profiles) and stores them.
+    Assignments store directly."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __get__(self, obj, owner=None):
+        if obj is None:
+            return self
+        d = obj.__dict__
+        if self.name not in d and d.get('_rb_pending') is not None:
+            _materialise(obj)
+        try:
+            return d[self.name]
+        except KeyError:
+            raise AttributeError(self.name) from None
+
+    def __set__(self, obj, value):
+        obj.__dict__[self.name] = value
+
+
+def _materialise(bright):
+    """Path and profiles of the pending ray of a batched run (one GPU call)."""
+    atm, alpha, b, freqs, orientation, eng = bright.__dict__.pop('_rb_pending')
+    gb = Brightness(bright.config, verbose=False, engine_=eng)
+    gb.single(b, freqs, atm, alpha, orientation)
+    for k in _RAY_STATE:
+        if hasattr(gb, k) and k not in bright.__dict__:   # an off-planet ray since set travel
+            bright.__dict__[k] = getattr(gb, k)
+
+
+def _run_batches(planet, eng):
+    """All numeric rays of Planet.run's b list (planet.py:118-133), grouped
+    by atmosphere (map_b_to_atm), through one rb_bright_run per atmosphere
+    with the absorption its Alpha computed; results kept on planet.bright
+    for the loop's Brightness.single calls."""
+    batches = {}
+    groups = {}
+    for bv in planet.b:
+        if isinstance(bv, str):
+            continue
+        groups.setdefault(planet.map_b_to_atm(bv), []).append(bv)
+    orientation = planet.config.orientation
+    for j, bl in groups.items():
+        atm, alpha = planet.atmos[j], planet.alpha[j]
+        if alpha.layers is None:
+            continue
+        R, N, Req, Rpol, orient, gtype = _geometry(atm, orientation, None)
+        bb = np.array([[float(v[0]), float(v[1])] for v in bl])
+        out = eng.bright_run(atm.gas[atm.config.C['T']], R, N, np.asarray(alpha.layers, dtype=np.float64),
+                             bb, Req, Rpol, orientation=orient, gtype=gtype)
+        rows = {}
+        for k in range(len(bl)):
+            rows[(bb[k, 0], bb[k, 1])] = (out['Tb'][k], out['intW'][k], int(out['nseg'][k]))
+        batches[(id(atm), id(alpha))] = dict(rows=rows, layers=alpha.layers, orient=orient)
+    planet.bright.__dict__['_rb_batches'] = batches
+
+
+def _from_batch(bright, b, freqs, atm, alpha, orientation, eng):
+    """Serve Brightness.single from the run's batch: True if it did."""
+    batches = bright.__dict__.get('_rb_batches')
+    if not batches or isinstance(b, str):
+        return False
+    ent = batches.get((id(atm), id(alpha)))
+    if ent is None or ent['layers'] is not alpha.layers:
+        return False
+    R, N, Req, Rpol, orient, gtype = _geometry(atm, orientation, None)
+    if orient != ent['orient']:
+        return False
+    row = ent['rows'].get((float(b[0]), float(b[1])))
+    if row is None or len(row[0]) != len(np.atleast_1d(freqs)):
+        return False
+    tb, iw, nseg = row
+    bright.alpha, bright.freqs, bright.b = alpha, freqs, b
+    if nseg == 0:                      # off the planet (brightness.py:45-50): tau, W, ... stay
+        bright.__dict__['travel'] = Ray()
+        bright.Tb = [T_CMB] * len(tb)
+        return True
+    for k in _RAY_STATE:
+        bright.__dict__.pop(k, None)
+    bright.__dict__['_rb_pending'] = (atm, alpha, b, freqs, orientation, eng)
+    bright.Tb = list(tb)
+    bright.integrated_W = np.array(iw)
+    return True
+
+
+def _reference_lines(ref_alpha, cdir):
+    """The catalogues a reference Alpha would load: the shipped .npz files
+    with the instance's truncation (alpha.py:72-78, the loaders of
+    h2s_ddb.py:14-39 and ph3_jh.py:18-61), and the h2o_bk lines its module
+    builds (h2o_bk.py:17-62) with that truncation."""
+    ts = {k: v for k, v in (getattr(ref_alpha, 'truncate_strength', None) or {}).items() if v is not None}
+    tf = {k: v for k, v in (getattr(ref_alpha, 'truncate_freq', None) or {}).items() if v is not None}
+    out = catalog.load_reference_catalogues(cdir, truncate_strength=ts, truncate_freq=tf)
+    m = (getattr(ref_alpha, 'absorptionModule', None) or {}).get('h2o')
+    if m is not None and hasattr(m, 'readInputFiles'):
+        if getattr(m, 'data', None) is None:
+            m.readInputFiles(Namespace(verbose=False, truncate_strength=ts.get('h2o'),
+                                       truncate_freq=tf.get('h2o'), path=os.path.join(cdir, 'h2o'),
+                                       units='invcm'))
+        out['h2o'] = {k: np.array(v, dtype=np.float64) for k, v in m.data.items()}
+    return out
+
+
 def install(radiobear_pkg=None, lines=None, device=0, engine_=None):
     """Route an importable radiobear package to the GPU implementations:
     Alpha.get_layers, raypath.compute_ds and Brightness.single of the
-    package are replaced; the Alpha's formalism choice and catalogues are
-    taken from the instance (``lines`` or the catalogues under the
-    package's constituents directory)."""
+    package are replaced, and Planet.init_run (called by Planet.run just
+    before its b loop, planet.py:122) runs every ray of the loop in one
+    rb_bright_run per atmosphere, which the loop's Brightness.single calls
+    then read.  The Alpha's formalism choice and catalogues are taken from
+    the instance; the catalogues are ``lines`` or, when None, the ones the
+    instance would load itself (its truncation, its h2o_bk lines)."""
     if radiobear_pkg is None:
         import radiobear as radiobear_pkg   # noqa: F811
     from importlib import import_module
     ra = import_module(radiobear_pkg.__name__ + '.alpha')
     rr = import_module(radiobear_pkg.__name__ + '.raypath')
     rbm = import_module(radiobear_pkg.__name__ + '.brightness')
+    try:
+        rpl = import_module(radiobear_pkg.__name__ + '.planet')
+    except ImportError:
+        rpl = None
     eng = engine_ or engine(device)
-    if lines is None:
-        cdir = os.path.join(os.path.dirname(radiobear_pkg.__file__), 'constituents')
-        lines = catalog.load_reference_catalogues(cdir)
+    cdir = os.path.join(os.path.dirname(radiobear_pkg.__file__), 'constituents')
     state = {}
 
     def get_layers(self, freqs, atm, scale=False, get_alpha='calc', save_alpha='none'):
-        key = id(self)
-        if state.get('alpha') is not key:
-            gpu = Alpha(self.idnum, config=self.config, engine_=eng, lines=lines)
-            state['alpha'], state['gpu'] = key, gpu
-        gpu = state['gpu']
+        gpu = self.__dict__.get('_rb_gpu')
+        if gpu is None:
+            own = lines if lines is not None else _reference_lines(self, cdir)
+            gpu = Alpha(self.idnum, config=self.config, engine_=eng, lines=own)
+            self._rb_gpu = gpu
+        elif state.get('active') is not gpu:
+            gpu.setup_formalisms()       # the engine last served another Alpha
+        state['active'] = gpu
         gpu.alphafile, gpu.memory = self.alphafile, self.memory
         out = gpu.get_layers(freqs, atm, scale=scale, get_alpha=get_alpha, save_alpha=save_alpha)
         self.freqs, self.P, self.layers = gpu.freqs, gpu.P, gpu.layers
@@ -409,6 +541,9 @@ def install(radiobear_pkg=None, lines=None, device=0, engine_=None):
         return ref
 
     def single(self, b, freqs, atm, alpha, orientation=None, taulimit=20.0):
+        if _from_batch(self, b, freqs, atm, alpha, orientation, eng):
+            return self.Tb
+        self.__dict__.pop('_rb_pending', None)
         gb = Brightness(self.config, engine_=eng)
         tb = gb.single(b, freqs, atm, alpha, orientation, taulimit)
         for k in ('alpha', 'freqs', 'b', 'travel', 'Tb', 'tau', 'W', 'Tb_lyr', 'integrated_W', 'P', 'z'):
@@ -420,4 +555,16 @@ def install(radiobear_pkg=None, lines=None, device=0, engine_=None):
     rr.compute_ds = compute_ds_gpu
     rbm.ray.compute_ds = compute_ds_gpu
     rbm.Brightness.single = single
-    return dict(alpha=ra.Alpha, compute_ds=compute_ds_gpu, brightness=rbm.Brightness)
+    for k in _RAY_STATE:
+        setattr(rbm.Brightness, k, _RayState(k))
+    out = dict(alpha=ra.Alpha, compute_ds=compute_ds_gpu, brightness=rbm.Brightness)
+    if rpl is not None and hasattr(rpl, 'Planet'):
+        init_run0 = rpl.Planet.init_run
+
+        def init_run(self):
+            init_run0(self)
+            _run_batches(self, eng)
+
+        rpl.Planet.init_run = init_run
+        out['planet'] = rpl.Planet
+    return out

@@ -1,10 +1,10 @@
 """Generate the golden fixtures in this folder by running the reference.
 
-Run from the repository root in a container that has the reference source
-(``RADIOBEAR_REF``, default ``/root/reference``):
+Run from the repository root with ``RADIOBEAR_REF`` naming the folder that
+holds the reference's ``radiobear`` package (its source tree or an install):
 
-    python tests/golden/make_golden.py            # all fixtures
-    python tests/golden/make_golden.py bench c0   # a subset
+    RADIOBEAR_REF=<path> python tests/golden/make_golden.py            # all fixtures
+    RADIOBEAR_REF=<path> python tests/golden/make_golden.py bench c0   # a subset
 
 Fixtures (all float64, ``numpy.savez_compressed``):
 

@@ -1,9 +1,11 @@
 """Harness that drives the unmodified radioBEAR reference in this container.
 
-Used only by ``make_golden.py`` to produce the committed golden fixtures; it
-needs the reference source tree (``RADIOBEAR_REF``, default
-``/root/reference``) and is never imported by tests, the bench or the
-package.
+Used by ``make_golden.py`` to produce the committed golden fixtures, and by
+``tests/ref_planet_run.py`` / the bench's stock-reference figure to run an
+installed copy of the reference.  The reference tree is named by the
+``RADIOBEAR_REF`` environment variable (or ``set_reference``): the folder
+that holds the ``radiobear`` package.  The package itself never imports
+this file.
 
 What it does to run the reference (none of it edits reference files):
 
@@ -27,7 +29,19 @@ import types
 
 import numpy as np
 
-REF = os.environ.get('RADIOBEAR_REF', '/root/reference')
+REF = os.environ.get('RADIOBEAR_REF')
+
+
+def set_reference(path):
+    """Use the reference tree at ``path`` (the folder holding ``radiobear``)."""
+    global REF
+    REF = path
+
+
+def _ref():
+    if not REF:
+        raise RuntimeError('set RADIOBEAR_REF to the folder that holds the radiobear package')
+    return REF
 
 
 def _stub_matplotlib():
@@ -46,8 +60,8 @@ def _stub_matplotlib():
 
 def import_reference():
     _stub_matplotlib()
-    if REF not in sys.path:
-        sys.path.insert(0, REF)
+    if _ref() not in sys.path:
+        sys.path.insert(0, _ref())
     import radiobear  # noqa: F401
     import radiobear.planet  # noqa: F401
     import radiobear.raypath  # noqa: F401
@@ -76,7 +90,7 @@ def patch_limb_sqrt(enable=True):
 
 
 def constituents_dir(c):
-    return os.path.join(REF, 'radiobear', 'constituents', c)
+    return os.path.join(_ref(), 'radiobear', 'constituents', c)
 
 
 def load_real_catalogues():
@@ -184,7 +198,7 @@ def scratch_planet_dir(workdir, gas_table, gas_columns, config_name='config_synt
         fp.write(CONFIG_TEMPLATE.format(gas='synth.gas', cloud='synth.cloud',
                                         orient0=orientation[0], orient1=orientation[1],
                                         gtype=gtype, limb=limb))
-    zonal_src = os.path.join(REF, 'radiobear', 'Jupiter', 'zonalJupiter.dat')
+    zonal_src = os.path.join(_ref(), 'radiobear', 'Jupiter', 'zonalJupiter.dat')
     shutil.copy(zonal_src, os.path.join(jdir, 'zonalJupiter.dat'))
     return jdir
 
@@ -193,7 +207,7 @@ def benchmark_planet_dir(workdir):
     """Copy the reference's benchmark inputs into workdir/Jupiter."""
     jdir = os.path.join(workdir, 'Jupiter')
     os.makedirs(jdir, exist_ok=True)
-    src = os.path.join(REF, 'radiobear', 'Jupiter')
+    src = os.path.join(_ref(), 'radiobear', 'Jupiter')
     for f in ('config_benchmark.par', 'jupiter.benchmark_gas', 'jupiter.benchmark_nocloud',
               'JupiterNoTweak.py', 'zonalJupiter.dat'):
         shutil.copy(os.path.join(src, f), os.path.join(jdir, f))

@@ -202,3 +202,72 @@ def test_compute_ds_and_brightness_benchmark(gpu_alpha):
     for i, b in enumerate(z['b']):
         tb = br.single(b, z['freqs'], atm, a)
         assert np.max(np.abs(np.array(tb) - z['Tb'][i])) < 1e-3
+
+
+class FakeRayEngine:
+    """Stands in for the GPU engine: rays with |b| < 0.9 have a 3-segment
+    path, the others miss; Tb = 100 + 10 b_x + f."""
+
+    def __init__(self):
+        self.calls = []
+
+    def bright_run(self, T, R, N, layers, b, Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse',
+                   limb='shape'):
+        self.calls.append(('bright_run', len(b)))
+        nf = layers.shape[0]
+        hit = np.hypot(b[:, 0], b[:, 1]) < 0.9
+        Tb = np.where(hit[:, None], 100.0 + 10.0 * b[:, :1] + np.arange(nf)[None, :], 2.725)
+        return dict(Tb=Tb, intW=np.ones((len(b), nf)), nseg=np.where(hit, 3, 0).astype(np.int32))
+
+    def raypath(self, R, N, b, Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse', extras=False):
+        self.calls.append(('raypath', len(b)))
+        ms = 2 * len(R) + 4
+        out = dict(nseg=np.array([3], dtype=np.int32), ds=np.zeros((1, ms)),
+                   layer=np.zeros((1, ms), dtype=np.int32), r4ds=np.zeros((1, ms)))
+        out['ds'][0, :3] = [1.0, 2.0, 3.0]
+        out['layer'][0, :3] = [0, 1, 2]
+        return out
+
+    def brightness(self, T, layers, nseg, ds, lay, disc=False, profiles=False):
+        self.calls.append(('brightness', len(nseg)))
+        nf, ms = layers.shape[0], ds.shape[1]
+        prof = np.full((1, nf, ms), 0.5)
+        return dict(Tb=np.full((1, nf), 123.0), intW=np.ones((1, nf)), tau=prof, W=prof, TbL=prof)
+
+
+def test_batched_planet_loop_serves_single_and_materialises_lazily():
+    """install()'s b-loop batching on a stand-in engine: one bright_run for
+    the whole loop, Brightness.single served from it in the loop's order,
+    the per-ray path/profiles evaluated only when read, and off-planet rays
+    leaving the previous ray's profiles in place (brightness.py:45-50)."""
+    eng = FakeRayEngine()
+    bright_cls = type('Brightness', (), {'config': None, 'verbose': False})
+    for k in dropin._RAY_STATE:
+        setattr(bright_cls, k, dropin._RayState(k))
+    bright = bright_cls()
+    nL = 4
+    gas = np.zeros((len(synth.GAS_COLUMNS), nL))
+    gas[G.C['T']] = [100.0, 150.0, 200.0, 250.0]
+    gas[G.C['P']] = [0.1, 1.0, 10.0, 100.0]
+    prop = np.zeros((len(synth.PROPERTY_COLUMNS), nL))
+    prop[LP['R']] = [71000.0, 70990.0, 70980.0, 70970.0]
+    prop[LP['N']] = 1.0
+    cfg = Namespace(C=G.C, LP=LP, Req=71492.0, Rpol=66854.0, gtype='ellipse', orientation=[0.0, 0.0])
+    atm = Namespace(gas=gas, property=prop, config=cfg)
+    alpha = Namespace(layers=np.full((2, nL), 1e-6), freqs=[1.0, 2.0])
+    planet = Namespace(b=[[0.0, 0.0], [0.5, 0.0], [0.95, 0.0]], atmos=[atm], alpha=[alpha],
+                       config=Namespace(orientation=[0.0, 0.0]), bright=bright,
+                       map_b_to_atm=lambda b: 0)
+    dropin._run_batches(planet, eng)
+    assert eng.calls == [('bright_run', 3)]
+    for bv, want in zip(planet.b, ([100.0, 101.0], [105.0, 106.0], [2.725, 2.725])):
+        assert dropin._from_batch(bright, bv, [1.0, 2.0], atm, alpha, None, eng)
+        assert np.allclose(bright.Tb, want)
+        if bv[0] == 0.5:
+            assert eng.calls == [('bright_run', 3)]          # nothing evaluated yet
+            assert bright.tau.shape == (2, 3)                # read -> one ray evaluated
+            assert [c[0] for c in eng.calls[1:]] == ['raypath', 'brightness']
+            assert bright.travel.layer4ds == [0, 1, 2]
+    assert bright.travel.ds is None                          # the off-planet ray's empty path
+    assert bright.tau.shape == (2, 3)                        # profiles of the previous ray stay
+    assert not dropin._from_batch(bright, [0.1, 0.1], [1.0, 2.0], atm, alpha, None, eng)

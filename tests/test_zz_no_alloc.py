@@ -86,3 +86,56 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
             ctypes.c_void_p(1), ctypes.c_void_p(1), ms, ctypes.c_void_p(1))
     assert rc == 1
     assert b'exceeds the fixed maximum' in lib.rb_last_error()
+
+
+def test_noalloc_many_rays_one_frequency_and_exact_tcmb():
+    """More rays than a grid's y or z dimension holds (65,535), one
+    frequency, short paths: every ray matches rb_brightness, and rays with
+    no path (off the planet) are T_cmb = 2.725 K exactly, as there."""
+    import torch
+    from radiobear_gb300 import _native
+    rng = np.random.default_rng(7)
+    nL, nf, nb, ms = 12, 1, 70000, 4
+    T = np.linspace(120.0, 400.0, nL)
+    layers = rng.uniform(1e-7, 1e-5, size=(nf, nL))
+    nseg = rng.integers(0, ms + 1, size=nb).astype(np.int32)
+    nseg[:5] = 0
+    ds = rng.uniform(10.0, 200.0, size=(nb, ms))
+    lay = np.sort(rng.integers(0, nL, size=(nb, ms)), axis=1).astype(np.int32)
+    for i in range(nb):
+        ds[i, nseg[i]:] = 0.0
+        lay[i, nseg[i]:] = 0
+    eng = _native.Engine(0)
+    try:
+        ref = eng.brightness(T, layers, nseg, ds, lay)['Tb']
+    finally:
+        eng.close()
+    lib, fn = _lib()
+    dev = torch.device('cuda', 0)
+    torch.cuda.set_device(dev)
+    d_a = torch.as_tensor(np.ascontiguousarray(layers.T), dtype=torch.float32, device=dev)
+    d_T = torch.as_tensor(T, dtype=torch.float64, device=dev)
+    d_n = torch.as_tensor(nseg, dtype=torch.int32, device=dev)
+    d_ds = torch.as_tensor(ds, dtype=torch.float64, device=dev)
+    d_l = torch.as_tensor(lay, dtype=torch.int32, device=dev)
+    d_Tb = torch.full((nb, nf), -1.0, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    rc = fn(ctypes.c_void_p(stream.cuda_stream), nL, nf, d_a.data_ptr(), d_T.data_ptr(), nb,
+            d_n.data_ptr(), d_ds.data_ptr(), d_l.data_ptr(), ms, d_Tb.data_ptr())
+    assert rc == 0, lib.rb_last_error().decode()
+    torch.cuda.synchronize(dev)
+    got = d_Tb.cpu().numpy()
+    assert np.max(np.abs(got - ref)) < TB_ATOL
+    off = nseg <= 1
+    assert off.any()
+    assert np.all(got[off] == 2.725) and np.all(ref[off] == 2.725)
+
+
+def test_noalloc_rejects_a_grid_beyond_its_limits():
+    lib, fn = _lib()
+    # one ray, one frequency, a path of 128 * 65536 segments: the scratch
+    # holds it but the chunk dimension of the grid does not
+    rc = fn(None, 10, 1, ctypes.c_void_p(1), ctypes.c_void_p(1), 1, ctypes.c_void_p(1),
+            ctypes.c_void_p(1), ctypes.c_void_p(1), 128 * 65536, ctypes.c_void_p(1))
+    assert rc == 1
+    assert b'launch grid' in lib.rb_last_error()
