@@ -27,6 +27,8 @@
  *   rb_brightness     Brightness.single, radiobear/brightness.py:30-126
  *   rb_forward        Planet.run's alpha_layers + b loop + bright_run,
  *                     radiobear/planet.py:59-160 (one call per spectrum set)
+ *   rb_bright_run     Planet.run's b loop given Alpha.layers,
+ *                     radiobear/planet.py:118-133, planet_base.py:244-274
  *   rb_atm_props      AtmosphereBase.computeProp, radiobear/atm_base.py:120-194
  *   rb_regrid         regrid.regrid (regridType = number of log-P steps or a
  *                     pressure grid), radiobear/regrid.py:11-176
@@ -40,7 +42,7 @@
 extern "C" {
 #endif
 
-#define RB_ABI_VERSION 2
+#define RB_ABI_VERSION 3
 
 typedef struct rb_handle rb_handle;
 
@@ -213,7 +215,9 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
 /* Same as rb_forward but every array argument is a device pointer, the
  * work is enqueued on `stream` (a cudaStream_t, 0 = legacy default) and the
  * call returns without synchronising.  Frequencies are planned from the
- * HOST array freqs_host (nf values) and cached on the handle. */
+ * HOST array freqs_host (nf values) and cached on the handle.  disc = 1
+ * applies the E2 weighting to the rays given (pass nadir rays for the
+ * reference's b = 'disc'; device arrays are not rewritten). */
 int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
                       const double* X, const double* R, const double* N, int nf,
                       const double* freqs_host, const double* scale, double Req, double Rpol,
@@ -222,28 +226,32 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
                       double* Tb_avg);
 
 /* Adjoint of the forward model (no reference counterpart: radioBEAR has
- * no derivatives).  Runs the forward (exp weighting) and returns Tb, the
- * weighted average (when weights are given) and the gradient of
+ * no derivatives).  Runs the forward and returns Tb, the weighted average
+ * (when weights are given) and the gradient of
  *   loss = sum_f grad[f] Tb_avg[f]           (weights given, grad [nf])
  *   loss = sum_{b,f} grad[b][f] Tb[b][f]     (no weights, grad [nb][nf])
  * with respect to each layer's T (K), P (bar) and ln X of NH3, H2O, H2S:
  * dT[nL], dP[nL], dlnX[3][nL] (rows NH3, H2O, H2S).  The ray paths are
  * held fixed (they depend on R and N only); alpha is recomputed with its
- * layer derivatives instead of being stored. */
+ * layer derivatives instead of being stored.  disc = 0: exp weighting;
+ * disc = 1: the b = 'disc' weighting 2 E2(tau) of brightness.py:96 on the
+ * nadir ray (as rb_forward), differentiated with dE2/dx = -E1(x). */
 int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const double* X,
                const double* R, const double* N, int nf, const double* freqs, const double* scale,
                double Req, double Rpol, double orient0, double orient1, int gtype, int limb, int nb,
-               const double* b, const double* weights, const double* grad, double* Tb_out,
-               double* Tb_avg, double* dT, double* dP, double* dlnX);
+               const double* b, const double* weights, int disc, const double* grad,
+               double* Tb_out, double* Tb_avg, double* dT, double* dP, double* dlnX);
 
 /* Device-pointer variant of rb_adjoint (freqs on the host), enqueued on
- * `stream`; Tb_out and Tb_avg may be null. */
+ * `stream`; Tb_out and Tb_avg may be null.  disc = 1 applies the E2
+ * weighting to the rays given (pass nadir rays for the reference's
+ * 'disc'). */
 int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const double* T,
                       const double* X, const double* R, const double* N, int nf,
                       const double* freqs_host, const double* scale, double Req, double Rpol,
                       double orient0, double orient1, int gtype, int limb, int nb, const double* b,
-                      const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
-                      double* dT, double* dP, double* dlnX);
+                      const double* weights, int disc, const double* grad, double* Tb_out,
+                      double* Tb_avg, double* dT, double* dP, double* dlnX);
 
 /* Batches of atmospheres (no reference counterpart: the reference runs one
  * atmosphere per Planet): nvar variants, variant v with nL_host[v] layers
@@ -253,21 +261,26 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
  * (device); Tb_avg[nvar][nf] (device) receives the weighted averages.  All
  * variants run in the same launches (one persistent absorption launch over
  * every variant's layers, one ray-walk launch over all nvar nb rays, ...).
- * Frequencies are planned from the host array freqs_host. */
+ * Frequencies are planned from the host array freqs_host.  scale
+ * (nullable, device) is [sum nL_v][RB_NGAS]: per variant, per layer and
+ * per gas multipliers, as rb_alpha's scale (the retrieval-reuse pattern of
+ * scripts/demo_batch.py:24-41 with a scale dict per walker). */
 int rb_forward_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
                             const double* P, const double* T, const double* X, const double* R,
-                            const double* N, int nf, const double* freqs_host, double Req,
-                            double Rpol, double orient0, double orient1, int gtype, int limb,
-                            int nb, const double* b, const double* weights, double* Tb_avg);
+                            const double* N, int nf, const double* freqs_host, const double* scale,
+                            double Req, double Rpol, double orient0, double orient1, int gtype,
+                            int limb, int nb, const double* b, const double* weights,
+                            double* Tb_avg);
 
 /* Forward and adjoint of a batch: grad[nvar][nf] = d loss / d Tb_avg;
  * dT, dP [sum nL_v], dlnX [3][sum nL_v] (device). */
 int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
                             const double* P, const double* T, const double* X, const double* R,
-                            const double* N, int nf, const double* freqs_host, double Req,
-                            double Rpol, double orient0, double orient1, int gtype, int limb,
-                            int nb, const double* b, const double* weights, const double* grad,
-                            double* Tb_avg, double* dT, double* dP, double* dlnX);
+                            const double* N, int nf, const double* freqs_host, const double* scale,
+                            double Req, double Rpol, double orient0, double orient1, int gtype,
+                            int limb, int nb, const double* b, const double* weights,
+                            const double* grad, double* Tb_avg, double* dT, double* dP,
+                            double* dlnX);
 
 /* Number of this library's kernel launches made by the last rb_forward /
  * rb_forward_device call (for launch accounting). */
@@ -369,6 +382,9 @@ int rb_brightness_noalloc(void* stream, int nL, int nf, const float* alpha32, co
 
 /* E2(x) evaluated by the device routine used for b = 'disc' (test hook). */
 int rb_debug_e2(rb_handle* h, int n, const double* x, double* out);
+/* E1(x) = -dE2/dx evaluated by the device routine of the disc adjoint
+ * (test hook). */
+int rb_debug_e1(rb_handle* h, int n, const double* x, double* out);
 
 #ifdef __cplusplus
 }

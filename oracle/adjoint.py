@@ -2,7 +2,8 @@
 and finite-difference gradients of the oracle forward model.
 
 TEST INFRASTRUCTURE ONLY (same rule as ``oracle/oracle.py``): imported by
-``tests/`` only, never by the ``radiobear_gb300`` package.
+``tests/`` and the accuracy leg of ``bench.py`` as the checker, never by the
+``radiobear_gb300`` package.
 
 The reference has no derivatives, so gradients are pinned by (1) central
 finite differences of the float64 oracle (``oracle.forward``), step 1e-4
@@ -93,3 +94,25 @@ def directional_fd(gas, C, R, N, freqs, rays, lines, Req, Rpol, weights, grad, d
     lm = loss_forward(perturb(gas, C, direction, -h), C, R, N, freqs, rays, lines, Req, Rpol,
                       weights, grad, h2state, **alpha_kw)
     return (lp - lm) / (2.0 * h)
+
+
+def random_direction(rng, gas, C):
+    """A perturbation of the benchmark's gradient checks: T Gaussian 5 K, ln X
+    of NH3 / H2O / H2S Gaussian 0.3 dex correlated over 5 layers (a 5-layer
+    moving average rescaled to the same variance), P Gaussian 1 %."""
+    nL = gas.shape[1]
+    k = np.ones(5) / 5.0
+
+    def corr(sigma):
+        return np.convolve(rng.normal(0.0, sigma, nL + 4), k, mode='valid') * np.sqrt(5.0)
+
+    dex = 0.3 * np.log(10.0)
+    return dict(T=rng.normal(0.0, 5.0, nL), P=0.01 * gas[C['P']] * rng.normal(0.0, 1.0, nL),
+                NH3=corr(dex), H2O=corr(dex), H2S=corr(dex))
+
+
+def dot(grad, direction):
+    """<gradient, direction> for a gradient dict (dT, dP, dlnX [3, nL])."""
+    return (np.dot(grad['dT'], direction['T']) + np.dot(grad['dP'], direction['P']) +
+            np.dot(grad['dlnX'][0], direction['NH3']) + np.dot(grad['dlnX'][1], direction['H2O']) +
+            np.dot(grad['dlnX'][2], direction['H2S']))

@@ -15,7 +15,7 @@ import numpy as np
 from . import build as _build
 
 LIB_PATH = _build.LIB
-ABI_VERSION = 2      # RB_ABI_VERSION of include/radiobear_gb300.h
+ABI_VERSION = 3      # RB_ABI_VERSION of include/radiobear_gb300.h
 
 RB_OK = 0
 FAM = dict(NH3_INV=0, NH3_ROT=1, NH3_V2=2, NH3_SJS=3, H2O=4, H2S=5, PH3=6, CO=7)
@@ -50,7 +50,7 @@ EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set
            'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
            'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device',
            'rb_set_co_clouds', 'rb_atm_props', 'rb_atm_props_device', 'rb_regrid',
-           'rb_regrid_device', 'rb_bright_run')
+           'rb_regrid_device', 'rb_bright_run', 'rb_debug_e1')
 
 _lib = None
 _lock = threading.Lock()
@@ -108,23 +108,24 @@ def load_library(path=None):
                                           c_int, _vp, _vp, c_int, _vp, _vp]
         lib.rb_last_launch_count.argtypes = [_vp]
         lib.rb_debug_e2.argtypes = [_vp, c_int, _d, _d]
+        lib.rb_debug_e1.argtypes = [_vp, c_int, _d, _d]
         lib.rb_set_profiling.argtypes = [_vp, c_int]
         lib.rb_phase_times.argtypes = [_vp, _d, c_int]
         lib.rb_probe_fp32_peak.argtypes = [_vp, _d]
         lib.rb_set_alpha_tiling.argtypes = [_vp, c_int, c_int, c_int]
         lib.rb_adjoint.argtypes = [_vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _vp, _vp, c_double,
-                                   c_double, c_double, c_double, c_int, c_int, c_int, _vp, _vp, _vp,
-                                   _vp, _vp, _vp, _vp, _vp]
+                                   c_double, c_double, c_double, c_int, c_int, c_int, _vp, _vp, c_int,
+                                   _vp, _vp, _vp, _vp, _vp, _vp]
         _ip = ctypes.POINTER(ctypes.c_int32)
         lib.rb_forward_batch_device.argtypes = [_vp, _vp, c_int, _ip, _vp, _vp, _vp, _vp, _vp, c_int, _d,
-                                                c_double, c_double, c_double, c_double, c_int, c_int,
-                                                c_int, _vp, _vp, _vp]
+                                                _vp, c_double, c_double, c_double, c_double, c_int,
+                                                c_int, c_int, _vp, _vp, _vp]
         lib.rb_adjoint_batch_device.argtypes = [_vp, _vp, c_int, _ip, _vp, _vp, _vp, _vp, _vp, c_int, _d,
-                                                c_double, c_double, c_double, c_double, c_int, c_int,
-                                                c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+                                                _vp, c_double, c_double, c_double, c_double, c_int,
+                                                c_int, c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
         lib.rb_adjoint_device.argtypes = [_vp, _vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _d, _vp,
                                           c_double, c_double, c_double, c_double, c_int, c_int,
-                                          c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+                                          c_int, _vp, _vp, c_int, _vp, _vp, _vp, _vp, _vp, _vp]
         for name in EXPORTS:
             getattr(lib, name).restype = getattr(lib, name).restype or c_int
         lib.rb_last_error.restype = ctypes.c_char_p
@@ -306,11 +307,12 @@ class Engine:
 
     def forward_device(self, stream, nL, nb, P, T, X, R, N, freqs_host, b, Req, Rpol, Tb_out,
                        weights=None, Tb_avg=None, orientation=(0.0, 0.0), gtype='ellipse',
-                       limb='shape', scale=None):
+                       limb='shape', scale=None, disc=False):
         """Device-pointer variant of :meth:`forward`: P, T, X, R, N, b,
         weights, scale, Tb_out and Tb_avg are integer device addresses (for
         example ``tensor.data_ptr()``), ``stream`` an integer cudaStream_t.
-        The work is enqueued on ``stream`` and the call returns at once."""
+        The work is enqueued on ``stream`` and the call returns at once.
+        disc applies the E2 weighting to the rays given."""
         f = _f64(freqs_host)
 
         def vp(x):
@@ -319,15 +321,17 @@ class Engine:
         rc = self.lib.rb_forward_device(
             self._h, _vp(int(stream)), int(nL), vp(P), vp(T), vp(X), vp(R), vp(N), f.size, _ptr(f),
             vp(scale), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]),
-            GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), 0, vp(Tb_out), vp(Tb_avg))
+            GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), int(bool(disc)), vp(Tb_out),
+            vp(Tb_avg))
         _check(self.lib, rc, 'rb_forward_device')
 
     def adjoint(self, P, T, X, R, N, freqs, b, Req, Rpol, grad, weights=None,
-                orientation=(0.0, 0.0), gtype='ellipse', limb='shape', scale=None):
+                orientation=(0.0, 0.0), gtype='ellipse', limb='shape', scale=None, disc=False):
         """Forward Tb and the gradient of sum(grad * Tb_avg) (weights given,
         grad [nf]) or sum(grad * Tb) (grad [nb, nf]) with respect to each
-        layer's T, P and ln X of NH3, H2O, H2S.  Returns dict(Tb, Tb_avg, dT,
-        dP, dlnX [3, nL])."""
+        layer's T, P and ln X of NH3, H2O, H2S.  disc: the b = 'disc' E2
+        weighting on the nadir ray.  Returns dict(Tb, Tb_avg, dT, dP,
+        dlnX [3, nL])."""
         P, T, X, R, N, f = (_f64(v) for v in (P, T, X, R, N, freqs))
         b = _f64(np.atleast_2d(b))
         nL, nf, nb = P.size, f.size, b.shape[0]
@@ -343,14 +347,14 @@ class Engine:
         rc = self.lib.rb_adjoint(self._h, nL, _addr(P), _addr(T), _addr(X), _addr(R), _addr(N), nf,
                                  _addr(f), _addr(sc), float(Req), float(Rpol), float(orientation[0]),
                                  float(orientation[1]), GTYPE[gtype], LIMB[limb], nb, _addr(b),
-                                 _addr(w), _addr(g), _addr(Tb), _addr(avg), _addr(dT), _addr(dP),
-                                 _addr(dlnX))
+                                 _addr(w), int(bool(disc)), _addr(g), _addr(Tb), _addr(avg),
+                                 _addr(dT), _addr(dP), _addr(dlnX))
         _check(self.lib, rc, 'rb_adjoint')
         return dict(Tb=Tb, Tb_avg=avg, dT=dT, dP=dP, dlnX=dlnX)
 
     def adjoint_device(self, stream, nL, nb, P, T, X, R, N, freqs_host, b, Req, Rpol, grad, dT,
                        dP, dlnX, weights=None, Tb_out=None, Tb_avg=None, orientation=(0.0, 0.0),
-                       gtype='ellipse', limb='shape', scale=None):
+                       gtype='ellipse', limb='shape', scale=None, disc=False):
         """Device-pointer variant of :meth:`adjoint` (integer device
         addresses, enqueued on ``stream``)."""
         f = _f64(freqs_host)
@@ -361,34 +365,35 @@ class Engine:
         rc = self.lib.rb_adjoint_device(
             self._h, _vp(int(stream)), int(nL), vp(P), vp(T), vp(X), vp(R), vp(N), f.size, _ptr(f),
             vp(scale), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]),
-            GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), vp(grad), vp(Tb_out),
-            vp(Tb_avg), vp(dT), vp(dP), vp(dlnX))
+            GTYPE[gtype], LIMB[limb], int(nb), vp(b), vp(weights), int(bool(disc)), vp(grad),
+            vp(Tb_out), vp(Tb_avg), vp(dT), vp(dP), vp(dlnX))
         _check(self.lib, rc, 'rb_adjoint_device')
 
     def forward_batch_device(self, stream, nL_list, P, T, X, R, N, freqs_host, b, weights, Tb_avg,
-                             Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse', limb='shape'):
+                             Req, Rpol, orientation=(0.0, 0.0), gtype='ellipse', limb='shape',
+                             scale=None):
         """Batch of atmospheres (see rb_forward_batch_device): nL_list host
-        layer counts; P, T, R, N, X, b, weights, Tb_avg integer device
-        addresses."""
+        layer counts; P, T, R, N, X, b, weights, Tb_avg (and scale
+        [sum nL][RB_NGAS], optional) integer device addresses."""
         nl = np.ascontiguousarray(nL_list, dtype=np.int32)
         f = _f64(freqs_host)
         rc = self.lib.rb_forward_batch_device(
             self._h, _vp(int(stream)), nl.size, nl.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
             _vp(int(P)), _vp(int(T)), _vp(int(X)), _vp(int(R)), _vp(int(N)), f.size, _ptr(f),
-            float(Req), float(Rpol), float(orientation[0]), float(orientation[1]), GTYPE[gtype],
+            None if scale is None else _vp(int(scale)), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]), GTYPE[gtype],
             LIMB[limb], int(self._nb(b)), _vp(int(b.data_ptr())), _vp(int(weights)), _vp(int(Tb_avg)))
         _check(self.lib, rc, 'rb_forward_batch_device')
 
     def adjoint_batch_device(self, stream, nL_list, P, T, X, R, N, freqs_host, b, weights, grad,
                              Tb_avg, dT, dP, dlnX, Req, Rpol, orientation=(0.0, 0.0),
-                             gtype='ellipse', limb='shape'):
+                             gtype='ellipse', limb='shape', scale=None):
         """Forward + adjoint of a batch (see rb_adjoint_batch_device)."""
         nl = np.ascontiguousarray(nL_list, dtype=np.int32)
         f = _f64(freqs_host)
         rc = self.lib.rb_adjoint_batch_device(
             self._h, _vp(int(stream)), nl.size, nl.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
             _vp(int(P)), _vp(int(T)), _vp(int(X)), _vp(int(R)), _vp(int(N)), f.size, _ptr(f),
-            float(Req), float(Rpol), float(orientation[0]), float(orientation[1]), GTYPE[gtype],
+            None if scale is None else _vp(int(scale)), float(Req), float(Rpol), float(orientation[0]), float(orientation[1]), GTYPE[gtype],
             LIMB[limb], int(self._nb(b)), _vp(int(b.data_ptr())), _vp(int(weights)), _vp(int(grad)),
             _vp(int(Tb_avg)), _vp(int(dT)), _vp(int(dP)), _vp(int(dlnX)))
         _check(self.lib, rc, 'rb_adjoint_batch_device')
@@ -427,6 +432,12 @@ class Engine:
         x = _f64(x)
         out = np.empty_like(x)
         _check(self.lib, self.lib.rb_debug_e2(self._h, x.size, _ptr(x), _ptr(out)), 'rb_debug_e2')
+        return out
+
+    def debug_e1(self, x):
+        x = _f64(x)
+        out = np.empty_like(x)
+        _check(self.lib, self.lib.rb_debug_e1(self._h, x.size, _ptr(x), _ptr(out)), 'rb_debug_e1')
         return out
 
 

@@ -9,7 +9,8 @@ frequencies, the abundances that are not retrieved) and maps per-layer
 float64 CUDA tensors to the disc-averaged brightness Tb_avg [nf] (K).  The
 backward pass calls ``rb_adjoint_device`` (reverse sweep of the brightness
 scan, alpha recomputed with its per-layer derivatives); the ray paths are
-held fixed.  The reference has no derivatives: this is an addition beside
+held fixed.  ``disc=True`` is the reference's ``b = 'disc'``: every ray is
+the nadir ray with the 2 E2(tau) weighting (brightness.py:32-34, 96).  The reference has no derivatives: this is an addition beside
 the drop-in path (see ``include/radiobear_gb300.h``).
 """
 from __future__ import annotations
@@ -25,8 +26,11 @@ _LNX_ROWS = (_native.X_ROWS.index('NH3'), _native.X_ROWS.index('H2O'), _native.X
 
 class TbModel:
     def __init__(self, engine, R, N, freqs, b, weights, X_fixed, Req, Rpol, device=None,
-                 orientation=(0.0, 0.0), gtype='ellipse', limb='shape'):
+                 orientation=(0.0, 0.0), gtype='ellipse', limb='shape', disc=False):
         self.engine = engine
+        self.disc = bool(disc)
+        if self.disc:
+            b = np.zeros_like(np.atleast_2d(np.asarray(b, dtype=np.float64)))
         self.device = torch.device(device or 'cuda')
         f64 = dict(dtype=torch.float64, device=self.device)
         self.R = torch.as_tensor(np.ascontiguousarray(R, dtype=np.float64), **f64)
@@ -67,7 +71,7 @@ class TbFunction(torch.autograd.Function):
                                     model.b.data_ptr(), model.Req, model.Rpol, Tb.data_ptr(),
                                     weights=model.w.data_ptr(), Tb_avg=avg.data_ptr(),
                                     orientation=model.orientation, gtype=model.gtype,
-                                    limb=model.limb)
+                                    limb=model.limb, disc=model.disc)
         ctx.model = model
         ctx.save_for_backward(T, P, X)
         return avg
@@ -86,5 +90,5 @@ class TbFunction(torch.autograd.Function):
                                     model.freqs, model.b.data_ptr(), model.Req, model.Rpol,
                                     g.data_ptr(), dT.data_ptr(), dP.data_ptr(), dlnX.data_ptr(),
                                     weights=model.w.data_ptr(), orientation=model.orientation,
-                                    gtype=model.gtype, limb=model.limb)
+                                    gtype=model.gtype, limb=model.limb, disc=model.disc)
         return dT, dP, dlnX, None

@@ -24,9 +24,17 @@
 //                           parameters (each family depends on T, P and its
 //                           own abundance), contracted with dTb/dalpha of
 //                           the layer and reduced over the frequencies.
+//   rb_tb_adj_disc_kernel   the same reverse sweep for the b = 'disc'
+//                           weighting W_i = 2 a_i E2(tau_i) (brightness.py:96):
+//                           E_k -> 2 E2(tau_k) in the direct and source terms and
+//                           a_k E_k -> 2 a_k E1(tau_k) in Lam (dE2/dx = -E1(x));
+//                           E2 does not factor over chunks, so one thread per
+//                           (ray, frequency) walks its whole path (forward pass
+//                           storing tau and 2 E2 per node, then the reverse pass).
 //   rb_adjoint_final_kernel adds the source-temperature term and writes
 //                           dTb/dT, dTb/dP, dTb/dln X.
 #include "rb_args.cuh"
+#include "rb_expint.cuh"
 #include <math_constants.h>
 
 namespace rb {
@@ -252,6 +260,92 @@ __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
   }
   if (c == 0 && g != 0.f)   // node 0: W_0 = 0, only the segment term
     atomicAdd(a.ga + sg.off[0] + f, g * 0.5f * (2.f * sg.hd[0]) * (Ln - Lc));
+}
+
+// b = 'disc': one thread per (ray, frequency).  The forward pass repeats
+// the sequential scan's arithmetic (rb_tb_seq_kernel with the E2 weighting,
+// so Tb and intW are the forward's), storing {tau_k, 2 E2(tau_k)} per node;
+// the reverse pass accumulates Lam_k = Lam_{k+1} - w_k 2 a_k E1(tau_k) and
+// adds g (w_k 2 E2_k + hd_{k-1} Lam_k + hd_k Lam_{k+1}) into galpha and
+// g W_k c_k / intW into the source term (hd = ds / 2, the node weight
+// c_k = hd_{k-1} + hd_k).  Threads past nf run with g = 0 so the warp's
+// source-term shuffle has every lane.
+__global__ void __launch_bounds__(128) rb_tb_adj_disc_kernel(TbAdjArgs a) {
+  const int b = blockIdx.x;
+  const int f = blockIdx.y * blockDim.x + threadIdx.x;
+  const bool inf = f < a.nf;
+  const int fc = inf ? f : 0;
+  const int n = min(max(a.nseg[b], 0), a.max_seg);
+  if (n < 2) return;                          // no path: Tb = T_cmb, no gradient (warp-uniform)
+  const float* hd = a.hds + (size_t)b * a.max_seg;
+  const int* lay = a.layer + (size_t)b * a.max_seg;
+  int off = 0, nLr = a.nL;
+  if (a.var_off) {
+    const int v = b / a.rays_per_var;
+    off = a.var_off[v];
+    nLr = a.var_off[v + 1] - off;
+  }
+  double2* tE = a.tauE + (size_t)b * a.max_seg * a.nf + fc;
+  const float* al = a.alpha32 + fc;
+  // forward pass (rb_tb_seq_kernel's arithmetic)
+  float th = 0.f, tl = 0.f, W0 = 0.f;
+  float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
+  int L0 = off + wrap_l(lay[0], nLr);
+  float T0 = (float)a.T[L0];
+  float a0 = al[(size_t)L0 * a.nf];
+  if (inf) tE[0] = make_double2(0.0, 0.0);
+  for (int i = 0; i + 1 < n; ++i) {
+    const int L1 = off + wrap_l(lay[i + 1], nLr);
+    const float h = hd[i];
+    const float a1 = al[(size_t)L1 * a.nf];
+    const float T1 = (float)a.T[L1];
+    dfs_add(th, tl, (a0 + a1) * h);
+    const double tau = (double)th + (double)tl;
+    const double e2 = 2.0 * expint2(tau);
+    const float W1 = (float)((double)a1 * e2);
+    float y = (W1 + W0) * h - iwc, t = iw + y;
+    iwc = (t - iw) - y;
+    iw = t;
+    y = fmaf(T1, W1, T0 * W0) * h - tbc;
+    t = tb + y;
+    tbc = (t - tb) - y;
+    tb = t;
+    if (inf) tE[(size_t)(i + 1) * a.nf] = make_double2(tau, e2);
+    W0 = W1;
+    T0 = T1;
+    a0 = a1;
+  }
+  const double TbL = (double)tb - (double)tbc, IW = (double)iw - (double)iwc;
+  const bool live = !(TbL < T_CMB_ADJ) && IW > 0.0;
+  double gb = (inf && live) ? adj_gb(a, b, fc) : 0.0;
+  if (__all_sync(0xffffffffu, gb == 0.0)) return;
+  const float Tb = live ? (float)(TbL / IW) : 0.f;
+  const float rIW = live ? (float)(1.0 / IW) : 0.f;
+  const float g = (float)gb;
+  // reverse pass: nodes n-1 .. 1, then node 0 (W_0 = 0: segment term only)
+  float Ln = 0.f, Lc = 0.f;                   // Lam_{k+1}, compensated
+  for (int k = n - 1; k > 0; --k) {
+    const int L = off + wrap_l(lay[k], nLr);
+    const float hprev = hd[k - 1];
+    const float hcur = k + 1 < n ? hd[k] : 0.f;   // the last ds is not used
+    const float ck = hprev + hcur;
+    const double2 te = inf ? tE[(size_t)k * a.nf] : make_double2(1.0, 0.0);
+    const float ak = al[(size_t)L * a.nf];
+    const float wk = ck * ((float)a.T[L] - Tb) * rIW;
+    const float Lnext = Ln - Lc;
+    const float e1 = g != 0.f ? (float)(2.0 * expint1(te.x)) : 0.f;
+    const float yv = -(wk * ak * e1) - Lc;
+    const float tt = Ln + yv;
+    Lc = (tt - Ln) - yv;
+    Ln = tt;
+    const float Lk = Ln - Lc;
+    if (g != 0.f)
+      atomicAdd(a.ga + (size_t)L * a.nf + f, g * (wk * (float)te.y + hprev * Lk + hcur * Lnext));
+    float src = g * ak * (float)te.y * ck * rIW;
+    for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(0xffffffffu, src, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(a.gs + L, (double)src);
+  }
+  if (g != 0.f) atomicAdd(a.ga + (size_t)L0 * a.nf + f, g * hd[0] * (Ln - Lc));
 }
 
 // ------------------------------------------------------------------ dual numbers
@@ -1041,7 +1135,10 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(float) * (size_t)ta.nL * ta.nf, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * (size_t)ta.nL, st);
   if (e != cudaSuccess) return e;
-  if (ta.nb > 0) {
+  if (ta.nb > 0 && ta.disc) {
+    const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
+    rb_tb_adj_disc_kernel<<<dim3(ta.nb, (ta.nf + blk - 1) / blk), blk, 0, st>>>(ta);
+  } else if (ta.nb > 0) {
     const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
     dim3 grid(ta.nb, ta.nchunk, (ta.nf + blk - 1) / blk);
     rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);

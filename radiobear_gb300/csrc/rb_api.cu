@@ -242,7 +242,7 @@ cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st);
 int tb_nchunk(int max_seg);
 cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, double* out,
                             cudaStream_t st, int nvar = 1);
-cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st);
+cudaError_t launch_e2(int order, int n, const double* x, double* out, cudaStream_t st);
 cudaError_t launch_fp32_probe(int blocks, int iters, float* sink, int packed, cudaStream_t st);
 }  // namespace rb
 
@@ -1384,7 +1384,6 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
     return fail(RB_EINVAL, "null array");
   if (nL < 2 || nb < 0) return fail(RB_EINVAL, "bad sizes");
   if (Tb_avg && !weights) return fail(RB_EINVAL, "Tb_avg needs weights");
-  if (disc) return fail(RB_EINVAL, "rb_forward_device: pass nadir rays explicitly for disc");
   if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
   if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
   RB_CUDA(cudaSetDevice(h->device));
@@ -1400,7 +1399,7 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
 static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, const double* T,
                         const double* X, const double* R, const double* N, const double* scale,
                         double Req, double Rpol, double orient0, double orient1, int gtype,
-                        int limb, int nb, const double* b, const double* weights,
+                        int limb, int nb, const double* b, const double* weights, int disc,
                         const double* grad, double* Tb_out, double* Tb_avg, double* dT, double* dP,
                         double* dlnX, const Batch* bt = nullptr) {
   const int nf = (int)h->plan_f.size();
@@ -1412,7 +1411,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   double* davg = Tb_avg ? Tb_avg : (weights ? h->d_avg.as<double>() : nullptr);
   int rc;
   if ((rc = forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
-                         nb, b, weights, 0, dTb, davg, nullptr, bt)))
+                         nb, b, weights, disc, dTb, davg, nullptr, bt)))
     return rc;
   const int launches = h->launches;
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
@@ -1438,9 +1437,15 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   ta.ga = h->d_ga.as<float>();
   ta.gs = h->d_gs.as<double>();
   ta.nchunk = rb::tb_nchunk(max_seg);
-  ta.part = h->d_part.as<float4>();
-  RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nbt * ta.nchunk * nf));
-  ta.S = h->d_adjS.as<float>();
+  ta.disc = disc != 0;
+  if (disc) {   // sequential E2 sweep: {tau, 2 E2} per node instead of chunk sums
+    RB_CUDA(h->d_adjS.ensure(sizeof(double2) * (size_t)nbt * max_seg * nf));
+    ta.tauE = h->d_adjS.as<double2>();
+  } else {
+    ta.part = h->d_part.as<float4>();
+    RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nbt * ta.nchunk * nf));
+    ta.S = h->d_adjS.as<float>();
+  }
   rb::TanArgs tn{};
   tn.nL = nL;
   tn.P = P;
@@ -1474,7 +1479,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   }
   RB_CUDA(rb::launch_adjoint(ta, tn, jv, extra ? &ea : nullptr, h->d_ga.as<float>(),
                              h->d_gs.as<double>(), dT, dP, dlnX, st));
-  h->launches = launches + (extra ? 7 : 6);
+  h->launches = launches + (extra ? 7 : 6) - (disc ? 1 : 0);
   return RB_OK;
 }
 
@@ -1482,8 +1487,8 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
                       const double* X, const double* R, const double* N, int nf,
                       const double* freqs_host, const double* scale, double Req, double Rpol,
                       double orient0, double orient1, int gtype, int limb, int nb, const double* b,
-                      const double* weights, const double* grad, double* Tb_out, double* Tb_avg,
-                      double* dT, double* dP, double* dlnX) {
+                      const double* weights, int disc, const double* grad, double* Tb_out,
+                      double* Tb_avg, double* dT, double* dP, double* dlnX) {
   if (!h) return fail(RB_EINVAL, "null handle");
   if (!P || !T || !X || !R || !N || !freqs_host || !grad || !dT || !dP || !dlnX ||
       (nb > 0 && !b))
@@ -1496,8 +1501,8 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   int rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
   return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), nL, P, T, X, R, N, scale, Req,
-                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, grad, Tb_out, Tb_avg,
-                      dT, dP, dlnX);
+                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, disc, grad, Tb_out,
+                      Tb_avg, dT, dP, dlnX);
 }
 
 // Batch descriptor from the host layer counts (offsets uploaded once per
@@ -1525,7 +1530,8 @@ static int make_batch(rb_handle* h, int nvar, const int32_t* nL_host, Batch& bt,
 
 int rb_forward_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
                             const double* P, const double* T, const double* X, const double* R,
-                            const double* N, int nf, const double* freqs_host, double Req,
+                            const double* N, int nf, const double* freqs_host, const double* scale,
+                            double Req,
                             double Rpol, double orient0, double orient1, int gtype, int limb,
                             int nb, const double* b, const double* weights, double* Tb_avg) {
   if (!h) return fail(RB_EINVAL, "null handle");
@@ -1540,14 +1546,15 @@ int rb_forward_batch_device(rb_handle* h, void* stream, int nvar, const int32_t*
   if ((rc = make_batch(h, nvar, nL_host, bt, NLT))) return rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nvar * nb * nf));
-  return forward_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, nullptr, Req,
+  return forward_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, scale, Req,
                       Rpol, orient0, orient1, gtype, limb, nb, b, weights, 0,
                       h->d_Tb.as<double>(), Tb_avg, nullptr, &bt);
 }
 
 int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
                             const double* P, const double* T, const double* X, const double* R,
-                            const double* N, int nf, const double* freqs_host, double Req,
+                            const double* N, int nf, const double* freqs_host, const double* scale,
+                            double Req,
                             double Rpol, double orient0, double orient1, int gtype, int limb,
                             int nb, const double* b, const double* weights, const double* grad,
                             double* Tb_avg, double* dT, double* dP, double* dlnX) {
@@ -1562,22 +1569,27 @@ int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t*
   Batch bt;
   if ((rc = make_batch(h, nvar, nL_host, bt, NLT))) return rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
-  return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, nullptr, Req,
-                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, grad, nullptr, Tb_avg,
+  return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, scale, Req,
+                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, 0, grad, nullptr, Tb_avg,
                       dT, dP, dlnX, &bt);
 }
 
 int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const double* X,
                const double* R, const double* N, int nf, const double* freqs, const double* scale,
                double Req, double Rpol, double orient0, double orient1, int gtype, int limb, int nb,
-               const double* b, const double* weights, const double* grad, double* Tb_out,
-               double* Tb_avg, double* dT, double* dP, double* dlnX) {
+               const double* b, const double* weights, int disc, const double* grad,
+               double* Tb_out, double* Tb_avg, double* dT, double* dP, double* dlnX) {
   if (!h) return fail(RB_EINVAL, "null handle");
   if (!P || !T || !X || !R || !N || !freqs || !grad || !dT || !dP || !dlnX || (nb > 0 && !b))
     return fail(RB_EINVAL, "null array");
   if (nL < 1) return fail(RB_EINVAL, "nL must be >= 1");
   if (nb < 1) return fail(RB_EINVAL, "nb must be >= 1");
   if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
+  std::vector<double> bb;
+  if (disc) {  // 'disc' evaluates the nadir ray (brightness.py:32-34)
+    bb.assign(2 * (size_t)nb, 0.0);
+    b = bb.data();
+  }
   int rc = validate_atm(nL, P, T, X);
   if (!rc) rc = validate_geom(nL, R, N, Req, Rpol, gtype, limb, nb, b);
   if (!rc && weights && !finite_all(weights, nb)) rc = fail(RB_EINVAL, "weights not finite");
@@ -1618,7 +1630,7 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
     RB_CUDA(cudaMemcpyAsync(h->d_in.p, hin, sizeof(double) * nin, cudaMemcpyHostToDevice, st));
     int r = adjoint_core(h, st, nL, din + oP, din + oT, din + oX, din + oR, din + oN,
                          scale ? din + osc : nullptr, Req, Rpol, orient0, orient1, gtype, limb, nb,
-                         din + ob, weights ? din + ow : nullptr, din + og, h->d_Tb.as<double>(),
+                         din + ob, weights ? din + ow : nullptr, disc, din + og, h->d_Tb.as<double>(),
                          weights ? h->d_avg.as<double>() : nullptr, dd, dd + nL, dd + 2 * (size_t)nL);
     if (r) return r;
     if (nTb) RB_CUDA(cudaMemcpyAsync(hout + oTb, h->d_Tb.p, sizeof(double) * nTb, cudaMemcpyDeviceToHost, st));
@@ -1633,6 +1645,7 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
   key.gtype = gtype;
   key.limb = limb;
   key.flags = (scale ? 1 : 0) | (weights ? 2 : 0) | (nTb ? 4 : 0) | (navg ? 8 : 0);
+  key.disc = disc;
   key.Req = Req;
   key.Rpol = Rpol;
   key.o0 = orient0;
@@ -1875,17 +1888,25 @@ int rb_probe_fp32_peak(rb_handle* h, double* tflops) {
   return RB_OK;
 }
 
-int rb_debug_e2(rb_handle* h, int n, const double* x, double* out) {
+static int debug_expint(rb_handle* h, int order, int n, const double* x, double* out) {
   if (!h) return fail(RB_EINVAL, "null handle");
   if (n < 0 || (n > 0 && (!x || !out))) return fail(RB_EINVAL, "bad arguments");
   if (n == 0) return RB_OK;
   RB_CUDA(cudaSetDevice(h->device));
   RB_CUDA(upload(h->d_x, x, n, h->st));
   RB_CUDA(h->d_iw.ensure(sizeof(double) * n));
-  RB_CUDA(rb::launch_e2(n, h->d_x.as<double>(), h->d_iw.as<double>(), h->st));
+  RB_CUDA(rb::launch_e2(order, n, h->d_x.as<double>(), h->d_iw.as<double>(), h->st));
   RB_CUDA(cudaMemcpyAsync(out, h->d_iw.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
   RB_CUDA(cudaStreamSynchronize(h->st));
   return RB_OK;
+}
+
+int rb_debug_e2(rb_handle* h, int n, const double* x, double* out) {
+  return debug_expint(h, 2, n, x, out);
+}
+
+int rb_debug_e1(rb_handle* h, int n, const double* x, double* out) {
+  return debug_expint(h, 1, n, x, out);
 }
 
 }  // extern "C"

@@ -250,6 +250,9 @@ struct TbAdjArgs {
   const float4* part;     // forward scan partials [nb][nchunk][nf]
   int nchunk;
   float* S;               // [nb][nchunk][nf] per-chunk sums of dTb/dtau
+  // b = 'disc' (E2 weighting): sequential reverse sweep, no chunk partials
+  int disc;
+  double2* tauE;          // [nb][max_seg][nf] {tau, 2 E2(tau)} per path node
 };
 
 struct JvpArgs {

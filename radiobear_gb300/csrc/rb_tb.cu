@@ -24,50 +24,12 @@
 // (tau, W, TbL) are requested.
 #include "rb_args.cuh"
 #include "rb_f32x2.cuh"
+#include "rb_expint.cuh"
 #include <math_constants.h>
 
 namespace rb {
 
 constexpr double T_CMB = 2.725;   // utils.py:77
-
-// Exponential integral E2(x), x >= 0, float64.
-// x <= 1: power series  E2(x) = 1 + x (ln x - 1 + gamma) - sum_{k>=2} (-x)^k / ((k-1) k!)
-//         (Abramowitz & Stegun 5.1.12 with the n = 2 digamma term).
-// x > 1:  continued fraction of A&S 5.1.22 evaluated by the modified Lentz
-//         method (Thompson & Barnett 1986).
-__device__ double expint2(double x) {
-  if (x == 0.0) return 1.0;
-  if (!(x > 0.0)) return CUDART_NAN;
-  if (x > 740.0) return 0.0;
-  if (x <= 1.0) {
-    const double euler = 0.57721566490153286061;
-    double sum = 0.0;
-    double fact = -x;  // (-x)^1 / 1!
-    for (int kk = 2; kk < 60; ++kk) {
-      fact *= -x / kk;                 // (-x)^k / k!
-      const double term = fact / (kk - 1);
-      sum += term;
-      if (fabs(term) < 1e-18 * fabs(sum) + 1e-300) break;
-    }
-    return 1.0 + x * (log(x) - 1.0 + euler) - sum;
-  }
-  const double tiny = 1e-300;
-  const int n = 2;
-  double bb = x + n;
-  double c = 1.0 / tiny;
-  double d = 1.0 / bb;
-  double h = d;
-  for (int i = 1; i < 200; ++i) {
-    const double an = -(double)i * (n - 1 + i);
-    bb += 2.0;
-    d = 1.0 / (an * d + bb);
-    c = bb + an / c;
-    const double del = c * d;
-    h *= del;
-    if (fabs(del - 1.0) < 1e-16) break;
-  }
-  return h * exp(-x);
-}
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   const float y = v - c;
@@ -421,9 +383,10 @@ __global__ void __launch_bounds__(128) rb_disc_avg_kernel(int nb, int nf, const 
   if (lane == 0) out[f] = s;
 }
 
-__global__ void rb_e2_kernel(int n, const double* x, double* out) {
+// Test hook: E1 (order 1) or E2 (order 2) of n arguments.
+__global__ void rb_e2_kernel(int order, int n, const double* x, double* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = expint2(x[i]);
+  if (i < n) out[i] = order == 1 ? expint1(x[i]) : expint2(x[i]);
 }
 
 int tb_nchunk(int max_seg) { return (max_seg + TB_CHUNK - 1) / TB_CHUNK; }
@@ -462,9 +425,9 @@ cudaError_t launch_disc_avg(int nb, int nf, const float* Tb32, const double* w, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_e2(int n, const double* x, double* out, cudaStream_t st) {
+cudaError_t launch_e2(int order, int n, const double* x, double* out, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  rb_e2_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, x, out);
+  rb_e2_kernel<<<(n + 127) / 128, 128, 0, st>>>(order, n, x, out);
   return cudaGetLastError();
 }
 

@@ -35,7 +35,7 @@ def test_library_builds_and_exports_every_declared_symbol():
 
 def test_abi_version_and_error_path_without_gpu():
     lib = _native.load_library()
-    assert lib.rb_abi_version() == _native.ABI_VERSION == 2
+    assert lib.rb_abi_version() == _native.ABI_VERSION == 3
     try:
         import torch
         has_gpu = torch.cuda.is_available()

@@ -34,21 +34,11 @@ def small_case(nL=40, Pmax=700.0, nrays=3):
 
 
 def random_direction(rng, gas):
-    nL = gas.shape[1]
-    k = np.ones(5) / 5.0
-
-    def corr(sigma):
-        return np.convolve(rng.normal(0.0, sigma, nL + 4), k, mode='valid') * np.sqrt(5.0)
-
-    dex = 0.3 * np.log(10.0)
-    return dict(T=rng.normal(0.0, 5.0, nL), P=0.01 * gas[C['P']] * rng.normal(0.0, 1.0, nL),
-                NH3=corr(dex), H2O=corr(dex), H2S=corr(dex))
+    return A.random_direction(rng, gas, C)
 
 
 def dot(grad, direction):
-    return (np.dot(grad['dT'], direction['T']) + np.dot(grad['dP'], direction['P']) +
-            np.dot(grad['dlnX'][0], direction['NH3']) + np.dot(grad['dlnX'][1], direction['H2O']) +
-            np.dot(grad['dlnX'][2], direction['H2S']))
+    return A.dot(grad, direction)
 
 
 def test_brightness_vjp_matches_finite_differences():
@@ -188,3 +178,107 @@ def test_autograd_function(engine, case):
     fd = A.directional_fd(gas, C, R, N, freqs, b, lines, G.REQ, G.RPOL, w, gw, d, h=1e-4)
     ad = dot(dict(dT=T.grad.cpu().numpy(), dP=P.grad.cpu().numpy(), dlnX=lnX.grad.cpu().numpy()), d)
     assert abs(ad - fd) <= DIR_RTOL * abs(fd) + 1e-7
+
+
+def _torch64_grad(case, grad, disc=False, device='cpu'):
+    from oracle import torch64 as T64
+    gas, R, N, freqs, b, w, lines = case
+    if disc:
+        b, w = np.zeros((1, 2)), np.ones(1)
+    paths = [O.compute_ds(R, N, bb, G.REQ, G.RPOL) for bb in b]
+    m = T64.Model(gas, C, lines, freqs, device=device)
+    lnX = np.log(np.stack([gas[C['NH3']], gas[C['H2O']], gas[C['H2S']]]))
+    tb, loss, dT, dP, dX = T64.gradients(m, gas[C['T']], gas[C['P']], lnX, paths, w, grad, disc=disc)
+    return dict(Tb=tb, dT=dT, dP=dP, dlnX=dX)
+
+
+def _vec_err(got, ref):
+    """max |got - ref| over the layers, relative to max |ref|, per parameter."""
+    out = {}
+    for k, (a, r) in dict(T=(got['dT'], ref['dT']), P=(got['dP'], ref['dP']),
+                          NH3=(got['dlnX'][0], ref['dlnX'][0]), H2O=(got['dlnX'][1], ref['dlnX'][1]),
+                          H2S=(got['dlnX'][2], ref['dlnX'][2])).items():
+        out[k] = float(np.max(np.abs(a - r)) / max(np.max(np.abs(r)), 1e-300))
+    return out
+
+
+# Per-layer gradient vectors against the float64 autograd reference: the
+# device's float32 line sums and tangents give ~1e-4 of the largest entry.
+VEC_RTOL = 2e-3
+
+
+@pytest.mark.gpu
+def test_adjoint_against_fp64_autograd(engine, case):
+    """Every layer's dTb/dT, dTb/dP, dTb/dlnX against torch autograd of the
+    float64 restatement (oracle/torch64.py), and 32 directional derivatives."""
+    gas, R, N, freqs, b, w, lines = case
+    rng = np.random.default_rng(21)
+    grad = rng.normal(size=freqs.size)
+    out = _run(engine, case, grad)
+    ref = _torch64_grad(case, grad)
+    errs = _vec_err(out, ref)
+    print('per-parameter max err / max |grad|', errs)
+    assert max(errs.values()) < VEC_RTOL, errs
+    for _ in range(32):
+        d = random_direction(rng, gas)
+        ad, rd = dot(out, d), dot(ref, d)
+        assert abs(ad - rd) <= DIR_RTOL * abs(rd) + 1e-7, (ad, rd)
+
+
+@pytest.mark.gpu
+def test_disc_mode_adjoint(engine, case):
+    """b = 'disc' (nadir ray, 2 E2(tau) weighting, brightness.py:96): the
+    gradient against the float64 autograd reference (dE2/dx = -E1 from
+    scipy) and against central differences of the oracle's disc forward."""
+    from radiobear_gb300 import catalog
+    from radiobear_gb300._native import x_matrix
+    gas, R, N, freqs, b, w, lines = case
+    catalog.upload(engine, lines)
+    engine.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    rng = np.random.default_rng(8)
+    grad = rng.normal(size=freqs.size)
+    out = engine.adjoint(gas[C['P']], gas[C['T']], x_matrix(gas, C), R, N, freqs, np.zeros((1, 2)),
+                         G.REQ, G.RPOL, grad, weights=np.ones(1), disc=True)
+    tb_ref, _, _ = O.forward(gas, C, R, N, freqs, np.zeros((1, 2)), lines, G.REQ, G.RPOL, disc=True)
+    assert np.max(np.abs(out['Tb'] - tb_ref)) < 1e-3
+    ref = _torch64_grad(case, grad, disc=True)
+    errs = _vec_err(out, ref)
+    print('disc: per-parameter max err / max |grad|', errs)
+    assert max(errs.values()) < VEC_RTOL, errs
+
+    def loss(gg):
+        tb, _, _ = O.forward(gg, C, R, N, freqs, np.zeros((1, 2)), lines, G.REQ, G.RPOL, disc=True)
+        return float(np.dot(grad, tb[0]))
+
+    for _ in range(4):
+        d = random_direction(rng, gas)
+        fd = (loss(A.perturb(gas, C, d, 1e-4)) - loss(A.perturb(gas, C, d, -1e-4))) / 2e-4
+        ad = dot(out, d)
+        assert abs(ad - fd) <= DIR_RTOL * abs(fd) + 1e-7, (ad, fd)
+
+
+@pytest.mark.gpu
+def test_autograd_function_disc(engine, case):
+    """TbFunction with disc=True equals rb_adjoint with disc = 1."""
+    import torch
+    from radiobear_gb300 import catalog
+    from radiobear_gb300._native import x_matrix
+    from radiobear_gb300.autograd import TbModel
+    gas, R, N, freqs, b, w, lines = case
+    catalog.upload(engine, lines)
+    engine.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    X = x_matrix(gas, C)
+    model = TbModel(engine, R, N, freqs, np.zeros((1, 2)), np.ones(1), X, G.REQ, G.RPOL, disc=True)
+    dev = torch.device('cuda')
+    T = torch.tensor(gas[C['T']], dtype=torch.float64, device=dev, requires_grad=True)
+    P = torch.tensor(gas[C['P']], dtype=torch.float64, device=dev, requires_grad=True)
+    lnX = torch.tensor(np.log(np.stack([gas[C['NH3']], gas[C['H2O']], gas[C['H2S']]])),
+                       dtype=torch.float64, device=dev, requires_grad=True)
+    gw = np.random.default_rng(2).normal(size=freqs.size)
+    avg = model(T, P, lnX)
+    (avg * torch.tensor(gw, dtype=torch.float64, device=dev)).sum().backward()
+    ref = engine.adjoint(gas[C['P']], gas[C['T']], X, R, N, freqs, np.zeros((1, 2)), G.REQ, G.RPOL,
+                         gw, weights=np.ones(1), disc=True)
+    np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=1e-9)
+    for got, want in ((T.grad, ref['dT']), (P.grad, ref['dP']), (lnX.grad, ref['dlnX'])):
+        np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-5, atol=1e-6 * np.max(np.abs(want)))

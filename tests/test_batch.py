@@ -93,3 +93,66 @@ def test_adjoint_batch_equals_single(setup):
             assert np.max(np.abs(got - want)) <= 1e-6 * scale, (v, np.max(np.abs(got - want)), scale)
         assert np.max(np.abs(avg.cpu().numpy()[v] - ref['Tb_avg'])) <= 1e-9
         o += n
+
+
+def _variant_scales(nl):
+    """Per-variant scale tables [sum nL][RB_NGAS]: variant 0 unscaled, 1 a
+    per-gas dict (nh3 ramp, h2o x2), 2 a per-layer list (the reference's
+    scale forms, alpha.py:235-259, one walker each)."""
+    from radiobear_gb300 import _native
+    ng = len(_native.GASES)
+    out = []
+    for v, n in enumerate(nl):
+        s = np.ones((n, ng))
+        if v == 1:
+            s[:, _native.GASES.index('nh3')] = np.linspace(0.5, 1.5, n)
+            s[:, _native.GASES.index('h2o')] = 2.0
+        elif v == 2:
+            s *= np.linspace(0.8, 1.3, n)[:, None]
+        out.append(s)
+    return out
+
+
+def test_batches_with_per_variant_scale(setup):
+    """scripts/demo_batch.py:24-41 reruns one atmosphere with different scale
+    dicts; here every variant of a batch carries its own scale table, and
+    the batch equals one scaled call per variant (forward and adjoint)."""
+    import torch
+    from radiobear_gb300._native import x_matrix
+    e, vs, freqs, b, w, t, nl = setup
+    NLT = sum(nl)
+    scales = _variant_scales(nl)
+    sc = torch.tensor(np.ascontiguousarray(np.concatenate(scales)), dtype=torch.float64, device='cuda')
+    s = torch.cuda.current_stream().cuda_stream
+    avg = torch.empty((len(vs), freqs.size), dtype=torch.float64, device='cuda')
+    e.forward_batch_device(s, nl, t['P'].data_ptr(), t['T'].data_ptr(), t['X'].data_ptr(),
+                           t['R'].data_ptr(), t['N'].data_ptr(), freqs, t['b'], t['w'].data_ptr(),
+                           avg.data_ptr(), G.REQ, G.RPOL, scale=sc.data_ptr())
+    grad = np.random.default_rng(9).normal(size=(len(vs), freqs.size))
+    g = torch.tensor(grad, dtype=torch.float64, device='cuda')
+    avg2 = torch.empty_like(avg)
+    dT, dP = (torch.empty(NLT, dtype=torch.float64, device='cuda') for _ in range(2))
+    dX = torch.empty((3, NLT), dtype=torch.float64, device='cuda')
+    e.adjoint_batch_device(s, nl, t['P'].data_ptr(), t['T'].data_ptr(), t['X'].data_ptr(),
+                           t['R'].data_ptr(), t['N'].data_ptr(), freqs, t['b'], t['w'].data_ptr(),
+                           g.data_ptr(), avg2.data_ptr(), dT.data_ptr(), dP.data_ptr(), dX.data_ptr(),
+                           G.REQ, G.RPOL, scale=sc.data_ptr())
+    torch.cuda.synchronize()
+    got, got2 = avg.cpu().numpy(), avg2.cpu().numpy()
+    dT, dP, dX = dT.cpu().numpy(), dP.cpu().numpy(), dX.cpu().numpy()
+    o = 0
+    unscaled = e.forward(vs[1][0][C['P']], vs[1][0][C['T']], x_matrix(vs[1][0], C), vs[1][1], vs[1][2],
+                         freqs, b, G.REQ, G.RPOL, weights=w, want_rays=False)['Tb_avg']
+    assert np.max(np.abs(got[1] - unscaled)) > 1e-3          # the scale does act
+    for v, (gas, R, N) in enumerate(vs):
+        n = gas.shape[1]
+        X = x_matrix(gas, C)
+        ref = e.forward(gas[C['P']], gas[C['T']], X, R, N, freqs, b, G.REQ, G.RPOL, weights=w,
+                        scale=scales[v], want_rays=False)['Tb_avg']
+        assert np.max(np.abs(got[v] - ref)) <= 1e-9, v
+        assert np.max(np.abs(got2[v] - ref)) <= 1e-9, v
+        ra = e.adjoint(gas[C['P']], gas[C['T']], X, R, N, freqs, b, G.REQ, G.RPOL, grad[v], weights=w,
+                       scale=scales[v])
+        for gg, want in ((dT[o:o + n], ra['dT']), (dP[o:o + n], ra['dP']), (dX[:, o:o + n], ra['dlnX'])):
+            assert np.max(np.abs(gg - want)) <= 1e-6 * (np.max(np.abs(want)) + 1e-300), v
+        o += n

@@ -198,6 +198,16 @@ def test_e2_against_scipy(engine):
     assert np.max(np.abs(got - ref) / np.maximum(ref, 1e-300)) < 1e-13
 
 
+def test_e1_against_scipy(engine):
+    """E1 = -dE2/dx, the derivative the disc-mode adjoint takes."""
+    from scipy.special import exp1
+    x = np.concatenate([[1e-12, 1e-6, 1e-3], np.linspace(0.01, 1.0, 50),
+                        np.linspace(1.0001, 30.0, 80), [50.0, 200.0, 700.0]])
+    got = engine.debug_e1(x)
+    ref = exp1(x)
+    assert np.max(np.abs(got - ref) / np.maximum(ref, 1e-300)) < 1e-13
+
+
 def test_forward_benchmark_golden_table(engine):
     """scripts/benchmark.py:20-24 through the fused GPU forward model."""
     z = G.load('benchmark')
