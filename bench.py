@@ -47,12 +47,15 @@ def parse():
     p.add_argument('--warmup', type=int, default=5)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     p.add_argument('--no-cpu-baseline', action='store_true')
-    p.add_argument('--cpu-sample-s', type=float, default=20.0)
     p.add_argument('--no-image', action='store_true', help='skip the C2 image measurement')
     p.add_argument('--batch-variants', type=int, default=4096,
                    help='atmospheres in the batched forward+adjoint measurement (0: skip)')
     p.add_argument('--alpha-tiling', default='',
                    help='line-sum tiling M,W,item_lines (default: automatic)')
+    p.add_argument('--no-accuracy', action='store_true',
+                   help='skip the per-workload accuracy checks against the float64 oracle')
+    p.add_argument('--no-stock-reference', action='store_true',
+                   help='reference arm: skip the stock-reference sample')
     return p.parse_args()
 
 
@@ -80,10 +83,13 @@ GRAD_WORKLOAD = ('C3 differentiable forward model: 1000 layers (1e-3..500 bar) x
                  'dTb/dT, dTb/dP, dTb/dlnX(NH3, H2O, H2S) per layer')
 
 
-def measure_gradients(args, dev, stream, flush):
+def measure_gradients(args, dev, stream, flush, pool=None):
     """Spectra + gradients per second on the C3 workload: each step runs
     rb_adjoint_device (forward, then the adjoint with alpha recomputed)
-    on device-resident inputs; e2e through rb_adjoint with host buffers."""
+    on device-resident inputs; e2e through rb_adjoint with host buffers.
+    With a pool, the last timed step's gradient is checked against the
+    float64 autograd reference (32 perturbations) and central differences
+    of the oracle (8 of them)."""
     import torch
     from radiobear_gb300 import _native, catalog, synth
     from tests import goldio
@@ -127,6 +133,8 @@ def measure_gradients(args, dev, stream, flush):
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
+    grad_gpu = dict(dT=gT.cpu().numpy(), dP=gP.cpu().numpy(), dlnX=gX.cpu().numpy().reshape(3, nL))
+    tb_avg_gpu = avg.cpu().numpy()
     host = {k: np.ascontiguousarray(a[k]) for k in ('P', 'T', 'X', 'R', 'N', 'b', 'w')}
     gh = g.cpu().numpy()
     e2e = []
@@ -139,13 +147,23 @@ def measure_gradients(args, dev, stream, flush):
     h2d = sum(v.nbytes for v in host.values()) + gh.nbytes + a['freqs'].nbytes
     d2h = out['dT'].nbytes + out['dP'].nbytes + out['dlnX'].nbytes + out['Tb'].nbytes + out['Tb_avg'].nbytes
     eng.close()
-    return dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second',
-                value=1e3 / ms, unit='spectra+gradients/s', ms_per_step=ms, steps=n,
-                config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb),
-                gpu_launches_per_step=int(launches),
-                e2e=dict(value=1.0 / float(np.mean(e2e)), unit='spectra+gradients/s',
-                         h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
-                         api='rb_adjoint (C ABI, host buffers)'))
+    out = dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second',
+               value=1e3 / ms, unit='spectra+gradients/s', ms_per_step=ms, steps=n,
+               config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb),
+               gpu_launches_per_step=int(launches),
+               e2e=dict(value=1.0 / float(np.mean(e2e)), unit='spectra+gradients/s',
+                        h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
+                        api='rb_adjoint (C ABI, host buffers)'))
+    if pool is not None:
+        from oracle import accuracy as ACC
+        from oracle import parallel as OP
+        acc = ACC.gradients(pool, wl.freqs, wl.gas, a['C'], a['R'], a['N'], a['b'], a['w'], wl.lines,
+                            71492.0, 66854.0, grad_gpu, gh, n_dir=32, n_fd=8, device=str(dev))
+        layers = OP.layers(pool, wl.freqs, wl.gas, a['C'], wl.lines)
+        tb, _ = OP.rays(pool, a['R'], a['N'], a['b'], 71492.0, 66854.0, layers, a['T'])
+        acc['max_abs_dTb_avg_K'] = float(np.max(np.abs(tb_avg_gpu - np.tensordot(a['w'], tb, axes=1))))
+        out['accuracy'] = acc
+    return out
 
 
 BATCH_WORKLOAD = ('C4 batched retrieval sweep: {n} variants of the 1e-3..100 bar recipe (deep NH3 '
@@ -155,10 +173,13 @@ BATCH_WORKLOAD = ('C4 batched retrieval sweep: {n} variants of the 1e-3..100 bar
                   'from one captured CUDA graph, line-sum tiling from the autotuner')
 
 
-def measure_batch(args, dev, n_var):
+def measure_batch(args, dev, n_var, pool=None):
     """Spectra + gradients per second for a batch of n_var atmospheres
     (rb_adjoint_batch_device captured in a CUDA graph and replayed), beside
-    the same variants run one call per atmosphere (rb_adjoint_device)."""
+    the same variants run one call per atmosphere (rb_adjoint_device).  With
+    a pool, 8 variants spread over the layer range are checked against the
+    float64 oracle (Tb_avg, and a gradient direction by central
+    differences)."""
     import torch
     from radiobear_gb300 import _native, catalog, synth, tune
     from tests import goldio
@@ -202,7 +223,8 @@ def measure_batch(args, dev, n_var):
                                  avg.data_ptr(), gT.data_ptr(), gP.data_ptr(), gX.data_ptr(),
                                  71492.0, 66854.0)
 
-    best, tt = tune.tune_alpha(eng, step, key=('C4', n_var, nf),
+    best, tt = tune.tune_alpha(eng, step, key=tune.workload_key('batch', dict(freqs=freqs, lines=lines),
+                                                             nb, layers=(300, 1200)),
                                candidates=((2, 2, 1024), (2, 4, 1024), (4, 1, 1024), (4, 2, 1024)),
                                reps=1, stream=stream)
     step()                                   # plan and buffers for the chosen tiling
@@ -221,6 +243,8 @@ def measure_batch(args, dev, n_var):
     torch.cuda.synchronize()
     ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
     ok = bool(torch.isfinite(avg).all().item() and torch.isfinite(gT).all().item())
+    res = dict(avg=avg.cpu().numpy(), dT=gT.cpu().numpy(), dP=gP.cpu().numpy(), dX=gX.cpu().numpy(),
+               grad=grad.cpu().numpy())
     # the same variants one atmosphere per call (plain path), a sample of 16
     one = _native.Engine(dev.index or 0)
     catalog.upload(one, lines)
@@ -281,19 +305,53 @@ def measure_batch(args, dev, n_var):
                     how='plain drop-in forward (rb_forward_device, one atmosphere per call) '
                         'times 1 + 2 x 5 x nL central differences per gradient set'),
                 speedup_vs_per_atmosphere_adjoint=value / plain,
-                speedup_vs_plain_dropin=value / fd_rate)
+                speedup_vs_plain_dropin=value / fd_rate,
+                accuracy=None if pool is None else batch_accuracy(pool, nLs, nh3, dT, freqs, b, w, lines,
+                                                                  C, LP, res))
+
+
+def batch_accuracy(pool, nLs, nh3, dT, freqs, b, w, lines, C, LP, res, n_sample=8):
+    """8 variants spread over the layer range: Tb_avg against the float64
+    oracle and one random perturbation's directional derivative against
+    central differences of the oracle."""
+    from oracle import adjoint as A
+    from oracle import parallel as OP
+    from radiobear_gb300 import synth
+    off = np.concatenate([[0], np.cumsum(nLs)])
+    pick = np.argsort(nLs, kind='stable')[np.linspace(0, len(nLs) - 1, n_sample).astype(int)]
+    worst_tb, worst_dir, layers_seen = 0.0, 0.0, []
+    for v in pick:
+        gas = synth.make_gas_table(int(nLs[v]), 1.0e-3, 100.0, nh3_deep=nh3[v], dT_deep=dT[v])
+        pr = synth.compute_properties(gas)
+        R, N = pr[LP['R']], pr[LP['N']]
+        lay = OP.layers(pool, freqs, gas, C, lines)
+        tb, _ = OP.rays(pool, R, N, b, 71492.0, 66854.0, lay, gas[C['T']])
+        worst_tb = max(worst_tb, float(np.max(np.abs(res['avg'][v] - np.tensordot(w, tb, axes=1)))))
+        sl = slice(int(off[v]), int(off[v + 1]))
+        got = dict(dT=res['dT'][sl], dP=res['dP'][sl], dlnX=res['dX'][:, sl])
+        d = A.random_direction(np.random.default_rng(1000 + int(v)), gas, C)
+        fd = OP.directional_fd(pool, gas, C, R, N, freqs, b, lines, 71492.0, 66854.0, w, res['grad'][v], [d])
+        worst_dir = max(worst_dir, float(abs(A.dot(got, d) - fd[0]) / abs(fd[0])))
+        layers_seen.append(int(nLs[v]))
+    return dict(variants=n_sample, layers=layers_seen, max_abs_dTb_avg_K=worst_tb,
+                dir_rel_err_vs_central_differences=worst_dir,
+                reference='float64 oracle; central differences step 1e-4')
 
 
 IMAGE_WORKLOAD = ('C2 batched image rays: 256 x 256 impact parameters at 0.01 planet radius '
                   '(31,397 on the disc incl. limb rays of up to ~2000 segments, the rest off the '
-                  'planet -> T_cmb) x 8 freqs (1.4..44 GHz), 1000 layers, C1 line lists')
+                  'planet -> T_cmb) x 8 freqs (1.4..44 GHz), 1000 layers, C1 line lists; one step = '
+                  'one image replayed from a captured CUDA graph, line-sum tiling from the autotuner')
 
 
-def measure_image(args, dev, stream, flush):
-    """Images per second (and rays/s) for the C2 grid: one rb_forward_device
-    call per image, every ray in the same launches."""
+def measure_image(args, dev, stream, flush, pool=None, fp32_peak=None):
+    """Images per second (and rays/s) for the C2 grid: every ray of an image
+    in one rb_forward_device, captured once into a CUDA graph and replayed;
+    the line-sum tiling chosen by the autotuner for this shape.  The scan's
+    HBM fraction (its segments stream from HBM here) and, with a pool, the
+    accuracy of a 256-ray sample against the float64 oracle."""
     import torch
-    from radiobear_gb300 import _native, catalog, synth
+    from radiobear_gb300 import _native, catalog, synth, tune
     from tests import goldio
     cats = goldio.real_catalogues()
     wl = synth.make_workload(2, real=cats)
@@ -309,38 +367,80 @@ def measure_image(args, dev, stream, flush):
 
     dP, dT, dX, dR, dN, db = (dt(a[k]) for k in ('P', 'T', 'X', 'R', 'N', 'b'))
     Tb = torch.empty((nb, nf), dtype=torch.float64, device=dev)
-    sp = stream.cuda_stream
 
     def step():
-        eng.forward_device(sp, nL, nb, dP.data_ptr(), dT.data_ptr(), dX.data_ptr(), dR.data_ptr(),
-                           dN.data_ptr(), a['freqs'], db.data_ptr(), 71492.0, 66854.0, Tb.data_ptr())
+        eng.forward_device(torch.cuda.current_stream(dev).cuda_stream, nL, nb, dP.data_ptr(),
+                           dT.data_ptr(), dX.data_ptr(), dR.data_ptr(), dN.data_ptr(), a['freqs'],
+                           db.data_ptr(), 71492.0, 66854.0, Tb.data_ptr())
 
-    step()
+    best, tt = tune.tune_alpha(eng, step, key=tune.workload_key('image', wl, nb),
+                               candidates=((2, 1, 1024), (2, 2, 1024), (4, 1, 1024), (2, 4, 1024),
+                                           (2, 1, 512)), reps=2, stream=stream)
+    step()                                   # plan and buffers for the chosen tiling
     torch.cuda.synchronize()
+    launches = eng.last_launch_count()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
     for _ in range(args.warmup):
         flush.zero_()
-        step()
+        graph.replay()
     n = max(3, min(args.steps, 20))
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
     torch.cuda.synchronize()
     for s, e in ev:
         flush.zero_()
         s.record(stream)
-        step()
+        graph.replay()
         e.record(stream)
     torch.cuda.synchronize()
     ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
     t = Tb.cpu().numpy()
     on = np.hypot(a['b'][:, 0], a['b'][:, 1]) < 1.0
-    rays = eng.raypath(a['R'], a['N'], a['b'][on][::97], 71492.0, 66854.0)
+    # scan phase (library events on the launching streams) and the rays' path lengths
+    eng.set_profiling(True)
+    phs = []
+    for _ in range(5):
+        flush.zero_()
+        step()
+        phs.append(eng.phase_times())
+    eng.set_profiling(False)
+    ph = {k: float(np.mean([p[k] for p in phs])) for k in phs[0]}
+    nseg = np.concatenate([eng.raypath(a['R'], a['N'], a['b'][k:k + 4096], 71492.0, 66854.0)['nseg']
+                           for k in range(0, nb, 4096)])
+    sbytes = scan_bytes(nseg, nf, nb)
+    hbm = measured_peaks().get('hbm_gbs')
+    scan_gbs = sbytes / (ph['brightness'] * 1e-3) / 1e9
+    out = dict(metric='brightness images per second', value=1e3 / ms, unit='images/s',
+               rays_per_s=nb * 1e3 / ms, ms_per_step=ms, steps=n, gpu_launches_per_step=int(launches),
+               config=dict(workload=IMAGE_WORKLOAD, layers=nL, freqs=nf, rays=nb,
+                           rays_on_disc=int(on.sum()), max_path_segments=int(nseg.max()),
+                           cuda_graph=True, tiling=dict(M=best[0], W=best[1], item_lines=best[2]),
+                           tuning_ms={'{},{},{}'.format(*k): v for k, v in tt.items()},
+                           l2='256 MiB buffer written between steps'),
+               phase_ms=ph,
+               roofline_scan=dict(bound='hbm', kernel='rb_tb_chunk2_kernel+rb_tb_combine_kernel',
+                                  achieved=scan_gbs, peak=hbm, unit='GB/s',
+                                  frac=(scan_gbs / hbm) if hbm else None,
+                                  algorithmic_bytes_per_launch=sbytes,
+                                  peak_source='MEASURED_PEAKS.json hbm_gbs (of measured)'),
+               finite=bool(np.isfinite(t).all()),
+               off_disc_is_tcmb=bool(np.all(t[~on] == 2.725)))
+    if pool is not None:
+        from oracle import accuracy as ACC
+        rng = np.random.default_rng(5)
+        onx = np.nonzero(on)[0]
+        r = np.hypot(a['b'][:, 0], a['b'][:, 1])
+        cand = np.union1d(onx[r[onx] > 0.985], rng.choice(onx, 1024, replace=False))
+        sel, _, _ = ACC.image_sample(a['b'][cand], nseg[cand])
+        idx = cand[sel]
+        acc, _, _ = ACC.image(pool, wl.freqs, wl.gas, a['C'], a['R'], a['N'], a['b'][idx], wl.lines,
+                              71492.0, 66854.0, t[idx])
+        acc['sample'] = ('{} rays reaching the planet: the 16 longest paths (limb rays), the 16 '
+                         'outermost, a seeded random fill').format(len(idx))
+        out['accuracy'] = acc
     eng.close()
-    return dict(metric='brightness images per second', value=1e3 / ms, unit='images/s',
-                rays_per_s=nb * 1e3 / ms, ms_per_step=ms, steps=n,
-                config=dict(workload=IMAGE_WORKLOAD, layers=nL, freqs=nf, rays=nb,
-                            rays_on_disc=int(on.sum()),
-                            max_path_segments_sampled=int(rays['nseg'].max())),
-                finite=bool(np.isfinite(t).all()),
-                off_disc_is_tcmb=bool(np.all(t[~on] == 2.725)))
+    return out
 
 
 def replica_time(tot_ms, dist=None, device=None):
@@ -372,6 +472,32 @@ def alpha_flops(wl):
     per = 10 * n_br + 8 * n_gross + 12 * n_vvw
     return nL * nf * per + n_blend * nf * 10 * n_sjs, dict(n_br=n_br, n_gross=n_gross, n_vvw=n_vvw,
                                                             n_sjs_blend_layers=n_blend, n_sjs=n_sjs)
+
+
+# Algorithmic FLOPs of the scan per (segment, frequency), exp counted as one:
+# optical depth (add, multiply, add), W = a exp(-tau) (exp, multiply), intW
+# (add, multiply, add), TbL (two multiplies, add, multiply, add).
+SCAN_FLOPS = 13
+
+
+def scan_flops(nseg, nf):
+    return int(np.sum(np.maximum(np.asarray(nseg) - 1, 0)) * nf * SCAN_FLOPS)
+
+
+def l2_bandwidth(dev, mib=16, reps=200):
+    """Read + write GB/s of copies between two L2-resident buffers."""
+    import torch
+    x = torch.ones(mib << 18, dtype=torch.float32, device=dev)
+    y = torch.empty_like(x)
+    for _ in range(10):
+        y.copy_(x)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        y.copy_(x)
+    e.record()
+    torch.cuda.synchronize()
+    return 2.0 * x.numel() * 4 * reps / (s.elapsed_time(e) * 1e-3) / 1e9
 
 
 def scan_bytes(nseg, nf, nb):
@@ -486,13 +612,14 @@ class ClockSampler:
                 'samples': len(use), 'in_timed_region': in_region}
 
 
-def read_profile_traffic():
-    """dram bytes per absorption launch from the committed ncu summary."""
-    path = os.path.join(ROOT, 'profiles', 'alpha_kernel_c1.md')
+def profile_traffic(name='alpha_kernel_c1.md'):
+    """dram bytes per launch from a committed ncu summary of the same
+    workload (a capture of that kernel, not a measurement of this run)."""
+    path = os.path.join(ROOT, 'profiles', name)
     try:
         with open(path) as fp:
             m = re.search(r'traffic_bytes_per_launch:\s*([0-9.eE+]+)', fp.read())
-        return float(m.group(1)) if m else None
+        return dict(file='profiles/' + name, dram_bytes_per_launch=float(m.group(1))) if m else None
     except OSError:
         return None
 
@@ -506,97 +633,105 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------------ CPU oracle
-def _cpu_alpha_job(args):
-    layers, freqs, gas, lines = args
-    os.environ.setdefault('OMP_NUM_THREADS', '1')
-    from oracle import oracle as O
-    from radiobear_gb300 import synth
-    C = {k: i for i, k in enumerate(synth.GAS_COLUMNS)}
-    O.alpha_per_gas(freqs, gas[:, layers], C, lines, chunk=4)
-    return len(layers)
-
-
-def _cpu_ray_job(args):
-    b, R, N, layers_alpha, T, Req, Rpol = args
-    from oracle import oracle as O
-    ds, lay = O.compute_ds(R, N, b, Req, Rpol)
-    O.brightness(ds, lay, layers_alpha, T)
-    return 1
-
-
-def cpu_sample(wl, pool, nL_sample, nb_sample, cores):
-    """Time alpha for nL_sample layers and ray path + Tb for nb_sample rays on
-    the pool; returns (seconds per full spectrum, description)."""
-    a = workload_arrays(wl)
-    nL = a['P'].size
-    idx = np.linspace(0, nL - 1, nL_sample).astype(int)
-    chunks = [idx[i::cores] for i in range(cores) if idx[i::cores].size]
-    t0 = time.perf_counter()
-    pool.map(_cpu_alpha_job, [(c, wl.freqs, wl.gas, wl.lines) for c in chunks])
-    t_alpha = time.perf_counter() - t0
-    layers_alpha = np.full((wl.freqs.size, nL), 1e-6)   # geometry + scan cost is alpha-independent
-    rays = wl.b[np.linspace(0, len(wl.b) - 1, nb_sample).astype(int)]
-    t0 = time.perf_counter()
-    pool.map(_cpu_ray_job, [(b, a['R'], a['N'], layers_alpha, a['T'], 71492.0, 66854.0) for b in rays])
-    t_rays = time.perf_counter() - t0
-    per_spec = t_alpha * nL / nL_sample + t_rays * len(wl.b) / nb_sample
-    desc = ('alpha of {} of {} layers + ray path and Tb scan of {} of {} rays, {} worker processes; '
-            'scaled to one spectrum').format(nL_sample, nL, nb_sample, len(wl.b), cores)
-    return per_spec, desc
-
-
 def make_pool():
+    """Spawn-context pool over the host cores (made before the first GPU call)."""
+    from oracle import parallel as OP
+    return OP.make_pool()
+
+
+def port_spectrum(pool, wl):
+    """One whole C1 disc-averaged spectrum by the float64 oracle on the pool:
+    alpha of every layer (blocks of layers per worker), the 64 ray paths and
+    scans (one ray per task) and the quadrature average.  Returns (seconds,
+    Tb_avg)."""
+    from oracle import parallel as OP
+    a = workload_arrays(wl)
+    t0 = time.perf_counter()
+    layers = OP.layers(pool, wl.freqs, wl.gas, a['C'], wl.lines)
+    tb, _ = OP.rays(pool, a['R'], a['N'], wl.b, 71492.0, 66854.0, layers, a['T'])
+    avg = np.tensordot(wl.weights, tb, axes=1)
+    return time.perf_counter() - t0, avg
+
+
+PORT_SAMPLE = ('one whole spectrum per step: alpha of all 1000 layers x 256 freqs, 64 ray paths '
+               'and scans, the disc average; float64 numpy oracle on {} worker processes')
+
+
+def cpu_baseline(wl, pool, cores):
+    sec, _ = port_spectrum(pool, wl)
+    return dict(value=1.0 / sec, unit=UNIT, cores=cores, kind='port', sample=PORT_SAMPLE.format(cores),
+                seconds_per_spectrum=sec)
+
+
+def stock_reference(cores, layers_per_worker=2):
+    """The unmodified reference (installed under baseline/_ref) timed on a
+    sample of the same C1 workload: its own Alpha.get_alpha_from_calc for
+    2 layers per worker and Brightness.single for one ray per worker, each
+    worker on its own core; wall times scaled to the 1000 layers and 64
+    rays of one spectrum (extrapolated)."""
+    ref = os.path.join(ROOT, 'baseline', '_ref')
+    if not os.path.isdir(os.path.join(ref, 'radiobear')):
+        return dict(unavailable='the reference is not installed under baseline/_ref')
     import multiprocessing as mp
-    cores = os.cpu_count() or 1
-    ctx = mp.get_context('spawn')
-    return ctx.Pool(cores, initializer=_pool_init), cores
-
-
-def _pool_init():
-    os.environ['OMP_NUM_THREADS'] = '1'
-    os.environ['OPENBLAS_NUM_THREADS'] = '1'
-    sys.path.insert(0, ROOT)
-
-
-def cpu_baseline(wl, budget_s, pool, cores):
-    # calibrate on a small sample, then scale the sample to the budget
-    per, _ = cpu_sample(wl, pool, nL_sample=cores, nb_sample=min(cores, 8), cores=cores)
-    frac = min(1.0, budget_s / max(per, 1e-3))
-    nL_s = max(cores, int(1000 * frac))
-    nb_s = max(min(cores, 8), int(64 * frac))
-    per, desc = cpu_sample(wl, pool, nL_sample=min(nL_s, 1000), nb_sample=min(nb_s, 64), cores=cores)
-    return dict(value=1.0 / per, unit=UNIT, cores=cores, kind='port', sample=desc)
+    sys.path.insert(0, os.path.join(ROOT, 'tests', 'golden'))
+    import refharness as H
+    pool = mp.get_context('spawn').Pool(cores, initializer=H.stock_init, initargs=(ref, ROOT))
+    try:
+        nL, nb = 1000, 64
+        lay = np.linspace(0, nL - 1, cores * layers_per_worker).astype(int)
+        jobs = [lay[k::cores].tolist() for k in range(cores)]
+        rays = np.linspace(1, nb - 1, min(cores, nb - 1)).astype(int).tolist()
+        pool.map(H.stock_ray_job, rays[:1])                  # first call warms the modules
+        t0 = time.perf_counter()
+        pool.map(H.stock_alpha_job, jobs, chunksize=1)
+        t_alpha = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        pool.map(H.stock_ray_job, rays, chunksize=1)
+        t_rays = time.perf_counter() - t0
+    finally:
+        pool.close()
+        pool.join()
+    per = t_alpha * nL / len(lay) + t_rays * nb / len(rays)
+    return dict(value=1.0 / per, unit=UNIT, cores=cores, kind='reference', extrapolated=True,
+                seconds_per_spectrum=per,
+                sample=('the unmodified reference (pip-installed from its source): '
+                        'Alpha.get_alpha_from_calc of {} of 1000 layers and Brightness.single of {} '
+                        'of 64 rays, one worker process per core, wall times scaled to one spectrum '
+                        '(limb branch of compute_ds restored as in the parity harness)').format(
+                            len(lay), len(rays)))
 
 
 # ------------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
+    """Rank 0 only.  Each step is one whole C1 spectrum by the float64 port on
+    every host core (nothing sampled or extrapolated); beside it, the stock
+    reference on a sample (extrapolated, marked so)."""
     if rank != 0:
         return
     wl = load_workload()
     pool, cores = make_pool()
     try:
-        budget = max(1.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
-        cal, _ = cpu_sample(wl, pool, nL_sample=cores, nb_sample=min(cores, 8), cores=cores)
-        frac = min(1.0, budget / max(cal, 1e-3))
-        nL_s = min(1000, max(cores, int(1000 * frac)))
-        nb_s = min(64, max(min(cores, 8), int(64 * frac)))
         for _ in range(args.warmup):
-            cpu_sample(wl, pool, nL_s, nb_s, cores)
-        pers = []
-        desc = ''
+            port_spectrum(pool, wl)
+        secs = []
+        t_wall = time.perf_counter()
         for _ in range(args.steps):
-            per, desc = cpu_sample(wl, pool, nL_s, nb_s, cores)
-            pers.append(per)
+            secs.append(port_spectrum(pool, wl)[0])
+        t_wall = time.perf_counter() - t_wall
     finally:
         pool.close()
         pool.join()
-    ms = 1e3 * float(np.mean(pers))
+    stock = None if args.no_stock_reference else stock_reference(cores)
+    ms = 1e3 * float(np.mean(secs))
     value = 1e3 / ms
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=args.gpus, steps=args.steps,
                 warmup=args.warmup, ms_per_step=ms, higher_is_better=True, scaling='weak',
                 vs_baseline=None, dtype='f64', data='synthetic', impl='reference',
                 config=dict(workload=WORKLOAD, layers=1000, freqs=256, rays=64),
-                cpu_baseline=dict(value=value, unit=UNIT, cores=cores, kind='port', sample=desc),
+                timed_region_s=t_wall,
+                cpu_baseline=dict(value=value, unit=UNIT, cores=cores, kind='port',
+                                  sample=PORT_SAMPLE.format(cores), extrapolated=False),
+                stock_reference=stock,
                 e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
 
@@ -607,8 +742,9 @@ def run_gpu(args, rank, world, local_rank):
     from radiobear_gb300 import _native, catalog
 
     pool = cores = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not (args.no_cpu_baseline and args.no_accuracy):
         pool, cores = make_pool()          # spawn before the first GPU call
+    acc_pool = None if args.no_accuracy else pool
 
     torch.cuda.set_device(local_rank)
     dev = torch.device('cuda', local_rank)
@@ -696,9 +832,16 @@ def run_gpu(args, rank, world, local_rank):
     h2d = sum(host[k].nbytes for k in host) + a['freqs'].nbytes
     d2h = out['Tb_avg'].nbytes
 
-    grads = measure_gradients(args, dev, stream, flush)
-    image = None if args.no_image else measure_image(args, dev, stream, flush)
-    batched = measure_batch(args, dev, args.batch_variants) if args.batch_variants > 0 else None
+    # the last timed step's outputs, and the absorption table, for the accuracy check
+    tb_gpu, avg_gpu = dTb.cpu().numpy(), davg.cpu().numpy()
+    layers_gpu = eng.forward(host['P'], host['T'], host['X'], host['R'], host['N'], a['freqs'],
+                             host['b'], 71492.0, 66854.0, want_rays=False, want_layers=True)['layers']
+
+    grads = measure_gradients(args, dev, stream, flush, acc_pool if rank == 0 else None)
+    image = None if args.no_image else measure_image(args, dev, stream, flush,
+                                                     acc_pool if rank == 0 else None)
+    batched = (measure_batch(args, dev, args.batch_variants, acc_pool if rank == 0 else None)
+               if args.batch_variants > 0 else None)
     if rank != 0:
         return
     # roofline of the dominant kernel (the line sums, timed alone on their
@@ -708,9 +851,9 @@ def run_gpu(args, rank, world, local_rank):
     ach = flops / (ph['alpha'] * 1e-3) / 1e12
     rays = eng.raypath(a['R'], a['N'], a['b'], 71492.0, 66854.0)
     sbytes = scan_bytes(rays['nseg'], nf, nb)
-    peaks = measured_peaks()
-    hbm = peaks.get('hbm_gbs')
-    scan_gbs = sbytes / (ph['brightness'] * 1e-3) / 1e9
+    sflops = scan_flops(rays['nseg'], nf)
+    l2 = l2_bandwidth(dev)
+    scan_s = ph['brightness'] * 1e-3
     value = world * args.steps / (tot_ms * 1e-3)
     line = dict(
         metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
@@ -724,20 +867,35 @@ def run_gpu(args, rank, world, local_rank):
                  d2h_bytes_per_step=int(d2h), api='rb_forward (C ABI, pinned host buffers)'),
         gpu_launches=int(launches_per_step * args.steps),
         roofline=dict(bound='fp32', kernel='rb_alpha_lines_kernel', achieved=ach, peak=fp32_peak,
-                      unit='TFLOP/s', frac=ach / fp32_peak, traffic=read_profile_traffic(),
+                      unit='TFLOP/s', frac=ach / fp32_peak, traffic=None,
+                      traffic_ncu_capture=profile_traffic(),
                       algorithmic_flops_per_launch=flops,
                       peak_source='in-run FFMA probe (no fp32 entry in MEASURED_PEAKS.json)'),
-        roofline_scan=dict(bound='hbm', kernel='rb_tb_chunk2_kernel+rb_tb_combine_kernel', achieved=scan_gbs, peak=hbm,
-                           unit='GB/s', frac=(scan_gbs / hbm) if hbm else None,
-                           algorithmic_bytes_per_launch=sbytes,
-                           peak_source='MEASURED_PEAKS.json hbm_gbs (of measured)'),
+        # C1's scan reads the 1 MB absorption table from L2 and is bound by
+        # the FMA pipe (ncu): its algorithmic flops against the FP32 peak,
+        # its algorithmic bytes against the measured L2 rate
+        roofline_scan=dict(bound='fp32', kernel='rb_tb_chunk2_kernel+rb_tb_combine_kernel',
+                           achieved=sflops / scan_s / 1e12, peak=fp32_peak, unit='TFLOP/s',
+                           frac=sflops / scan_s / 1e12 / fp32_peak,
+                           algorithmic_flops_per_launch=sflops,
+                           flops_per_segment_and_freq=SCAN_FLOPS,
+                           l2=dict(achieved=sbytes / scan_s / 1e9, peak=l2, unit='GB/s',
+                                   frac=sbytes / scan_s / 1e9 / l2,
+                                   algorithmic_bytes_per_launch=sbytes,
+                                   peak_source='in-run copy of an L2-resident 2 x 16 MiB buffer pair'),
+                           traffic_ncu_capture=profile_traffic('tb_scan_c1.md'),
+                           peak_source='in-run FFMA probe'),
         phase_ms=ph, clocks=clocks, gradients=grads, batched=batched, image=image)
+    if acc_pool is not None:
+        from oracle import accuracy as ACC
+        acc = ACC.spectra(acc_pool, wl.freqs, wl.gas, a['C'], a['R'], a['N'], a['b'], a['w'], wl.lines,
+                          71492.0, 66854.0, tb_gpu, avg_gpu, layers_gpu)
+        line['accuracy'] = acc
+    if pool is not None and not args.no_cpu_baseline:
+        line['cpu_baseline'] = cpu_baseline(wl, pool, cores)
     if pool is not None:
-        try:
-            line['cpu_baseline'] = cpu_baseline(wl, args.cpu_sample_s, pool, cores)
-        finally:
-            pool.close()
-            pool.join()
+        pool.close()
+        pool.join()
     print(json.dumps(line), flush=True)
 
 

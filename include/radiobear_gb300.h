@@ -5,7 +5,11 @@
  * exceptions across the boundary.  The caller owns every buffer it passes;
  * the library owns the device memory behind a handle.  One handle per host
  * thread; calls on a handle are synchronous unless the name ends in
- * _device (those enqueue on the given CUDA stream and return).
+ * _device (those enqueue on the given CUDA stream and return).  Every call
+ * on a handle is ordered after the work the handle's last _device call
+ * enqueued (an event on that call's stream), so host calls and _device
+ * calls on other streams may follow it at once; work captured into a CUDA
+ * graph by the caller is not tracked: order its replays yourself.
  *
  * Units follow the reference: frequencies GHz, pressure bar, temperature K,
  * radii and path lengths km, absorption cm^-1 (dB/km when units_db = 1).

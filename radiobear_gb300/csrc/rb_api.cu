@@ -178,6 +178,11 @@ struct rb_handle {
   int device = 0;
   cudaStream_t st = nullptr, side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // The last _device call's work on its stream (recorded when that stream
+  // was not capturing): later calls on other streams, and the handle's own
+  // stream, wait for it before touching the handle's workspaces.
+  cudaEvent_t ev_dev = nullptr;
+  bool dev_pending = false;
   FamilyStore fam[rb::NFAM];
   rb::AlphaConfig cfg{rb::NH3_HS_SJS, 1, 1, 1, 1, 'e', 0, 0, 0, rb::CO_VOIGT, 0, 0};
   // co_ddb lines (co.npz: f0 GHz, I0, E cm^-1), float64
@@ -219,6 +224,31 @@ namespace rb {
 // Lets other translation units of the library report through rb_last_error.
 void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace rb
+
+namespace {
+bool capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+// A call about to use the handle's workspaces on `st` waits for the work the
+// last _device call enqueued on its own stream (a _device call returns
+// before its kernels run; a host call or a _device call on another stream
+// would otherwise overwrite buffers those kernels still read or
+// accumulate into).  Skipped while `st` is being captured: a captured
+// graph may not wait on work outside it.
+cudaError_t order_after_device(rb_handle* h, cudaStream_t st) {
+  if (!h->dev_pending || capturing(st)) return cudaSuccess;
+  return cudaStreamWaitEvent(st, h->ev_dev, 0);
+}
+
+// After a _device call enqueued its work on `st`.
+cudaError_t mark_device(rb_handle* h, cudaStream_t st) {
+  if (capturing(st)) return cudaSuccess;
+  h->dev_pending = true;
+  return cudaEventRecord(h->ev_dev, st);
+}
+}  // namespace
 
 // launchers implemented in the kernel translation units
 namespace rb {
@@ -732,6 +762,7 @@ int rb_create(rb_handle** out, int device) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_dev, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     rb_destroy(h);
     return fail(RB_ECUDA, "stream/event creation: %s", cudaGetErrorString(e));
@@ -770,6 +801,7 @@ int rb_destroy(rb_handle* h) {
   h->g_adj.release();
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->ev_dev) cudaEventDestroy(h->ev_dev);
   if (h->st) cudaStreamDestroy(h->st);
   if (h->side) cudaStreamDestroy(h->side);
   delete h;
@@ -784,6 +816,7 @@ static int set_co_lines(rb_handle* h, int n, int ncols, const double* cols) {
   for (int i = 0; i < n; ++i)
     if (!(cols[i] > 0.0)) return fail(RB_EINVAL, "line %d: centre must be > 0", i);
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   h->nco = 0;
   cudaStream_t st = h->st;
   RB_CUDA(upload(h->d_co_f0, cols, n, st));
@@ -803,6 +836,7 @@ int rb_set_lines(rb_handle* h, int family, int n, int ncols, const double* cols)
     return fail(RB_EINVAL, "family %d takes %d columns, got %d", family, family_ncols(family), ncols);
   if (n < 0 || (n > 0 && !cols)) return fail(RB_EINVAL, "bad line count / pointer");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   FamilyStore& F = h->fam[family];
   h->plan_f.clear();
   if (!finite_all(cols, (size_t)n * ncols)) return fail(RB_EINVAL, "line columns not finite");
@@ -965,6 +999,7 @@ int rb_alpha(rb_handle* h, int nL, const double* P, const double* T, const doubl
   if (rc) return rc;
   if (scale && !finite_all(scale, (size_t)nL * rb::NGAS)) return fail(RB_EINVAL, "scale not finite");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
   RB_CUDA(upload(h->d_P, P, nL, st));
@@ -1008,6 +1043,7 @@ int rb_raypath(rb_handle* h, int nL, const double* R, const double* N, double Re
   if (max_seg < 1) return fail(RB_EINVAL, "max_seg must be >= 1");
   if (nb == 0) return RB_OK;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   RB_CUDA(upload(h->d_R, R, nL, st));
   RB_CUDA(upload(h->d_N, N, nL, st));
@@ -1056,6 +1092,7 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
     }
   }
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   // absorption as float32 [nL][nf], T as float, ds/2 in cm as float
   std::vector<float> a32((size_t)nL * nf), t32(nL), hd((size_t)nb * max_seg, 0.f);
@@ -1133,6 +1170,7 @@ int rb_bright_run(rb_handle* h, int nL, const double* T, const double* R, const 
   if (!finite_all(layers, (size_t)nf * nL)) return fail(RB_EINVAL, "layers not finite");
   if (nb == 0) return RB_OK;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   const int max_seg = 2 * nL + 4;
   const size_t ns = (size_t)nb * max_seg;
@@ -1312,6 +1350,7 @@ int rb_forward(rb_handle* h, int nL, const double* P, const double* T, const dou
   if (!rc && scale && !finite_all(scale, (size_t)nL * rb::NGAS)) rc = fail(RB_EINVAL, "scale not finite");
   if (rc) return rc;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
   // one staged input block (each array at a 256-byte boundary) and one output block
@@ -1387,11 +1426,16 @@ int rb_forward_device(rb_handle* h, void* stream, int nL, const double* P, const
   if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
   if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RB_CUDA(order_after_device(h, st));
   int rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
-  return forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
-                      nb, b, weights, disc, Tb_out, Tb_avg, nullptr);
+  if ((rc = forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
+                         nb, b, weights, disc, Tb_out, Tb_avg, nullptr)))
+    return rc;
+  RB_CUDA(mark_device(h, st));
+  return RB_OK;
 }
 
 // Forward (recomputed) then the adjoint sweep: d loss / d alpha from the
@@ -1498,11 +1542,16 @@ int rb_adjoint_device(rb_handle* h, void* stream, int nL, const double* P, const
   if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
   if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RB_CUDA(order_after_device(h, st));
   int rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
-  return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), nL, P, T, X, R, N, scale, Req,
-                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, disc, grad, Tb_out,
-                      Tb_avg, dT, dP, dlnX);
+  if ((rc = adjoint_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
+                         nb, b, weights, disc, grad, Tb_out, Tb_avg, dT, dP, dlnX)))
+    return rc;
+  RB_CUDA(mark_device(h, st));
+  return RB_OK;
 }
 
 // Batch descriptor from the host layer counts (offsets uploaded once per
@@ -1541,14 +1590,19 @@ int rb_forward_batch_device(rb_handle* h, void* stream, int nvar, const int32_t*
   if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
   if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   int rc, NLT = 0;
   Batch bt;
   if ((rc = make_batch(h, nvar, nL_host, bt, NLT))) return rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
   RB_CUDA(h->d_Tb.ensure(sizeof(double) * (size_t)nvar * nb * nf));
-  return forward_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, scale, Req,
-                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, 0,
-                      h->d_Tb.as<double>(), Tb_avg, nullptr, &bt);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RB_CUDA(order_after_device(h, st));
+  if ((rc = forward_core(h, st, NLT, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
+                         nb, b, weights, 0, h->d_Tb.as<double>(), Tb_avg, nullptr, &bt)))
+    return rc;
+  RB_CUDA(mark_device(h, st));
+  return RB_OK;
 }
 
 int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_host,
@@ -1565,13 +1619,18 @@ int rb_adjoint_batch_device(rb_handle* h, void* stream, int nvar, const int32_t*
   if (gtype != RB_GTYPE_ELLIPSE && gtype != RB_GTYPE_SPHERE) return fail(RB_EINVAL, "bad gtype");
   if (limb != RB_LIMB_SHAPE && limb != RB_LIMB_SEC) return fail(RB_EINVAL, "bad limb");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   int rc, NLT = 0;
   Batch bt;
   if ((rc = make_batch(h, nvar, nL_host, bt, NLT))) return rc;
   if ((rc = plan_frequencies(h, nf, freqs_host, h->st))) return rc;
-  return adjoint_core(h, reinterpret_cast<cudaStream_t>(stream), NLT, P, T, X, R, N, scale, Req,
-                      Rpol, orient0, orient1, gtype, limb, nb, b, weights, 0, grad, nullptr, Tb_avg,
-                      dT, dP, dlnX, &bt);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RB_CUDA(order_after_device(h, st));
+  if ((rc = adjoint_core(h, st, NLT, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype,
+                         limb, nb, b, weights, 0, grad, nullptr, Tb_avg, dT, dP, dlnX, &bt)))
+    return rc;
+  RB_CUDA(mark_device(h, st));
+  return RB_OK;
 }
 
 int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const double* X,
@@ -1598,6 +1657,7 @@ int rb_adjoint(rb_handle* h, int nL, const double* P, const double* T, const dou
   if (!rc && scale && !finite_all(scale, (size_t)nL * rb::NGAS)) rc = fail(RB_EINVAL, "scale not finite");
   if (rc) return rc;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   if ((rc = plan_frequencies(h, nf, freqs, st))) return rc;
   // one staged input block (each array at a 256-byte boundary) and one output block
@@ -1717,6 +1777,7 @@ int rb_atm_props_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_
   int rc;
   if ((rc = atm_cols(ncol, roles, chem, a.cols))) return rc;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   int tot = 0;
   if ((rc = atm_offsets(h, nvar, nL_host, 1, tot))) return rc;
   a.gas = gas;
@@ -1726,8 +1787,11 @@ int rb_atm_props_device(rb_handle* h, void* stream, int nvar, const int32_t* nL_
   a.p_ref = p_ref;
   a.GM_ref = GM_ref;
   a.prop = prop;
-  RB_CUDA(rb::launch_atm_props(a, nvar, reinterpret_cast<cudaStream_t>(stream)));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RB_CUDA(order_after_device(h, st));
+  RB_CUDA(rb::launch_atm_props(a, nvar, st));
   h->launches = 1;
+  RB_CUDA(mark_device(h, st));
   return RB_OK;
 }
 
@@ -1741,6 +1805,7 @@ int rb_atm_props(rb_handle* h, int nL, int ncol, const int32_t* roles, const dou
   if ((rc = atm_cols(ncol, roles, chem, c))) return rc;
   if ((rc = atm_check_table(nL, ncol, c.ip, c.it, gas, true))) return rc;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   RB_CUDA(upload(h->d_agas, gas, (size_t)ncol * nL, st));
   RB_CUDA(h->d_aprop.ensure(sizeof(double) * rb::NPROP * (size_t)nL));
@@ -1769,6 +1834,7 @@ int rb_regrid_device(rb_handle* h, void* stream, int nvar, const int32_t* nin_ho
   if ((rc = atm_cols(ncol, roles, chem, a.cols))) return rc;
   if (cloud_in && (rc = atm_cols(ncl, roles_cl, nullptr, a.cloud_cols))) return rc;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   int tot = 0;
   if ((rc = atm_offsets(h, nvar, nin_host, 2, tot))) return rc;
   a.gas_in = gas_in;
@@ -1784,8 +1850,11 @@ int rb_regrid_device(rb_handle* h, void* stream, int nvar, const int32_t* nin_ho
   a.GM_ref = GM_ref;
   a.gas_out = gas_out;
   a.cloud_out = cloud_out;
-  RB_CUDA(rb::launch_atm_regrid(a, nvar, reinterpret_cast<cudaStream_t>(stream)));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RB_CUDA(order_after_device(h, st));
+  RB_CUDA(rb::launch_atm_regrid(a, nvar, st));
   h->launches = 1;
+  RB_CUDA(mark_device(h, st));
   return RB_OK;
 }
 
@@ -1809,6 +1878,7 @@ int rb_regrid(rb_handle* h, int nin, int ncol, const int32_t* roles, const doubl
     if (i && !(Pgrid[i] > Pgrid[i - 1])) return fail(RB_EINVAL, "Pgrid must increase");
   }
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   cudaStream_t st = h->st;
   RB_CUDA(upload(h->d_agas, gas_in, (size_t)ncol * nin, st));
   RB_CUDA(upload(h->d_agrid, Pgrid, (size_t)nout, st));
@@ -1835,6 +1905,7 @@ int rb_regrid(rb_handle* h, int nin, int ncol, const int32_t* roles, const doubl
 int rb_set_profiling(rb_handle* h, int on) {
   if (!h) return fail(RB_EINVAL, "null handle");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   if (on && !h->pev[0])
     for (auto& e : h->pev) RB_CUDA(cudaEventCreate(&e));
   h->profiling = on != 0;
@@ -1845,6 +1916,7 @@ int rb_phase_times(rb_handle* h, double* ms, int n) {
   if (!h || !ms) return fail(RB_EINVAL, "null argument");
   if (!h->profiling) return fail(RB_ESTATE, "profiling is off (rb_set_profiling)");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   RB_CUDA(cudaEventSynchronize(h->pev[7]));
   float t[6] = {0, 0, 0, 0, 0, 0};
   RB_CUDA(cudaEventElapsedTime(&t[0], h->pev[0], h->pev[1]));
@@ -1860,6 +1932,7 @@ int rb_phase_times(rb_handle* h, double* ms, int n) {
 int rb_probe_fp32_peak(rb_handle* h, double* tflops) {
   if (!h || !tflops) return fail(RB_EINVAL, "null argument");
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   int sms = 0;
   RB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
   RB_CUDA(h->d_probe.ensure(256 * sizeof(float)));
@@ -1893,6 +1966,7 @@ static int debug_expint(rb_handle* h, int order, int n, const double* x, double*
   if (n < 0 || (n > 0 && (!x || !out))) return fail(RB_EINVAL, "bad arguments");
   if (n == 0) return RB_OK;
   RB_CUDA(cudaSetDevice(h->device));
+  RB_CUDA(order_after_device(h, h->st));
   RB_CUDA(upload(h->d_x, x, n, h->st));
   RB_CUDA(h->d_iw.ensure(sizeof(double) * n));
   RB_CUDA(rb::launch_e2(order, n, h->d_x.as<double>(), h->d_iw.as<double>(), h->st));

@@ -218,3 +218,58 @@ def make_planet(config_file, **kw):
     import radiobear.planet as rbp
     return rbp.Planet('jupiter', config_file=config_file, plot_atm=False, plot_bright=False,
                       verbose=False, **kw)
+
+
+# ------------------------------------------------------------ stock timing
+# Workers of a spawn pool that time the unmodified reference's own hot-path
+# calls on the synthetic C1 workload (1000 layers, 256 freqs, 64 disc rays):
+# Alpha.get_alpha_from_calc per layer (the call Alpha.get_layers loops
+# over, alpha.py:261-305) and Brightness.single per ray (the call of
+# Planet.run's b loop, planet_base.py:268).  Each worker builds its own
+# Planet in a scratch folder once (untimed).
+_STOCK = {}
+
+
+def stock_init(ref, root):
+    import tempfile
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    os.environ['OMP_NUM_THREADS'] = '1'
+    set_reference(ref)
+    import_reference()
+    from radiobear_gb300 import synth
+    from tests import goldio
+    cats = goldio.real_catalogues()
+    wl = synth.make_workload(1, real=cats)
+    lines = dict(wl.lines)
+    lines['ph3wgt'] = cats['ph3wgt']
+    work = tempfile.mkdtemp(prefix='rbstock_')
+    os.chdir(work)
+    scratch_planet_dir(work, wl.gas, synth.GAS_COLUMNS)
+    reset_lines()
+    j = make_planet('config_synth.par')
+    inject_lines(lines)
+    patch_limb_sqrt(True)
+    atm = j.atmos[0]
+    j.alpha[0].layers = np.full((len(wl.freqs), atm.gas.shape[1]), 1.0e-6)
+    _STOCK.update(j=j, atm=atm, freqs=wl.freqs.tolist(), b=wl.b)
+
+
+def stock_alpha_job(layers):
+    import time
+    j, atm, freqs = _STOCK['j'], _STOCK['atm'], _STOCK['freqs']
+    C = atm.config.C
+    t0 = time.perf_counter()
+    for layer in layers:
+        j.alpha[0].get_alpha_from_calc(freqs, atm.gas[C['T']][layer], atm.gas[C['P']][layer],
+                                       atm.gas[:, layer], C, atm.cloud[:, layer], atm.config.Cl,
+                                       units='invcm')
+    return time.perf_counter() - t0
+
+
+def stock_ray_job(k):
+    import time
+    j, atm = _STOCK['j'], _STOCK['atm']
+    t0 = time.perf_counter()
+    j.bright.single(_STOCK['b'][k].tolist(), _STOCK['freqs'], atm, j.alpha[0], j.config.orientation)
+    return time.perf_counter() - t0

@@ -7,7 +7,10 @@
 * rb_forward / rb_adjoint with host buffers, which replay a captured CUDA
   graph from the second call of a shape on: repeated calls with new inputs
   and a configuration change in between must equal the device-pointer
-  entry points (same kernels, no graph) exactly.
+  entry points (same kernels, no graph) exactly;
+* a _device call returns before its kernels run: a host call, or a _device
+  call on another stream, made right after it on the same handle waits for
+  that work instead of overwriting the workspaces it still uses.
 """
 import numpy as np
 import pytest
@@ -160,3 +163,42 @@ def test_adjoint_graph_replay_matches_device_path(engine):
         for a, d in ((out['dT'], dT), (out['dP'], dP), (out['dlnX'], dX)):
             d = d.cpu().numpy()
             assert np.max(np.abs(a - d)) <= 1e-6 * np.max(np.abs(d)), step
+
+
+def test_calls_after_an_unfinished_device_call_are_ordered(engine):
+    """C3-sized adjoint (1000 layers, 64 freqs, 16 rays) enqueued on a side
+    stream, then at once the same adjoint from host buffers and a second
+    _device call on another stream, with no synchronisation in between:
+    both equal a clean host call (float atomics: ~1e-6 relative)."""
+    import torch
+    from radiobear_gb300 import catalog, synth
+    cats = G.real_catalogues()
+    wl = synth.make_workload(3, real=cats)
+    wl['lines']['ph3wgt'] = cats['ph3wgt']
+    catalog.upload(engine, wl.lines)
+    engine.set_formalisms('nh3_hs_sjs', True, True, True, True, 'e')
+    LP = {k: i for i, k in enumerate(synth.PROPERTY_COLUMNS)}
+    g = wl.gas
+    P, T, X = g[G.C['P']], g[G.C['T']], _X(g)
+    R, N = wl.prop[LP['R']], wl.prop[LP['N']]
+    nL, nb, nf = P.size, len(wl.b), wl.freqs.size
+    grad = np.random.default_rng(6).normal(size=nf)
+    ref = engine.adjoint(P, T, X, R, N, wl.freqs, wl.b, G.REQ, G.RPOL, grad, weights=wl.weights)
+    dev = torch.device('cuda')
+    dt = lambda v: torch.as_tensor(np.ascontiguousarray(v), dtype=torch.float64, device=dev)
+    tP, tT, tX, tR, tN, tb, tw, tg = (dt(v) for v in (P, T, X, R, N, wl.b, wl.weights, grad))
+    outs = []
+    streams = (torch.cuda.Stream(), torch.cuda.Stream())
+    for s in streams:
+        dT, dP = torch.empty(nL, dtype=torch.float64, device=dev), torch.empty(nL, dtype=torch.float64, device=dev)
+        dX = torch.empty((3, nL), dtype=torch.float64, device=dev)
+        engine.adjoint_device(s.cuda_stream, nL, nb, tP.data_ptr(), tT.data_ptr(), tX.data_ptr(),
+                              tR.data_ptr(), tN.data_ptr(), wl.freqs, tb.data_ptr(), G.REQ, G.RPOL,
+                              tg.data_ptr(), dT.data_ptr(), dP.data_ptr(), dX.data_ptr(),
+                              weights=tw.data_ptr())
+        outs.append((dT, dP, dX))
+    host = engine.adjoint(P, T, X, R, N, wl.freqs, wl.b, G.REQ, G.RPOL, grad, weights=wl.weights)
+    torch.cuda.synchronize()
+    for got in [(host['dT'], host['dP'], host['dlnX'])] + [tuple(v.cpu().numpy() for v in o) for o in outs]:
+        for a, want in zip(got, (ref['dT'], ref['dP'], ref['dlnX'])):
+            assert np.max(np.abs(a - want)) <= 1e-6 * np.max(np.abs(want))

@@ -1,0 +1,44 @@
+"""CPU: the autotuner's JSON cache (keyed by device, step kind,
+frequencies, layer range, line counts and rays) is written and read back,
+and a cached key sets its tiling without timing anything."""
+import json
+
+import numpy as np
+import pytest
+
+pytest.importorskip('torch')
+
+from radiobear_gb300 import tune   # noqa: E402
+
+
+class FakeEngine:
+    def __init__(self):
+        self.tiling = None
+
+    def set_alpha_tiling(self, M=0, W=0, item_lines=0):
+        self.tiling = (M, W, item_lines)
+
+
+def test_workload_key_and_json_cache(tmp_path, monkeypatch):
+    monkeypatch.setenv('RB_TUNING_CACHE', str(tmp_path / 'tuning.json'))
+    monkeypatch.setattr(tune, '_CACHE', {})
+    wl = dict(freqs=np.ones(8), gas=np.zeros((16, 1000)),
+              lines=dict(ammonia=dict(fo=np.ones(1500)), h2o=dict(f_o=np.ones(500))))
+    key = tune.workload_key('image', wl, 65536)
+    assert key == dict(kind='image', nf=8, layers=[1000, 1000], lines=dict(ammonia=1500, h2o=500),
+                       rays=65536)
+    k = tune._key_str(key)
+    tune._store(k, (2, 1, 1024), {(2, 1, 1024): 1.0, (4, 1, 1024): 1.5})
+    on_disk = json.loads((tmp_path / 'tuning.json').read_text())
+    assert on_disk[k]['best'] == [2, 1, 1024]
+
+    def never():
+        raise AssertionError('a cached key must not time the step')
+
+    eng = FakeEngine()
+    best, times = tune.tune_alpha(eng, never, key=key)
+    assert best == (2, 1, 1024) and eng.tiling == (2, 1, 1024)
+    assert times[(4, 1, 1024)] == 1.5
+    other = tune.workload_key('batch', dict(freqs=np.ones(128), lines=wl['lines']), 32,
+                              layers=(300, 1200))
+    assert tune._key_str(other) not in on_disk
