@@ -791,8 +791,16 @@ __device__ __forceinline__ void store_rec(float* dst, const float* r) {
 // lines grp, grp + NG, ...; value terms are added in blocks of 16 into a
 // compensated sum.  The groups' sums (value and three derivatives) go to
 // sh.fam[fam][fi], added in group order.  Called by every thread.
+// Not inlined: each line kind's sweep gets the kernel's whole register budget
+// for its own loop state (inlined into the family switch, the union of the
+// four kinds' live values spilled to local memory at 64 registers).
+#ifndef RB_JVP_INLINE
+#define RB_JVP_FAMILY __noinline__
+#else
+#define RB_JVP_FAMILY __forceinline__
+#endif
 template <int KIND>
-__device__ __forceinline__ void jv_family(const JvpArgs& a, JvpShared& sh, int L, int fam,
+__device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, int fam,
                                           const JvFreq& fr, bool on, float& base, float* dbase) {
   const int tid = threadIdx.x;
   const int FTL = a.ft, NG = blockDim.x / a.ft;
@@ -1146,8 +1154,14 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   }
   rb_layer_tan_kernel<<<(((tn.nL + 31) & ~31) * 8 + 63) / 64, 64, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
-  if (jv.ft >= 128) rb_alpha_jvp_kernel<4><<<grid, 256, 0, st>>>(jv);
-  else rb_alpha_jvp_kernel<3><<<grid, 256, 0, st>>>(jv);
+#ifndef RB_JVP_MINB128
+#define RB_JVP_MINB128 4
+#endif
+#ifndef RB_JVP_MINB
+#define RB_JVP_MINB 3
+#endif
+  if (jv.ft >= 128) rb_alpha_jvp_kernel<RB_JVP_MINB128><<<grid, 256, 0, st>>>(jv);
+  else rb_alpha_jvp_kernel<RB_JVP_MINB><<<grid, 256, 0, st>>>(jv);
   if (ea) {
     cudaError_t x = launch_extra_vjp(*ea, st);
     if (x != cudaSuccess) return x;
