@@ -35,6 +35,7 @@
 //                           dTb/dT, dTb/dP, dTb/dln X.
 #include "rb_args.cuh"
 #include "rb_expint.cuh"
+#include "rb_f32x2.cuh"
 #include <math_constants.h>
 
 namespace rb {
@@ -611,9 +612,14 @@ constexpr int JV_NREC = 16;
 
 constexpr int JV_FTMAX = 128;   // frequencies per CTA at most
 
+// Line pairs: field f of lines (2p, 2p+1) is one f32x2 (first line in the
+// low half); two fields per 16-byte word, JV_NU2 words per pair.
+constexpr int JV_PAIRS = JV_CHUNK / 2;
+constexpr int JV_NU2 = 9;
+
 struct JvpShared {
-  float rec[2][2][JV_CHUNK][JV_NREC];   // [buffer][coefficient set][line][field], 64 B per line
-  float fam[NFAM][JV_FTMAX][4];         // per family and frequency: value, three derivatives
+  ulonglong2 rec[2][2][JV_PAIRS][JV_NU2];   // [buffer][coefficient set][pair][word], 144 B per pair
+  float fam[NFAM][JV_FTMAX][4];             // per family and frequency: value, three derivatives
   double red[8][NTH + 1];
 };
 
@@ -755,42 +761,125 @@ __device__ __forceinline__ void jv_sjs_record(const LineTable& t, const LayerFam
   for (int q = 0; q < 3; ++q) r[(9 + q) * stride] = 2.f * (fo + shift) * tan3(LT.dsjs[0][4], q, TH_XNH3);
 }
 
-// Ben-Reuven term t = S n / den; its three derivatives are added to d.
-__device__ __forceinline__ float br_eval(float F, float FL, float g, float z, float KH, float KL,
-                                         float S, float dlnS, const float* dg, const float* dz,
-                                         const float* dK, float* d) {
-  const float e = (F - KH) + (FL - KL);
-  const float K = KH + KL;
-  const float den = fmaf(e, e, 4.f * F * g * g);
-  const float r = rcp_approx(den);
-  const float gp = g + z, gm = g - z;
-  const float n = fmaf(gm, F, gp * K);
-  const float t = S * n * r;
-  // dt = S r [dn - n r dden] + t dlnS with dn = (F + K) dg + (K - F) dz + gp dK,
-  // dden = 8 F g dg - 2 e dK, collected per tangent of g, z, K
-  const float nr = n * r, Sr = S * r;
-  const float Ag = Sr * ((F + K) - 8.f * F * g * nr);
-  const float Az = Sr * (K - F);
-  const float AK = Sr * fmaf(2.f * e, nr, gp);
+// Fields of one line in the pair records, by line kind (f32x2 packing of
+// two lines; the sweep reads words 0..nw-1 of a pair):
+//   Ben-Reuven  0 g  1 g+z  2 g-z  3 K  4 -K_hi  5 -K_lo  6 S  7 dlnS/dT  8 4g^2
+//               9..11 dg  12..14 dz  15..17 dK                       (9 words)
+//   Gross       0 g  1 4g^2  2 S  3 dlnS/dT  4 -K_hi  5 -K_lo  6..8 dg  (5 words)
+//   VVW         0 df  1 df^2  2 -fo_hi  3 -fo_lo  4 S  5 dlnS/dT  6..8 d(df)  (5 words)
+//   nh3_sjs     0 K0_hi  1 K0_lo  2 S  3 dlnS/dT  4 G0  5..7 dK0      (4 words)
+// (K = (fo + delta)^2 + g^2 - z^2, exact as a double-float; nh3_sjs: K0 =
+// (fo + shift)^2, g, z and K per frequency in the sweep.)  A padding line
+// (odd line count) has S = 0 and zero derivatives, so it adds exactly 0.
+constexpr int JV_NF = 18;
+
+// Padding line: zero strength and derivatives, a finite positive denominator.
+template <int KIND>
+__device__ __forceinline__ void jv_pad_fields(float* v) {
+  for (int k = 0; k < JV_NF; ++k) v[k] = 0.f;
+  if (KIND == JK_BR) {          // g = g+z = g-z = K = 1, 4g^2 = 4
+    v[0] = 1.f; v[1] = 1.f; v[2] = 1.f; v[3] = 1.f; v[4] = -1.f; v[8] = 4.f;
+  } else if (KIND == JK_GROSS) {   // g = 1, 4g^2 = 4, K = 1
+    v[0] = 1.f; v[1] = 4.f; v[4] = -1.f;
+  } else if (KIND == JK_VVW) {  // df = df^2 = 1
+    v[0] = 1.f; v[1] = 1.f;
+  } else {                      // K0 = 1e18: the denominator ~1e36
+    v[0] = 1e18f;
+  }
+}
+
+__device__ __forceinline__ void jv_br_fields(const LineTable& t, const LayerFam& LF, const FamTan& FT,
+                                             int set, int li, int xt, float* v) {
+  float r[JV_NREC];
+  jv_br_record(t, LF, FT, set, li, xt, r, 1);   // 0 g, 1 z, 2 KH, 3 KL, 4 S, 5 dlnS, 6.. dg dz dK
+  const float g = r[0], z = r[1];
+  v[0] = g;
+  v[1] = g + z;
+  v[2] = g - z;
+  v[3] = r[2] + r[3];
+  v[4] = -r[2];
+  v[5] = -r[3];
+  v[6] = r[4];
+  v[7] = r[5];
+  v[8] = 4.f * g * g;
+  for (int k = 0; k < 9; ++k) v[9 + k] = r[6 + k];
+}
+
+__device__ __forceinline__ void jv_gross_fields(const LineTable& t, const LayerFam& LF, const FamTan& FT,
+                                                int li, int xt, float* v) {
+  float r[JV_NREC];
+  jv_gross_record(t, LF, FT, li, xt, r, 1);     // 0 g, 2 KH, 3 KL, 4 S, 5 dlnS, 6..8 dg
+  v[0] = r[0];
+  v[1] = 4.f * r[0] * r[0];
+  v[2] = r[4];
+  v[3] = r[5];
+  v[4] = -r[2];
+  v[5] = -r[3];
+  v[6] = r[6];
+  v[7] = r[7];
+  v[8] = r[8];
+}
+
+__device__ __forceinline__ void jv_vvw_fields(const LineTable& t, const LayerFam& LF, const FamTan& FT,
+                                              int li, int xt, float* v, float* base, float* dbase) {
+  float r[JV_NREC];
+  jv_vvw_record(t, LF, FT, li, xt, r, 1, base, dbase);   // 0 df, 2 fo_hi, 3 fo_lo, 4 S, 5 dlnS, 6..8 ddf
+  v[0] = r[0];
+  v[1] = r[0] * r[0];
+  v[2] = -r[2];
+  v[3] = -r[3];
+  v[4] = r[4];
+  v[5] = r[5];
+  v[6] = r[6];
+  v[7] = r[7];
+  v[8] = r[8];
+}
+
+__device__ __forceinline__ void jv_sjs_fields(const LineTable& t, const LayerFam& LF, const FamTan& FT,
+                                              const LayerTan& LT, float shift, int li, float* v) {
+  float r[JV_NREC];
+  jv_sjs_record(t, LF, FT, LT, shift, li, r, 1);   // 2 KH0, 3 KL0, 4 S, 5 dlnS, 6 G0, 9..11 dK0
+  v[0] = r[2];
+  v[1] = r[3];
+  v[2] = r[4];
+  v[3] = r[5];
+  v[4] = r[6];
+  v[5] = r[9];
+  v[6] = r[10];
+  v[7] = r[11];
+}
+
+// Packed two-sum of f32x2 lanes: s + e = a + b exactly, lane by lane.
+__device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
+  s = add2(a, b);
+  const f2 bb = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+__device__ __forceinline__ f2 rcp2(f2 x) { return pk(rcp_approx(lo2(x)), rcp_approx(hi2(x))); }
+
+// Ben-Reuven pair: t = S n / den, n = (g - z) F + (g + z) K,
+// den = e^2 + 4 g^2 F with e = F - K (double-float); dt along each tangent
+// = Ag dg + Az dz + AK dK (+ t dlnS for T), accumulated into d.
+__device__ __forceinline__ f2 br_eval2(f2 F, f2 FL, f2 m8F, f2 g, f2 gp, f2 gm, f2 K, f2 mKH,
+                                       f2 mKL, f2 S, f2 dlnS, f2 G4, const f2* dg, const f2* dz,
+                                       const f2* dK, f2* d) {
+  const f2 e = add2(add2(F, mKH), add2(FL, mKL));
+  const f2 den = fma2(e, e, mul2(G4, F));
+  const f2 r = rcp2(den);
+  const f2 n = fma2(gm, F, mul2(gp, K));
+  const f2 nr = mul2(n, r);
+  const f2 t = mul2(S, nr);
+  const f2 Sr = mul2(S, r);
+  const f2 Ag = mul2(Sr, fma2(mul2(m8F, g), nr, add2(F, K)));
+  const f2 Az = mul2(Sr, sub2(K, F));
+  const f2 AK = mul2(Sr, fma2(add2(e, e), nr, gp));
 #pragma unroll
-  for (int q = 0; q < 3; ++q) d[q] += fmaf(Ag, dg[q], fmaf(Az, dz[q], AK * dK[q]));
-  d[0] += t * dlnS;
+  for (int q = 0; q < 3; ++q) d[q] = fma2(Ag, dg[q], fma2(Az, dz[q], fma2(AK, dK[q], d[q])));
+  d[0] = fma2(t, dlnS, d[0]);
   return t;
 }
 
-// A record of JV_NREC fields as four 16-byte stores.
-__device__ __forceinline__ void store_rec(float* dst, const float* r) {
-  float4* d4 = reinterpret_cast<float4*>(dst);
-#pragma unroll
-  for (int k = 0; k < JV_NREC / 4; ++k) d4[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
-}
-
-// One family of one layer for the CTA's frequencies.  Records of JV_CHUNK
-// lines at a time, double-buffered (chunk c+1 is built, one line per
-// thread, while chunk c is swept); the NG line groups of a frequency sweep
-// lines grp, grp + NG, ...; value terms are added in blocks of 16 into a
-// compensated sum.  The groups' sums (value and three derivatives) go to
-// sh.fam[fam][fi], added in group order.  Called by every thread.
 // Not inlined: each line kind's sweep gets the kernel's whole register budget
 // for its own loop state (inlined into the family switch, the union of the
 // four kinds' live values spilled to local memory at 64 registers).
@@ -799,9 +888,18 @@ __device__ __forceinline__ void store_rec(float* dst, const float* r) {
 #else
 #define RB_JVP_FAMILY __forceinline__
 #endif
+
+// One family of one layer for the CTA's frequencies.  Records of JV_CHUNK
+// lines at a time, double-buffered (chunk c+1 is built, one line per
+// thread, while chunk c is swept), stored as line pairs so every f32x2
+// instruction of the sweep serves two lines; the NG line groups of a
+// frequency sweep pairs grp, grp + NG, ...; value terms are added in blocks
+// of 16 lines into a compensated sum.  The groups' sums (value and three
+// derivatives) go to sh.fam[fam][fi], added in group order.  Called by
+// every thread.
 template <int KIND>
 __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, int fam,
-                                          const JvFreq& fr, bool on, float& base, float* dbase) {
+                                        const JvFreq& fr, bool on, float& base, float* dbase) {
   const int tid = threadIdx.x;
   const int FTL = a.ft, NG = blockDim.x / a.ft;
   const int fi = tid % FTL, grp = tid / FTL;
@@ -814,29 +912,38 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
   const bool two = fam == FAM_NH3_INV;
   const bool hsf = fam == FAM_NH3_INV || fam == FAM_NH3_ROT || fam == FAM_NH3_V2;
   const float Fx = hsf ? fr.Fh : fr.F, FLx = hsf ? fr.FhL : fr.FL;
+  auto put = [&](int bi, int set, int i, const float* v, int nf) {
+    float* o = reinterpret_cast<float*>(sh.rec[bi][set][i >> 1]) + (i & 1);
+    for (int k = 0; k < nf; ++k) o[2 * k] = v[k];
+  };
   auto build = [&](int bi, int c0) {
     const int nc = min(JV_CHUNK, t.n - c0);
-    for (int i = tid; i < nc; i += blockDim.x) {
+    const int ncp = (nc + 1) & ~1;
+    for (int i = tid; i < ncp; i += blockDim.x) {
       const int li = c0 + i;
-      float r[JV_NREC];
-#pragma unroll
-      for (int k = 0; k < JV_NREC; ++k) r[k] = 0.f;
+      float v[JV_NF];
+      if (i >= nc) {
+        jv_pad_fields<KIND>(v);
+        put(bi, 0, i, v, JV_NF);
+        if (two) put(bi, 1, i, v, JV_NF);
+        continue;
+      }
       if (KIND == JK_BR) {
-        jv_br_record(t, LF, FT, 0, li, xt, r, 1);
-        store_rec(sh.rec[bi][0][i], r);
+        jv_br_fields(t, LF, FT, 0, li, xt, v);
+        put(bi, 0, i, v, JV_NF);
         if (two) {
-          jv_br_record(t, LF, FT, 1, li, xt, r, 1);
-          store_rec(sh.rec[bi][1][i], r);
+          jv_br_fields(t, LF, FT, 1, li, xt, v);
+          put(bi, 1, i, v, JV_NF);
         }
       } else if (KIND == JK_GROSS) {
-        jv_gross_record(t, LF, FT, li, xt, r, 1);
-        store_rec(sh.rec[bi][0][i], r);
+        jv_gross_fields(t, LF, FT, li, xt, v);
+        put(bi, 0, i, v, 10);
       } else if (KIND == JK_VVW) {
-        jv_vvw_record(t, LF, FT, li, xt, r, 1, &base, dbase);
-        store_rec(sh.rec[bi][0][i], r);
+        jv_vvw_fields(t, LF, FT, li, xt, v, &base, dbase);
+        put(bi, 0, i, v, 10);
       } else {
-        jv_sjs_record(t, LF, FT, LT, lp.sjs[0][4], li, r, 1);
-        store_rec(sh.rec[bi][0][i], r);
+        jv_sjs_fields(t, LF, FT, LT, lp.sjs[0][4], li, v);
+        put(bi, 0, i, v, 8);
       }
     }
   };
@@ -856,86 +963,92 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
       dD[q] = lerp(tan3(LT.dsjs[0][3], q, xt), tan3(LT.dsjs[1][3], q, xt));
     }
   }
+  const f2 F2 = dup(Fx), FL2 = dup(FLx), m8F = dup(-8.f * Fx);
   KSum val;
   val.init();
-  float vp = 0.f, der[3] = {0.f, 0.f, 0.f};
+  f2 vp = 0ull, der[3] = {0ull, 0ull, 0ull};
   int nv = 0;
   const int nchunks = (t.n + JV_CHUNK - 1) / JV_CHUNK;
   build(0, 0);
   __syncthreads();
   for (int ci = 0; ci < nchunks; ++ci) {
     const int c0 = ci * JV_CHUNK;
-    const int nc = min(JV_CHUNK, t.n - c0);
+    const int np = (min(JV_CHUNK, t.n - c0) + 1) >> 1;
     if (ci + 1 < nchunks) build((ci + 1) & 1, c0 + JV_CHUNK);
     if (on) {
-      const float(*Rl)[JV_NREC] = sh.rec[ci & 1][two ? fr.set : 0];
-      for (int i = grp; i < nc; i += NG) {
-        const float4* r4 = reinterpret_cast<const float4*>(Rl[i]);
-        // fields 0..15 = q0.xyzw q1.xyzw q2.xyzw q3.xyzw
-        const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2];
-        float tv;
+      const ulonglong2(*Rp)[JV_NU2] = sh.rec[ci & 1][two ? fr.set : 0];
+      for (int p = grp; p < np; p += NG) {
+        const ulonglong2* w = Rp[p];
+        f2 tv;
         if (KIND == JK_BR) {
-          const float4 q3 = r4[3];
-          const float dg[3] = {q1.z, q1.w, q2.x};
-          const float dz[3] = {q2.y, q2.z, q2.w};
-          const float dK[3] = {q3.x, q3.y, q3.z};
-          tv = br_eval(Fx, FLx, q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, dg, dz, dK, der);
+          const ulonglong2 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4], w5 = w[5],
+                           w6 = w[6], w7 = w[7], w8 = w[8];
+          const f2 dg[3] = {w4.y, w5.x, w5.y};
+          const f2 dz[3] = {w6.x, w6.y, w7.x};
+          const f2 dK[3] = {w7.y, w8.x, w8.y};
+          tv = br_eval2(F2, FL2, m8F, w0.x, w0.y, w1.x, w1.y, w2.x, w2.y, w3.x, w3.y, w4.x, dg, dz,
+                        dK, der);
         } else if (KIND == JK_GROSS) {
-          const float g = q0.x, S = q1.x;
-          const float e = (Fx - q0.z) + (FLx - q0.w);
-          const float den = fmaf(e, e, 4.f * Fx * g * g);
-          const float r = rcp_approx(den);
-          tv = S * g * r;
-          const float dgv[3] = {q1.z, q1.w, q2.x};
-          const float k8 = 8.f * Fx * g * g * r;
-#pragma unroll
-          for (int q = 0; q < 3; ++q) der[q] += (q == 0 ? tv * q1.y : 0.f) + S * dgv[q] * (1.f - k8) * r;
+          // t = S g / den, den = e^2 + 4 g^2 F; dt = (t dlnS) + S dg (1 - 8 F g^2 / den) / den
+          const ulonglong2 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4];
+          const f2 e = add2(add2(F2, w2.x), add2(FL2, w2.y));
+          const f2 r = rcp2(fma2(e, e, mul2(w0.y, F2)));
+          const f2 Sr = mul2(w1.x, r);
+          tv = mul2(Sr, w0.x);
+          const f2 k = mul2(Sr, fma2(mul2(m8F, mul2(w0.x, w0.x)), r, dup(1.f)));
+          der[0] = fma2(k, w3.x, fma2(tv, w1.y, der[0]));
+          der[1] = fma2(k, w3.y, der[1]);
+          der[2] = fma2(k, w4.x, der[2]);
         } else if (KIND == JK_VVW) {
-          const float df = q0.x, S = q1.x;
-          const float dm = (fr.fq - q0.z) + (fr.fql - q0.w);
-          const float dp = fr.fq + q0.z;
-          const float d1 = fmaf(dm, dm, df * df), d2 = fmaf(dp, dp, df * df);
-          const float r1 = rcp_approx(d1), r2 = rcp_approx(d2);
-          const float h = S * df, u = r1 + r2;
-          tv = h * u;
-          const float ddf[3] = {q1.z, q1.w, q2.x};
-          const float k2 = 2.f * h * df * (r1 * r1 + r2 * r2);
-#pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const float dh = (q == 0 ? h * q1.y : 0.f) + S * ddf[q];
-            der[q] += dh * u - k2 * ddf[q];
-          }
+          // t = h (r1 + r2), h = S df, r1 = 1/((f - fo)^2 + df^2), r2 = 1/((f + fo)^2 + df^2);
+          // dt = t dlnS (T) + (S u - 2 h df (r1^2 + r2^2)) d(df)
+          const ulonglong2 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4];
+          const f2 fq = dup(fr.fq), fql = dup(fr.fql);
+          const f2 dm = add2(add2(fq, w1.x), add2(fql, w1.y));
+          const f2 dp = sub2(fq, w1.x);
+          const f2 r1 = rcp2(fma2(dm, dm, w0.y)), r2 = rcp2(fma2(dp, dp, w0.y));
+          const f2 h = mul2(w2.x, w0.x), u = add2(r1, r2);
+          tv = mul2(h, u);
+          const f2 k2 = mul2(add2(h, h), mul2(w0.x, fma2(r1, r1, mul2(r2, r2))));
+          const f2 c = sub2(mul2(w2.x, u), k2);
+          der[0] = fma2(c, w3.x, fma2(tv, w2.y, der[0]));
+          der[1] = fma2(c, w3.y, der[1]);
+          der[2] = fma2(c, w4.x, der[2]);
         } else {
-          const float G0 = q1.z, S = q1.x;
-          const float g = fmaf(B, G0, A), z = fmaf(D, G0, C);
-          const float g2z2 = (g - z) * (g + z);
-          const float dK0[3] = {q2.y, q2.z, q2.w};
-          float dg[3], dz[3], dK[3];
+          const ulonglong2 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
+          const f2 G0 = w2.x;
+          const f2 g = fma2(dup(B), G0, dup(A)), z = fma2(dup(D), G0, dup(C));
+          const f2 gp = add2(g, z), gm = sub2(g, z);
+          f2 dg[3], dz[3], dK[3];
+          const f2 dK0[3] = {w2.y, w3.x, w3.y};
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
-            dg[q] = fmaf(dB[q], G0, dA[q]);
-            dz[q] = fmaf(dD[q], G0, dC[q]);
-            dK[q] = dK0[q] + 2.f * g * dg[q] - 2.f * z * dz[q];
+            dg[q] = fma2(dup(dB[q]), G0, dup(dA[q]));
+            dz[q] = fma2(dup(dD[q]), G0, dup(dC[q]));
+            dK[q] = fma2(add2(g, g), dg[q], fma2(mul2(dup(-2.f), z), dz[q], dK0[q]));
           }
-          float KH, e;
-          two_sum(q0.z, g2z2, KH, e);
-          tv = br_eval(Fx, FLx, g, z, KH, e + q0.w, S, q1.y, dg, dz, dK, der);
+          f2 KH, e;
+          two_sum2(w0.x, mul2(gm, gp), KH, e);
+          const f2 KL = add2(e, w0.y);
+          const f2 mone = dup(-1.f);
+          tv = br_eval2(F2, FL2, m8F, g, gp, gm, add2(KH, KL), mul2(KH, mone), mul2(KL, mone), w1.x,
+                        w1.y, mul2(dup(4.f), mul2(g, g)), dg, dz, dK, der);
         }
-        vp += tv;
-        if (++nv == 16) {
-          val.add(vp);
-          vp = 0.f;
+        vp = add2(vp, tv);
+        if (++nv == 8) {
+          val.add(lo2(vp) + hi2(vp));
+          vp = 0ull;
           nv = 0;
         }
       }
     }
     __syncthreads();
   }
-  val.add(vp);
+  val.add(lo2(vp) + hi2(vp));
   // the line groups' sums, staged in the (now free) record buffer
   float(*s_grp)[4] = reinterpret_cast<float(*)[4]>(&sh.rec[0][0][0][0]);
   s_grp[tid][0] = val.val();
-  for (int q = 0; q < 3; ++q) s_grp[tid][1 + q] = der[q];
+  for (int q = 0; q < 3; ++q) s_grp[tid][1 + q] = lo2(der[q]) + hi2(der[q]);
   __syncthreads();
   if (grp == 0) {
     float v4[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1155,7 +1268,7 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   rb_layer_tan_kernel<<<(((tn.nL + 31) & ~31) * 8 + 63) / 64, 64, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
 #ifndef RB_JVP_MINB128
-#define RB_JVP_MINB128 4
+#define RB_JVP_MINB128 3
 #endif
 #ifndef RB_JVP_MINB
 #define RB_JVP_MINB 3
