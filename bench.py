@@ -117,6 +117,9 @@ def measure_gradients(args, dev, stream, flush, pool=None):
                            g.data_ptr(), gT.data_ptr(), gP.data_ptr(), gX.data_ptr(),
                            weights=dw.data_ptr(), Tb_avg=avg.data_ptr())
 
+    from radiobear_gb300 import tune
+    jbest, jt = tune.tune_adjoint(eng, step, key=tune.workload_key('gradients', wl, nb), reps=5,
+                                  stream=stream)
     step()
     torch.cuda.synchronize()
     launches = eng.last_launch_count()
@@ -149,7 +152,9 @@ def measure_gradients(args, dev, stream, flush, pool=None):
     eng.close()
     out = dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second',
                value=1e3 / ms, unit='spectra+gradients/s', ms_per_step=ms, steps=n,
-               config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb),
+               config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb,
+                           jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1]),
+                           jvp_tuning_ms={'{},{}'.format(*k): v for k, v in jt.items()}),
                gpu_launches_per_step=int(launches),
                e2e=dict(value=1.0 / float(np.mean(e2e)), unit='spectra+gradients/s',
                         h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
@@ -170,7 +175,8 @@ BATCH_WORKLOAD = ('C4 batched retrieval sweep: {n} variants of the 1e-3..100 bar
                   'log-U 1e-4..1e-3, deep T offset U(-10, 10) K, 300..1200 layers), 128 freqs '
                   '(0.5..50 GHz log), 32-ray disc quadrature, configuration-0 line lists; forward '
                   'Tb_avg + adjoint dTb/dT, dTb/dP, dTb/dlnX for every variant per step, replayed '
-                  'from one captured CUDA graph, line-sum tiling from the autotuner')
+                  'from one captured CUDA graph, line-sum tiling and JVP launch shape from the '
+                  'autotuner')
 
 
 def measure_batch(args, dev, n_var, pool=None):
@@ -227,6 +233,9 @@ def measure_batch(args, dev, n_var, pool=None):
                                                              nb, layers=(300, 1200)),
                                candidates=((2, 2, 1024), (2, 4, 1024), (4, 1, 1024), (4, 2, 1024)),
                                reps=1, stream=stream)
+    jbest, jt = tune.tune_adjoint(eng, step, key=tune.workload_key('batch', dict(freqs=freqs, lines=lines),
+                                                                  nb, layers=(300, 1200)),
+                                  reps=1, stream=stream)
     step()                                   # plan and buffers for the chosen tiling
     torch.cuda.synchronize()
     graph = torch.cuda.CUDAGraph()
@@ -296,6 +305,8 @@ def measure_batch(args, dev, n_var, pool=None):
                             layers_total=NLT, freqs=nf, rays_per_variant=nb,
                             tiling=dict(M=best[0], W=best[1], item_lines=best[2]),
                             tuning_ms={'{},{},{}'.format(*k): v for k, v in tt.items()},
+                            jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1]),
+                            jvp_tuning_ms={'{},{}'.format(*k): v for k, v in jt.items()},
                             l2='working set of tens of GB, larger than L2'),
                 per_atmosphere_adjoint=dict(value=plain, unit='spectra+gradients/s',
                                             api='rb_adjoint_device, one atmosphere per call, '
@@ -341,10 +352,11 @@ def batch_accuracy(pool, nLs, nh3, dT, freqs, b, w, lines, C, LP, res, n_sample=
 IMAGE_WORKLOAD = ('C2 batched image rays: 256 x 256 impact parameters at 0.01 planet radius '
                   '(31,397 on the disc incl. limb rays of up to ~2000 segments, the rest off the '
                   'planet -> T_cmb) x 8 freqs (1.4..44 GHz), 1000 layers, C1 line lists; one step = '
-                  'one image replayed from a captured CUDA graph, line-sum tiling from the autotuner')
+                  'one image replayed from a captured CUDA graph, line-sum tiling from the '
+                  'autotuner')
 
 
-def measure_image(args, dev, stream, flush, pool=None, fp32_peak=None):
+def measure_image(args, dev, stream, flush, pool=None):
     """Images per second (and rays/s) for the C2 grid: every ray of an image
     in one rb_forward_device, captured once into a CUDA graph and replayed;
     the line-sum tiling chosen by the autotuner for this shape.  The scan's
@@ -773,6 +785,18 @@ def run_gpu(args, rank, world, local_rank):
                            dN.data_ptr(), a['freqs'], db.data_ptr(), 71492.0, 66854.0,
                            dTb.data_ptr(), weights=dw.data_ptr(), Tb_avg=davg.data_ptr())
 
+    from radiobear_gb300 import tune
+    tuned = {}
+    if not args.alpha_tiling:
+        key = tune.workload_key('spectrum', wl, nb)
+        ab, at = tune.tune_alpha(eng, step, key=key, candidates=((2, 4, 1024), (2, 2, 1024),
+                                                                 (4, 2, 1024), (2, 4, 512)),
+                                 reps=5, stream=stream)
+        sb, st_ = tune.tune_scan(eng, step, key=key, candidates=((32,), (64,), (128,)), reps=5,
+                                 stream=stream)
+        tuned = dict(tiling=dict(M=ab[0], W=ab[1], item_lines=ab[2]),
+                     tuning_ms={'{},{},{}'.format(*k): v for k, v in at.items()},
+                     scan_lanes=sb[0], scan_tuning_ms={str(k[0]): v for k, v in st_.items()})
     step()
     torch.cuda.synchronize()
     launches_per_step = eng.last_launch_count()
@@ -862,7 +886,8 @@ def run_gpu(args, rank, world, local_rank):
         config=dict(workload=WORKLOAD, layers=nL, freqs=nf, rays=nb, lines=counts,
                     parallelism='replicas' if world > 1 else 'single',
                     l2='256 MiB buffer written between steps; per-step CUDA events',
-                    precision='f32 compensated line sums, f64 ray geometry, f32x2 tau'),
+                    precision='f32 compensated line sums, f64 ray geometry, f32x2 tau',
+                    autotuned=tuned),
         e2e=dict(value=1.0 / float(np.mean(e2e_times)), unit=UNIT, h2d_bytes_per_step=int(h2d),
                  d2h_bytes_per_step=int(d2h), api='rb_forward (C ABI, pinned host buffers)'),
         gpu_launches=int(launches_per_step * args.steps),

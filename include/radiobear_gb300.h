@@ -156,6 +156,18 @@ int rb_set_co_clouds(rb_handle* h, int co, int coshape, int clouds, int cloud_ma
  * (radiobear_gb300.tune) drives it. */
 int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines);
 
+/* Launch shapes of the adjoint and scan kernels (no reference counterpart),
+ * driven by the autotuner (radiobear_gb300.tune); 0 restores the automatic
+ * choice.  RB_TUNE_JVP_FREQS: frequencies per CTA of the absorption JVP
+ * (32, 64 or 128); RB_TUNE_JVP_CTAS: resident CTAs per SM it is compiled
+ * for (3: 80 registers, 4: 64); RB_TUNE_SCAN_LANES: frequency-pair lanes
+ * per (ray, chunk) item of the brightness scan (a power of two in 4..128;
+ * a CTA of 128 threads takes 128 / lanes items). */
+#define RB_TUNE_JVP_FREQS 1
+#define RB_TUNE_JVP_CTAS 2
+#define RB_TUNE_SCAN_LANES 3
+int rb_set_tuning(rb_handle* h, int param, int value);
+
 /* Absorption of nL layers at nf frequencies.
  *   P[nL] bar, T[nL] K, X[RB_NX][nL] composition (rows above), freqs[nf] GHz.
  *   scale:      nullable, [nL][RB_NGAS] multipliers (number, per-layer list

@@ -50,7 +50,7 @@ EXPORTS = ('rb_abi_version', 'rb_last_error', 'rb_create', 'rb_destroy', 'rb_set
            'rb_probe_fp32_peak', 'rb_debug_e2', 'rb_set_alpha_tiling', 'rb_adjoint',
            'rb_adjoint_device', 'rb_forward_batch_device', 'rb_adjoint_batch_device',
            'rb_set_co_clouds', 'rb_atm_props', 'rb_atm_props_device', 'rb_regrid',
-           'rb_regrid_device', 'rb_bright_run', 'rb_debug_e1')
+           'rb_regrid_device', 'rb_bright_run', 'rb_debug_e1', 'rb_set_tuning')
 
 _lib = None
 _lock = threading.Lock()
@@ -113,6 +113,7 @@ def load_library(path=None):
         lib.rb_phase_times.argtypes = [_vp, _d, c_int]
         lib.rb_probe_fp32_peak.argtypes = [_vp, _d]
         lib.rb_set_alpha_tiling.argtypes = [_vp, c_int, c_int, c_int]
+        lib.rb_set_tuning.argtypes = [_vp, c_int, c_int]
         lib.rb_adjoint.argtypes = [_vp, c_int, _vp, _vp, _vp, _vp, _vp, c_int, _vp, _vp, c_double,
                                    c_double, c_double, c_double, c_int, c_int, c_int, _vp, _vp, c_int,
                                    _vp, _vp, _vp, _vp, _vp, _vp]
@@ -411,6 +412,14 @@ class Engine:
         item (zeros: automatic)."""
         _check(self.lib, self.lib.rb_set_alpha_tiling(self._h, int(M), int(W), int(item_lines)),
                'rb_set_alpha_tiling')
+
+    TUNING = dict(jvp_freqs=1, jvp_ctas=2, scan_lanes=3)   # RB_TUNE_*
+
+    def set_tuning(self, **kw):
+        """Launch shapes (rb_set_tuning): jvp_freqs (32/64/128), jvp_ctas (3/4),
+        scan_lanes (power of two in 4..128); 0 = automatic."""
+        for k, v in kw.items():
+            _check(self.lib, self.lib.rb_set_tuning(self._h, self.TUNING[k], int(v)), 'rb_set_tuning')
 
     def set_profiling(self, on=True):
         _check(self.lib, self.lib.rb_set_profiling(self._h, int(on)), 'rb_set_profiling')

@@ -1273,8 +1273,9 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
 #ifndef RB_JVP_MINB
 #define RB_JVP_MINB 3
 #endif
-  if (jv.ft >= 128) rb_alpha_jvp_kernel<RB_JVP_MINB128><<<grid, 256, 0, st>>>(jv);
-  else rb_alpha_jvp_kernel<RB_JVP_MINB><<<grid, 256, 0, st>>>(jv);
+  const int ctas = jv.ctas ? jv.ctas : (jv.ft >= 128 ? RB_JVP_MINB128 : RB_JVP_MINB);
+  if (ctas >= 4) rb_alpha_jvp_kernel<4><<<grid, 256, 0, st>>>(jv);
+  else rb_alpha_jvp_kernel<3><<<grid, 256, 0, st>>>(jv);
   if (ea) {
     cudaError_t x = launch_extra_vjp(*ea, st);
     if (x != cudaSuccess) return x;
@@ -1286,7 +1287,14 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
 
 // Frequencies per CTA of rb_alpha_jvp_kernel (the rest of its 256 threads
 // split the lines).
-int adjoint_ft(int nf) { return nf >= 128 ? 128 : (nf >= 64 ? 64 : 32); }
-int adjoint_tiles(int nf) { return (nf + adjoint_ft(nf) - 1) / adjoint_ft(nf); }
+// (ft_forced: rb_set_tuning's choice, 0 = automatic.)
+int adjoint_ft(int nf, int ft_forced) {
+  if (ft_forced) return ft_forced;
+  return nf >= 128 ? 128 : (nf >= 64 ? 64 : 32);
+}
+int adjoint_tiles(int nf, int ft_forced) {
+  const int ft = adjoint_ft(nf, ft_forced);
+  return (nf + ft - 1) / ft;
+}
 
 }  // namespace rb

@@ -196,6 +196,7 @@ struct rb_handle {
   int plan_grid = 0;
   int plan_vbeg[rb::NFAM] = {}, plan_vend[rb::NFAM] = {};
   int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
+  int jvp_ft = 0, jvp_ctas = 0, scan_lanes = 0;   // rb_set_tuning (0: automatic)
   DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base;
   // adjoint workspaces
@@ -262,8 +263,8 @@ int alpha_lines_occupancy(int M, int W);
 cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
                            const ExtraArgs* ea, float* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st);
-int adjoint_tiles(int nf);
-int adjoint_ft(int nf);
+int adjoint_tiles(int nf, int ft_forced);
+int adjoint_ft(int nf, int ft_forced);
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
                              float* R32, float* T32, const int* var_off, int nvar, cudaStream_t st);
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st);
@@ -990,6 +991,32 @@ int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines) {
   return RB_OK;
 }
 
+int rb_set_tuning(rb_handle* h, int param, int value) {
+  if (!h) return fail(RB_EINVAL, "null handle");
+  const bool pow2 = value > 0 && (value & (value - 1)) == 0;
+  switch (param) {
+    case RB_TUNE_JVP_FREQS:
+      if (!(value == 0 || value == 32 || value == 64 || value == 128))
+        return fail(RB_EINVAL, "RB_TUNE_JVP_FREQS must be 0, 32, 64 or 128");
+      h->jvp_ft = value;
+      break;
+    case RB_TUNE_JVP_CTAS:
+      if (!(value == 0 || value == 3 || value == 4))
+        return fail(RB_EINVAL, "RB_TUNE_JVP_CTAS must be 0, 3 or 4");
+      h->jvp_ctas = value;
+      break;
+    case RB_TUNE_SCAN_LANES:
+      if (!(value == 0 || (pow2 && value >= 4 && value <= 128)))
+        return fail(RB_EINVAL, "RB_TUNE_SCAN_LANES must be 0 or a power of two in 4..128");
+      h->scan_lanes = value;
+      break;
+    default:
+      return fail(RB_EINVAL, "unknown tuning parameter %d", param);
+  }
+  ++h->cfg_gen;
+  return RB_OK;
+}
+
 int rb_alpha(rb_handle* h, int nL, const double* P, const double* T, const double* X, int nf,
              const double* freqs, const double* scale, int units_db, double* layers_out,
              double* gas_out) {
@@ -1136,6 +1163,7 @@ int rb_brightness(rb_handle* h, int nL, const double* T, int nf, const double* l
     RB_CUDA(rb::launch_tb_seq(ta, st));
   } else {
     ta.nchunk = rb::tb_nchunk(max_seg);
+    ta.lanes = h->scan_lanes;
     RB_CUDA(h->d_part.ensure(sizeof(float4) * (size_t)nb * ta.nchunk * nf));
     ta.part = h->d_part.as<float4>();
     h->launches = 2;
@@ -1208,6 +1236,7 @@ int rb_bright_run(rb_handle* h, int nL, const double* T, const double* R, const 
   ta.Tb = h->d_Tb.as<double>();
   ta.intW = h->d_iw.as<double>();
   ta.nchunk = nchunk;
+  ta.lanes = h->scan_lanes;
   ta.part = h->d_part.as<float4>();
   RB_CUDA(rb::launch_tb_chunked(ta, st));
   h->launches += 2;
@@ -1310,6 +1339,7 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
     ta.Tb = dTb;
     ta.Tb32 = h->d_Tb32.as<float>();
     ta.nchunk = nchunk;
+    ta.lanes = h->scan_lanes;
     ta.part = h->d_part.as<float4>();
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[5], st));
     if (disc) {
@@ -1459,7 +1489,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
     return rc;
   const int launches = h->launches;
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
-  const int ntile = rb::adjoint_tiles(nf);
+  const int ntile = rb::adjoint_tiles(nf, h->jvp_ft);
   RB_CUDA(h->d_ga.ensure(sizeof(float) * (size_t)nL * nf));
   RB_CUDA(h->d_gs.ensure(sizeof(double) * (size_t)nL));
   RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
@@ -1502,7 +1532,8 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   rb::JvpArgs jv{};
   jv.nL = nL;
   jv.nf = nf;
-  jv.ft = rb::adjoint_ft(nf);
+  jv.ft = rb::adjoint_ft(nf, h->jvp_ft);
+  jv.ctas = h->jvp_ctas;
   jv.freqs = h->d_f.as<double>();
   jv.freqs_hs = h->d_fhs.as<double>();
   jv.lp = h->d_lp.as<rb::LayerParams>();

@@ -199,6 +199,7 @@ struct TbArgs {
   double* TbL;
   // chunked scan
   int chunk, nchunk;      // segments per chunk, chunks per ray
+  int lanes;              // frequency-pair lanes per (ray, chunk) item of the packed scan (0: automatic)
   float4* part;           // [nb][nchunk][nf] {dtau_hi, dtau_lo, intW, TbL} per chunk
 };
 
@@ -258,6 +259,7 @@ struct TbAdjArgs {
 struct JvpArgs {
   int nL, nf;
   int ft;                 // frequencies per CTA
+  int ctas;               // resident CTAs per SM the kernel is compiled for (3 or 4)
   const double* freqs;
   const double* freqs_hs;
   const LayerParams* lp;

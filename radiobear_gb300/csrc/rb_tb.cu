@@ -225,7 +225,7 @@ constexpr int SCAN_ITEM_WORDS = 3 * TB_CHUNK + 2;   // staged words per item
 // steps), C1's scan 0.0368 -> 0.0316 ms and C2's 0.416 -> 0.401 ms.
 __global__ void __launch_bounds__(128, 6) rb_tb_chunk2_kernel(TbArgs a) {
   const int npair = a.nf / 2;
-  const int FP = scan_lanes(npair);
+  const int FP = a.lanes ? a.lanes : scan_lanes(npair);
   const int IPB = 128 / FP;
   const int sub = threadIdx.x / FP, fl = threadIdx.x % FP;
   const long long item = (long long)blockIdx.x * IPB + sub;
@@ -401,7 +401,7 @@ cudaError_t launch_tb_seq(const TbArgs& a, cudaStream_t st) {
 cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
   if (a.nb <= 0 || a.nf <= 0) return cudaSuccess;
   if (a.nf % 2 == 0) {
-    const int FP = scan_lanes(a.nf / 2);
+    const int FP = a.lanes ? a.lanes : scan_lanes(a.nf / 2);
     const long long nitem = (long long)a.nb * a.nchunk;
     const long long nblk = (nitem + 128 / FP - 1) / (128 / FP);
     dim3 grid((unsigned)nblk, 1, (a.nf / 2 + FP - 1) / FP);

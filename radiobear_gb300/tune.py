@@ -1,4 +1,4 @@
-"""Autotuner for the absorption line sums.
+"""Autotuner for the kernels' launch shapes.
 
 The line-sum kernel's tiling (frequency slots per thread M, warps per CTA W,
 lines per work item) trades shared-record reuse against occupancy and load
@@ -6,7 +6,9 @@ balance, and the best choice depends on the number of frequencies, layers
 and lines.  ``tune_alpha`` times a caller-supplied step (any sequence of
 library calls on the engine, e.g. one batched forward + adjoint, or one
 image) for each candidate tiling with CUDA events and leaves the fastest
-one set on the engine.
+one set on the engine; ``tune_adjoint`` does the same for the adjoint's
+JVP launch shape (frequencies per CTA, resident CTAs per SM) and
+``tune_scan`` for the brightness scan's lanes per (ray, chunk) item.
 
 Results are cached per key -- the device, the kind of step, the number of
 frequencies, the layer range, the line counts per family and the rays --
@@ -67,7 +69,7 @@ def _store(k, best, times):
     try:
         os.makedirs(os.path.dirname(path), exist_ok=True)
         data = _load()
-        data[k] = dict(best=list(best), ms={'{},{},{}'.format(*c): v for c, v in times.items()})
+        data[k] = dict(best=list(best), ms={','.join(str(x) for x in c): v for c, v in times.items()})
         tmp = path + '.tmp'
         with open(tmp, 'w') as fp:
             json.dump(data, fp, indent=1, sort_keys=True)
@@ -76,12 +78,9 @@ def _store(k, best, times):
         pass                       # a read-only home: the in-memory cache still holds it
 
 
-def tune_alpha(engine, step, key=None, candidates=DEFAULT_CANDIDATES, reps=3, stream=None):
-    """Time ``step()`` for each (M, W, item_lines) candidate; set and return
-    the fastest.  ``step`` must enqueue its work on ``stream`` (default: the
-    current torch stream).  ``key`` (a dict from :func:`workload_key`, or
-    None for no caching) selects the cache entry.  Returns (best,
-    {candidate: ms}); a cached result returns the times it was chosen by."""
+def _search(apply, step, candidates, key, reps, stream):
+    """Time ``step()`` under each candidate (``apply(c)`` sets it), keep the
+    fastest; cached per key (memory and JSON)."""
     import torch
     k = _key_str(key) if key is not None else None
     if k is not None:
@@ -93,12 +92,13 @@ def tune_alpha(engine, step, key=None, candidates=DEFAULT_CANDIDATES, reps=3, st
                        {tuple(int(v) for v in c.split(',')): t for c, t in rec['ms'].items()})
                 _CACHE[k] = hit
         if hit is not None:
-            engine.set_alpha_tiling(*hit[0])
+            apply(hit[0])
             return hit
     stream = stream or torch.cuda.current_stream()
     times = {}
     for cand in candidates:
-        engine.set_alpha_tiling(*cand)
+        cand = tuple(int(v) for v in cand)
+        apply(cand)
         step()                       # plan + warm-up
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -110,8 +110,39 @@ def tune_alpha(engine, step, key=None, candidates=DEFAULT_CANDIDATES, reps=3, st
         torch.cuda.synchronize()
         times[cand] = min(s.elapsed_time(e) for s, e in ev)
     best = min(times, key=times.get)
-    engine.set_alpha_tiling(*best)
+    apply(best)
     if k is not None:
         _CACHE[k] = (best, times)
         _store(k, best, times)
     return best, times
+
+
+def tune_alpha(engine, step, key=None, candidates=DEFAULT_CANDIDATES, reps=3, stream=None):
+    """Time ``step()`` for each (M, W, item_lines) line-sum tiling; set and
+    return the fastest.  ``step`` must enqueue its work on ``stream``
+    (default: the current torch stream).  ``key`` (a dict from
+    :func:`workload_key`, or None for no caching) selects the cache entry.
+    Returns (best, {candidate: ms}); a cached result returns the times it
+    was chosen by."""
+    key = None if key is None else dict(key, knob='alpha_tiling')
+    return _search(lambda c: engine.set_alpha_tiling(*c), step, candidates, key, reps, stream)
+
+
+# (frequencies per CTA, resident CTAs per SM) of the absorption JVP
+JVP_CANDIDATES = ((128, 3), (128, 4), (64, 3), (64, 4))
+
+
+def tune_adjoint(engine, step, key=None, candidates=JVP_CANDIDATES, reps=1, stream=None):
+    """The adjoint's JVP launch shape: frequencies per CTA and resident CTAs
+    per SM (rb_set_tuning), timed on the caller's forward + adjoint step."""
+    key = None if key is None else dict(key, knob='jvp')
+
+    def apply(c):
+        engine.set_tuning(jvp_freqs=c[0], jvp_ctas=c[1])
+    return _search(apply, step, candidates, key, reps, stream)
+
+
+def tune_scan(engine, step, key=None, candidates=((4,), (8,), (16,)), reps=2, stream=None):
+    """Frequency-pair lanes per (ray, chunk) item of the brightness scan."""
+    key = None if key is None else dict(key, knob='scan_lanes')
+    return _search(lambda c: engine.set_tuning(scan_lanes=c[0]), step, candidates, key, reps, stream)

@@ -202,3 +202,34 @@ def test_calls_after_an_unfinished_device_call_are_ordered(engine):
     for got in [(host['dT'], host['dP'], host['dlnX'])] + [tuple(v.cpu().numpy() for v in o) for o in outs]:
         for a, want in zip(got, (ref['dT'], ref['dP'], ref['dlnX'])):
             assert np.max(np.abs(a - want)) <= 1e-6 * np.max(np.abs(want))
+
+
+def test_launch_shape_knobs_keep_the_results(engine):
+    """rb_set_tuning: every JVP launch shape (frequencies per CTA, CTAs per
+    SM) gives the same gradient (the per-tile partial sums change their
+    float64 summation order only), and every scan lane count the same Tb
+    bit for bit (each (ray, chunk, frequency) runs the same arithmetic)."""
+    from radiobear_gb300 import synth
+    z, g = G.load('c0'), G.gas_table(G.load('c0'))
+    _load(engine, G.c0_lines())
+    freqs = np.logspace(0.0, np.log10(50.0), 64)
+    b, w = synth.gauss_legendre_disc(6)
+    args = (g[G.C['P']], g[G.C['T']], _X(g), z['prop_R'], z['prop_N'], freqs, b, G.REQ, G.RPOL)
+    grad = np.random.default_rng(2).normal(size=freqs.size)
+    try:
+        ref = engine.adjoint(*args, grad, weights=w)
+        for ft, ctas in ((32, 3), (64, 4), (128, 3), (128, 4)):
+            engine.set_tuning(jvp_freqs=ft, jvp_ctas=ctas)
+            out = engine.adjoint(*args, grad, weights=w)
+            for k in ('dT', 'dP', 'dlnX'):
+                assert np.max(np.abs(out[k] - ref[k])) <= 1e-6 * np.max(np.abs(ref[k])), (ft, ctas, k)
+        engine.set_tuning(jvp_freqs=0, jvp_ctas=0)
+        tb0 = engine.forward(*args, weights=w)['Tb']
+        for lanes in (4, 8, 16, 32, 64, 128):
+            engine.set_tuning(scan_lanes=lanes)
+            assert np.array_equal(engine.forward(*args, weights=w)['Tb'], tb0), lanes
+    finally:
+        engine.set_tuning(jvp_freqs=0, jvp_ctas=0, scan_lanes=0)
+    from radiobear_gb300._native import RBError
+    with pytest.raises((RBError, ValueError)):
+        engine.set_tuning(scan_lanes=6)

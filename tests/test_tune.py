@@ -14,9 +14,13 @@ from radiobear_gb300 import tune   # noqa: E402
 class FakeEngine:
     def __init__(self):
         self.tiling = None
+        self.tuning = {}
 
     def set_alpha_tiling(self, M=0, W=0, item_lines=0):
         self.tiling = (M, W, item_lines)
+
+    def set_tuning(self, **kw):
+        self.tuning.update(kw)
 
 
 def test_workload_key_and_json_cache(tmp_path, monkeypatch):
@@ -27,7 +31,7 @@ def test_workload_key_and_json_cache(tmp_path, monkeypatch):
     key = tune.workload_key('image', wl, 65536)
     assert key == dict(kind='image', nf=8, layers=[1000, 1000], lines=dict(ammonia=1500, h2o=500),
                        rays=65536)
-    k = tune._key_str(key)
+    k = tune._key_str(dict(key, knob='alpha_tiling'))
     tune._store(k, (2, 1, 1024), {(2, 1, 1024): 1.0, (4, 1, 1024): 1.5})
     on_disk = json.loads((tmp_path / 'tuning.json').read_text())
     assert on_disk[k]['best'] == [2, 1, 1024]
@@ -42,3 +46,19 @@ def test_workload_key_and_json_cache(tmp_path, monkeypatch):
     other = tune.workload_key('batch', dict(freqs=np.ones(128), lines=wl['lines']), 32,
                               layers=(300, 1200))
     assert tune._key_str(other) not in on_disk
+
+
+def test_jvp_and_scan_knobs_are_cached_separately(tmp_path, monkeypatch):
+    monkeypatch.setenv('RB_TUNING_CACHE', str(tmp_path / 'tuning.json'))
+    monkeypatch.setattr(tune, '_CACHE', {})
+    key = dict(kind='batch', nf=128, layers=[300, 1200], lines=dict(ammonia=200), rays=32)
+    tune._store(tune._key_str(dict(key, knob='jvp')), (64, 4), {(64, 4): 1.0, (128, 3): 2.0})
+    tune._store(tune._key_str(dict(key, knob='scan_lanes')), (8,), {(8,): 1.0, (4,): 1.2})
+
+    def never():
+        raise AssertionError('a cached key must not time the step')
+
+    eng = FakeEngine()
+    assert tune.tune_adjoint(eng, never, key=key)[0] == (64, 4)
+    assert tune.tune_scan(eng, never, key=key)[0] == (8,)
+    assert eng.tuning == dict(jvp_freqs=64, jvp_ctas=4, scan_lanes=8)
