@@ -620,20 +620,11 @@ constexpr int JV_NU2 = 9;
 struct JvpShared {
   ulonglong2 rec[2][2][JV_PAIRS][JV_NU2];   // [buffer][coefficient set][pair][word], 144 B per pair
   float fam[NFAM][JV_FTMAX][4];             // per family and frequency: value, three derivatives
-  double red[8][NTH + 1];
+  float2 red[8][NTH + 1];
 };
 
 // Line kinds of the JVP sweep.
 enum JvKind : int { JK_BR = 0, JK_GROSS = 1, JK_VVW = 2, JK_SJS = 3 };
-
-// Frequency of one thread of rb_alpha_jvp_kernel.
-struct JvFreq {
-  float F, FL;     // f^2 (hi, lo)
-  float Fh, FhL;   // f^2 of the frequency nh3_hs evaluates in this slot
-  float fq, fql;   // f (hi, lo)
-  float wJ;        // nh3_sjs Spilker / Joiner weight
-  int set;         // inversion coefficient set
-};
 
 // Compensated float sum.
 struct KSum {
@@ -1076,15 +1067,9 @@ __global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
   const bool on = j < a.nf;
   const LayerParams& lp = a.lp[L];
   const LayerTan& LT = a.lt[L];
-  // this thread's frequency
-  const double f = on ? a.freqs[j] : 1.0, fh = on ? a.freqs_hs[j] : 1.0;
-  JvFreq fr;
-  split_double(f * f, fr.F, fr.FL);
-  split_double(fh * fh, fr.Fh, fr.FhL);
-  split_double(f, fr.fq, fr.fql);
-  const int set = fh > 30.0 ? 1 : 0;
-  fr.set = set;
-  fr.wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)(f - 26.0) * 0.125f);   // (f - 26) / 8
+  // this thread's frequency (lanes past nf take f = 1 GHz and add nothing)
+  const JvFreq fr = on ? a.fplan[j] : JvFreq{1.f, 0.f, 1.f, 0.f, 1.f, 0.f, 0.f, 0};
+  const int set = fr.set;
   const bool nh3 = a.cfg.nh3_mode != NH3_OFF;
   // families that are off keep zero sums (read back by the same thread)
   if (grp == 0)
@@ -1206,36 +1191,54 @@ __global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
     }
     for (int q = 0; q < NTH; ++q) g5[q] = gal * dal[q];
   }
-  // reduce over the CTA's frequencies (float64; only the warps of line
-  // group 0 hold values: FTL is a multiple of 32)
+  // reduce over the CTA's frequencies as double-floats (terms of both signs
+  // meet here; GB300's float64 rate made the float64 shuffles a tenth of the
+  // batched kernel); only the warps of line group 0 hold values: FTL is a
+  // multiple of 32.  The final kernel adds hi + lo in float64 per layer.
   const int nw0 = FTL >> 5;
   if (grp == 0) {
     for (int q = 0; q < NTH; ++q) {
-      double g = (double)g5[q];
-      for (int o = 16; o; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
-      if ((tid & 31) == 0) sh.red[tid >> 5][q] = g;
+      float hi = g5[q], lo = 0.f;
+      for (int o = 16; o; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        float s, e;
+        two_sum(hi, h2, s, e);
+        e += lo + l2;
+        hi = s + e;
+        lo = e - (hi - s);
+      }
+      if ((tid & 31) == 0) sh.red[tid >> 5][q] = make_float2(hi, lo);
     }
   }
   __syncthreads();
-  if (tid == 0) {
-    for (int q = 0; q < NTH; ++q) {
-      double sq = 0.0;
-      for (int w = 0; w < nw0; ++w) sq += sh.red[w][q];
-      a.part[((size_t)L * gridDim.y + blockIdx.y) * NTH + q] = sq;
+  if (tid < NTH) {
+    float hi = 0.f, lo = 0.f;
+    for (int w = 0; w < nw0; ++w) {
+      const float2 v = sh.red[w][tid];
+      float s, e;
+      two_sum(hi, v.x, s, e);
+      e += lo + v.y;
+      hi = s + e;
+      lo = e - (hi - s);
     }
+    a.part[((size_t)L * gridDim.y + blockIdx.y) * NTH + tid] = make_float2(hi, lo);
   }
 }
 
 // dT = sum of tiles + source term (summed over frequencies); dP; dln X
 // for NH3, H2O, H2S.
-__global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const double* part,
+__global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const float2* part,
                                         const double* gsrc, const double* gextra, double* dT,
                                         double* dP, double* dlnX) {
   const int L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nL) return;
   double s[NTH] = {0, 0, 0, 0, 0};
   for (int t = 0; t < ntile; ++t)
-    for (int q = 0; q < NTH; ++q) s[q] += part[((size_t)L * ntile + t) * NTH + q];
+    for (int q = 0; q < NTH; ++q) {
+      const float2 v = part[((size_t)L * ntile + t) * NTH + q];
+      s[q] += (double)v.x + (double)v.y;
+    }
   if (gextra) {
     s[TH_T] += gextra[2 * L];
     s[TH_P] += gextra[2 * L + 1];

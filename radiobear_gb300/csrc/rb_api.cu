@@ -197,7 +197,7 @@ struct rb_handle {
   int plan_vbeg[rb::NFAM] = {}, plan_vend[rb::NFAM] = {};
   int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
   int jvp_ft = 0, jvp_ctas = 0, scan_lanes = 0;   // rb_set_tuning (0: automatic)
-  DBuf d_f, d_fhs, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
+  DBuf d_f, d_fhs, d_jfreq, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base;
   // adjoint workspaces
   DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff;
@@ -519,6 +519,18 @@ int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st)
   const int occ = std::max(1, rb::alpha_lines_occupancy(M, W));
   RB_CUDA(upload(h->d_f, freqs, nf, st));
   RB_CUDA(upload(h->d_fhs, fhs.data(), nf, st));
+  // per-frequency values of the absorption JVP (see rb::JvFreq)
+  std::vector<rb::JvFreq> jfreq(nf);
+  for (int i = 0; i < nf; ++i) {
+    const double f = freqs[i], fh = fhs[i];
+    rb::JvFreq& q = jfreq[i];
+    rb::split_double(f * f, q.F, q.FL);
+    rb::split_double(fh * fh, q.Fh, q.FhL);
+    rb::split_double(f, q.fq, q.fql);
+    q.set = fh > 30.0 ? 1 : 0;
+    q.wJ = f <= 26.0 ? 0.f : (f >= 34.0 ? 1.f : (float)(f - 26.0) * 0.125f);   // (f - 26) / 8
+  }
+  RB_CUDA(upload(h->d_jfreq, jfreq.data(), jfreq.size(), st));
   RB_CUDA(upload(h->d_chains, chains.data(), chains.size(), st));
   RB_CUDA(upload(h->d_tflags, tflags.data(), tflags.size(), st));
   RB_CUDA(upload(h->d_wsets, wsets.data(), wsets.size(), st));
@@ -787,7 +799,7 @@ int rb_destroy(rb_handle* h) {
                   &h->d_xgrad, &h->d_agas, &h->d_acl, &h->d_aout, &h->d_aclout, &h->d_aprop,
                   &h->d_agrid, &h->d_aoff})
     b->release();
-  for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
+  for (DBuf* b : {&h->d_f, &h->d_fhs, &h->d_jfreq, &h->d_P, &h->d_T, &h->d_X, &h->d_scale, &h->d_lp,
                   &h->d_a32, &h->d_l64, &h->d_g64, &h->d_R, &h->d_N, &h->d_b, &h->d_w, &h->d_nseg,
                   &h->d_ds, &h->d_layer, &h->d_r4, &h->d_ll, &h->d_end, &h->d_Tb, &h->d_avg,
                   &h->d_iw, &h->d_tau, &h->d_W, &h->d_tbl, &h->d_x})
@@ -1493,7 +1505,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   RB_CUDA(h->d_ga.ensure(sizeof(float) * (size_t)nL * nf));
   RB_CUDA(h->d_gs.ensure(sizeof(double) * (size_t)nL));
   RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
-  RB_CUDA(h->d_jpart.ensure(sizeof(double) * (size_t)nL * ntile * rb::NTH));
+  RB_CUDA(h->d_jpart.ensure(sizeof(float2) * (size_t)nL * ntile * rb::NTH));
   rb::TbAdjArgs ta{};
   ta.nL = nL;
   ta.nf = nf;
@@ -1534,15 +1546,14 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   jv.nf = nf;
   jv.ft = rb::adjoint_ft(nf, h->jvp_ft);
   jv.ctas = h->jvp_ctas;
-  jv.freqs = h->d_f.as<double>();
-  jv.freqs_hs = h->d_fhs.as<double>();
+  jv.fplan = h->d_jfreq.as<rb::JvFreq>();
   jv.lp = h->d_lp.as<rb::LayerParams>();
   jv.lt = h->d_lt.as<rb::LayerTan>();
   for (int f = 0; f < rb::NFAM; ++f) jv.tab[f] = h->fam[f].table();
   jv.cfg = h->cfg;
   jv.cfg.units_db = 0;
   jv.galpha = h->d_ga.as<float>();
-  jv.part = h->d_jpart.as<double>();
+  jv.part = h->d_jpart.as<float2>();
   rb::ExtraArgs ea{};
   const bool extra = h->cfg.use_co || h->cfg.use_clouds;
   if (extra) {

@@ -256,18 +256,27 @@ struct TbAdjArgs {
   double2* tauE;          // [nb][max_seg][nf] {tau, 2 E2(tau)} per path node
 };
 
+// Frequency of one thread of the absorption JVP, precomputed per frequency
+// with the plan (float pairs, so the kernel does no float64 arithmetic).
+struct JvFreq {
+  float F, FL;     // f^2 (hi, lo)
+  float Fh, FhL;   // f^2 of the frequency nh3_hs evaluates in this slot
+  float fq, fql;   // f (hi, lo)
+  float wJ;        // nh3_sjs Spilker / Joiner weight
+  int set;         // inversion coefficient set
+};
+
 struct JvpArgs {
   int nL, nf;
+  const JvFreq* fplan;    // [nf]
   int ft;                 // frequencies per CTA
   int ctas;               // resident CTAs per SM the kernel is compiled for (3 or 4)
-  const double* freqs;
-  const double* freqs_hs;
   const LayerParams* lp;
   const LayerTan* lt;
   LineTable tab[NFAM];
   AlphaConfig cfg;
   const float* galpha;    // [nL][nf] d loss / d alpha
-  double* part;           // [nL][ntile][NTH]
+  float2* part;           // [nL][ntile][NTH] double-float sums over the tile's frequencies
 };
 
 }  // namespace rb
