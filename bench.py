@@ -119,6 +119,7 @@ def measure_gradients(args, dev, stream, flush, pool=None):
 
     from radiobear_gb300 import tune
     jbest, jt = tune.tune_adjoint(eng, step, key=tune.workload_key('gradients', wl, nb), reps=5,
+                                  candidates=[c for c in tune.JVP_CANDIDATES if c[0] <= nf],
                                   stream=stream)
     step()
     torch.cuda.synchronize()
@@ -153,8 +154,8 @@ def measure_gradients(args, dev, stream, flush, pool=None):
     out = dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second',
                value=1e3 / ms, unit='spectra+gradients/s', ms_per_step=ms, steps=n,
                config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb,
-                           jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1]),
-                           jvp_tuning_ms={'{},{}'.format(*k): v for k, v in jt.items()}),
+                           jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1], threads=jbest[2]),
+                           jvp_tuning_ms={','.join(map(str, k)): v for k, v in jt.items()}),
                gpu_launches_per_step=int(launches),
                e2e=dict(value=1.0 / float(np.mean(e2e)), unit='spectra+gradients/s',
                         h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
@@ -305,8 +306,8 @@ def measure_batch(args, dev, n_var, pool=None):
                             layers_total=NLT, freqs=nf, rays_per_variant=nb,
                             tiling=dict(M=best[0], W=best[1], item_lines=best[2]),
                             tuning_ms={'{},{},{}'.format(*k): v for k, v in tt.items()},
-                            jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1]),
-                            jvp_tuning_ms={'{},{}'.format(*k): v for k, v in jt.items()},
+                            jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1], threads=jbest[2]),
+                            jvp_tuning_ms={','.join(map(str, k)): v for k, v in jt.items()},
                             l2='working set of tens of GB, larger than L2'),
                 per_atmosphere_adjoint=dict(value=plain, unit='spectra+gradients/s',
                                             api='rb_adjoint_device, one atmosphere per call, '

@@ -160,12 +160,15 @@ int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines);
  * driven by the autotuner (radiobear_gb300.tune); 0 restores the automatic
  * choice.  RB_TUNE_JVP_FREQS: frequencies per CTA of the absorption JVP
  * (32, 64 or 128); RB_TUNE_JVP_CTAS: resident CTAs per SM it is compiled
- * for (3: 80 registers, 4: 64); RB_TUNE_SCAN_LANES: frequency-pair lanes
- * per (ray, chunk) item of the brightness scan (a power of two in 4..128;
- * a CTA of 128 threads takes 128 / lanes items). */
+ * for at 256 threads (3: 80 registers, 4: 64); RB_TUNE_JVP_THREADS: threads
+ * per CTA (128 or 256, a multiple of the frequencies per CTA; the threads
+ * beyond the frequencies split the lines); RB_TUNE_SCAN_LANES:
+ * frequency-pair lanes per (ray, chunk) item of the brightness scan (a
+ * power of two in 4..128; a CTA of 128 threads takes 128 / lanes items). */
 #define RB_TUNE_JVP_FREQS 1
 #define RB_TUNE_JVP_CTAS 2
 #define RB_TUNE_SCAN_LANES 3
+#define RB_TUNE_JVP_THREADS 4
 int rb_set_tuning(rb_handle* h, int param, int value);
 
 /* Absorption of nL layers at nf frequencies.

@@ -1036,6 +1036,11 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
     __syncthreads();
   }
   val.add(lo2(vp) + hi2(vp));
+  if (NG == 1) {   // one line group: the thread's sums are the family's (read back by itself)
+    sh.fam[fam][fi][0] = val.val();
+    for (int q = 0; q < 3; ++q) sh.fam[fam][fi][1 + q] = lo2(der[q]) + hi2(der[q]);
+    return;
+  }
   // the line groups' sums, staged in the (now free) record buffer
   float(*s_grp)[4] = reinterpret_cast<float(*)[4]>(&sh.rec[0][0][0][0]);
   s_grp[tid][0] = val.val();
@@ -1052,12 +1057,13 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
 
 // Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
 // sweeps lines g, g + NG, ... of every chunk and the groups' sums are added
-// per family.  MINB resident CTAs per SM: 4 (64 registers) for 128-frequency
+// per family (with one group, 128 threads for 128 frequencies, each thread
+// holds its frequency's family sums itself).  MINB resident CTAs per SM: 4 (64 registers) for 128-frequency
 // tiles, 3 (80 registers) for smaller ones (measured: C4's 128 frequencies
 // 68.4 -> 64.2 ms per 512 variants at 4; C3's 64 frequencies 0.693 -> 0.719
 // ms per step at 4).
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
+template <int MINB, int NT>
+__global__ void __launch_bounds__(NT, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
   __shared__ __align__(16) JvpShared sh;
   const int L = blockIdx.x;
   const int tid = threadIdx.x;
@@ -1277,8 +1283,12 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
 #define RB_JVP_MINB 3
 #endif
   const int ctas = jv.ctas ? jv.ctas : (jv.ft >= 128 ? RB_JVP_MINB128 : RB_JVP_MINB);
-  if (ctas >= 4) rb_alpha_jvp_kernel<4><<<grid, 256, 0, st>>>(jv);
-  else rb_alpha_jvp_kernel<3><<<grid, 256, 0, st>>>(jv);
+  // threads per CTA: one line group for 128-frequency tiles (no per-family
+  // reduction across groups; C4 412 -> 371 ms), two or four otherwise
+  const int nt = jv.threads ? jv.threads : (jv.ft >= 128 ? 128 : 256);
+  if (nt == 128) rb_alpha_jvp_kernel<4, 128><<<grid, 128, 0, st>>>(jv);
+  else if (ctas >= 4) rb_alpha_jvp_kernel<4, 256><<<grid, 256, 0, st>>>(jv);
+  else rb_alpha_jvp_kernel<3, 256><<<grid, 256, 0, st>>>(jv);
   if (ea) {
     cudaError_t x = launch_extra_vjp(*ea, st);
     if (x != cudaSuccess) return x;

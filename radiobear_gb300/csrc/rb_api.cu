@@ -196,7 +196,7 @@ struct rb_handle {
   int plan_grid = 0;
   int plan_vbeg[rb::NFAM] = {}, plan_vend[rb::NFAM] = {};
   int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
-  int jvp_ft = 0, jvp_ctas = 0, scan_lanes = 0;   // rb_set_tuning (0: automatic)
+  int jvp_ft = 0, jvp_ctas = 0, jvp_threads = 0, scan_lanes = 0;   // rb_set_tuning (0: automatic)
   DBuf d_f, d_fhs, d_jfreq, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base;
   // adjoint workspaces
@@ -1017,6 +1017,11 @@ int rb_set_tuning(rb_handle* h, int param, int value) {
         return fail(RB_EINVAL, "RB_TUNE_JVP_CTAS must be 0, 3 or 4");
       h->jvp_ctas = value;
       break;
+    case RB_TUNE_JVP_THREADS:
+      if (!(value == 0 || value == 128 || value == 256))
+        return fail(RB_EINVAL, "RB_TUNE_JVP_THREADS must be 0, 128 or 256");
+      h->jvp_threads = value;
+      break;
     case RB_TUNE_SCAN_LANES:
       if (!(value == 0 || (pow2 && value >= 4 && value <= 128)))
         return fail(RB_EINVAL, "RB_TUNE_SCAN_LANES must be 0 or a power of two in 4..128");
@@ -1546,6 +1551,10 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   jv.nf = nf;
   jv.ft = rb::adjoint_ft(nf, h->jvp_ft);
   jv.ctas = h->jvp_ctas;
+  jv.threads = h->jvp_threads;
+  if (jv.threads && jv.threads % jv.ft)
+    return fail(RB_EINVAL, "JVP threads per CTA (%d) must be a multiple of its frequencies per CTA (%d)",
+                jv.threads, jv.ft);
   jv.fplan = h->d_jfreq.as<rb::JvFreq>();
   jv.lp = h->d_lp.as<rb::LayerParams>();
   jv.lt = h->d_lt.as<rb::LayerTan>();

@@ -271,6 +271,7 @@ struct JvpArgs {
   const JvFreq* fplan;    // [nf]
   int ft;                 // frequencies per CTA
   int ctas;               // resident CTAs per SM the kernel is compiled for (3 or 4)
+  int threads;            // threads per CTA (128 or 256; 0: automatic)
   const LayerParams* lp;
   const LayerTan* lt;
   LineTable tab[NFAM];

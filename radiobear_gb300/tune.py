@@ -128,17 +128,21 @@ def tune_alpha(engine, step, key=None, candidates=DEFAULT_CANDIDATES, reps=3, st
     return _search(lambda c: engine.set_alpha_tiling(*c), step, candidates, key, reps, stream)
 
 
-# (frequencies per CTA, resident CTAs per SM) of the absorption JVP
-JVP_CANDIDATES = ((128, 3), (128, 4), (64, 3), (64, 4))
+# (frequencies per CTA, resident CTAs per SM at 256 threads, threads per CTA)
+# of the absorption JVP
+JVP_CANDIDATES = ((128, 4, 128), (128, 3, 256), (128, 4, 256), (64, 3, 256), (64, 4, 256),
+                  (64, 4, 128))
 
 
 def tune_adjoint(engine, step, key=None, candidates=JVP_CANDIDATES, reps=1, stream=None):
-    """The adjoint's JVP launch shape: frequencies per CTA and resident CTAs
-    per SM (rb_set_tuning), timed on the caller's forward + adjoint step."""
+    """The adjoint's JVP launch shape: frequencies per CTA, resident CTAs
+    per SM and threads per CTA (rb_set_tuning), timed on the caller's
+    forward + adjoint step.  Candidates with more frequencies per CTA than
+    the step has are skipped by the caller's choice of list."""
     key = None if key is None else dict(key, knob='jvp')
 
     def apply(c):
-        engine.set_tuning(jvp_freqs=c[0], jvp_ctas=c[1])
+        engine.set_tuning(jvp_freqs=c[0], jvp_ctas=c[1], jvp_threads=c[2] if len(c) > 2 else 0)
     return _search(apply, step, candidates, key, reps, stream)
 
 

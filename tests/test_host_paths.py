@@ -218,18 +218,19 @@ def test_launch_shape_knobs_keep_the_results(engine):
     grad = np.random.default_rng(2).normal(size=freqs.size)
     try:
         ref = engine.adjoint(*args, grad, weights=w)
-        for ft, ctas in ((32, 3), (64, 4), (128, 3), (128, 4)):
-            engine.set_tuning(jvp_freqs=ft, jvp_ctas=ctas)
+        for ft, ctas, nt in ((32, 3, 256), (64, 4, 256), (64, 4, 128), (128, 3, 256), (128, 4, 256),
+                             (128, 4, 128)):
+            engine.set_tuning(jvp_freqs=ft, jvp_ctas=ctas, jvp_threads=nt)
             out = engine.adjoint(*args, grad, weights=w)
             for k in ('dT', 'dP', 'dlnX'):
-                assert np.max(np.abs(out[k] - ref[k])) <= 1e-6 * np.max(np.abs(ref[k])), (ft, ctas, k)
-        engine.set_tuning(jvp_freqs=0, jvp_ctas=0)
+                assert np.max(np.abs(out[k] - ref[k])) <= 1e-6 * np.max(np.abs(ref[k])), (ft, ctas, nt, k)
+        engine.set_tuning(jvp_freqs=0, jvp_ctas=0, jvp_threads=0)
         tb0 = engine.forward(*args, weights=w)['Tb']
         for lanes in (4, 8, 16, 32, 64, 128):
             engine.set_tuning(scan_lanes=lanes)
             assert np.array_equal(engine.forward(*args, weights=w)['Tb'], tb0), lanes
     finally:
-        engine.set_tuning(jvp_freqs=0, jvp_ctas=0, scan_lanes=0)
+        engine.set_tuning(jvp_freqs=0, jvp_ctas=0, jvp_threads=0, scan_lanes=0)
     from radiobear_gb300._native import RBError
     with pytest.raises((RBError, ValueError)):
         engine.set_tuning(scan_lanes=6)

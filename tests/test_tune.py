@@ -61,4 +61,4 @@ def test_jvp_and_scan_knobs_are_cached_separately(tmp_path, monkeypatch):
     eng = FakeEngine()
     assert tune.tune_adjoint(eng, never, key=key)[0] == (64, 4)
     assert tune.tune_scan(eng, never, key=key)[0] == (8,)
-    assert eng.tuning == dict(jvp_freqs=64, jvp_ctas=4, scan_lanes=8)
+    assert eng.tuning == dict(jvp_freqs=64, jvp_ctas=4, jvp_threads=0, scan_lanes=8)
