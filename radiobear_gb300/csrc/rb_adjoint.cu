@@ -607,6 +607,8 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
 // ------------------------------------------------------------------ alpha JVP
 // Records of one line, float: value fields and derivatives along the
 // family's three tangents (T, P, ln X of its own gas).
+// Lines per record chunk: 128 for 256-thread CTAs, 64 for 128-thread CTAs
+// (half the shared memory, so 5 CTAs fit per SM; C4 371 -> 358 ms).
 constexpr int JV_CHUNK = 128;
 constexpr int JV_NREC = 16;
 
@@ -614,11 +616,12 @@ constexpr int JV_FTMAX = 128;   // frequencies per CTA at most
 
 // Line pairs: field f of lines (2p, 2p+1) is one f32x2 (first line in the
 // low half); two fields per 16-byte word, JV_NU2 words per pair.
-constexpr int JV_PAIRS = JV_CHUNK / 2;
 constexpr int JV_NU2 = 9;
 
+template <int CH>
 struct JvpShared {
-  ulonglong2 rec[2][2][JV_PAIRS][JV_NU2];   // [buffer][coefficient set][pair][word], 144 B per pair
+  static constexpr int PAIRS = CH / 2;
+  ulonglong2 rec[2][2][CH / 2][JV_NU2];     // [buffer][coefficient set][pair][word], 144 B per pair
   float fam[NFAM][JV_FTMAX][4];             // per family and frequency: value, three derivatives
   float2 red[8][NTH + 1];
 };
@@ -888,8 +891,8 @@ __device__ __forceinline__ f2 br_eval2(f2 F, f2 FL, f2 m8F, f2 g, f2 gp, f2 gm, 
 // of 16 lines into a compensated sum.  The groups' sums (value and three
 // derivatives) go to sh.fam[fam][fi], added in group order.  Called by
 // every thread.
-template <int KIND>
-__device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, int fam,
+template <int KIND, int CH>
+__device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared<CH>& sh, int L, int fam,
                                         const JvFreq& fr, bool on, float& base, float* dbase) {
   const int tid = threadIdx.x;
   const int FTL = a.ft, NG = blockDim.x / a.ft;
@@ -908,7 +911,7 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
     for (int k = 0; k < nf; ++k) o[2 * k] = v[k];
   };
   auto build = [&](int bi, int c0) {
-    const int nc = min(JV_CHUNK, t.n - c0);
+    const int nc = min(CH, t.n - c0);
     const int ncp = (nc + 1) & ~1;
     for (int i = tid; i < ncp; i += blockDim.x) {
       const int li = c0 + i;
@@ -959,13 +962,13 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
   val.init();
   f2 vp = 0ull, der[3] = {0ull, 0ull, 0ull};
   int nv = 0;
-  const int nchunks = (t.n + JV_CHUNK - 1) / JV_CHUNK;
+  const int nchunks = (t.n + CH - 1) / CH;
   build(0, 0);
   __syncthreads();
   for (int ci = 0; ci < nchunks; ++ci) {
-    const int c0 = ci * JV_CHUNK;
-    const int np = (min(JV_CHUNK, t.n - c0) + 1) >> 1;
-    if (ci + 1 < nchunks) build((ci + 1) & 1, c0 + JV_CHUNK);
+    const int c0 = ci * CH;
+    const int np = (min(CH, t.n - c0) + 1) >> 1;
+    if (ci + 1 < nchunks) build((ci + 1) & 1, c0 + CH);
     if (on) {
       const ulonglong2(*Rp)[JV_NU2] = sh.rec[ci & 1][two ? fr.set : 0];
       for (int p = grp; p < np; p += NG) {
@@ -1064,7 +1067,8 @@ __device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared& sh, int L, 
 // ms per step at 4).
 template <int MINB, int NT>
 __global__ void __launch_bounds__(NT, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
-  __shared__ __align__(16) JvpShared sh;
+  constexpr int CH = NT == 128 ? 64 : JV_CHUNK;
+  __shared__ __align__(16) JvpShared<CH> sh;
   const int L = blockIdx.x;
   const int tid = threadIdx.x;
   const int FTL = a.ft;
@@ -1097,11 +1101,11 @@ __global__ void __launch_bounds__(NT, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
     switch (fam) {
       case FAM_NH3_INV:
       case FAM_H2S:
-      case FAM_PH3: jv_family<JK_BR>(a, sh, L, fam, fr, on, base, dbase); break;
+      case FAM_PH3: jv_family<JK_BR, CH>(a, sh, L, fam, fr, on, base, dbase); break;
       case FAM_NH3_ROT:
-      case FAM_NH3_V2: jv_family<JK_GROSS>(a, sh, L, fam, fr, on, base, dbase); break;
-      case FAM_H2O: jv_family<JK_VVW>(a, sh, L, fam, fr, on, base, dbase); break;
-      default: jv_family<JK_SJS>(a, sh, L, fam, fr, on, base, dbase); break;
+      case FAM_NH3_V2: jv_family<JK_GROSS, CH>(a, sh, L, fam, fr, on, base, dbase); break;
+      case FAM_H2O: jv_family<JK_VVW, CH>(a, sh, L, fam, fr, on, base, dbase); break;
+      default: jv_family<JK_SJS, CH>(a, sh, L, fam, fr, on, base, dbase); break;
     }
   }
   // h2o base term summed over the CTA (every thread built some lines)
@@ -1286,7 +1290,7 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   // threads per CTA: one line group for 128-frequency tiles (no per-family
   // reduction across groups; C4 412 -> 371 ms), two or four otherwise
   const int nt = jv.threads ? jv.threads : (jv.ft >= 128 ? 128 : 256);
-  if (nt == 128) rb_alpha_jvp_kernel<4, 128><<<grid, 128, 0, st>>>(jv);
+  if (nt == 128) rb_alpha_jvp_kernel<5, 128><<<grid, 128, 0, st>>>(jv);
   else if (ctas >= 4) rb_alpha_jvp_kernel<4, 256><<<grid, 256, 0, st>>>(jv);
   else rb_alpha_jvp_kernel<3, 256><<<grid, 256, 0, st>>>(jv);
   if (ea) {
