@@ -210,18 +210,37 @@ __device__ __forceinline__ double edge_dist(const double* rot, double b0, double
 // meets the sphere of radius max(1, k) that encloses the top shell at
 // z = -B +/- sqrt(B^2 - A + K^2); every trial above the upper crossing is
 // outside.  i0 = -1: the line misses that sphere (no trial is inside).
+// Guard band of the float32 trial test: |g| below it is decided in float64.
+// g = |v|^2 - |v|^4 - (1 - k^2) v_y^2 with |v| <= ~1.1 carries a float32
+// error below ~2e-6 (trial point, rotation and products each within a few
+// ulp of 1).
+constexpr float EDGE_G_BAND = 3e-5f;
+
 struct EdgeMarch {
   double b0, b1, start, delta, c, ef2_eq;
   long ntrial, i0;
+  float px, py, pz, qx, qy, qz, startf, deltaf, cf;   // trial point = P + z Q in float32
   __device__ __forceinline__ double z(long i) const { return i == 0 ? start : start + (double)i * delta; }
   // r1 < r2 of raypath.py:66-80 without square roots:
   // |v|^2 < (k^2 v_y^2 + v_x^2 + v_z^2) / |v|^2  <=>  |v|^2 - |v|^4 > (1 - k^2) v_y^2
   // (v_y == 0 takes the reference's lat = 1e-6 rad rule).
-  __device__ __forceinline__ bool inside(const double* rot, long i) const {
+  __device__ __forceinline__ bool inside64(const double* rot, long i) const {
     double vx, vy, vz;
     rot_apply(rot, b0, b1, z(i), vx, vy, vz);
     const double rho = vx * vx + vy * vy + vz * vz;
     return vy == 0.0 ? rho < ef2_eq : rho - rho * rho > c * (vy * vy);
+  }
+  // The same test, decided in float32 where g is outside the guard band
+  // (GB300 runs float32 ~64x faster per warp instruction than float64); the
+  // first inside trial is therefore the float64 march's.
+  __device__ __forceinline__ bool inside(const double* rot, long i) const {
+    const float zf = i == 0 ? startf : fmaf((float)i, deltaf, startf);
+    const float vx = fmaf(zf, qx, px), vy = fmaf(zf, qy, py), vz = fmaf(zf, qz, pz);
+    const float rho = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+    const float g = fmaf(-rho, rho, rho) - cf * (vy * vy);
+    if (g > EDGE_G_BAND) return true;
+    if (g < -EDGE_G_BAND) return false;
+    return inside64(rot, i);
   }
 };
 
@@ -238,6 +257,15 @@ __device__ __forceinline__ EdgeMarch edge_march(const double* rot, double b0, do
   double px, py, pz, qx, qy, qz;
   rot_apply(rot, b0, b1, 0.0, px, py, pz);
   rot_apply(rot, 0.0, 0.0, 1.0, qx, qy, qz);
+  m.px = (float)px;
+  m.py = (float)py;
+  m.pz = (float)pz;
+  m.qx = (float)qx;
+  m.qy = (float)qy;
+  m.qz = (float)qz;
+  m.startf = (float)m.start;
+  m.deltaf = (float)m.delta;
+  m.cf = (float)m.c;
   const double K2 = k > 1.0 ? k * k : 1.0;
   const double A = px * px + py * py + pz * pz, B = px * qx + py * qy + pz * qz;
   const double disc = B * B - A + K2;

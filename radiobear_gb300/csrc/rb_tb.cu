@@ -123,10 +123,7 @@ __global__ void __launch_bounds__(128) rb_tb_chunk_kernel(TbArgs a) {
   const int nsteps = nseg - 1;                 // segments used by the scan
   const int i0 = ch * TB_CHUNK;
   float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
-  if (i0 >= nsteps) {                          // chunk past the end of this ray
-    if (f < a.nf) part[f] = make_float4(0.f, 0.f, 0.f, 0.f);
-    return;
-  }
+  if (i0 >= nsteps) return;                    // chunk past the end of this ray (never read)
   const int n = min(TB_CHUNK, nsteps - i0);
   __shared__ int s_off[TB_CHUNK + 1];
   __shared__ float s_T[TB_CHUNK + 1];
@@ -218,20 +215,82 @@ __host__ __device__ __forceinline__ int scan_lanes(int npair) {
   while (l < npair && l < 128) l <<= 1;
   return l;
 }
-constexpr int SCAN_ITEM_WORDS = 3 * TB_CHUNK + 2;   // staged words per item
+// Staged float4 per item: entry 0 {T_0, w_0, T_0 w_0, row offset of node 0},
+// entry k + 1 {hd_k, w_{k+1}, T_{k+1} w_{k+1}, row offset of node k + 1} for
+// step k (node k -> k + 1), with the trapezoid weight of node j inside the
+// chunk w_j = hd_{j-1} + hd_j (hd_{-1} = hd_n = 0 at the chunk's ends).
+constexpr int SCAN_ITEM_F4 = TB_CHUNK + 1;
+constexpr int SCAN_FLUSH = 16;   // steps per float32 block sum
 
-// The 6-CTA bound lets the compiler keep 32 steps of alpha loads in flight
-// (~70 registers): measured against the unbounded kernel (54 registers, 16
-// steps), C1's scan 0.0368 -> 0.0316 ms and C2's 0.416 -> 0.401 ms.
-__global__ void __launch_bounds__(128, 6) rb_tb_chunk2_kernel(TbArgs a) {
+// exp(-x) of both halves as 2^(-x log2(e)): one packed multiply and the
+// PTX base-2 exponential approximation with flush to zero (a result below
+// 2^-126, an optical depth above ~87, is 0: its weight in every sum is far
+// below the float32 rounding of the sum).
+__device__ __forceinline__ f2 exp_neg2(f2 x) {
+  const f2 y = mul2(x, dup(-1.4426950408889634f));
+  float lo = lo2(y), hi = hi2(y);
+  asm("ex2.approx.ftz.f32 %0, %0;" : "+f"(lo));
+  asm("ex2.approx.ftz.f32 %0, %0;" : "+f"(hi));
+  return pk(lo, hi);
+}
+
+// Running state of one thread's frequency pair in the packed scan.
+struct ScanPair {
+  f2 a0;                    // alpha at the previous node
+  f2 th, ntl;               // optical depth th - ntl
+  f2 iwb, tbb;              // current float32 block sums
+  f2 iw, iwc, tb, tbc;      // Kahan sums of the blocks
+  __device__ __forceinline__ void init(f2 a, f2 iw0, f2 tb0) {
+    a0 = a;
+    th = ntl = 0ull;
+    iwb = iw0;
+    tbb = tb0;
+    iw = iwc = tb = tbc = 0ull;
+  }
+  // step k: e = {hd_k, w_{k+1}, T_{k+1} w_{k+1}, -}, a1 = alpha at node k + 1
+  __device__ __forceinline__ void step(f2 a1, const float4& e) {
+    const f2 x = mul2(add2(a0, a1), dup(e.x));
+    const f2 s = add2(th, x);
+    ntl = add2(ntl, sub2(sub2(s, th), x));   // -(Fast2Sum error)
+    th = s;
+    const f2 ax = mul2(a1, exp_neg2(th));
+    const f2 W1 = fma2(ax, ntl, ax);
+    iwb = fma2(W1, dup(e.y), iwb);
+    tbb = fma2(W1, dup(e.z), tbb);
+    a0 = a1;
+  }
+  __device__ __forceinline__ void flush() {
+    kahan_add2(iw, iwc, iwb);
+    kahan_add2(tb, tbc, tbb);
+    iwb = tbb = 0ull;
+    const f2 s = sub2(th, ntl);              // renormalise: (th, tl) = Fast2Sum(th, tl)
+    ntl = add2(ntl, sub2(s, th));
+    th = s;
+  }
+};
+
+// The chunk's sums regrouped by node: sum_k (W_{k+1} + W_k) hd_k =
+// sum_j W_j w_j, and likewise for T W, so a step adds W_{k+1} times two
+// staged per-node weights.  The node sums run as float32 blocks of
+// SCAN_FLUSH terms (all positive: <= 16 ulp each) added into Kahan sums.
+// The optical depth is a float32 running sum th with its rounding errors
+// collected exactly (Fast2Sum) in tl, renormalised into (th, tl) once per
+// block: exp(-tau) = exp(-th) (1 - tl) to O(tl^2).  Fast2Sum is exact while
+// th >= the step's increment; a step larger than the running sum at least
+// doubles it, so such steps are few and their error stays ~ulp(tau).
+//
+// The 5-CTA bound (96 registers) lets the compiler keep 32 steps of alpha
+// loads in flight without spilling: C1 scan 0.0292 ms unbounded (46
+// registers) / 0.0272 ms at 6 CTAs (80 registers, spills) / 0.0272 ms at 5;
+// C2 0.52 / 0.43 / 0.39 ms.
+__global__ void __launch_bounds__(128, 5) rb_tb_chunk2_kernel(TbArgs a) {
   const int npair = a.nf / 2;
   const int FP = a.lanes ? a.lanes : scan_lanes(npair);
   const int IPB = 128 / FP;
   const int sub = threadIdx.x / FP, fl = threadIdx.x % FP;
   const long long item = (long long)blockIdx.x * IPB + sub;
   const long long nitem = (long long)a.nb * a.nchunk;
-  // per item: offsets, T (TB_CHUNK + 1 each) and ds / 2 (TB_CHUNK)
-  extern __shared__ __align__(16) int s_scan[];
+  extern __shared__ __align__(16) float4 s_scan4[];
   int ray = 0, ch = 0, n = 0, i0 = 0;
   bool live = false;
   if (item < nitem) {
@@ -245,81 +304,101 @@ __global__ void __launch_bounds__(128, 6) rb_tb_chunk2_kernel(TbArgs a) {
     n = live ? min(TB_CHUNK, nsteps - i0) : 0;
   }
   const int f = 2 * (blockIdx.z * FP + fl);   // first of the pair
-  float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
-  if (item < nitem && !live && f < a.nf) {     // chunk past the end of this ray
-    part[f] = make_float4(0.f, 0.f, 0.f, 0.f);
-    part[f + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  int* s_off = s_scan + sub * SCAN_ITEM_WORDS;
-  float* s_T = reinterpret_cast<float*>(s_off + TB_CHUNK + 1);
-  float* s_hd = s_T + TB_CHUNK + 1;
+  // a chunk past the end of its ray writes nothing: the combine and the
+  // adjoint read the partials of a ray's live chunks only
+  float4* sp = s_scan4 + sub * SCAN_ITEM_F4;
+  // Staging in two passes.  1: the item's lanes load node t's layer, T and
+  // hd_t (four nodes per lane at a time, independent loads) into entry t
+  // {-, -, T_t, offset} and entry t + 1 {hd_t, ...}.  2: the node weights
+  // from the staged hd.
   if (live) {
     const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
     const int* lay = a.layer + (size_t)ray * a.max_seg + i0;
     int off, nLr;
     ray_layers(a, ray, off, nLr);
+    for (int t0 = fl; t0 <= n; t0 += 4 * FP) {
+      int lv[4];
+      float hv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * FP;
+        lv[u] = t <= n ? lay[t] : 0;
+        hv[u] = t < n ? hds[t] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * FP;
+        if (t > n) break;
+        const int l = off + wrap_layer(lv[u], nLr);
+        sp[t].z = a.T32[l];
+        sp[t].w = __int_as_float(l * a.nf);
+        if (t < n) sp[t + 1].x = hv[u];
+      }
+    }
+  }
+  __syncthreads();
+  if (live) {
     for (int t = fl; t <= n; t += FP) {
-      const int l = off + wrap_layer(lay[t], nLr);
-      s_off[t] = l * a.nf;
-      s_T[t] = a.T32[l];
-      if (t < n) s_hd[t] = hds[t];
+      const float hp = t > 0 ? sp[t].x : 0.f;
+      const float hc = t < n ? sp[t + 1].x : 0.f;
+      const float w = hp + hc, T = sp[t].z;
+      sp[t].y = w;
+      sp[t].z = T * w;
+      if (t == 0) sp[0].x = T;
     }
   }
   __syncthreads();
   if (!live || f >= a.nf) return;
   const float* al = a.alpha32 + f;
-  auto ld = [&](int o) -> f2 { return *reinterpret_cast<const f2*>(al + o); };
-  f2 th = 0ull, tl = 0ull;
-  f2 a0 = ld(s_off[0]);
-  f2 W0 = (i0 == 0) ? 0ull : a0;
-  f2 T0 = dup(s_T[0]);
-  f2 iw = 0ull, iwc = 0ull, tb = 0ull, tbc = 0ull;
-  const f2 one = dup(1.f);
+  auto ld = [&](const float4& e) -> f2 {
+    return *reinterpret_cast<const f2*>(al + __float_as_int(e.w));
+  };
+  // alpha row of node j read ahead: the offset alone, by its own shared
+  // load, so the step's record is not kept in registers from the prefetch
+  auto ld_ahead = [&](int j) -> f2 {
+    int o;
+    asm volatile("ld.shared.b32 %0, [%1];"
+                 : "=r"(o)
+                 : "r"((unsigned)__cvta_generic_to_shared(&sp[j].w)));
+    return *reinterpret_cast<const f2*>(al + o);
+  };
+  const float4 e0 = sp[0];
+  f2 a0 = ld(e0);
+  // node 0: W_0 = 0 on a path's first chunk, exp(0) a_0 otherwise
+  f2 iwb = 0ull, tbb = 0ull;
+  if (i0 > 0) {
+    iwb = mul2(a0, dup(e0.y));
+    tbb = mul2(a0, dup(e0.z));
+  }
+  ScanPair st;
+  st.init(a0, iwb, tbb);
   int i = 0;
   constexpr int BLK = 32;   // steps whose alpha loads are in flight together
   for (; i + BLK <= n; i += BLK) {
     f2 an[BLK];
 #pragma unroll
-    for (int k = 0; k < BLK; ++k) an[k] = ld(s_off[i + 1 + k]);
+    for (int k = 0; k < BLK; ++k) an[k] = ld_ahead(i + 1 + k);
 #pragma unroll
     for (int k = 0; k < BLK; ++k) {
-      const f2 hd = dup(s_hd[i + k]);
-      const f2 a1 = an[k];
-      const f2 T1 = dup(s_T[i + 1 + k]);
-      f2 ss, e;
-      two_sum2(th, mul2(add2(a0, a1), hd), ss, e);
-      e = add2(e, tl);
-      th = add2(ss, e);
-      tl = sub2(e, sub2(th, ss));
-      const f2 ex = pk(__expf(-lo2(th)), __expf(-hi2(th)));
-      const f2 W1 = mul2(mul2(a1, ex), sub2(one, tl));
-      kahan_add2(iw, iwc, mul2(add2(W1, W0), hd));
-      kahan_add2(tb, tbc, mul2(fma2(T1, W1, mul2(T0, W0)), hd));
-      W0 = W1;
-      T0 = T1;
-      a0 = a1;
+      st.step(an[k], sp[i + 1 + k]);
+      if (k % SCAN_FLUSH == SCAN_FLUSH - 1) st.flush();
     }
   }
-  for (; i < n; ++i) {
-    const f2 hd = dup(s_hd[i]);
-    const f2 a1 = ld(s_off[i + 1]);
-    const f2 T1 = dup(s_T[i + 1]);
-    f2 ss, e;
-    two_sum2(th, mul2(add2(a0, a1), hd), ss, e);
-    e = add2(e, tl);
-    th = add2(ss, e);
-    tl = sub2(e, sub2(th, ss));
-    const f2 ex = pk(__expf(-lo2(th)), __expf(-hi2(th)));
-    const f2 W1 = mul2(mul2(a1, ex), sub2(one, tl));
-    kahan_add2(iw, iwc, mul2(add2(W1, W0), hd));
-    kahan_add2(tb, tbc, mul2(fma2(T1, W1, mul2(T0, W0)), hd));
-    W0 = W1;
-    T0 = T1;
-    a0 = a1;
+#pragma unroll 1
+  for (int k = 0; i < n; ++i) {
+    const float4 e = sp[i + 1];
+    st.step(ld(e), e);
+    if (++k == SCAN_FLUSH) {
+      k = 0;
+      st.flush();
+    }
   }
-  const f2 IW = sub2(iw, iwc), TB = sub2(tb, tbc);
-  part[f] = make_float4(lo2(th), lo2(tl), lo2(IW), lo2(TB));
-  part[f + 1] = make_float4(hi2(th), hi2(tl), hi2(IW), hi2(TB));
+  st.flush();
+  const f2 IW = sub2(st.iw, st.iwc), TB = sub2(st.tb, st.tbc);
+  const f2 tl = sub2(0ull, st.ntl);
+  float4* part = a.part + ((size_t)ray * a.nchunk + ch) * a.nf;
+  part[f] = make_float4(lo2(st.th), lo2(tl), lo2(IW), lo2(TB));
+  part[f + 1] = make_float4(hi2(st.th), hi2(tl), hi2(IW), hi2(TB));
 }
 
 // Combine chunk partials of each (ray, frequency) into Tb.
@@ -405,7 +484,7 @@ cudaError_t launch_tb_chunked(const TbArgs& a, cudaStream_t st) {
     const long long nitem = (long long)a.nb * a.nchunk;
     const long long nblk = (nitem + 128 / FP - 1) / (128 / FP);
     dim3 grid((unsigned)nblk, 1, (a.nf / 2 + FP - 1) / FP);
-    const size_t smem = sizeof(int) * SCAN_ITEM_WORDS * (128 / FP);
+    const size_t smem = sizeof(float4) * SCAN_ITEM_F4 * (128 / FP);
     rb_tb_chunk2_kernel<<<grid, 128, smem, st>>>(a);
   } else {
     dim3 grid(a.nb, a.nchunk, (a.nf + 127) / 128);
