@@ -83,6 +83,17 @@ GRAD_WORKLOAD = ('C3 differentiable forward model: 1000 layers (1e-3..500 bar) x
                  'dTb/dT, dTb/dP, dTb/dlnX(NH3, H2O, H2S) per layer')
 
 
+def adjoint_mode(dev, nL, nf):
+    """How the adjoint entry points get d alpha / d theta at this size
+    (RB_TUNE_ADJ_MODE automatic: stored when nL x nf x 5 floats take at most
+    an eighth of the device memory)."""
+    import torch
+    nbytes = 4 * 5 * int(nL) * int(nf)
+    stored = nbytes <= torch.cuda.get_device_properties(dev).total_memory // 8
+    return dict(mode='stored d alpha/d theta' if stored else 'recomputed after the reverse sweep',
+                stored_bytes=nbytes if stored else 0)
+
+
 def measure_gradients(args, dev, stream, flush, pool=None):
     """Spectra + gradients per second on the C3 workload: each step runs
     rb_adjoint_device (forward, then the adjoint with alpha recomputed)
@@ -154,6 +165,7 @@ def measure_gradients(args, dev, stream, flush, pool=None):
     out = dict(metric='disc-avg Tb spectra + dTb/dT, dTb/dP, dTb/dlnX gradients per second',
                value=1e3 / ms, unit='spectra+gradients/s', ms_per_step=ms, steps=n,
                config=dict(workload=GRAD_WORKLOAD, layers=nL, freqs=nf, rays=nb,
+                           adjoint=adjoint_mode(dev, nL, nf),
                            jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1], threads=jbest[2]),
                            jvp_tuning_ms={','.join(map(str, k)): v for k, v in jt.items()}),
                gpu_launches_per_step=int(launches),
@@ -176,8 +188,9 @@ BATCH_WORKLOAD = ('C4 batched retrieval sweep: {n} variants of the 1e-3..100 bar
                   'log-U 1e-4..1e-3, deep T offset U(-10, 10) K, 300..1200 layers), 128 freqs '
                   '(0.5..50 GHz log), 32-ray disc quadrature, configuration-0 line lists; forward '
                   'Tb_avg + adjoint dTb/dT, dTb/dP, dTb/dlnX for every variant per step, replayed '
-                  'from one captured CUDA graph, line-sum tiling and JVP launch shape from the '
-                  'autotuner')
+                  'from one captured CUDA graph; alpha and d alpha/d theta from one JVP pass before '
+                  'the scan (d alpha/d theta stored, contracted after the reverse sweep), JVP '
+                  'launch shape from the autotuner')
 
 
 def measure_batch(args, dev, n_var, pool=None):
@@ -230,10 +243,6 @@ def measure_batch(args, dev, n_var, pool=None):
                                  avg.data_ptr(), gT.data_ptr(), gP.data_ptr(), gX.data_ptr(),
                                  71492.0, 66854.0)
 
-    best, tt = tune.tune_alpha(eng, step, key=tune.workload_key('batch', dict(freqs=freqs, lines=lines),
-                                                             nb, layers=(300, 1200)),
-                               candidates=((2, 2, 1024), (2, 4, 1024), (4, 1, 1024), (4, 2, 1024)),
-                               reps=1, stream=stream)
     jbest, jt = tune.tune_adjoint(eng, step, key=tune.workload_key('batch', dict(freqs=freqs, lines=lines),
                                                                   nb, layers=(300, 1200)),
                                   reps=1, stream=stream)
@@ -304,8 +313,7 @@ def measure_batch(args, dev, n_var, pool=None):
                 value=value, unit='spectra+gradients/s', ms_per_step=ms, steps=n, finite=ok,
                 config=dict(workload=BATCH_WORKLOAD.format(n=n_var), variants=n_var,
                             layers_total=NLT, freqs=nf, rays_per_variant=nb,
-                            tiling=dict(M=best[0], W=best[1], item_lines=best[2]),
-                            tuning_ms={'{},{},{}'.format(*k): v for k, v in tt.items()},
+                            adjoint=adjoint_mode(dev, NLT, nf),
                             jvp=dict(freqs_per_cta=jbest[0], ctas_per_sm=jbest[1], threads=jbest[2]),
                             jvp_tuning_ms={','.join(map(str, k)): v for k, v in jt.items()},
                             l2='working set of tens of GB, larger than L2'),

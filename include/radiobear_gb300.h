@@ -164,11 +164,19 @@ int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines);
  * per CTA (128 or 256, a multiple of the frequencies per CTA; the threads
  * beyond the frequencies split the lines); RB_TUNE_SCAN_LANES:
  * frequency-pair lanes per (ray, chunk) item of the brightness scan (a
- * power of two in 4..128; a CTA of 128 threads takes 128 / lanes items). */
+ * power of two in 4..128; a CTA of 128 threads takes 128 / lanes items).
+ * RB_TUNE_ADJ_MODE: how the adjoint entry points get d alpha / d theta.
+ * 1 (stored): the JVP runs before the scan, gives the scan's alpha and
+ * stores d alpha / d theta (nL x nf x 20 bytes), contracted with
+ * d loss / d alpha after the reverse sweep; 2 (recomputed): the forward
+ * line sums give alpha and the JVP runs after the reverse sweep, contracting
+ * as it goes (no per-frequency storage); 0 (automatic): stored when that
+ * takes at most an eighth of the device memory. */
 #define RB_TUNE_JVP_FREQS 1
 #define RB_TUNE_JVP_CTAS 2
 #define RB_TUNE_SCAN_LANES 3
 #define RB_TUNE_JVP_THREADS 4
+#define RB_TUNE_ADJ_MODE 5
 int rb_set_tuning(rb_handle* h, int param, int value);
 
 /* Absorption of nL layers at nf frequencies.

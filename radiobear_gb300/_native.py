@@ -413,7 +413,7 @@ class Engine:
         _check(self.lib, self.lib.rb_set_alpha_tiling(self._h, int(M), int(W), int(item_lines)),
                'rb_set_alpha_tiling')
 
-    TUNING = dict(jvp_freqs=1, jvp_ctas=2, scan_lanes=3, jvp_threads=4)   # RB_TUNE_*
+    TUNING = dict(jvp_freqs=1, jvp_ctas=2, scan_lanes=3, jvp_threads=4, adj_mode=5)   # RB_TUNE_*
 
     def set_tuning(self, **kw):
         """Launch shapes (rb_set_tuning): jvp_freqs (32/64/128), jvp_ctas (3/4),

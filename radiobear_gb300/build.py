@@ -25,7 +25,7 @@ LIB = os.path.join(LIBDIR, 'librbgpu.so')
 SOURCES = ['rb_alpha.cu', 'rb_raypath.cu', 'rb_tb.cu', 'rb_probe.cu', 'rb_noalloc.cu', 'rb_adjoint.cu',
            'rb_extra.cu', 'rb_atm.cu',
            'rb_api.cu']
-HEADERS = ['rb_common.cuh', 'rb_args.cuh', 'rb_f32x2.cuh', 'rb_expint.cuh']
+HEADERS = ['rb_common.cuh', 'rb_args.cuh', 'rb_f32x2.cuh', 'rb_expint.cuh', 'rb_assemble.cuh']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
               '-Xptxas', '-v'] + ARCH

@@ -34,6 +34,7 @@
 //   rb_adjoint_final_kernel adds the source-temperature term and writes
 //                           dTb/dT, dTb/dP, dTb/dln X.
 #include "rb_args.cuh"
+#include "rb_assemble.cuh"
 #include "rb_expint.cuh"
 #include "rb_f32x2.cuh"
 #include <math_constants.h>
@@ -1134,7 +1135,7 @@ __global__ void __launch_bounds__(NT, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
   if (on && grp == 0) {
     auto fv = [&](int fam) { return sh.fam[fam][fi][0]; };
     auto fd = [&](int fam) { return &sh.fam[fam][fi][1]; };
-    const float gal = a.galpha[(size_t)L * a.nf + j];
+    const float gal = a.alpha_out ? 0.f : a.galpha[(size_t)L * a.nf + j];
     const float Fd = fr.F + fr.FL, Fhd = fr.Fh + fr.FhL;
     auto pref = [&](int fam) { return ldexpf(lp.fam[fam].fm, lp.fam[fam].fe); };
     // d(pref * S) / dtheta for a family with tangent triple (T, P, X_own)
@@ -1199,8 +1200,25 @@ __global__ void __launch_bounds__(NT, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
       }
       for (int q = 0; q < NTH; ++q) dal[q] += lp.scale[GAS_NH3] * dn[q];
     }
+    if (a.alpha_out) {
+      // stored-tangent mode: the scan's alpha (the assembly kernel's float32
+      // arithmetic on the same family sums) and d alpha / d theta
+      double co = 0.0, cl = 0.0;
+      if (a.extra) {
+        co = a.extra[(size_t)L * a.nf + j];
+        cl = a.extra[((size_t)a.nL + L) * a.nf + j];
+      }
+      float g32[NGAS];
+      assemble<float>(lp, a.cfg, Fd, Fhd, set, fv(FAM_NH3_INV), fv(FAM_NH3_ROT), fv(FAM_NH3_V2),
+                      fv(FAM_NH3_SJS), fv(FAM_H2O), base, fv(FAM_H2S), fv(FAM_PH3), co, cl, g32);
+      float tot = 0.f;
+      for (int k = 0; k < NGAS; ++k) tot += g32[k];
+      a.alpha_out[(size_t)L * a.nf + j] = tot;
+      for (int q = 0; q < NTH; ++q) a.dal_out[((size_t)L * NTH + q) * a.nf + j] = dal[q];
+    }
     for (int q = 0; q < NTH; ++q) g5[q] = gal * dal[q];
   }
+  if (a.alpha_out) return;   // uniform: a kernel argument
   // reduce over the CTA's frequencies as double-floats (terms of both signs
   // meet here; GB300's float64 rate made the float64 shuffles a tenth of the
   // batched kernel); only the warps of line group 0 hold values: FTL is a
@@ -1260,12 +1278,59 @@ __global__ void rb_adjoint_final_kernel(int nL, int nf, int ntile, const float2*
   dlnX[2 * nL + L] = s[TH_XH2S];
 }
 
+// Stored-tangent adjoint: d loss / d theta of each layer is the sum over
+// frequencies of d loss / d alpha times the stored d alpha / d theta, plus
+// the source term (dT) and the co_ddb / clouds_idp terms.  One warp per
+// layer, lanes over frequencies: products in float32 as in the contracting
+// JVP, sums as double-floats (terms of both signs), hi + lo in float64.
+__global__ void __launch_bounds__(128) rb_adjoint_contract_kernel(int nL, int nf, const float* galpha,
+                                                                  const float* dal, const double* gsrc,
+                                                                  const double* gextra, double* dT,
+                                                                  double* dP, double* dlnX) {
+  const int L = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (L >= nL) return;   // whole warps: L is uniform in a warp
+  const float* g = galpha + (size_t)L * nf;
+  const float* d = dal + (size_t)L * NTH * nf;
+  float hi[NTH], lo[NTH];
+#pragma unroll
+  for (int q = 0; q < NTH; ++q) hi[q] = lo[q] = 0.f;
+  for (int j = lane; j < nf; j += 32) {
+    const float gj = __ldcs(g + j);
+#pragma unroll
+    for (int q = 0; q < NTH; ++q) dfs_add(hi[q], lo[q], gj * __ldcs(d + (size_t)q * nf + j));
+  }
+  double s[NTH];
+#pragma unroll
+  for (int q = 0; q < NTH; ++q) {
+    for (int o = 16; o; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, hi[q], o);
+      const float l2 = __shfl_xor_sync(0xffffffffu, lo[q], o);
+      float t, e;
+      two_sum(hi[q], h2, t, e);
+      e += lo[q] + l2;
+      hi[q] = t + e;
+      lo[q] = e - (hi[q] - t);
+    }
+    s[q] = (double)hi[q] + (double)lo[q];
+  }
+  if (lane) return;
+  if (gextra) {
+    s[TH_T] += gextra[2 * L];
+    s[TH_P] += gextra[2 * L + 1];
+  }
+  dT[L] = s[TH_T] + gsrc[L];
+  dP[L] = s[TH_P];
+  dlnX[L] = s[TH_XNH3];
+  dlnX[nL + L] = s[TH_XH2O];
+  dlnX[2 * nL + L] = s[TH_XH2S];
+}
+
 // ------------------------------------------------------------------ launch
 cudaError_t launch_extra_vjp(const ExtraArgs& ea, cudaStream_t st);
 
-cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
-                           const ExtraArgs* ea, float* galpha, double* gsrc, double* dT, double* dP,
-                           double* dlnX, cudaStream_t st) {
+// d loss / d alpha and the source term: zeroed, then the reverse sweep.
+cudaError_t launch_adjoint_sweep(const TbAdjArgs& ta, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(ta.ga, 0, sizeof(float) * (size_t)ta.nL * ta.nf, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(ta.gs, 0, sizeof(double) * (size_t)ta.nL, st);
   if (e != cudaSuccess) return e;
@@ -1278,6 +1343,11 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
     rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);
     rb_tb_adj_grad_kernel<<<grid, blk, 0, st>>>(ta);
   }
+  return cudaGetLastError();
+}
+
+// Layer tangents, then the JVP kernel in the launch shape of jv.
+static cudaError_t launch_tan_jvp(const TanArgs& tn, const JvpArgs& jv, cudaStream_t st) {
   rb_layer_tan_kernel<<<(((tn.nL + 31) & ~31) * 8 + 63) / 64, 64, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
 #ifndef RB_JVP_MINB128
@@ -1293,12 +1363,44 @@ cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs
   if (nt == 128) rb_alpha_jvp_kernel<5, 128><<<grid, 128, 0, st>>>(jv);
   else if (ctas >= 4) rb_alpha_jvp_kernel<4, 256><<<grid, 256, 0, st>>>(jv);
   else rb_alpha_jvp_kernel<3, 256><<<grid, 256, 0, st>>>(jv);
+  return cudaGetLastError();
+}
+
+// Recomputing adjoint: the reverse sweep, then alpha's JVP contracted with
+// d loss / d alpha, then the per-layer sums.
+cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
+                           const ExtraArgs* ea, float* galpha, double* gsrc, double* dT, double* dP,
+                           double* dlnX, cudaStream_t st) {
+  cudaError_t e = launch_adjoint_sweep(ta, st);
+  if (e == cudaSuccess) e = launch_tan_jvp(tn, jv, st);
+  if (e != cudaSuccess) return e;
   if (ea) {
     cudaError_t x = launch_extra_vjp(*ea, st);
     if (x != cudaSuccess) return x;
   }
+  const int ntile = (jv.nf + jv.ft - 1) / jv.ft;
   rb_adjoint_final_kernel<<<(jv.nL + 127) / 128, 128, 0, st>>>(
-      jv.nL, jv.nf, grid.y, jv.part, gsrc, ea ? ea->grad : nullptr, dT, dP, dlnX);
+      jv.nL, jv.nf, ntile, jv.part, gsrc, ea ? ea->grad : nullptr, dT, dP, dlnX);
+  return cudaGetLastError();
+}
+
+// Stored-tangent adjoint, forward half: layer tangents and the JVP writing
+// alpha and d alpha / d theta (jv.alpha_out, jv.dal_out) for the scan.
+cudaError_t launch_jvp_store(const TanArgs& tn, const JvpArgs& jv, cudaStream_t st) {
+  return launch_tan_jvp(tn, jv, st);
+}
+
+// Stored-tangent adjoint, after the reverse sweep: [co / clouds VJP,]
+// the contraction with d loss / d alpha.
+cudaError_t launch_adjoint_contract(const JvpArgs& jv, const ExtraArgs* ea, const float* galpha,
+                                    const double* gsrc, double* dT, double* dP, double* dlnX,
+                                    cudaStream_t st) {
+  if (ea) {
+    cudaError_t x = launch_extra_vjp(*ea, st);
+    if (x != cudaSuccess) return x;
+  }
+  rb_adjoint_contract_kernel<<<(jv.nL + 3) / 4, 128, 0, st>>>(
+      jv.nL, jv.nf, galpha, jv.dal_out, gsrc, ea ? ea->grad : nullptr, dT, dP, dlnX);
   return cudaGetLastError();
 }
 

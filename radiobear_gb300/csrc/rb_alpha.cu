@@ -40,6 +40,7 @@
 // double-float and split into integer and fractional parts before exp2.
 #include "rb_args.cuh"
 #include "rb_f32x2.cuh"
+#include "rb_assemble.cuh"
 #include <math_constants.h>
 
 #include <algorithm>
@@ -84,7 +85,7 @@ constexpr float HS_COEF = (float)(1.0E6 * 6.02297E23 / 8.31432E7);   // nh3_hs.p
 // GAMMA_H2, GAMMA_He, GAMMA_NH3, zeta_H2, zeta_He, zeta_NH3, Z_H2, Z_He,
 // Z_NH3, d; set 0 for f <= 30 GHz, set 1 above.  Table 0 nh3_hs
 // (nh3_hs.py:139-168), table 1 nh3_dbs (nh3_dbs.py:133-162: its own set 0,
-// set 1 equal to nh3_hs's).  INV_CON holds each set's Con.
+// set 1 equal to nh3_hs's).  Each set's Con is INV_CON (rb_assemble.cuh).
 __device__ constexpr float INV_SET[2][2][13] = {
     {{1.640f, 0.75f, 0.852f, 0.7756f, 0.666f, 1.0f, 1.262f, 0.3f, 0.5296f, 0.7964f, 0.667f, 1.554f,
       -0.0498f},
@@ -94,7 +95,6 @@ __device__ constexpr float INV_SET[2][2][13] = {
       1.3832f, -0.0139f},
      {1.7465f, 0.9779f, 0.7298f, 0.8202f, 1.0f, 1.0f, 1.2163f, 0.0291f, 0.5152f, 0.8873f, 0.8994f,
       0.66666667f, -0.0627f}}};
-__device__ constexpr float INV_CON[2][2] = {{0.9301f, 0.9862f}, {0.9619f, 0.9862f}};
 
 __device__ __forceinline__ float pw(float lg2x, float e) { return exp2f(e * lg2x); }
 
@@ -332,47 +332,6 @@ __global__ void __launch_bounds__(256) rb_layer_prep_kernel(PrepArgs a) {
       return;
     }
   }
-}
-
-// Assemble one slot: per-gas absorption (T = float or double), scaled.
-// co / cl are the co_ddb and clouds_idp absorption in cm^-1 (0 when off).
-template <typename T>
-__device__ __forceinline__ void assemble(const LayerParams& lp, const AlphaConfig& cfg, T F, T Fhs,
-                                         int set, float inv, float rot, float v2, float sjs,
-                                         float h2o, float base_h2o, float h2s, float ph3, double co,
-                                         double cl, T* g) {
-  const T U = cfg.units_db ? (T)434294.5 : (T)1;
-  for (int k = 0; k < NGAS; ++k) g[k] = (T)0;
-  auto sc = [](float m, int e, float v) -> T {
-    if (sizeof(T) == 4) return (T)ldexpf(m * v, e);
-    return (T)ldexp((double)m * (double)v, e);
-  };
-  if (cfg.use_h2) g[GAS_H2] = (T)lp.h2_cia * F * U;
-  if (cfg.use_h2o) {
-    const LayerFam& L = lp.fam[FAM_H2O];
-    g[GAS_H2O] = (sc(L.fm, L.fe, h2o - base_h2o) * F + (T)lp.h2o_cont * F) * U;
-  }
-  if (cfg.use_h2s) g[GAS_H2S] = sc(lp.fam[FAM_H2S].fm, lp.fam[FAM_H2S].fe, h2s) * F * U;
-  if (cfg.use_ph3) g[GAS_PH3] = sc(lp.fam[FAM_PH3].fm, lp.fam[FAM_PH3].fe, ph3) * F * U;
-  if (cfg.nh3_mode != NH3_OFF) {
-    T hs = (T)0, sj = (T)0;
-    if (lp.use_hs) {
-      hs = Fhs * (sc(lp.fam[FAM_NH3_INV].fm * INV_CON[cfg.inv_table][set], lp.fam[FAM_NH3_INV].fe, inv) +
-                  sc(lp.fam[FAM_NH3_ROT].fm, lp.fam[FAM_NH3_ROT].fe, rot) +
-                  sc(lp.fam[FAM_NH3_V2].fm, lp.fam[FAM_NH3_V2].fe, v2));
-      hs *= U;
-      if (hs < (T)0) hs = (T)1.0E-8;           // nh3_hs.py:311-312
-    }
-    if (lp.use_sjs) sj = sc(lp.fam[FAM_NH3_SJS].fm, lp.fam[FAM_NH3_SJS].fe, sjs) * F * U;
-    const T W = (T)lp.blendW;
-    if (lp.use_hs && lp.use_sjs)
-      g[GAS_NH3] = W * sj + ((T)1 - W) * hs;
-    else
-      g[GAS_NH3] = lp.use_hs ? hs : sj;
-  }
-  if (cfg.use_co) g[GAS_CO] = (T)co * U;
-  if (cfg.use_clouds) g[GAS_CLOUDS] = (T)cl * U;
-  for (int k = 0; k < NGAS; ++k) g[k] *= (T)lp.scale[k];
 }
 
 // ------------------------------------------------------------------ records

@@ -197,10 +197,12 @@ struct rb_handle {
   int plan_vbeg[rb::NFAM] = {}, plan_vend[rb::NFAM] = {};
   int tile_M = 0, tile_W = 0, item_lines = 0;   // rb_set_alpha_tiling (0: automatic)
   int jvp_ft = 0, jvp_ctas = 0, jvp_threads = 0, scan_lanes = 0;   // rb_set_tuning (0: automatic)
+  int adj_mode = 0;                                                  // RB_TUNE_ADJ_MODE
+  size_t dev_mem = 0;                                                // device memory (bytes)
   DBuf d_f, d_fhs, d_jfreq, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base;
   // adjoint workspaces
-  DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff;
+  DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff, d_dal;
   std::vector<int> batch_off;   // layer offsets of the last batch (d_voff)
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
@@ -263,6 +265,11 @@ int alpha_lines_occupancy(int M, int W);
 cudaError_t launch_adjoint(const TbAdjArgs& ta, const TanArgs& tn, const JvpArgs& jv,
                            const ExtraArgs* ea, float* galpha,
                            double* gsrc, double* dT, double* dP, double* dlnX, cudaStream_t st);
+cudaError_t launch_adjoint_sweep(const TbAdjArgs& ta, cudaStream_t st);
+cudaError_t launch_jvp_store(const TanArgs& tn, const JvpArgs& jv, cudaStream_t st);
+cudaError_t launch_adjoint_contract(const JvpArgs& jv, const ExtraArgs* ea, const float* galpha,
+                                    const double* gsrc, double* dT, double* dP, double* dlnX,
+                                    cudaStream_t st);
 int adjoint_tiles(int nf, int ft_forced);
 int adjoint_ft(int nf, int ft_forced);
 cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* dR2, float* dR,
@@ -583,12 +590,9 @@ void extra_args(rb_handle* h, rb::ExtraArgs& ea, int nL, const double* dP, const
   ea.out = h->d_extra.as<double>();
 }
 
-int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
-                  const double* dX, const double* dscale, int units_db, double* d_layers64,
-                  double* d_gas64) {
-  RB_CUDA(h->d_lp.ensure(sizeof(rb::LayerParams) * (size_t)nL));
-  const int nf = (int)h->plan_f.size();
-  RB_CUDA(h->d_a32.ensure(sizeof(float) * (size_t)nL * nf));
+// Layer prep arguments (d_lp must hold nL LayerParams).
+static rb::PrepArgs prep_args(rb_handle* h, int nL, const double* dP, const double* dT,
+                              const double* dX, const double* dscale, int units_db) {
   rb::PrepArgs pa{};
   pa.nL = nL;
   pa.P = dP;
@@ -606,6 +610,63 @@ int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const
   }
   pa.out = h->d_lp.as<rb::LayerParams>();
   pa.counter = h->d_counter.as<int>();
+  return pa;
+}
+
+// Layer tangents and the JVP of the stored-tangent adjoint (launched in
+// place of the forward line sums).
+struct AlphaJvp {
+  rb::TanArgs tn;
+  rb::JvpArgs jv;
+};
+
+// Stored-tangent forward absorption: prep, [co / clouds,] layer tangents and
+// the JVP, which writes the scan's float32 alpha into d_a32 and
+// d alpha / d theta into d_dal.
+static int enqueue_alpha_jvp(rb_handle* h, cudaStream_t st, int nL, const double* dP,
+                             const double* dT, const double* dX, const double* dscale,
+                             const AlphaJvp& aj) {
+  const int nf = (int)h->plan_f.size();
+  RB_CUDA(h->d_lp.ensure(sizeof(rb::LayerParams) * (size_t)nL));
+  RB_CUDA(h->d_a32.ensure(sizeof(float) * (size_t)nL * nf));
+  RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
+  RB_CUDA(h->d_dal.ensure(sizeof(float) * (size_t)nL * rb::NTH * nf));
+  const rb::PrepArgs pa = prep_args(h, nL, dP, dT, dX, dscale, 0);
+  rb::TanArgs tn = aj.tn;
+  tn.out = h->d_lt.as<rb::LayerTan>();
+  rb::JvpArgs jv = aj.jv;
+  jv.lp = h->d_lp.as<rb::LayerParams>();
+  jv.lt = h->d_lt.as<rb::LayerTan>();
+  jv.alpha_out = h->d_a32.as<float>();
+  jv.dal_out = h->d_dal.as<float>();
+  jv.galpha = nullptr;
+  jv.extra = nullptr;
+  rb::ExtraArgs ea{};
+  const bool extra = h->cfg.use_co || h->cfg.use_clouds;
+  if (extra) {
+    if (h->cfg.use_co && h->nco == 0) return fail(RB_ESTATE, "co_ddb selected but no CO lines uploaded");
+    RB_CUDA(h->d_extra.ensure(sizeof(double) * 2 * (size_t)nL * nf));
+    extra_args(h, ea, nL, dP, dT, dX);
+    jv.extra = ea.out;
+  }
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[0], st));
+  RB_CUDA(rb::launch_prep(pa, st));
+  if (extra) RB_CUDA(rb::launch_extra(ea, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[1], st));
+  RB_CUDA(rb::launch_jvp_store(tn, jv, st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[8], st));
+  if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[2], st));
+  h->launches += (extra ? 1 : 0) + 3;   // prep, [extra,] tangents, JVP
+  return RB_OK;
+}
+
+int enqueue_alpha(rb_handle* h, cudaStream_t st, int nL, const double* dP, const double* dT,
+                  const double* dX, const double* dscale, int units_db, double* d_layers64,
+                  double* d_gas64) {
+  RB_CUDA(h->d_lp.ensure(sizeof(rb::LayerParams) * (size_t)nL));
+  const int nf = (int)h->plan_f.size();
+  RB_CUDA(h->d_a32.ensure(sizeof(float) * (size_t)nL * nf));
+  const rb::PrepArgs pa = prep_args(h, nL, dP, dT, dX, dscale, units_db);
   rb::AlphaArgs aa{};
   aa.nL = nL;
   aa.nf = nf;
@@ -776,6 +837,8 @@ int rb_create(rb_handle** out, int device) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_dev, cudaEventDisableTiming);
+  size_t mem_free = 0;
+  if (e == cudaSuccess) e = cudaMemGetInfo(&mem_free, &h->dev_mem);
   if (e != cudaSuccess) {
     rb_destroy(h);
     return fail(RB_ECUDA, "stream/event creation: %s", cudaGetErrorString(e));
@@ -1026,6 +1089,10 @@ int rb_set_tuning(rb_handle* h, int param, int value) {
       if (!(value == 0 || (pow2 && value >= 4 && value <= 128)))
         return fail(RB_EINVAL, "RB_TUNE_SCAN_LANES must be 0 or a power of two in 4..128");
       h->scan_lanes = value;
+      break;
+    case RB_TUNE_ADJ_MODE:
+      if (value < 0 || value > 2) return fail(RB_EINVAL, "RB_TUNE_ADJ_MODE must be 0, 1 or 2");
+      h->adj_mode = value;
       break;
     default:
       return fail(RB_EINVAL, "unknown tuning parameter %d", param);
@@ -1314,7 +1381,7 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
                         const double* dX, const double* dR, const double* dN, const double* dscale,
                         double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
                         const double* db, const double* dw, int disc, double* dTb, double* davg,
-                        double* dl64, const Batch* bt = nullptr) {
+                        double* dl64, const Batch* bt = nullptr, const AlphaJvp* aj = nullptr) {
   const int nf = (int)h->plan_f.size();
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
   const int nvar = bt ? bt->nvar : 1;
@@ -1337,7 +1404,9 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
                             bt, nb)))
     return rc;
   RB_CUDA(cudaEventRecord(h->ev_join, h->side));
-  if ((rc = enqueue_alpha(h, st, nL, dP, dT, dX, dscale, 0, dl64, nullptr))) return rc;
+  if (aj) rc = enqueue_alpha_jvp(h, st, nL, dP, dT, dX, dscale, *aj);
+  else rc = enqueue_alpha(h, st, nL, dP, dT, dX, dscale, 0, dl64, nullptr);
+  if (rc) return rc;
   RB_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
   if (nbt > 0) {
     rb::TbArgs ta{};
@@ -1500,9 +1569,35 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   RB_CUDA(h->d_avg.ensure(sizeof(double) * (size_t)nvar * nf));
   double* dTb = Tb_out ? Tb_out : h->d_Tb.as<double>();
   double* davg = Tb_avg ? Tb_avg : (weights ? h->d_avg.as<double>() : nullptr);
+  rb::TanArgs tn{};
+  tn.nL = nL;
+  tn.P = P;
+  tn.T = T;
+  tn.X = X;
+  tn.nh3_mode = h->cfg.nh3_mode;
+  tn.h2state = h->cfg.h2state;
+  tn.inv_table = h->cfg.inv_table;
+  rb::JvpArgs jv{};
+  jv.nL = nL;
+  jv.nf = nf;
+  jv.ft = rb::adjoint_ft(nf, h->jvp_ft);
+  jv.ctas = h->jvp_ctas;
+  jv.threads = h->jvp_threads;
+  if (jv.threads && jv.threads % jv.ft)
+    return fail(RB_EINVAL, "JVP threads per CTA (%d) must be a multiple of its frequencies per CTA (%d)",
+                jv.threads, jv.ft);
+  jv.fplan = h->d_jfreq.as<rb::JvFreq>();
+  for (int f = 0; f < rb::NFAM; ++f) jv.tab[f] = h->fam[f].table();
+  jv.cfg = h->cfg;
+  jv.cfg.units_db = 0;
+  // d alpha / d theta stored from a JVP run before the scan (which also
+  // gives the scan's alpha), or recomputed after the reverse sweep
+  const size_t dal_bytes = sizeof(float) * (size_t)nL * rb::NTH * nf;
+  const bool store = h->adj_mode == 1 || (h->adj_mode == 0 && dal_bytes <= h->dev_mem / 8);
+  AlphaJvp aj{tn, jv};
   int rc;
   if ((rc = forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
-                         nb, b, weights, disc, dTb, davg, nullptr, bt)))
+                         nb, b, weights, disc, dTb, davg, nullptr, bt, store ? &aj : nullptr)))
     return rc;
   const int launches = h->launches;
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
@@ -1510,7 +1605,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   RB_CUDA(h->d_ga.ensure(sizeof(float) * (size_t)nL * nf));
   RB_CUDA(h->d_gs.ensure(sizeof(double) * (size_t)nL));
   RB_CUDA(h->d_lt.ensure(sizeof(rb::LayerTan) * nL));
-  RB_CUDA(h->d_jpart.ensure(sizeof(float2) * (size_t)nL * ntile * rb::NTH));
+  if (!store) RB_CUDA(h->d_jpart.ensure(sizeof(float2) * (size_t)nL * ntile * rb::NTH));
   rb::TbAdjArgs ta{};
   ta.nL = nL;
   ta.nf = nf;
@@ -1537,32 +1632,12 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
     RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nbt * ta.nchunk * nf));
     ta.S = h->d_adjS.as<float>();
   }
-  rb::TanArgs tn{};
-  tn.nL = nL;
-  tn.P = P;
-  tn.T = T;
-  tn.X = X;
-  tn.nh3_mode = h->cfg.nh3_mode;
-  tn.h2state = h->cfg.h2state;
-  tn.inv_table = h->cfg.inv_table;
   tn.out = h->d_lt.as<rb::LayerTan>();
-  rb::JvpArgs jv{};
-  jv.nL = nL;
-  jv.nf = nf;
-  jv.ft = rb::adjoint_ft(nf, h->jvp_ft);
-  jv.ctas = h->jvp_ctas;
-  jv.threads = h->jvp_threads;
-  if (jv.threads && jv.threads % jv.ft)
-    return fail(RB_EINVAL, "JVP threads per CTA (%d) must be a multiple of its frequencies per CTA (%d)",
-                jv.threads, jv.ft);
-  jv.fplan = h->d_jfreq.as<rb::JvFreq>();
   jv.lp = h->d_lp.as<rb::LayerParams>();
   jv.lt = h->d_lt.as<rb::LayerTan>();
-  for (int f = 0; f < rb::NFAM; ++f) jv.tab[f] = h->fam[f].table();
-  jv.cfg = h->cfg;
-  jv.cfg.units_db = 0;
   jv.galpha = h->d_ga.as<float>();
   jv.part = h->d_jpart.as<float2>();
+  jv.dal_out = h->d_dal.as<float>();
   rb::ExtraArgs ea{};
   const bool extra = h->cfg.use_co || h->cfg.use_clouds;
   if (extra) {
@@ -1572,9 +1647,17 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
     ea.scale = scale;
     ea.grad = h->d_xgrad.as<double>();
   }
-  RB_CUDA(rb::launch_adjoint(ta, tn, jv, extra ? &ea : nullptr, h->d_ga.as<float>(),
-                             h->d_gs.as<double>(), dT, dP, dlnX, st));
-  h->launches = launches + (extra ? 7 : 6) - (disc ? 1 : 0);
+  const int nsweep = disc ? 1 : 2;
+  if (store) {
+    RB_CUDA(rb::launch_adjoint_sweep(ta, st));
+    RB_CUDA(rb::launch_adjoint_contract(jv, extra ? &ea : nullptr, h->d_ga.as<float>(),
+                                        h->d_gs.as<double>(), dT, dP, dlnX, st));
+    h->launches = launches + nsweep + (extra ? 1 : 0) + 1;
+  } else {
+    RB_CUDA(rb::launch_adjoint(ta, tn, jv, extra ? &ea : nullptr, h->d_ga.as<float>(),
+                               h->d_gs.as<double>(), dT, dP, dlnX, st));
+    h->launches = launches + nsweep + (extra ? 1 : 0) + 3;   // sweep, tangents, JVP, [extra,] final
+  }
   return RB_OK;
 }
 

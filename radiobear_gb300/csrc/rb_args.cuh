@@ -278,6 +278,12 @@ struct JvpArgs {
   AlphaConfig cfg;
   const float* galpha;    // [nL][nf] d loss / d alpha
   float2* part;           // [nL][ntile][NTH] double-float sums over the tile's frequencies
+  // Stored-tangent mode (alpha_out set): before the scan, the kernel writes
+  // the layer's float32 alpha and d alpha / d theta per frequency instead of
+  // contracting with galpha after the reverse sweep.
+  float* alpha_out;       // [nL][nf] cm^-1 (the scan's alpha)
+  float* dal_out;         // [nL][NTH][nf] d alpha / d (T, P, ln X_NH3, ln X_H2O, ln X_H2S)
+  const double* extra;    // co_ddb / clouds_idp alpha [2][nL][nf] in cm^-1, or null
 };
 
 }  // namespace rb

@@ -147,6 +147,28 @@ def test_adjoint_single_layers(engine, case, param):
 
 
 @pytest.mark.gpu
+def test_adjoint_modes_agree(engine, case):
+    """The stored-tangent adjoint (the JVP before the scan gives alpha and
+    stores d alpha / d theta) against the recomputing one (forward line
+    sums, JVP contracted after the reverse sweep): the same JVP arithmetic,
+    alpha from two float32 kernels."""
+    gas, R, N, freqs, b, w, lines = case
+    grad = np.random.default_rng(5).normal(size=freqs.size)
+    try:
+        engine.set_tuning(adj_mode=1)
+        st = _run(engine, case, grad)
+        engine.set_tuning(adj_mode=2)
+        rc = _run(engine, case, grad)
+    finally:
+        engine.set_tuning(adj_mode=0)
+    assert np.max(np.abs(st['Tb'] - rc['Tb'])) < 2e-4
+    assert np.max(np.abs(st['Tb_avg'] - rc['Tb_avg'])) < 2e-4
+    for k in ('dT', 'dP', 'dlnX'):
+        scale = np.max(np.abs(rc[k]))
+        assert np.max(np.abs(st[k] - rc[k])) <= 1e-4 * scale, (k, np.max(np.abs(st[k] - rc[k])), scale)
+
+
+@pytest.mark.gpu
 def test_autograd_function(engine, case):
     """torch.autograd through TbFunction: forward equals rb_forward, the
     gradient equals rb_adjoint and a finite difference of the oracle."""
@@ -170,7 +192,11 @@ def test_autograd_function(engine, case):
     loss = (avg * torch.tensor(gw, dtype=torch.float64, device=dev)).sum()
     loss.backward()
     ref = _run(engine, case, gw)
-    np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=1e-9)
+    fwd = engine.forward(gas[C['P']], gas[C['T']], X, R, N, freqs, b, G.REQ, G.RPOL, weights=w)
+    np.testing.assert_allclose(avg.detach().cpu().numpy(), fwd['Tb_avg'], rtol=0, atol=1e-9)
+    # the stored-tangent adjoint's own forward takes alpha from the JVP
+    # kernel (float32 sums in another order): within rounding of rb_forward
+    np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=2e-4)
     # the adjoint's layer sums are float32 atomics: run-to-run rounding ~1e-7
     for got, want in ((T.grad, ref['dT']), (P.grad, ref['dP']), (lnX.grad, ref['dlnX'])):
         np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-5, atol=1e-6 * np.max(np.abs(want)))
@@ -279,6 +305,10 @@ def test_autograd_function_disc(engine, case):
     (avg * torch.tensor(gw, dtype=torch.float64, device=dev)).sum().backward()
     ref = engine.adjoint(gas[C['P']], gas[C['T']], X, R, N, freqs, np.zeros((1, 2)), G.REQ, G.RPOL,
                          gw, weights=np.ones(1), disc=True)
-    np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=1e-9)
+    fwd = engine.forward(gas[C['P']], gas[C['T']], X, R, N, freqs, np.zeros((1, 2)), G.REQ, G.RPOL,
+                         weights=np.ones(1), disc=True)
+    np.testing.assert_allclose(avg.detach().cpu().numpy(), fwd['Tb_avg'], rtol=0, atol=1e-9)
+    # the stored-tangent adjoint's alpha comes from the JVP kernel
+    np.testing.assert_allclose(avg.detach().cpu().numpy(), ref['Tb_avg'], rtol=0, atol=2e-4)
     for got, want in ((T.grad, ref['dT']), (P.grad, ref['dP']), (lnX.grad, ref['dlnX'])):
         np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-5, atol=1e-6 * np.max(np.abs(want)))

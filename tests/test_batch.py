@@ -150,9 +150,12 @@ def test_batches_with_per_variant_scale(setup):
         ref = e.forward(gas[C['P']], gas[C['T']], X, R, N, freqs, b, G.REQ, G.RPOL, weights=w,
                         scale=scales[v], want_rays=False)['Tb_avg']
         assert np.max(np.abs(got[v] - ref)) <= 1e-9, v
-        assert np.max(np.abs(got2[v] - ref)) <= 1e-9, v
+        # the adjoint's forward (stored-tangent mode) takes alpha from the JVP
+        # kernel: within float32 rounding of the forward's line sums
+        assert np.max(np.abs(got2[v] - ref)) <= 2e-4, v
         ra = e.adjoint(gas[C['P']], gas[C['T']], X, R, N, freqs, b, G.REQ, G.RPOL, grad[v], weights=w,
                        scale=scales[v])
+        assert np.max(np.abs(got2[v] - ra['Tb_avg'])) <= 1e-9, v
         for gg, want in ((dT[o:o + n], ra['dT']), (dP[o:o + n], ra['dP']), (dX[:, o:o + n], ra['dlnX'])):
             assert np.max(np.abs(gg - want)) <= 1e-6 * (np.max(np.abs(want)) + 1e-300), v
         o += n

@@ -234,3 +234,5 @@ def test_launch_shape_knobs_keep_the_results(engine):
     from radiobear_gb300._native import RBError
     with pytest.raises((RBError, ValueError)):
         engine.set_tuning(scan_lanes=6)
+    with pytest.raises((RBError, ValueError)):
+        engine.set_tuning(adj_mode=3)
