@@ -85,38 +85,29 @@ struct ChunkState {
   bool live;       // TbL >= T_cmb (else Tb is clamped and has no gradient)
 };
 
-// Combine of the forward's partials (the arithmetic of rb_tb_combine_kernel).
-__device__ __forceinline__ ChunkState adj_combine(const TbAdjArgs& a, int b, int c, int f, int nc) {
-  const float4* part = a.part + (size_t)b * a.nchunk * a.nf + f;
-  float ph = 0.f, pl = 0.f;
-  float iw = 0.f, iwc = 0.f, tb = 0.f, tbc = 0.f;
+// The state of chunk c of ray b at frequency f, written by the forward's
+// combine (rb_tb_combine_kernel with iw32): the optical depth at the chunk's
+// first node, Tb and intW of the ray (intW 0 where Tb is clamped to T_cmb,
+// which has no gradient).
+__device__ __forceinline__ ChunkState adj_state(const TbAdjArgs& a, int b, int c, int f) {
   ChunkState st;
-  st.tch = st.tcl = 0.f;
-  for (int k = 0; k < nc; ++k) {
-    if (k == c) {
-      st.tch = ph;
-      st.tcl = pl;
-    }
-    const float4 p = part[(size_t)k * a.nf];
-    const float sc = __expf(-ph) * (1.f - pl);
-    float y = sc * p.z - iwc, t = iw + y;
-    iwc = (t - iw) - y;
-    iw = t;
-    y = sc * p.w - tbc;
-    t = tb + y;
-    tbc = (t - tb) - y;
-    tb = t;
-    float s, e;
-    two_sum(ph, p.x, s, e);
-    e += pl + p.y;
-    ph = s + e;
-    pl = e - (ph - s);
-  }
-  const float TbL = tb - tbc, IW = iw - iwc;
-  st.live = !(TbL < (float)T_CMB_ADJ) && IW > 0.f;
-  st.Tb = st.live ? TbL / IW : (float)T_CMB_ADJ;
-  st.rIW = st.live ? 1.f / IW : 0.f;
+  const float4* p = a.part + ((size_t)b * a.nchunk + c) * a.nf + f;
+  const float2 t0 = *reinterpret_cast<const float2*>(&p->z);
+  st.tch = t0.x;
+  st.tcl = t0.y;
+  const float iw = a.iw32[(size_t)b * a.nf + f];
+  st.live = iw > 0.f;
+  st.Tb = st.live ? a.Tb32[(size_t)b * a.nf + f] : (float)T_CMB_ADJ;
+  st.rIW = st.live ? 1.f / iw : 0.f;
   return st;
+}
+
+// exp(-x) as 2^(-x log2(e)) with the PTX base-2 exponential approximation,
+// flushing results below 2^-126 (optical depths above ~87) to zero.
+__device__ __forceinline__ float exp_neg(float x) {
+  float y = x * -1.4426950408889634f;
+  asm("ex2.approx.ftz.f32 %0, %0;" : "+f"(y));
+  return y;
 }
 
 // The chunk's path nodes staged in shared memory (layer offsets, T,
@@ -165,7 +156,7 @@ __global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
   __syncthreads();
   if (f >= a.nf) return;
   float* S = a.S + ((size_t)b * a.nchunk + c) * a.nf + f;
-  const ChunkState st = adj_combine(a, b, c, f, nc);
+  const ChunkState st = adj_state(a, b, c, f);
   if (!st.live) {
     *S = 0.f;
     return;
@@ -179,7 +170,7 @@ __global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
     dfs_add(th, tlo, (a0 + ak) * d * 0.5f);
     const float dk = 2.f * sg.hd[s + 1];
     const float ck = 0.5f * (d + dk);
-    const float Ek = __expf(-th) * (1.f - tlo);
+    const float Ek = exp_neg(th) * (1.f - tlo);
     const float wk = ck * (sg.T[s + 1] - st.Tb) * st.rIW;
     const float y = -(wk * ak * Ek) - lamc;
     const float tt = lam + y;
@@ -187,81 +178,109 @@ __global__ void __launch_bounds__(128) rb_tb_adj_lambda_kernel(TbAdjArgs a) {
     lam = tt;
     a0 = ak;
   }
-  *S = __expf(-st.tch) * (1.f - st.tcl) * (lam - lamc);
+  *S = exp_neg(st.tch) * (1.f - st.tcl) * (lam - lamc);
+}
+
+// In place: S[b][c][f] becomes the sum of S over the chunks after c
+// (compensated, from the last chunk back), Lam after chunk c's last node.
+__global__ void __launch_bounds__(128) rb_tb_adj_suffix_kernel(TbAdjArgs a) {
+  const int b = blockIdx.x;
+  const int f = blockIdx.y * blockDim.x + threadIdx.x;
+  if (f >= a.nf) return;
+  const int n = min(max(a.nseg[b], 0), a.max_seg);
+  const int N = n - 1;
+  const int nc = N > 0 ? (N + ADJ_CHUNK - 1) / ADJ_CHUNK : 0;
+  float* S = a.S + (size_t)b * a.nchunk * a.nf + f;
+  float ln = 0.f, lc = 0.f;
+  for (int k = nc - 1; k >= 0; --k) {
+    const float v = S[(size_t)k * a.nf];
+    S[(size_t)k * a.nf] = ln - lc;
+    const float y = v - lc;
+    const float t = ln + y;
+    lc = (t - ln) - y;
+    ln = t;
+  }
 }
 
 __global__ void __launch_bounds__(128) rb_tb_adj_grad_kernel(TbAdjArgs a) {
   __shared__ AdjStage sg;
+  __shared__ float s_src[ADJ_CHUNK + 1][4];   // source term per node and warp
   const int f = blockIdx.z * blockDim.x + threadIdx.x;
   const int c = blockIdx.y, b = blockIdx.x;   // rays in x: batches have more than 65535
   const int n = min(max(a.nseg[b], 0), a.max_seg);
   const int N = n - 1;
   const int nc = N > 0 ? (N + ADJ_CHUNK - 1) / ADJ_CHUNK : 0;
-  if (c >= nc) return;
+  if (c >= nc) return;   // the whole CTA
   const int i0 = c * ADJ_CHUNK;
   const int ns = min(ADJ_CHUNK, N - i0);
   adj_stage(a, sg, b, i0, ns, N);
+  for (int t = threadIdx.x; t < (ADJ_CHUNK + 1) * 4; t += blockDim.x) (&s_src[0][0])[t] = 0.f;
   __syncthreads();
-  // lanes past nf or without a gradient run with gb = 0 so the warp's
+  // lanes past nf or without a gradient run with g = 0 so the warp's
   // source-term shuffle has every lane
   const bool inf = f < a.nf;
   const int nf = a.nf;
   const int fc = inf ? f : 0;
+  const int warp = threadIdx.x >> 5;
   double gb = inf ? adj_gb(a, b, fc) : 0.0;
-  const ChunkState st = adj_combine(a, b, c, fc, nc);
+  const ChunkState st = adj_state(a, b, c, fc);
   if (!st.live) gb = 0.0;
-  if (__all_sync(0xffffffffu, gb == 0.0)) return;
-  const unsigned am_mask = 0xffffffffu;
-  const float* S = a.S + (size_t)b * a.nchunk * a.nf + fc;
-  // Lam of the node after this chunk's last node, compensated
-  float Ln = 0.f, Lc = 0.f;
-  for (int k = c + 1; k < nc; ++k) {
-    const float y = S[(size_t)k * a.nf] - Lc;
-    const float t = Ln + y;
-    Lc = (t - Ln) - y;
-    Ln = t;
-  }
-  const float* al = a.alpha32 + fc;
-  // local optical depth at the chunk's last node (double-float)
-  float th = 0.f, tlo = 0.f;
-  {
-    float ap = al[sg.off[0]];
-    for (int s = 0; s < ns; ++s) {
-      const float ak = al[sg.off[s + 1]];
-      dfs_add(th, tlo, (ap + ak) * (2.f * sg.hd[s]) * 0.5f);
-      ap = ak;
-    }
-  }
-  const float Ec = __expf(-st.tch) * (1.f - st.tcl);
   const float g = (float)gb;
-  // nodes i0+ns .. i0+1 in reverse (node i0 belongs to the previous chunk,
-  // except node 0, which chunk 0 handles last); the sums over the rays and
-  // the visits of a layer are atomic adds into galpha[layer][f] and gsrc[layer]
-  float ak = al[sg.off[ns]];
-  for (int t = ns; t > 0; --t) {
-    const float dprev = 2.f * sg.hd[t - 1];
-    const float dcur = 2.f * sg.hd[t];
-    const float ck = 0.5f * (dprev + dcur);
-    const float Ek = Ec * __expf(-th) * (1.f - tlo);
-    const float wk = ck * (sg.T[t] - st.Tb) * st.rIW;
-    const float Lnext = Ln - Lc;
-    // Lam_k = Lam_{k+1} - w_k a_k E_k
-    const float y = -(wk * ak * Ek) - Lc;
-    const float tt = Ln + y;
-    Lc = (tt - Ln) - y;
-    Ln = tt;
-    const float Lk = Ln - Lc;
-    if (g != 0.f) atomicAdd(a.ga + sg.off[t] + f, g * (wk * Ek + 0.5f * dprev * Lk + 0.5f * dcur * Lnext));
-    // source term: summed over the warp's frequencies before the atomic
-    float src = g * ak * Ek * ck * st.rIW;
-    for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(am_mask, src, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(a.gs + sg.lay[t], (double)src);
-    const float am = al[sg.off[t - 1]];
-    dfs_add(th, tlo, -(am + ak) * dprev * 0.5f);
-    ak = am;
+  if (!__all_sync(0xffffffffu, g == 0.f)) {
+    // Lam after this chunk's last node: the suffix sum of the later chunks
+    float Ln = a.S[((size_t)b * a.nchunk + c) * nf + fc], Lc = 0.f;
+    const float* al = a.alpha32 + fc;
+    // local optical depth at the chunk's last node, recomputed as an exact
+    // double-float sum: the reverse recurrence subtracts from it down to the
+    // chunk's first node, so it needs it to ~ulp^2 (the forward partial
+    // carries ~ulp(tau) from steps larger than its running sum)
+    float th = 0.f, tlo = 0.f;
+    {
+      float ap = al[sg.off[0]];
+      for (int s = 0; s < ns; ++s) {
+        const float aq = al[sg.off[s + 1]];
+        dfs_add(th, tlo, (ap + aq) * (2.f * sg.hd[s]) * 0.5f);
+        ap = aq;
+      }
+    }
+    const float Ec = exp_neg(st.tch) * (1.f - st.tcl);
+    // nodes i0+ns .. i0+1 in reverse (node i0 belongs to the previous chunk,
+    // except node 0, which chunk 0 handles last); the sums over the rays and
+    // the visits of a layer are atomic adds into galpha[layer][f], the
+    // source term per node summed over the warp's frequencies, then over
+    // the CTA's warps, into gsrc[layer]
+    float ak = al[sg.off[ns]];
+    for (int t = ns; t > 0; --t) {
+      const float dprev = 2.f * sg.hd[t - 1];
+      const float dcur = 2.f * sg.hd[t];
+      const float ck = 0.5f * (dprev + dcur);
+      const float Ek = Ec * exp_neg(th) * (1.f - tlo);
+      const float wk = ck * (sg.T[t] - st.Tb) * st.rIW;
+      const float Lnext = Ln - Lc;
+      // Lam_k = Lam_{k+1} - w_k a_k E_k
+      const float y = -(wk * ak * Ek) - Lc;
+      const float tt = Ln + y;
+      Lc = (tt - Ln) - y;
+      Ln = tt;
+      const float Lk = Ln - Lc;
+      if (g != 0.f) atomicAdd(a.ga + sg.off[t] + f, g * (wk * Ek + 0.5f * dprev * Lk + 0.5f * dcur * Lnext));
+      float src = g * ak * Ek * ck * st.rIW;
+      for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(0xffffffffu, src, o);
+      if ((threadIdx.x & 31) == 0) s_src[t][warp] = src;
+      const float am = al[sg.off[t - 1]];
+      dfs_add(th, tlo, -(am + ak) * dprev * 0.5f);
+      ak = am;
+    }
+    if (c == 0 && g != 0.f)   // node 0: W_0 = 0, only the segment term
+      atomicAdd(a.ga + sg.off[0] + f, g * 0.5f * (2.f * sg.hd[0]) * (Ln - Lc));
   }
-  if (c == 0 && g != 0.f)   // node 0: W_0 = 0, only the segment term
-    atomicAdd(a.ga + sg.off[0] + f, g * 0.5f * (2.f * sg.hd[0]) * (Ln - Lc));
+  __syncthreads();
+  const int nwarp = (blockDim.x + 31) >> 5;
+  for (int t = threadIdx.x + 1; t <= ns; t += blockDim.x) {
+    float v = 0.f;
+    for (int w = 0; w < nwarp; ++w) v += s_src[t][w];
+    if (v != 0.f) atomicAdd(a.gs + sg.lay[t], (double)v);
+  }
 }
 
 // b = 'disc': one thread per (ray, frequency).  The forward pass repeats
@@ -446,11 +465,19 @@ __device__ constexpr float INV_SET_D[2][2][13] = {
 // rb_layer_prep_kernel: 0 shared, 1 inversion, 2 rotational, 3 nu2,
 // 4 nh3_sjs, 5 H2S, 6 PH3, 7 H2O), threads numbered part-major over the
 // layers padded to a multiple of 32 (one part per warp).
+constexpr int FAMTAN_WORDS = (int)(sizeof(FamTan) / sizeof(float));
+
 __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
+  // a warp's 32 FamTan, written out layer by layer with consecutive lanes
+  // (a thread's own 344-byte struct, 2.4 KB from its neighbours', turned
+  // every 4-byte store into its own sector request)
+  __shared__ float s_tan[2][32][FAMTAN_WORDS];
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nLp = (a.nL + 31) & ~31;
-  const int part = gid / nLp, L = gid - part * nLp;
-  if (part >= 8 || L >= a.nL) return;
+  const int part = gid / nLp, Lg = gid - part * nLp;
+  if (part >= 8) return;   // whole warps: nLp is a multiple of 32
+  const bool valid = Lg < a.nL;
+  const int L = valid ? Lg : a.nL - 1;   // lanes past nL evaluate the last layer, store nothing
   const int nL = a.nL;
   const double Pd = a.P[L], Td = a.T[L];
   const double* X = a.X;
@@ -476,10 +503,12 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
   const double invT2 = 1.0 / (Td * Td);
   FamTan F;
   zero_tan(F);
+  int famo = FAM_H2O;
   switch (part) {
     case 0: {
       // blend weight of nh3_hs_sjs (nh3_hs_sjs.py:6-26)
-      o.dblendW_dP = (a.nh3_mode == NH3_HS_SJS && Pd >= 400.0 && Pd <= 2000.0) ? (float)(1.0 / 1600.0) : 0.f;
+      if (valid)
+        o.dblendW_dP = (a.nh3_mode == NH3_HS_SJS && Pd >= 400.0 && Pd <= 2000.0) ? (float)(1.0 / 1600.0) : 0.f;
       const D5 th = dc(273.0) / T;
       const D5 lth = dlog2(th);
       D5 pre;
@@ -492,8 +521,9 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
       const D5 cia = 3.9522E-14 * (Ph2 * pre *
                                    (Ph2 * dpw(lth, 3.12) + 1.382 * (Phe * dpw(lth, 2.24)) +
                                     9.322 * (Pch4 * dpw(lth, 3.34))));
-      for (int q = 0; q < NTH; ++q) o.dh2_cia[q] = (float)cia.d[q];
-      return;
+      if (valid)
+        for (int q = 0; q < NTH; ++q) o.dh2_cia[q] = (float)cia.d[q];
+      return;   // the whole warp: no FamTan in part 0
     }
     case 1: {
       for (int s = 0; s < 2; ++s) {
@@ -505,8 +535,8 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
       }
       store_pref(F, TWO_PI * hs_base);
       F.dcE = (float)(19.858252418E-24 / 1.38E-23 * LOG2E_D * invT2);
-      o.fam[FAM_NH3_INV] = F;
-      return;
+      famo = FAM_NH3_INV;
+      break;
     }
     case 2: {
       store_tan(F, 0, 1, 0.2984 * (Ph2 * dpw(lTdiv, 0.8730)));
@@ -514,8 +544,8 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
       store_tan(F, 0, 3, 3.1789 * (Pnh3 * Tdiv));
       store_pref(F, (2.4268 * FOUR_PI) * hs_base);
       F.dcE = (float)(19.858252418E-24 / 1.38E-23 * LOG2E_D * invT2);
-      o.fam[FAM_NH3_ROT] = F;
-      return;
+      famo = FAM_NH3_ROT;
+      break;
     }
     case 3: {
       store_tan(F, 0, 1, Ph2 * dpw(lTdiv, 0.73));
@@ -523,13 +553,14 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
       store_tan(F, 0, 3, Pnh3 * Tdiv);
       store_pref(F, (1.1206 * FOUR_PI) * hs_base);
       F.dcE = (float)(19.858252418E-24 / 1.38E-23 * LOG2E_D * invT2);
-      o.fam[FAM_NH3_V2] = F;
-      return;
+      famo = FAM_NH3_V2;
+      break;
     }
     case 4: {
-      for (int s = 0; s < 2; ++s)
-        for (int k = 0; k < 5; ++k)
-          for (int q = 0; q < NTH; ++q) o.dsjs[s][k][q] = 0.f;
+      if (valid)
+        for (int s = 0; s < 2; ++s)
+          for (int k = 0; k < 5; ++k)
+            for (int q = 0; q < NTH; ++q) o.dsjs[s][k][q] = 0.f;
       const bool use_sjs = a.nh3_mode == NH3_SJS || (a.nh3_mode == NH3_HS_SJS && Pd >= 400.0);
       if (use_sjs) {
         const D5 rexp = 8.79 * dexp((-1.0 / 83.0) * T);
@@ -556,15 +587,16 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
           for (int k = 0; k < 7; ++k) c[k] = s == 0 ? dc(J[k]) : S[k];
           const D5 v[5] = {tt * (c[0] * Ph2 + c[1] * Phe), tt * (c[2] * Pnh3),
                            tt * (c[3] * Ph2 + c[4] * Phe), tt * (c[5] * Pnh3), c[6] * Pnh3};
-          for (int k = 0; k < 5; ++k)
-            for (int q = 0; q < NTH; ++q) o.dsjs[s][k][q] = (float)v[k].d[q];
+          if (valid)
+            for (int k = 0; k < 5; ++k)
+              for (int q = 0; q < NTH; ++q) o.dsjs[s][k][q] = (float)v[k].d[q];
         }
         const D5 Pscale = dc(1.0) + 1.0E-5 * P;
         store_pref(F, (7.244E+21 * GHZ * TWO_PI / 296.0) * (Pnh3 * dpw(l296, 3.5) * Pscale));
         F.dcE = (float)(1.438396 * LOG2E_D * invT2);
       }
-      o.fam[FAM_NH3_SJS] = F;
-      return;
+      famo = FAM_NH3_SJS;
+      break;
     }
     case 5: {
       const D5 l296 = dlog2(dc(296.0) / T);
@@ -574,16 +606,16 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
       store_tan(F, 0, 7, 1.28 * Ph2s);
       store_pref(F, (7.244E+21 * GHZ * TWO_PI / 296.0) * (Ph2s * dpw(l296, 3.5)));
       F.dcE = (float)(1.438396 * LOG2E_D * invT2);
-      o.fam[FAM_H2S] = F;
-      return;
+      famo = FAM_H2S;
+      break;
     }
     case 6: {
       store_tan(F, 0, 1, dpw(lTdiv, 2.0 / 3.0) * (3.2930 * Ph2 + 1.6803 * Phe));
       store_tan(F, 0, 2, 4.2157 * (Tdiv * Pph3));
       store_pref(F, (7.244E+21 * GHZ * TWO_PI / 300.0) * (Pph3 * dpw(lTdiv, 3.5)));
       F.dcE = (float)(1.438396 * LOG2E_D * invT2);
-      o.fam[FAM_PH3] = F;
-      return;
+      famo = FAM_PH3;
+      break;
     }
     default: {
       store_tan(F, 0, 0, lTdiv);
@@ -593,15 +625,26 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
       const D5 density = (0.997317 * 6.0221415e17 / 8.314472e-5) * (Ph2o / T);
       store_pref(F, (4.342945e-4 / 434294.5) * (density * dpw(lTdiv, 2.5)));
       F.dcE = (float)(300.0 * LOG2E_D * invT2);
-      o.fam[FAM_H2O] = F;
+      famo = FAM_H2O;
       const double Cf_he = 1.0e6 * 1.03562010226e-10, Cf_h2 = 1.0e6 * 5.07722009423e-11;
       const D5 th3 = Tdiv * Tdiv * Tdiv;
       const D5 foreign = Cf_he * (Phe * Ph2o * th3) + Cf_h2 * (Ph2 * Ph2o * th3);
       const D5 selfc = 3.1e-07 * (dpw(lTdiv, 12.0) * (1.0e6 * (Ph2o * Ph2o)));
       const D5 cont = (4.342945 / 434294.5) * (foreign + selfc);
-      for (int q = 0; q < NTH; ++q) o.dh2o_cont[q] = (float)cont.d[q];
-      return;
+      if (valid)
+        for (int q = 0; q < NTH; ++q) o.dh2o_cont[q] = (float)cont.d[q];
+      break;
     }
+  }
+  // famo is the same on every lane of the warp (one part per warp)
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float* src = reinterpret_cast<const float*>(&F);
+  for (int k = 0; k < FAMTAN_WORDS; ++k) s_tan[w][lane][k] = src[k];
+  __syncwarp();
+  const int L0 = Lg - lane;
+  for (int j = 0; j < 32 && L0 + j < nL; ++j) {
+    float* dst = reinterpret_cast<float*>(&a.out[L0 + j].fam[famo]);
+    for (int k = lane; k < FAMTAN_WORDS; k += 32) dst[k] = s_tan[w][j][k];
   }
 }
 
@@ -1341,6 +1384,7 @@ cudaError_t launch_adjoint_sweep(const TbAdjArgs& ta, cudaStream_t st) {
     const int blk = ta.nf >= 128 ? 128 : ((ta.nf + 31) / 32) * 32;
     dim3 grid(ta.nb, ta.nchunk, (ta.nf + blk - 1) / blk);
     rb_tb_adj_lambda_kernel<<<grid, blk, 0, st>>>(ta);
+    rb_tb_adj_suffix_kernel<<<dim3(ta.nb, (ta.nf + blk - 1) / blk), blk, 0, st>>>(ta);
     rb_tb_adj_grad_kernel<<<grid, blk, 0, st>>>(ta);
   }
   return cudaGetLastError();

@@ -202,7 +202,7 @@ struct rb_handle {
   DBuf d_f, d_fhs, d_jfreq, d_chains, d_tflags, d_wsets, d_tmpl, d_sj, d_sF, d_sFhs, d_sf, d_swJ, d_sset, d_counter,
       d_res, d_base;
   // adjoint workspaces
-  DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff, d_dal;
+  DBuf d_ga, d_gs, d_lt, d_jpart, d_grad, d_dth, d_adjS, d_voff, d_dal, d_iw32;
   std::vector<int> batch_off;   // layer offsets of the last batch (d_voff)
   // workspaces
   DBuf d_P, d_T, d_X, d_scale, d_lp, d_a32, d_l64, d_g64, d_R, d_N, d_b, d_w, d_nseg, d_ds,
@@ -858,7 +858,7 @@ int rb_destroy(rb_handle* h) {
     b->release();
   for (DBuf* b : {&h->d_chains, &h->d_tflags, &h->d_wsets, &h->d_tmpl, &h->d_counter, &h->d_res, &h->d_base,
                   &h->d_ga, &h->d_gs, &h->d_lt, &h->d_jpart, &h->d_grad, &h->d_dth,
-                  &h->d_adjS, &h->d_voff, &h->d_co_f0, &h->d_co_I0, &h->d_co_E, &h->d_extra,
+                  &h->d_adjS, &h->d_voff, &h->d_dal, &h->d_iw32, &h->d_co_f0, &h->d_co_I0, &h->d_co_E, &h->d_extra,
                   &h->d_xgrad, &h->d_agas, &h->d_acl, &h->d_aout, &h->d_aclout, &h->d_aprop,
                   &h->d_agrid, &h->d_aoff})
     b->release();
@@ -1381,7 +1381,8 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
                         const double* dX, const double* dR, const double* dN, const double* dscale,
                         double Req, double Rpol, double o0, double o1, int gtype, int limb, int nb,
                         const double* db, const double* dw, int disc, double* dTb, double* davg,
-                        double* dl64, const Batch* bt = nullptr, const AlphaJvp* aj = nullptr) {
+                        double* dl64, const Batch* bt = nullptr, const AlphaJvp* aj = nullptr,
+                        float* iw32 = nullptr) {
   const int nf = (int)h->plan_f.size();
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
   const int nvar = bt ? bt->nvar : 1;
@@ -1427,6 +1428,7 @@ static int forward_core(rb_handle* h, cudaStream_t st, int nL, const double* dP,
     ta.nchunk = nchunk;
     ta.lanes = h->scan_lanes;
     ta.part = h->d_part.as<float4>();
+    ta.iw32 = iw32;   // the adjoint's chunk state (null: forward only)
     if (h->profiling) RB_CUDA(cudaEventRecord(h->pev[5], st));
     if (disc) {
       RB_CUDA(rb::launch_tb_seq(ta, st));
@@ -1595,9 +1597,11 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
   const size_t dal_bytes = sizeof(float) * (size_t)nL * rb::NTH * nf;
   const bool store = h->adj_mode == 1 || (h->adj_mode == 0 && dal_bytes <= h->dev_mem / 8);
   AlphaJvp aj{tn, jv};
+  RB_CUDA(h->d_iw32.ensure(sizeof(float) * (size_t)std::max(nbt, 1) * nf));
   int rc;
   if ((rc = forward_core(h, st, nL, P, T, X, R, N, scale, Req, Rpol, orient0, orient1, gtype, limb,
-                         nb, b, weights, disc, dTb, davg, nullptr, bt, store ? &aj : nullptr)))
+                         nb, b, weights, disc, dTb, davg, nullptr, bt, store ? &aj : nullptr,
+                         disc ? nullptr : h->d_iw32.as<float>())))
     return rc;
   const int launches = h->launches;
   const int max_seg = 2 * (bt ? bt->max_nL : nL) + 4;
@@ -1629,6 +1633,8 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
     ta.tauE = h->d_adjS.as<double2>();
   } else {
     ta.part = h->d_part.as<float4>();
+    ta.Tb32 = h->d_Tb32.as<float>();
+    ta.iw32 = h->d_iw32.as<float>();
     RB_CUDA(h->d_adjS.ensure(sizeof(float) * (size_t)nbt * ta.nchunk * nf));
     ta.S = h->d_adjS.as<float>();
   }
@@ -1647,7 +1653,7 @@ static int adjoint_core(rb_handle* h, cudaStream_t st, int nL, const double* P, 
     ea.scale = scale;
     ea.grad = h->d_xgrad.as<double>();
   }
-  const int nsweep = disc ? 1 : 2;
+  const int nsweep = disc ? 1 : 3;   // [lambda, suffix, grad] or the sequential 'disc' sweep
   if (store) {
     RB_CUDA(rb::launch_adjoint_sweep(ta, st));
     RB_CUDA(rb::launch_adjoint_contract(jv, extra ? &ea : nullptr, h->d_ga.as<float>(),

@@ -201,6 +201,10 @@ struct TbArgs {
   int chunk, nchunk;      // segments per chunk, chunks per ray
   int lanes;              // frequency-pair lanes per (ray, chunk) item of the packed scan (0: automatic)
   float4* part;           // [nb][nchunk][nf] {dtau_hi, dtau_lo, intW, TbL} per chunk
+  // adjoint state (null for a forward-only call): the combine writes intW
+  // per (ray, frequency) (0 where Tb is clamped to T_cmb) and replaces each
+  // chunk's {intW, TbL} by its starting optical depth {tau_hi, tau_lo}
+  float* iw32;            // [nb][nf]
 };
 
 // ---------------------------------------------------------------- adjoint
@@ -248,7 +252,9 @@ struct TbAdjArgs {
   const double* grad;     // [nf] (with weights: d loss / d Tb_avg) or [nb][nf]
   float* ga;              // [nL][nf] d loss / d alpha (atomic sums over rays and visits)
   double* gs;             // [nL] d loss / d T through the source term
-  const float4* part;     // forward scan partials [nb][nchunk][nf]
+  const float4* part;     // forward scan partials [nb][nchunk][nf]: {dtau_hi, dtau_lo, tau0_hi, tau0_lo}
+  const float* Tb32;      // [nb][nf] forward Tb
+  const float* iw32;      // [nb][nf] forward intW, 0 where Tb is clamped (no gradient)
   int nchunk;
   float* S;               // [nb][nchunk][nf] per-chunk sums of dTb/dtau
   // b = 'disc' (E2 weighting): sequential reverse sweep, no chunk partials

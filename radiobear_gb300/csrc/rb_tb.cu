@@ -274,10 +274,12 @@ struct ScanPair {
 // staged per-node weights.  The node sums run as float32 blocks of
 // SCAN_FLUSH terms (all positive: <= 16 ulp each) added into Kahan sums.
 // The optical depth is a float32 running sum th with its rounding errors
-// collected exactly (Fast2Sum) in tl, renormalised into (th, tl) once per
-// block: exp(-tau) = exp(-th) (1 - tl) to O(tl^2).  Fast2Sum is exact while
-// th >= the step's increment; a step larger than the running sum at least
-// doubles it, so such steps are few and their error stays ~ulp(tau).
+// collected (Fast2Sum) in tl, renormalised into (th, tl) once per block:
+// exp(-tau) = exp(-th) (1 - tl) to O(tl^2).  Fast2Sum is exact while th >=
+// the step's increment; a larger step errs by ~ulp of itself and at least
+// doubles the sum, so those errors form a geometric series below ~2 ulp of
+// the optical depth reached (the exponent's error; the adjoint, which
+// subtracts back from a chunk's total, recomputes that total exactly).
 //
 // The 5-CTA bound (96 registers) lets the compiler keep 32 steps of alpha
 // loads in flight without spilling: C1 scan 0.0292 ms unbounded (46
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
   const int ray = blockIdx.x * (128 / FT) + threadIdx.x / FT;
   const int f = blockIdx.y * FT + threadIdx.x % FT;
   if (ray >= a.nb || f >= a.nf) return;
-  const float4* part = a.part + (size_t)ray * a.nchunk * a.nf + f;
+  float4* part = a.part + (size_t)ray * a.nchunk * a.nf + f;
   const int nsteps = a.nseg[ray] - 1;
   const int nc = nsteps > 0 ? (nsteps + TB_CHUNK - 1) / TB_CHUNK : 0;
   float ph = 0.f, pl = 0.f;          // optical depth at the chunk start
@@ -428,6 +430,8 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
     for (int k = 0; k < CB; ++k) {
       if (c0 + k >= nc) break;
       const float4 p = pb[k];
+      if (a.iw32)   // the chunk's starting optical depth for the adjoint
+        *reinterpret_cast<float2*>(&part[(size_t)(c0 + k) * a.nf].z) = make_float2(ph, pl);
       const float sc = __expf(-ph) * (1.f - pl);
       kahan_add(iw, iwc, sc * p.z);
       kahan_add(tb, tbc, sc * p.w);
@@ -444,6 +448,7 @@ __global__ void __launch_bounds__(128) rb_tb_combine_kernel(TbArgs a) {
   a.Tb[(size_t)ray * a.nf + f] = clamped ? T_CMB : (double)out;
   if (a.Tb32) a.Tb32[(size_t)ray * a.nf + f] = out;
   if (a.intW) a.intW[(size_t)ray * a.nf + f] = (double)IW;
+  if (a.iw32) a.iw32[(size_t)ray * a.nf + f] = clamped || !(IW > 0.f) ? 0.f : IW;
 }
 
 // Weighted sum over rays (disc quadrature): one warp per frequency, lane i
