@@ -160,7 +160,8 @@ int rb_set_alpha_tiling(rb_handle* h, int M, int W, int item_lines);
  * driven by the autotuner (radiobear_gb300.tune); 0 restores the automatic
  * choice.  RB_TUNE_JVP_FREQS: frequencies per CTA of the absorption JVP
  * (32, 64 or 128); RB_TUNE_JVP_CTAS: resident CTAs per SM it is compiled
- * for at 256 threads (3: 80 registers, 4: 64); RB_TUNE_JVP_THREADS: threads
+ * for (256 threads: 3 or 4, default 3; 128 threads: 4, 5 or 6, default 5);
+ * RB_TUNE_JVP_THREADS: threads
  * per CTA (128 or 256, a multiple of the frequencies per CTA; the threads
  * beyond the frequencies split the lines); RB_TUNE_SCAN_LANES:
  * frequency-pair lanes per (ray, chunk) item of the brightness scan (a

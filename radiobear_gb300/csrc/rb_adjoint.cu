@@ -1402,11 +1402,18 @@ static cudaError_t launch_tan_jvp(const TanArgs& tn, const JvpArgs& jv, cudaStre
 #endif
   const int ctas = jv.ctas ? jv.ctas : (jv.ft >= 128 ? RB_JVP_MINB128 : RB_JVP_MINB);
   // threads per CTA: one line group for 128-frequency tiles (no per-family
-  // reduction across groups; C4 412 -> 371 ms), two or four otherwise
+  // reduction across groups; C4 412 -> 371 ms), two or four otherwise.
+  // 128-thread CTAs: 5 per SM (96 registers) unless 4 (120) or 6 (80) are asked.
   const int nt = jv.threads ? jv.threads : (jv.ft >= 128 ? 128 : 256);
-  if (nt == 128) rb_alpha_jvp_kernel<5, 128><<<grid, 128, 0, st>>>(jv);
-  else if (ctas >= 4) rb_alpha_jvp_kernel<4, 256><<<grid, 256, 0, st>>>(jv);
-  else rb_alpha_jvp_kernel<3, 256><<<grid, 256, 0, st>>>(jv);
+  if (nt == 128) {
+    if (jv.ctas == 4) rb_alpha_jvp_kernel<4, 128><<<grid, 128, 0, st>>>(jv);
+    else if (jv.ctas == 6) rb_alpha_jvp_kernel<6, 128><<<grid, 128, 0, st>>>(jv);
+    else rb_alpha_jvp_kernel<5, 128><<<grid, 128, 0, st>>>(jv);
+  } else if (ctas >= 4) {
+    rb_alpha_jvp_kernel<4, 256><<<grid, 256, 0, st>>>(jv);
+  } else {
+    rb_alpha_jvp_kernel<3, 256><<<grid, 256, 0, st>>>(jv);
+  }
   return cudaGetLastError();
 }
 

@@ -1076,8 +1076,8 @@ int rb_set_tuning(rb_handle* h, int param, int value) {
       h->jvp_ft = value;
       break;
     case RB_TUNE_JVP_CTAS:
-      if (!(value == 0 || value == 3 || value == 4))
-        return fail(RB_EINVAL, "RB_TUNE_JVP_CTAS must be 0, 3 or 4");
+      if (!(value == 0 || (value >= 3 && value <= 6)))
+        return fail(RB_EINVAL, "RB_TUNE_JVP_CTAS must be 0 or 3..6");
       h->jvp_ctas = value;
       break;
     case RB_TUNE_JVP_THREADS:

@@ -130,8 +130,8 @@ def tune_alpha(engine, step, key=None, candidates=DEFAULT_CANDIDATES, reps=3, st
 
 # (frequencies per CTA, resident CTAs per SM at 256 threads, threads per CTA)
 # of the absorption JVP
-JVP_CANDIDATES = ((128, 4, 128), (128, 3, 256), (128, 4, 256), (64, 3, 256), (64, 4, 256),
-                  (64, 4, 128), (32, 3, 256), (32, 4, 128))
+JVP_CANDIDATES = ((128, 5, 128), (128, 4, 128), (128, 6, 128), (128, 3, 256), (64, 3, 256),
+                  (64, 4, 256), (64, 4, 128), (32, 3, 256), (32, 5, 128))
 
 
 def tune_adjoint(engine, step, key=None, candidates=JVP_CANDIDATES, reps=1, stream=None):

@@ -218,7 +218,7 @@ def test_launch_shape_knobs_keep_the_results(engine):
     grad = np.random.default_rng(2).normal(size=freqs.size)
     try:
         ref = engine.adjoint(*args, grad, weights=w)
-        for ft, ctas, nt in ((32, 3, 256), (64, 4, 256), (64, 4, 128), (128, 3, 256), (128, 4, 256),
+        for ft, ctas, nt in ((32, 3, 256), (64, 4, 256), (64, 4, 128), (64, 6, 128), (128, 3, 256), (128, 4, 256),
                              (128, 4, 128)):
             engine.set_tuning(jvp_freqs=ft, jvp_ctas=ctas, jvp_threads=nt)
             out = engine.adjoint(*args, grad, weights=w)
