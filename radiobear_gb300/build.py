@@ -29,6 +29,11 @@ HEADERS = ['rb_common.cuh', 'rb_args.cuh', 'rb_f32x2.cuh', 'rb_expint.cuh', 'rb_
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
               '-Xptxas', '-v'] + ARCH
+# Per-file flags.  The ray set-up and walk run their float64 set-up in two
+# kernels (one ray per thread, or inside the walk's warp) and their float32
+# steps from it: without implicit multiply-add contraction both compile to
+# the same roundings (explicit fmaf calls stay fused).
+FILE_FLAGS = {'rb_raypath.cu': ['-fmad=false']}
 
 
 def nvcc_path():
@@ -46,6 +51,7 @@ def _digest():
     with open(os.path.join(ROOT, 'include', 'radiobear_gb300.h'), 'rb') as fp:
         h.update(fp.read())
     h.update(' '.join(NVCC_FLAGS).encode())
+    h.update(repr(sorted(FILE_FLAGS.items())).encode())
     return h.hexdigest()
 
 
@@ -63,7 +69,7 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD, src.replace('.cu', '.o'))
-        cmd = [nvcc, '-c', os.path.join(CSRC, src), '-o', obj] + NVCC_FLAGS
+        cmd = [nvcc, '-c', os.path.join(CSRC, src), '-o', obj] + NVCC_FLAGS + FILE_FLAGS.get(src, [])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError('nvcc failed for {}:\n{}\n{}'.format(src, r.stdout, r.stderr))

@@ -144,11 +144,14 @@ __host__ __device__ inline void split_double(double v, float& hi, float& lo) {
   lo = (float)(v - (double)hi);
 }
 
-// Error-free transformation a + b = s + e (Knuth TwoSum), float.
+// Error-free transformation a + b = s + e (Knuth TwoSum), float.  The
+// _rn intrinsics keep the compiler from contracting a product that feeds
+// a or b into the first addition (s would then round the exact product
+// while e accounts for the rounded one).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 __device__ __forceinline__ float rcp_approx(float x) {

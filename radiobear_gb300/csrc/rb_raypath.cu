@@ -124,7 +124,9 @@ __global__ void rb_geom_prep_kernel(int nL, const double* R, const double* T, fl
   if (T) T32[c] = (float)T[c];
 }
 
-// ---------------- double-float helpers
+// ---------------- double-float helpers (products and renormalisations in
+// _rn intrinsics, which the compiler does not contract into neighbouring
+// additions: the error terms must describe the rounded values actually used)
 struct df {
   float h, l;
 };
@@ -138,18 +140,18 @@ __device__ __forceinline__ df df_add(df a, df b) {
   two_sum(a.h, b.h, s, e);
   e += a.l + b.l;
   df r;
-  r.h = s + e;
-  r.l = e - (r.h - s);
+  r.h = __fadd_rn(s, e);
+  r.l = __fsub_rn(e, __fsub_rn(r.h, s));
   return r;
 }
 __device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
 // a * b for a double-float and a float
 __device__ __forceinline__ df df_mulf(df a, float b) {
-  const float p = a.h * b;
+  const float p = __fmul_rn(a.h, b);
   const float e = fmaf(a.h, b, -p) + a.l * b;
   df r;
-  r.h = p + e;
-  r.l = e - (r.h - p);
+  r.h = __fadd_rn(p, e);
+  r.l = __fsub_rn(e, __fsub_rn(r.h, p));
   return r;
 }
 // a + b without the final renormalisation (prefix scans: the low words
@@ -167,13 +169,13 @@ __device__ __forceinline__ float df_sum(df a, df b) {
 }
 // a * b for a double-float and a float, not renormalised
 __device__ __forceinline__ df df_mulf_lazy(df a, float b) {
-  const float p = a.h * b;
+  const float p = __fmul_rn(a.h, b);
   return {p, fmaf(a.h, b, -p) + a.l * b};
 }
 __device__ __forceinline__ df df_norm(df a) {
   df r;
-  r.h = a.h + a.l;
-  r.l = a.l - (r.h - a.h);
+  r.h = __fadd_rn(a.h, a.l);
+  r.l = __fsub_rn(a.l, __fsub_rn(r.h, a.h));
   return r;
 }
 // sqrt of a positive double-float: one Newton correction of sqrtf(hi); the
@@ -185,8 +187,8 @@ __device__ __forceinline__ df df_sqrt(df a) {
   df o;
   o.h = y;
   o.l = r * rcp_approx(2.f * y);
-  const float t = o.h + o.l;
-  o.l = o.l - (t - o.h);
+  const float t = __fadd_rn(o.h, o.l);
+  o.l = __fsub_rn(o.l, __fsub_rn(t, o.h));
   o.h = t;
   return o;
 }
@@ -408,10 +410,12 @@ __device__ __forceinline__ void ray_setup_warp(const RayArgs& a, int ray, int la
   if (edge_point(a, m, hit, rNorm, a.k, zQ)) ray_start(a, b0, b1, zQ, rNorm, a.k, a.N + off, o);
 }
 
-__global__ void __launch_bounds__(32, 32) rb_raypath_kernel(RayArgs a) {
-  const int ray = blockIdx.x;
-  const int lane = threadIdx.x;
-  if (ray >= a.nb) return;
+// One warp per ray, WPC rays per CTA (64 registers either way).
+template <int WPC>
+__global__ void __launch_bounds__(32 * WPC, 32 / WPC) rb_raypath_kernel(RayArgs a) {
+  const int ray = blockIdx.x * WPC + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (ray >= a.nb) return;   // whole warps
   int off = 0, nL = a.nL;
   if (a.var_off) {
     const int v = ray / a.rays_per_var;
@@ -686,10 +690,17 @@ cudaError_t launch_geom_prep(int nL, const double* R, const double* T, float2* d
   return cudaGetLastError();
 }
 
+// Few rays (the walk then runs beside the absorption's line sums): four
+// rays per CTA, one warp on each scheduler of an SM.  A walk warp's 64
+// registers do not fit in a scheduler's register file beside six line-sum
+// warps, so each SM holding walk warps gives up one line-sum CTA while they
+// run; packed four to a CTA they hold 16 SMs for 64 rays instead of 64.
+// Many rays: one per CTA (a CTA's slot frees as soon as its ray ends).
 cudaError_t launch_raypath(const RayArgs& a, cudaStream_t st) {
   if (a.nb <= 0) return cudaSuccess;
   if (a.start) rb_ray_setup_kernel<<<(a.nb + 127) / 128, 128, 0, st>>>(a);
-  rb_raypath_kernel<<<a.nb, 32, 0, st>>>(a);
+  if (a.nb < 2048) rb_raypath_kernel<4><<<(a.nb + 3) / 4, 128, 0, st>>>(a);
+  else rb_raypath_kernel<1><<<a.nb, 32, 0, st>>>(a);
   return cudaGetLastError();
 }
 
