@@ -895,7 +895,7 @@ def run_gpu(args, rank, world, local_rank):
         config=dict(workload=WORKLOAD, layers=nL, freqs=nf, rays=nb, lines=counts,
                     parallelism='replicas' if world > 1 else 'single',
                     l2='256 MiB buffer written between steps; per-step CUDA events',
-                    precision='f32 compensated line sums, f64 ray geometry, f32x2 tau',
+                    precision='f32 compensated (Kahan) line sums; f64 ray set-up, double-float (float pair) ray walk; double-float optical depth, compensated f32 weighted sums',
                     autotuned=tuned),
         e2e=dict(value=1.0 / float(np.mean(e2e_times)), unit=UNIT, h2d_bytes_per_step=int(h2d),
                  d2h_bytes_per_step=int(d2h), api='rb_forward (C ABI, pinned host buffers)'),
