@@ -921,11 +921,6 @@ __device__ __forceinline__ f2 br_eval2(f2 F, f2 FL, f2 m8F, f2 g, f2 gp, f2 gm, 
 // Not inlined: each line kind's sweep gets the kernel's whole register budget
 // for its own loop state (inlined into the family switch, the union of the
 // four kinds' live values spilled to local memory at 64 registers).
-#ifndef RB_JVP_INLINE
-#define RB_JVP_FAMILY __noinline__
-#else
-#define RB_JVP_FAMILY __forceinline__
-#endif
 
 // One family of one layer for the CTA's frequencies.  Records of JV_CHUNK
 // lines at a time, double-buffered (chunk c+1 is built, one line per
@@ -936,7 +931,7 @@ __device__ __forceinline__ f2 br_eval2(f2 F, f2 FL, f2 m8F, f2 g, f2 gp, f2 gm, 
 // derivatives) go to sh.fam[fam][fi], added in group order.  Called by
 // every thread.
 template <int KIND, int CH>
-__device__ RB_JVP_FAMILY void jv_family(const JvpArgs& a, JvpShared<CH>& sh, int L, int fam,
+__device__ __noinline__ void jv_family(const JvpArgs& a, JvpShared<CH>& sh, int L, int fam,
                                         const JvFreq& fr, bool on, float& base, float* dbase) {
   const int tid = threadIdx.x;
   const int FTL = a.ft, NG = blockDim.x / a.ft;
@@ -1394,13 +1389,7 @@ cudaError_t launch_adjoint_sweep(const TbAdjArgs& ta, cudaStream_t st) {
 static cudaError_t launch_tan_jvp(const TanArgs& tn, const JvpArgs& jv, cudaStream_t st) {
   rb_layer_tan_kernel<<<(((tn.nL + 31) & ~31) * 8 + 63) / 64, 64, 0, st>>>(tn);
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
-#ifndef RB_JVP_MINB128
-#define RB_JVP_MINB128 3
-#endif
-#ifndef RB_JVP_MINB
-#define RB_JVP_MINB 3
-#endif
-  const int ctas = jv.ctas ? jv.ctas : (jv.ft >= 128 ? RB_JVP_MINB128 : RB_JVP_MINB);
+  const int ctas = jv.ctas ? jv.ctas : 3;   // 256-thread CTAs: 3 per SM unless asked
   // threads per CTA: one line group for 128-frequency tiles (no per-family
   // reduction across groups; C4 412 -> 371 ms), two or four otherwise.
   // 128-thread CTAs: 5 per SM (96 registers) unless 4 (120) or 6 (80) are asked.
