@@ -1,0 +1,104 @@
+"""CPU: the algebra the packed brightness scan (rb_tb_chunk2_kernel) rests on,
+restated in float64 numpy and checked against the oracle's direct
+recurrence (oracle.brightness, brightness.py:53-117).
+
+* Chunks: a path's steps are cut into chunks scanned from tau = 0 each;
+  exp(-(tau_c + t)) = exp(-tau_c) exp(-t), so the chunk sums, scaled by
+  exp(-tau) at each chunk's first node, add up to the path's sums.
+* Node weights: sum_k (W_{k+1} + W_k) hd_k = sum_j W_j (hd_{j-1} + hd_j)
+  inside a chunk, with hd_{-1} = hd_n = 0 at the chunk's ends; a chunk's
+  first node carries W = exp(0) a_0 (none on the path's first chunk).
+* Optical depth: a float32 running sum with its rounding errors collected
+  by Fast2Sum and renormalised every 16 steps stays within a few float32
+  ulp of the exact sum, including paths whose increments grow faster than
+  the sum (deep layers), where Fast2Sum is not exact.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def _random_path(rng, nseg, nL=400, nf=5):
+    ds = rng.uniform(0.1, 30.0, nseg + 1)                     # km
+    layer = rng.integers(0, nL, nseg + 1)
+    alpha = 10.0 ** rng.uniform(-9.0, -4.0, (nf, nL))         # cm^-1
+    T = rng.uniform(100.0, 600.0, nL)
+    return ds, layer, alpha, T
+
+
+def _chunked(ds, layer, alpha, T, chunk):
+    """The packed scan's decomposition in float64: per chunk the local
+    optical depth and the node-weighted sums, then the combine."""
+    hd = np.asarray(ds[:-1], dtype=float) * 1.0e5 / 2.0        # half ds, cm
+    a = alpha[:, layer]                                        # [nf, nodes]
+    Tn = T[layer]
+    nsteps = len(hd)
+    nf = alpha.shape[0]
+    parts = []
+    for i0 in range(0, nsteps, chunk):
+        n = min(chunk, nsteps - i0)
+        h = hd[i0:i0 + n]
+        w = np.zeros(n + 1)                                    # node weights
+        w[:-1] += h
+        w[1:] += h
+        x = (a[:, i0:i0 + n] + a[:, i0 + 1:i0 + n + 1]) * h    # step increments
+        t = np.concatenate([np.zeros((nf, 1)), np.cumsum(x, axis=1)], axis=1)
+        W = a[:, i0:i0 + n + 1] * np.exp(-t)
+        if i0 == 0:
+            W[:, 0] = 0.0                                      # W_0 = 0 on a path
+        parts.append((t[:, -1], W @ w, W @ (Tn[i0:i0 + n + 1] * w)))
+    tau0 = np.zeros(nf)
+    iw = np.zeros(nf)
+    tb = np.zeros(nf)
+    for dt, piw, ptb in parts:
+        sc = np.exp(-tau0)
+        iw += sc * piw
+        tb += sc * ptb
+        tau0 = tau0 + dt
+    return np.where(tb < O.T_CMB, O.T_CMB, tb / np.where(tb < O.T_CMB, 1.0, iw)), iw
+
+
+@pytest.mark.parametrize('chunk', [1, 7, 64])
+@pytest.mark.parametrize('nseg', [1, 63, 64, 65, 300])
+def test_chunks_and_node_weights_reproduce_the_recurrence(chunk, nseg):
+    rng = np.random.default_rng(nseg * 100 + chunk)
+    ds, layer, alpha, T = _random_path(rng, nseg)
+    tb_ref, _, _, iw_ref = O.brightness(ds, layer, alpha, T)
+    tb, iw = _chunked(ds, layer, alpha, T, chunk)
+    np.testing.assert_allclose(iw, iw_ref, rtol=1e-12)
+    np.testing.assert_allclose(tb, tb_ref, rtol=1e-12)
+
+
+def _fast2sum_tau(x, flush=16):
+    """The kernel's optical depth in float32: th += x with the Fast2Sum
+    error collected in ntl, renormalised every `flush` steps; returns
+    th - ntl after each step (as float64)."""
+    th = np.float32(0.0)
+    ntl = np.float32(0.0)
+    out = []
+    for k, xk in enumerate(x.astype(np.float32)):
+        s = np.float32(th + xk)
+        ntl = np.float32(ntl + np.float32(np.float32(s - th) - xk))
+        th = s
+        out.append(float(th) - float(ntl))
+        if k % flush == flush - 1:
+            s = np.float32(th - ntl)
+            ntl = np.float32(ntl + np.float32(s - th))
+            th = s
+    return np.array(out)
+
+
+@pytest.mark.parametrize('growth', [1.0, 1.5, 3.0])
+def test_fast2sum_optical_depth_tracks_the_exact_sum(growth):
+    """Increments of one size, and increments growing geometrically (each
+    step larger than the whole sum before it for growth > 2)."""
+    rng = np.random.default_rng(int(growth * 10))
+    n = 2000 if growth == 1.0 else int(30 / np.log10(growth))   # sums below ~1e25
+    x = (rng.uniform(0.5, 1.5, n) * growth ** np.arange(n) * 1e-6).astype(np.float32)
+    exact = np.cumsum(x.astype(np.float64))
+    got = _fast2sum_tau(x)
+    err = np.abs(got - exact) / exact
+    # a plain float32 running sum drifts by ~n ulp; the collected errors
+    # keep each prefix within a few ulp of its exact value
+    assert np.max(err) < 4 * np.finfo(np.float32).eps, np.max(err)
