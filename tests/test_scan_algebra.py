@@ -12,6 +12,10 @@ recurrence (oracle.brightness, brightness.py:53-117).
   by Fast2Sum and renormalised every 16 steps stays within a few float32
   ulp of the exact sum, including paths whose increments grow faster than
   the sum (deep layers), where Fast2Sum is not exact.
+* Reverse sweep (rb_tb_adj_lambda / _suffix / _grad kernels): per-chunk
+  sums of dTb/dtau, their suffix sums over the later chunks, then each
+  chunk's nodes in reverse equal the oracle's vector-Jacobian product
+  (oracle/adjoint.py brightness_vjp).
 """
 import numpy as np
 import pytest
@@ -102,3 +106,68 @@ def test_fast2sum_optical_depth_tracks_the_exact_sum(growth):
     # a plain float32 running sum drifts by ~n ulp; the collected errors
     # keep each prefix within a few ulp of its exact value
     assert np.max(err) < 4 * np.finfo(np.float32).eps, np.max(err)
+
+
+def _chunked_vjp(ds, layer, alpha, T, gTb, chunk):
+    """The reverse sweep as the adjoint kernels split it: each chunk's sum of
+    dTb/dtau over its nodes (scaled by exp(-tau) at its first node), the
+    suffix sums of those over the later chunks, then each chunk's nodes in
+    reverse from its suffix (node i0 of a chunk belongs to the chunk before;
+    node 0 takes only its segment term)."""
+    nf, nL = alpha.shape
+    d = np.asarray(ds[:-1], dtype=float) * 1.0e5                # cm
+    lay = np.asarray(layer) % nL
+    a = alpha[:, lay]
+    Tn = T[lay]
+    N = len(d)                                                  # steps
+    dt = (a[:, :-1] + a[:, 1:]) * d / 2.0
+    tau = np.concatenate([np.zeros((nf, 1)), np.cumsum(dt, axis=1)], axis=1)
+    E = np.exp(-tau)
+    E[:, 0] = 0.0
+    c = np.zeros(N + 1)
+    c[:-1] += d / 2.0
+    c[1:] += d / 2.0
+    iw = (a * E * c).sum(axis=1)
+    tbl = (a * E * Tn * c).sum(axis=1)
+    live = tbl >= O.T_CMB
+    Tb = np.where(live, tbl / np.where(live, iw, 1.0), O.T_CMB)
+    g = np.where(live, gTb, 0.0)
+    rIW = np.where(live, 1.0 / np.where(live, iw, 1.0), 0.0)
+    chunks = [(i0, min(chunk, N - i0)) for i0 in range(0, N, chunk)]
+    # per-chunk sums of dTb/dtau over nodes i0+1 .. i0+ns
+    S = []
+    for i0, ns in chunks:
+        k = np.arange(i0 + 1, i0 + ns + 1)
+        wk = c[k] * (Tn[k] - Tb[:, None]) * rIW[:, None]
+        S.append(-(wk * a[:, k] * E[:, k]).sum(axis=1))
+    suffix = [sum(S[j + 1:], np.zeros(nf)) for j in range(len(S))]
+    galpha = np.zeros((nf, nL))
+    gT = np.zeros(nL)
+    for (i0, ns), Ln in zip(chunks, suffix):
+        Ln = Ln.copy()
+        for t in range(i0 + ns, i0, -1):
+            dprev = d[t - 1]
+            dcur = d[t] if t < N else 0.0
+            ck = 0.5 * (dprev + dcur)
+            wk = ck * (Tn[t] - Tb) * rIW
+            Lnext = Ln.copy()
+            Ln = Ln - wk * a[:, t] * E[:, t]
+            galpha[:, lay[t]] += g * (wk * E[:, t] + 0.5 * dprev * Ln + 0.5 * dcur * Lnext)
+            gT[lay[t]] += np.sum(g * a[:, t] * E[:, t] * ck * rIW)
+        if i0 == 0:
+            galpha[:, lay[0]] += g * 0.5 * d[0] * Ln
+    return galpha, gT
+
+
+@pytest.mark.parametrize('chunk', [1, 7, 64])
+@pytest.mark.parametrize('nseg', [1, 64, 65, 300])
+def test_chunked_reverse_sweep_equals_the_vjp(chunk, nseg):
+    from oracle import adjoint as A
+    rng = np.random.default_rng(7 * nseg + chunk)
+    ds, layer, alpha, T = _random_path(rng, nseg, nL=60)
+    gTb = rng.normal(size=alpha.shape[0])
+    ga_ref, gT_ref = A.brightness_vjp(ds, layer, alpha, T, gTb)
+    ga, gT = _chunked_vjp(ds, layer, alpha, T, gTb, chunk)
+    scale = np.max(np.abs(ga_ref))
+    np.testing.assert_allclose(ga, ga_ref, rtol=0, atol=1e-10 * scale)
+    np.testing.assert_allclose(gT, gT_ref, rtol=0, atol=1e-10 * np.max(np.abs(gT_ref)))
