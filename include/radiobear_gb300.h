@@ -13,6 +13,8 @@
  *
  * Units follow the reference: frequencies GHz, pressure bar, temperature K,
  * radii and path lengths km, absorption cm^-1 (dB/km when units_db = 1).
+ * Frequencies lie in [0, 2e4] GHz and line centres in (0, 2e4] GHz (the
+ * float32 line sums' range); others are rejected with RB_EINVAL.
  *
  * Reference interfaces each entry point replaces (paths relative to the
  * david-deboer/radiobear project root):

@@ -315,9 +315,12 @@ cudaError_t upload(DBuf& b, const T* src, size_t count, cudaStream_t st) {
 //    when the tile needs both.
 int plan_frequencies(rb_handle* h, int nf, const double* freqs, cudaStream_t st) {
   if (nf < 1) return fail(RB_EINVAL, "nf must be >= 1");
+  // Frequencies, like line centres, at most 2e4 GHz: the line sums multiply
+  // two lines' float32 denominators ((f^2 + fo^2)^2 each), whose product
+  // then stays over two decades below the float32 range.
   for (int i = 0; i < nf; ++i)
-    if (!std::isfinite(freqs[i]) || freqs[i] < 0.0)
-      return fail(RB_EINVAL, "frequency %d is not a finite non-negative number", i);
+    if (!std::isfinite(freqs[i]) || freqs[i] < 0.0 || freqs[i] > 2.0e4)
+      return fail(RB_EINVAL, "frequency %d: %g GHz outside [0, 2e4]", i, freqs[i]);
   if ((int)h->plan_f.size() == nf && std::equal(freqs, freqs + nf, h->plan_f.begin()))
     return RB_OK;
   std::vector<double> fhs;

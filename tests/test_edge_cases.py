@@ -123,6 +123,12 @@ def test_host_rejections(engine):
     Xb[3, 5] = np.nan
     with pytest.raises(ValueError):
         engine.alpha(P, T, Xb, z['freqs'])
+    for bad in (-1.0, np.nan, 2.5e4):     # frequencies in [0, 2e4] GHz
+        with pytest.raises(ValueError, match='frequency 1'):
+            engine.alpha(P, T, X, np.array([10.0, bad]))
+        with pytest.raises(ValueError, match='frequency 1'):
+            engine.forward(P, T, X, z['prop_R'], z['prop_N'], np.array([10.0, bad]), [[0.0, 0.0]],
+                           G.REQ, G.RPOL)
     with pytest.raises(ValueError):
         engine.set_formalisms('nh3_xyz' if False else 'nh3_hs', True, True, True, True, 'x')
     with pytest.raises(ValueError):
