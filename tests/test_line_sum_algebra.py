@@ -27,6 +27,9 @@ ULP = 2.0 ** -23                        # float32 ulp of 1.0
 # the 256 log-spaced frequencies from 0.5 to 100 GHz of the 1000-layer disc
 # spectrum, in chains of 32
 FREQS = np.logspace(np.log10(0.5), np.log10(100.0), 256)
+# and 64 from 100 GHz to 2 THz, where the rotational, H2S, PH3 and water
+# lines fall inside the chains' windows
+GRIDS = {'radio': FREQS, 'submm': np.logspace(2.0, np.log10(2000.0), 64)}
 
 
 def _cat():
@@ -172,8 +175,10 @@ def _inversion(cat, T, P, coefs):
     return gamma, zeta, d * gamma, floor
 
 
+@pytest.mark.parametrize('grid', sorted(GRIDS))
 @pytest.mark.parametrize('T,P', LAYERS)
-def test_inversion_line_sum_matches_the_oracle(T, P):
+def test_inversion_line_sum_matches_the_oracle(grid, T, P):
+    freqs = GRIDS[grid]
     cat = _cat()
     order = np.argsort(cat['ammonia__fo'], kind='stable')
     fo, Io = cat['ammonia__fo'][order], cat['ammonia__Io'][order]
@@ -182,23 +187,25 @@ def test_inversion_line_sum_matches_the_oracle(T, P):
     wide = all(fl >= 0.32 * fo.max() for fl in floors)
     S = Io / np.square(fo)
     smax = S.max()
-    got = np.empty(len(FREQS))
-    ref = np.empty(len(FREQS))
+    got = np.empty(len(freqs))
+    ref = np.empty(len(freqs))
     for lo_set in (True, False):        # coefficient set by frequency (30 GHz)
-        sel = FREQS <= O.F_SPLIT if lo_set else FREQS > O.F_SPLIT
+        sel = freqs <= O.F_SPLIT if lo_set else freqs > O.F_SPLIT
         g, z, d, _ = _inversion(cat, T, P, O.HS_INV_LO if lo_set else O.HS_INV_HI)
         r = br_records(fo, g, z, d, S / smax)
-        pq = window_quads(fo, FREQS, force_fast=wide)[:, sel]
-        got[sel] = kernel_sum('br', r, FREQS[sel], pq) * smax
-        f = FREQS[sel]
+        pq = window_quads(fo, freqs, force_fast=wide)[:, sel]
+        got[sel] = kernel_sum('br', r, freqs[sel], pq) * smax
+        f = freqs[sel]
         ref[sel] = np.sum(Io[:, None] * O._ben_reuven_hs(f[None, :], fo[:, None], g[:, None],
                                                          z[:, None], d[:, None]), axis=0) \
             * np.pi / (2.0 * np.square(f))
     np.testing.assert_allclose(got, ref, rtol=1e-6)
 
 
+@pytest.mark.parametrize('grid', sorted(GRIDS))
 @pytest.mark.parametrize('T,P', LAYERS)
-def test_rotational_line_sum_matches_the_oracle(T, P):
+def test_rotational_line_sum_matches_the_oracle(grid, T, P):
+    freqs = GRIDS[grid]
     cat = _cat()
     order = np.argsort(cat['ammonia__fo_rot'], kind='stable')
     fo, Io = cat['ammonia__fo_rot'][order], cat['ammonia__Io_rot'][order]
@@ -210,9 +217,42 @@ def test_rotational_line_sum_matches_the_oracle(T, P):
         + (nNH3 * P * XNH3 * cat['ammonia__gNH3_rot'][order]) * Td ** eNH3
     smax = Io.max()
     r = gross_records(fo, g, Io / smax)
-    got = kernel_sum('gross', r, FREQS, window_quads(fo, FREQS)) * smax
-    ref = np.sum(Io[:, None] * O._gross(FREQS[None, :], fo[:, None], g[:, None]), axis=0) \
-        * np.pi / (4.0 * np.square(FREQS))
+    got = kernel_sum('gross', r, freqs, window_quads(fo, freqs)) * smax
+    ref = np.sum(Io[:, None] * O._gross(freqs[None, :], fo[:, None], g[:, None]), axis=0) \
+        * np.pi / (4.0 * np.square(freqs))
+    np.testing.assert_allclose(got, ref, rtol=1e-6)
+
+
+@pytest.mark.parametrize('grid', sorted(GRIDS))
+@pytest.mark.parametrize('gas', ['h2s', 'ph3'])
+@pytest.mark.parametrize('T,P', LAYERS)
+def test_geisa_line_sums_match_the_oracle(grid, gas, T, P):
+    """h2s_ddb (zeta = gamma, a constant pressure shift; h2s_ddb.py:74-80)
+    and ph3_jh (zeta = delta = 0; ph3_jh.py:95-101) through the oracle's
+    _br_geisa, which carries 2 GHZ f^2 / pi outside the kernel's sum."""
+    freqs = GRIDS[grid]
+    cat = _cat()
+    if gas == 'h2s':
+        fo, I0, E = cat['h2s__f0'], cat['h2s__I0'], cat['h2s__E']
+        T0, Ps = 296.0, P * 1e-5
+        g = (T0 / T) ** 0.7 * (1.960 * P * XH2 + 1.200 * P * XHE + cat['h2s__GH2S'] * Ps)
+        z, d = g, np.full_like(g, 1.28 * Ps)
+        itg = I0 * np.exp(-(1.0 / T - 1.0 / T0) * E * O.HCK)
+    else:
+        fo, I0, E = cat['ph3__f0'], cat['ph3__I0'], cat['ph3__E']
+        T0, Ps = 300.0, P * 5e-6
+        g = (T0 / T) ** (2.0 / 3.0) * (3.2930 * P * XH2 + 1.6803 * P * XHE) * cat['ph3wgt__WgtFGB'] \
+            + (T0 / T) * 4.2157 * Ps * cat['ph3wgt__WgtSB']
+        z = d = np.zeros_like(g)
+        itg = I0 * cat['ph3wgt__WgtI0'] * np.exp(-(1.0 / T - 1.0 / T0) * E * O.HCK)
+    order = np.argsort(fo, kind='stable')
+    fo, g, z, d, itg = fo[order], g[order], z[order], d[order], itg[order]
+    S = itg / np.square(fo)
+    smax = S.max()
+    r = br_records(fo, g, z, d, S / smax)
+    got = kernel_sum('br', r, freqs, window_quads(fo, freqs)) * smax
+    ref = O._br_geisa(freqs, fo[None, :], g[None, :], z[None, :], d[None, :], itg[None, :])[0] \
+        * np.pi / (2.0 * O.GHZ * np.square(freqs))
     np.testing.assert_allclose(got, ref, rtol=1e-6)
 
 
@@ -228,15 +268,17 @@ def _water(T, P):
     return centre[order], df[order], S[order]
 
 
+@pytest.mark.parametrize('grid', sorted(GRIDS))
 @pytest.mark.parametrize('T,P', LAYERS)
-def test_water_line_sum_matches_the_oracle(T, P):
+def test_water_line_sum_matches_the_oracle(grid, T, P):
     """The two resonant terms of h2o_bk.py:177-187 (oracle alpha_h2o_bk's B
     and Cc), without the 750 GHz base term the kernel adds per layer."""
+    freqs = GRIDS[grid]
     centre, df, S = _water(T, P)
     smax = S.max()
     r = vvw_records(centre, df, S / smax)
-    got = kernel_sum('vvw', r, FREQS, window_quads(centre, FREQS)) * smax
-    f = FREQS[None, :]
+    got = kernel_sum('vvw', r, freqs, window_quads(centre, freqs)) * smax
+    f = freqs[None, :]
     c, w = centre[:, None], df[:, None]
     ref = np.sum(S[:, None] * (w / (np.square(f - c) + w * w) + w / (np.square(f + c) + w * w)),
                  axis=0)
