@@ -4,7 +4,8 @@ oracle's float64 line shapes on the real line catalogues.
 
 * Record fields per line as the kernel forms them: K = (fo + d)^2 + g^2 - z^2
   as a float pair, G4 - 2K, K^2, S(g - z), S(g + z)K (Ben-Reuven, nh3_hs.py:
-  193-226); G4 - 2K, K^2, S g with K = fo^2 (Gross, nh3_hs.py:259-263);
+  193-226); G4 - 2K, K^2, S g with K = fo^2 (Gross, nh3_hs.py:259-263,
+  296-300);
   2(d2 - c2), C^2, 2h, 2hC (VVW, h2o_bk.py:174-187).
 * The two-operation far-line denominator F (F + (G4 - 2K)) + K^2 for lines
   whose centre lies outside [0.75 fmin, 1.3 fmax] of a chain of 32
@@ -203,18 +204,29 @@ def test_inversion_line_sum_matches_the_oracle(grid, T, P):
 
 
 @pytest.mark.parametrize('grid', sorted(GRIDS))
+@pytest.mark.parametrize('band', ['rot', 'v2'])
 @pytest.mark.parametrize('T,P', LAYERS)
-def test_rotational_line_sum_matches_the_oracle(grid, T, P):
+def test_gross_line_sums_match_the_oracle(grid, band, T, P):
+    """The Gross families: rotational lines with per-line widths
+    (nh3_hs.py:232-265) and nu2 lines with fixed widths (nh3_hs.py:269-302)."""
     freqs = GRIDS[grid]
     cat = _cat()
-    order = np.argsort(cat['ammonia__fo_rot'], kind='stable')
-    fo, Io = cat['ammonia__fo_rot'][order], cat['ammonia__Io_rot'][order]
-    eH2, eHe, eNH3 = O.HS_ROT['eta']
-    nH2, nHe, nNH3 = O.HS_ROT['gnu']
     Td = 300.0 / T
-    g = (nH2 * P * XH2 * cat['ammonia__gH2_rot'][order]) * Td ** eH2 \
-        + (nHe * P * XHE * cat['ammonia__gHe_rot'][order]) * Td ** eHe \
-        + (nNH3 * P * XNH3 * cat['ammonia__gNH3_rot'][order]) * Td ** eNH3
+    if band == 'rot':
+        order = np.argsort(cat['ammonia__fo_rot'], kind='stable')
+        fo, Io = cat['ammonia__fo_rot'][order], cat['ammonia__Io_rot'][order]
+        eH2, eHe, eNH3 = O.HS_ROT['eta']
+        nH2, nHe, nNH3 = O.HS_ROT['gnu']
+        g = (nH2 * P * XH2 * cat['ammonia__gH2_rot'][order]) * Td ** eH2 \
+            + (nHe * P * XHE * cat['ammonia__gHe_rot'][order]) * Td ** eHe \
+            + (nNH3 * P * XNH3 * cat['ammonia__gNH3_rot'][order]) * Td ** eNH3
+    else:
+        order = np.argsort(cat['ammonia__fo_v2'], kind='stable')
+        fo, Io = cat['ammonia__fo_v2'][order], cat['ammonia__Io_v2'][order]
+        eH2, eHe, eNH3 = O.HS_V2['eta']
+        wH2, wHe, wNH3 = O.HS_V2['width']
+        g = np.full_like(fo, (P * XH2 * wH2) * Td ** eH2 + (P * XHE * wHe) * Td ** eHe
+                         + (P * XNH3 * wNH3) * Td ** eNH3)
     smax = Io.max()
     r = gross_records(fo, g, Io / smax)
     got = kernel_sum('gross', r, freqs, window_quads(fo, freqs)) * smax
