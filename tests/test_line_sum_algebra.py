@@ -14,6 +14,8 @@ oracle's float64 line shapes on the real line catalogues.
   lanes of a quad of four lines; compensated sums flushed every 64 lines.
 * Ben-Reuven layers whose width floor is at least 0.32 of the largest line
   centre ("wide") take the far-line form for every line.
+* nh3_sjs: widths from per-frequency blended coefficients, every line on
+  the float-pair form with its own reciprocal.
 Float32 operations are exact numpy float32 arithmetic; a fused multiply-add
 is the float64 product (exact for float32 operands) plus the addend, rounded
 to float32.
@@ -264,6 +266,73 @@ def test_geisa_line_sums_match_the_oracle(grid, gas, T, P):
     r = br_records(fo, g, z, d, S / smax)
     got = kernel_sum('br', r, freqs, window_quads(fo, freqs)) * smax
     ref = O._br_geisa(freqs, fo[None, :], g[None, :], z[None, :], d[None, :], itg[None, :])[0] \
+        * np.pi / (2.0 * O.GHZ * np.square(freqs))
+    np.testing.assert_allclose(got, ref, rtol=1e-6)
+
+
+def sjs_kernel_sum(fo, G0, S, shift, coef, freqs):
+    """The nh3_sjs item (sjs_item): coefficients A..D of
+    gamma = A + B G0, zeta = C + D G0 blended per frequency, every line on
+    the float-pair form with its own reciprocal, lanes (4q, 4q+2) and
+    (4q+1, 4q+3), flushed every 8 quads and at each 128-line chunk's end."""
+    shift = f32(shift)
+    c2h, c2l = split(np.square(fo))
+    KH, e = two_sum32(c2h, (f32(2) * fo.astype(f32) + shift) * shift)
+    KL = e + c2l
+    mKH, mKL = _pad(-KH, -1e18), _pad(-KL, 0)
+    w, st = _pad(np.asarray(G0).astype(f32), 0), _pad(np.asarray(S).astype(f32), 0)
+    F, FL = split(np.square(freqs))
+    F4 = f32(4) * F
+    A, B, C, D = (np.asarray(c).astype(f32) for c in coef)          # [nf] each
+    nq = len(w) // 4
+    s = np.zeros((2, len(freqs)), f32)
+    c = np.zeros_like(s)
+    p = np.zeros_like(s)
+    for q in range(nq):
+        for lane in range(2):
+            for i in (4 * q + lane, 4 * q + 2 + lane):
+                g = fma32(B, w[i], A)
+                z = fma32(D, w[i], C)
+                gm = fma32(z, f32(-1), g)
+                gp = g + z
+                g2z2 = gm * gp
+                d1 = fma32(g2z2, f32(-1), (F + mKH[i]) + (FL + mKL[i]))
+                den = fma32(d1, d1, F4 * (g * g))
+                num = fma32(gm, F, gp * fma32(mKH[i], f32(-1), g2z2))
+                p[lane] = fma32(st[i] * num, f32(1) / den, p[lane])
+        if q % 8 == 7 or q % 32 == 31 or q == nq - 1:
+            y = p - c
+            t = s + y
+            c = (t - s) - y
+            s = t
+            p[:] = 0
+    return ((s[0] - c[0]) + (s[1] - c[1])).astype(np.float64)
+
+
+@pytest.mark.parametrize('grid', sorted(GRIDS))
+@pytest.mark.parametrize('T,P', LAYERS)
+def test_sjs_line_sum_matches_the_oracle(grid, T, P):
+    """nh3_sjs (nh3_sjs.py:37-124) against the oracle's alpha_nh3_sjs with
+    its layer prefactor and the 2 GHZ f^2 / pi of the shape taken out."""
+    freqs = GRIDS[grid]
+    cat = _cat()
+    sc = {k.split('__')[1]: v for k, v in cat.items() if k.startswith('nh3__')}
+    order = np.argsort(sc['f0'], kind='stable')
+    sc = {k: v[order] for k, v in sc.items()}
+    Ta = np.array([T])
+    Ph2, Phe, Pnh3 = P * XH2, P * XHE, P * XNH3
+    join, spil = O._sjs_coefficients(Ta, np.array([P]), np.array([Ph2]))
+    wJ = np.clip((freqs - 26.0) / 8.0, 0.0, 1.0)          # Spilker <= 26 GHz, Joiner >= 34
+    tt = (296.0 / T) ** (2.0 / 3.0)
+    blend = {k: spil[k][0] + (join[k][0] - spil[k][0]) * wJ for k in join}
+    coef = (tt * (blend['GH2'] * Ph2 + blend['GHe'] * Phe), tt * blend['GNH3'] * Pnh3,
+            tt * (blend['ZH2'] * Ph2 + blend['ZHe'] * Phe), tt * blend['ZNH3'] * Pnh3)
+    itg = sc['I0'] * np.exp(-(1.0 / T - 1.0 / 296.0) * sc['E'] * O.HCK)
+    S = itg / np.square(sc['f0'])
+    smax = S.max()
+    got = sjs_kernel_sum(sc['f0'], sc['G0'], S / smax, -0.45 * Pnh3, coef, freqs) * smax
+    pre = O.GEISA_COEF * (Pnh3 / 296.0) * (296.0 / T) ** 3.5 * (1.0 + P / 1.0e5)
+    ref = O.alpha_nh3_sjs(freqs, Ta, np.array([P]), XH2, XHE, XNH3, sc)[0] / pre \
         * np.pi / (2.0 * O.GHZ * np.square(freqs))
     np.testing.assert_allclose(got, ref, rtol=1e-6)
 
