@@ -16,6 +16,7 @@ oracle's float64 line shapes on the real line catalogues.
   centre ("wide") take the far-line form for every line.
 * nh3_sjs: widths from per-frequency blended coefficients, every line on
   the float-pair form with its own reciprocal.
+* Line strengths 2^(l2I + cE E - M2) with the exponent as a float pair.
 Float32 operations are exact numpy float32 arithmetic; a fused multiply-add
 is the float64 product (exact for float32 operands) plus the addend, rounded
 to float32.
@@ -463,3 +464,47 @@ def test_compensated_block_sums():
                 p[:] = 0
         got = float((s[0] - c[0]) + (s[1] - c[1]))
         assert abs(got - exact) / exact < 18 * 2.0 ** -24
+
+
+def kernel_strength(l2I, E, cE, M2, single=False):
+    """line_strength: S = 2^(l2I + cE E - M2) with the exponent as a float
+    pair (log2 of intensity / centre^2, lower-state energy and the layer's
+    cE each split hi/lo, the product's error by fma), split into integer
+    and fractional parts before exp2.  single: the exponent in one float32
+    (the planted variant)."""
+    if single:
+        s = (f32(l2I) - f32(M2)) + f32(cE) * f32(E)
+        ti = np.rint(s)
+        return np.ldexp(np.exp2(s - ti), ti.astype(int)).astype(f32)
+    l2Ih, l2Il = split(l2I)
+    Eh, El = split(E)
+    cEh, cEl = split(cE)
+    ph = cEh * Eh
+    pl = fma32(cEh, Eh, -ph) + fma32(cEh, El, cEl * Eh)
+    s, e = two_sum32(l2Ih - f32(M2), ph)
+    lo = (e + pl) + l2Il
+    ti = np.rint(s)
+    out = np.ldexp(np.exp2((s - ti) + lo), ti.astype(int)).astype(f32)
+    return np.where(ti < -140, f32(0), out)
+
+
+@pytest.mark.parametrize('T', [100.0, 300.0, 1000.0])
+@pytest.mark.parametrize('cols', [('ammonia__fo', 'ammonia__Io', 'ammonia__Eo'),
+                                  ('ammonia__fo_rot', 'ammonia__Io_rot', 'ammonia__Eo_rot'),
+                                  ('nh3__f0', 'nh3__I0', 'nh3__E'), ('h2s__f0', 'h2s__I0', 'h2s__E'),
+                                  ('ph3__f0', 'ph3__I0', 'ph3__E')])
+def test_line_strength_exponent_as_float_pair(cols, T):
+    """Strengths relative to the layer's bound M2 = ceil(max exponent) + 1
+    (scale_bound): within 2.5e-7 of float64 (measured 1.0e-7, the exp2
+    rounding; CUDA's exp2f adds at most 2 ulp more), where one float32
+    exponent loses 2.5e-6 to 8e-6 (exponents down to -170)."""
+    cat = _cat()
+    fo, I, E = (cat[c] for c in cols)
+    l2I = np.log2(I) - 2.0 * np.log2(fo)
+    cE = -(1.0 / T - 1.0 / 300.0) * 1.438396 / np.log(2.0)
+    M2 = np.ceil(f32(l2I.max() + max(cE * E.min(), cE * E.max()))) + 1.0
+    exact = np.exp2(l2I + cE * E - M2)
+    ok = exact > 2.0 ** -126
+    err = {single: np.max(np.abs(kernel_strength(l2I, E, cE, M2, single)[ok] / exact[ok] - 1.0))
+           for single in (False, True)}
+    assert err[False] < 2.5e-7 and err[True] > 2e-6, err
