@@ -652,7 +652,8 @@ __global__ void __launch_bounds__(64) rb_layer_tan_kernel(TanArgs a) {
 // Records of one line, float: value fields and derivatives along the
 // family's three tangents (T, P, ln X of its own gas).
 // Lines per record chunk: 128 for 256-thread CTAs, 64 for 128-thread CTAs
-// (half the shared memory, so 5 CTAs fit per SM; C4 371 -> 358 ms).
+// (half the shared memory, so 5 CTAs fit per SM; 4096 atmospheres of
+// 300-1200 layers at 128 frequencies: 371 -> 358 ms).
 constexpr int JV_CHUNK = 128;
 constexpr int JV_NREC = 16;
 
@@ -1100,10 +1101,14 @@ __device__ __noinline__ void jv_family(const JvpArgs& a, JvpShared<CH>& sh, int 
 // Threads: JV_FT frequencies x (blockDim / JV_FT) line groups; group g
 // sweeps lines g, g + NG, ... of every chunk and the groups' sums are added
 // per family (with one group, 128 threads for 128 frequencies, each thread
-// holds its frequency's family sums itself).  MINB resident CTAs per SM: 4 (64 registers) for 128-frequency
-// tiles, 3 (80 registers) for smaller ones (measured: C4's 128 frequencies
-// 68.4 -> 64.2 ms per 512 variants at 4; C3's 64 frequencies 0.693 -> 0.719
-// ms per step at 4).
+// holds its frequency's family sums itself).  MINB resident CTAs per SM
+// (launch_tan_jvp): 128-thread CTAs with 64-line chunks at 5 (96
+// registers; 4 or 6 when asked), the 128-frequency tiles' default;
+// 256-thread CTAs with 128-line chunks at 3 (80 registers; 4 when asked)
+// for smaller tiles (measured: 4096 atmospheres of 300-1200 layers at 128
+// frequencies, 290 / 278 / 284 ms at 4 / 5 / 6; one 1000-layer atmosphere
+// at 64 frequencies, 0.474 ms per adjoint with 256 threads at 3 against
+// 0.533 with 128 threads at 5).
 template <int MINB, int NT>
 __global__ void __launch_bounds__(NT, MINB) rb_alpha_jvp_kernel(JvpArgs a) {
   constexpr int CH = NT == 128 ? 64 : JV_CHUNK;
@@ -1391,7 +1396,8 @@ static cudaError_t launch_tan_jvp(const TanArgs& tn, const JvpArgs& jv, cudaStre
   dim3 grid(jv.nL, (jv.nf + jv.ft - 1) / jv.ft);
   const int ctas = jv.ctas ? jv.ctas : 3;   // 256-thread CTAs: 3 per SM unless asked
   // threads per CTA: one line group for 128-frequency tiles (no per-family
-  // reduction across groups; C4 412 -> 371 ms), two or four otherwise.
+  // reduction across groups; 4096 atmospheres at 128 frequencies 412 -> 371
+  // ms), two or four otherwise.
   // 128-thread CTAs: 5 per SM (96 registers) unless 4 (120) or 6 (80) are asked.
   const int nt = jv.threads ? jv.threads : (jv.ft >= 128 ? 128 : 256);
   if (nt == 128) {
@@ -1444,8 +1450,8 @@ cudaError_t launch_adjoint_contract(const JvpArgs& jv, const ExtraArgs* ea, cons
   return cudaGetLastError();
 }
 
-// Frequencies per CTA of rb_alpha_jvp_kernel (the rest of its 256 threads
-// split the lines).
+// Frequencies per CTA of rb_alpha_jvp_kernel (threads beyond them split
+// the lines).
 // (ft_forced: rb_set_tuning's choice, 0 = automatic.)
 int adjoint_ft(int nf, int ft_forced) {
   if (ft_forced) return ft_forced;

@@ -311,9 +311,10 @@ __device__ __forceinline__ void stage_nodes(const TbArgs& a, float4* sp, const f
 // subtracts back from a chunk's total, recomputes that total exactly).
 //
 // The 5-CTA bound (96 registers) lets the compiler keep 32 steps of alpha
-// loads in flight without spilling: C1 scan 0.0292 ms unbounded (46
-// registers) / 0.0272 ms at 6 CTAs (80 registers, spills) / 0.0272 ms at 5;
-// C2 0.52 / 0.43 / 0.39 ms.
+// loads in flight without spilling: 64 rays x 256 frequencies through 1000
+// layers 0.0292 ms unbounded (46 registers) / 0.0272 ms at 6 CTAs (80
+// registers, spills) / 0.0272 ms at 5; a 256 x 256 image (31,405 rays on
+// the disc) at 8 frequencies 0.52 / 0.43 / 0.39 ms.
 __global__ void __launch_bounds__(128, 5) rb_tb_chunk2_kernel(TbArgs a) {
   const int npair = a.nf / 2;
   const int FP = a.lanes ? a.lanes : scan_lanes(npair);
@@ -340,7 +341,8 @@ __global__ void __launch_bounds__(128, 5) rb_tb_chunk2_kernel(TbArgs a) {
   float4* sp = s_scan4 + sub * SCAN_ITEM_F4;
   // Staging in two passes.  1 (stage_nodes): the item's lanes load node
   // t's layer, T and hd_t; with at most 8 lanes per item a lane's up to 17
-  // nodes are loaded at once (C2, 8 frequencies: 0.364 -> 0.337 ms), else
+  // nodes are loaded at once (the 256 x 256 image at 8 frequencies: 0.364
+  // -> 0.337 ms), else
   // 4 at a time.  2: the node weights from the staged hd.
   if (live) {
     const float* hds = a.hds + (size_t)ray * a.max_seg + i0;
