@@ -70,7 +70,9 @@ def _store(k, best, times):
         os.makedirs(os.path.dirname(path), exist_ok=True)
         data = _load()
         data[k] = dict(best=list(best), ms={','.join(str(x) for x in c): v for c, v in times.items()})
-        tmp = path + '.tmp'
+        # one temporary file per process: replicas tuning at once each move a
+        # whole file into place (the last one wins; no reader sees a torn one)
+        tmp = '{}.{}.tmp'.format(path, os.getpid())
         with open(tmp, 'w') as fp:
             json.dump(data, fp, indent=1, sort_keys=True)
         os.replace(tmp, path)

@@ -62,3 +62,29 @@ def test_jvp_and_scan_knobs_are_cached_separately(tmp_path, monkeypatch):
     assert tune.tune_adjoint(eng, never, key=key)[0] == (64, 4)
     assert tune.tune_scan(eng, never, key=key)[0] == (8,)
     assert eng.tuning == dict(jvp_freqs=64, jvp_ctas=4, jvp_threads=0, scan_lanes=8)
+
+
+def _write_keys(path, tag, n):
+    import os
+    os.environ['RB_TUNING_CACHE'] = path
+    from radiobear_gb300 import tune as T
+    for i in range(n):
+        T._store('{}-{}'.format(tag, i), (2, 1, 512), {(2, 1, 512): float(i)})
+
+
+def test_cache_written_by_replicas_at_once(tmp_path):
+    """Replicas under torchrun tune at once and write the same cache: each
+    moves a whole file of its own into place, so the file always parses and
+    no temporary files are left (entries may be lost to the last writer)."""
+    import multiprocessing as mp
+    path = str(tmp_path / 'tuning.json')
+    ctx = mp.get_context('spawn')
+    procs = [ctx.Process(target=_write_keys, args=(path, 'r{}'.format(r), 40)) for r in range(3)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    data = json.loads((tmp_path / 'tuning.json').read_text())
+    assert any(k.endswith('-39') for k in data)
+    assert sorted(f.name for f in tmp_path.iterdir()) == ['tuning.json']
