@@ -171,3 +171,73 @@ def test_chunked_reverse_sweep_equals_the_vjp(chunk, nseg):
     scale = np.max(np.abs(ga_ref))
     np.testing.assert_allclose(ga, ga_ref, rtol=0, atol=1e-10 * scale)
     np.testing.assert_allclose(gT, gT_ref, rtol=0, atol=1e-10 * np.max(np.abs(gT_ref)))
+
+
+def _f32_dfs_add(h, l, v):
+    """dfs_add of the adjoint kernels: (h, l) += v as a float pair."""
+    f = np.float32
+    s = f(h + v)
+    bb = f(s - h)
+    e = f(f(h - f(s - bb)) + f(v - bb))
+    e = f(e + l)
+    h2 = f(s + e)
+    return h2, f(e - f(h2 - s))
+
+
+def _f32_fast2sum_total(x, flush=16):
+    """The forward scan's chunk total (th, -ntl) from its Fast2Sum steps."""
+    f = np.float32
+    th, ntl = f(0), f(0)
+    for k, xk in enumerate(x):
+        s = f(th + xk)
+        ntl = f(ntl + f(f(s - th) - xk))
+        th = s
+        if k % flush == flush - 1:
+            s = f(th - ntl)
+            ntl = f(ntl + f(s - th))
+            th = s
+    return th, f(-ntl)
+
+
+@pytest.mark.parametrize('profile', ['even', 'growth3', 'jump'])
+def test_reverse_sweep_restarts_from_an_exact_chunk_sum(profile):
+    """rb_tb_adj_grad_kernel subtracts a chunk's step increments in reverse
+    from its local optical depth at the chunk's last node, so that depth
+    must be the float-pair sum of the same float32 increments: the
+    subtraction then returns every node's depth to float-pair accuracy.
+    Started instead from the forward scan's Fast2Sum total (accurate to ~2
+    ulp of the depth reached, not to ulp^2), steps larger than the sum
+    before them (deep layers: 3x per step, or a jump from thin to opaque
+    layers) leave up to ~1e-2 in the depth of the chunk's first nodes,
+    i.e. ~1 % in exp(-tau) and in the gradients there."""
+    rng = np.random.default_rng({'even': 1, 'growth3': 2, 'jump': 3}[profile])
+    f = np.float32
+    worst = {False: 0.0, True: 0.0}
+    for _ in range(100):
+        if profile == 'even':
+            x = rng.uniform(0.5, 1.5, 64) * 10.0 ** rng.uniform(-3.0, 0.0)
+        elif profile == 'growth3':
+            n = int(rng.integers(10, 20))
+            x = rng.uniform(0.5, 1.5, n) * 3.0 ** np.arange(n) * 10.0 ** rng.uniform(-6.0, -3.0)
+        else:
+            k = int(rng.integers(1, 60))
+            x = np.concatenate([rng.uniform(0.5, 1.5, k) * 10.0 ** rng.uniform(-6.0, -2.0),
+                                rng.uniform(0.5, 1.5, 64 - k) * 10.0 ** rng.uniform(0.0, 3.0)])
+        x = x.astype(f)
+        exact = np.concatenate([[0.0], np.cumsum(x.astype(np.float64))])
+        h, l = f(0), f(0)
+        for v in x:
+            h, l = _f32_dfs_add(h, l, v)
+        for fast, start in ((False, (h, l)), (True, _f32_fast2sum_total(x))):
+            th, tl = start
+            tau = [float(th) + float(tl)]
+            for v in x[::-1]:
+                th, tl = _f32_dfs_add(th, tl, f(-v))
+                tau.append(float(th) + float(tl))
+            tau = np.array(tau[::-1])
+            live = exact < 80.0                       # nodes whose exp(-tau) is not 0
+            err = np.max(np.abs(tau[live] - exact[live])) / max(1.0, exact[-1] * 2.0 ** -44)
+            worst[fast] = max(worst[fast], err)
+    assert worst[False] < 1e-8, worst
+    if profile != 'even':
+        assert worst[True] > 1e-5, worst
