@@ -241,3 +241,49 @@ def test_reverse_sweep_restarts_from_an_exact_chunk_sum(profile):
     assert worst[False] < 1e-8, worst
     if profile != 'even':
         assert worst[True] > 1e-5, worst
+
+
+def _expint_cf(n, x):
+    """A&S 5.1.22 by the modified Lentz method, as rb_expint.cuh."""
+    tiny = 1e-300
+    bb = x + n
+    c = 1.0 / tiny
+    d = 1.0 / bb
+    h = d
+    for i in range(1, 200):
+        an = -float(i) * (n - 1 + i)
+        bb += 2.0
+        d = 1.0 / (an * d + bb)
+        c = bb + an / c
+        de = c * d
+        h *= de
+        if abs(de - 1.0) < 1e-16:
+            break
+    return h * np.exp(-x)
+
+
+def _expint_series(n, x):
+    """A&S 5.1.11 (E1) / 5.1.12 (E2) power series, as rb_expint.cuh."""
+    euler = 0.57721566490153286061
+    s = 0.0
+    fact = 1.0 if n == 1 else -x
+    for k in range(n, 60):
+        fact *= -x / k
+        term = fact / (k if n == 1 else k - 1)
+        s += term
+        if abs(term) < 1e-18 * abs(s) + 1e-300:
+            break
+    if n == 1:
+        return -euler - np.log(x) - s
+    return 1.0 + x * (np.log(x) - 1.0 + euler) - s
+
+
+def test_disc_weighting_e2_and_its_derivative_e1():
+    """The 'disc' weighting 2 E2(tau) (brightness.py:96, scipy.special.expn)
+    and dE2/dx = -E1 of its adjoint: series up to x = 1, continued fraction
+    above, 0 past 740; within 1e-14 relative of scipy from 1e-12 to 700."""
+    from scipy.special import exp1, expn
+    x = np.concatenate([np.logspace(-12, np.log10(700.0), 400), np.linspace(0.95, 1.05, 41)])
+    for n, ref in ((2, expn(2, x)), (1, exp1(x))):
+        got = np.array([_expint_series(n, v) if v <= 1.0 else _expint_cf(n, v) for v in x])
+        np.testing.assert_allclose(got, ref, rtol=1e-14)
